@@ -1,0 +1,183 @@
+/*
+ * scopyon_gb300 — C ABI of the GB300 image-formation engine.
+ *
+ * Every function takes device pointers (memory the caller allocated on the
+ * current CUDA device), sizes, a host pointer to a parameter struct where
+ * needed, and a cudaStream_t passed as void*.  Functions only enqueue work on
+ * that stream; they never allocate device memory and never synchronise except
+ * where stated.  Return value: 0 on success, a negative SC_ERR_* code
+ * otherwise; sc_last_error() gives a message (thread-local).
+ *
+ * Reference citations are paths inside the ecell/scopyon source tree.
+ */
+#ifndef SCOPYON_GB300_H
+#define SCOPYON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SC_OK 0
+#define SC_ERR_ARG (-1)      /* invalid argument (host-side validation)      */
+#define SC_ERR_CUDA (-2)     /* a CUDA call or launch failed                  */
+#define SC_ERR_TIMEOUT (-3)  /* a bounded device-side wait ran out            */
+#define SC_ERR_NAN (-4)      /* non-finite input detected                     */
+#define SC_ERR_CAPACITY (-5) /* a caller buffer is too small                  */
+
+#define SC_PSF_BORN_WOLF 0
+#define SC_PSF_GAUSSIAN 1
+
+#define SC_CAM_EMCCD 0
+#define SC_CAM_CCD 1
+#define SC_CAM_CMOS_TABLE 2
+#define SC_CAM_SCMOS 3
+
+/* Status word written by kernels into a caller buffer (int[4]):
+ * [0] error flags (bit0 bad PSF key, bit1 missing table, bit2 bounds overflow,
+ *     bit3 RNG loop bound hit, bit4 capacity), [1..3] first offending index. */
+#define SC_STATUS_WORDS 4
+
+/* One emitter during one exposure sub-step, ready to be splatted (48 bytes). */
+typedef struct {
+    double x0, y0;       /* footprint origin along x / y in metres (exact FP64)      */
+    float ax_hi, ax_lo;  /* (i_start*px - x0)/res as a double-float                   */
+    float ay_hi, ay_lo;  /* (j_start*px - y0)/res as a double-float                   */
+    int16_t i_start, n_i;/* first pixel index and number of footprint bounds along x  */
+    int16_t j_start, n_j;/* same along y; n_i < 2 or n_j < 2 means nothing to splat   */
+    int32_t slot;        /* PSF table slot of the depth key                           */
+    float w;             /* normalisation * res^2: photons per unit table sum          */
+} ScStepRec;
+
+typedef struct {
+    /* optics and geometry */
+    double px;               /* pixel length on the sample: pixel_length / magnification */
+    double res;              /* PSF grid resolution (1 nm)                                */
+    double depth_cutoff;     /* fluorophore.depth_cutoff                                  */
+    double focal[3];         /* detector.focal_point                                      */
+    int32_t nw, nh;          /* image size (pixels along x, y)                            */
+    int32_t n_signal;        /* cartesian PSF grid edge, 2 * n_r - 1                       */
+    int32_t n_sub;           /* sub-steps in this frame                                   */
+    int32_t n_particles;     /* particles per sub-step                                    */
+    int32_t max_key;         /* largest valid depth key; key -1 maps to slot max_key + 1   */
+    /* emission physics (reference _epifm.py:1267-1360) */
+    double amplitude0;       /* Snell's-law amplitude, photons / s / m^2                   */
+    double penetration;      /* evanescent penetration depth (inf for EPI)                */
+    double x_sec;            /* absorption cross-section ln(10) * eps * 0.1 / N_A, m^2     */
+    double qy;               /* quantum yield                                              */
+    double beer;             /* 1 - 10^-A, fraction absorbed (Beer-Lambert)                */
+    double norm_coeff;       /* sum(fluoem_norm) * psf_normalization                       */
+    int32_t bleaching;       /* 1: photon-budget bleaching on                              */
+    int32_t with_optinfo;    /* 1: accumulate the 8-vector true_data per particle          */
+} ScStepParams;
+
+typedef struct {
+    int32_t nw, nh;          /* image size                                                 */
+    int32_t tile;            /* tile edge in pixels (8..64, multiple of 8)                 */
+    int32_t tiles_x, tiles_y;
+    int32_t n_r;             /* radial samples; quadrant table is (n_r+1)^2               */
+    int32_t sat_pitch;       /* row pitch of one quadrant table in float2 entries          */
+    int32_t n_images;        /* frames/images splatted by one launch                        */
+    int32_t rec_per_image;   /* records per image (record r is in image r / rec_per_image); */
+                             /* 0 means every record belongs to image 0                     */
+    double px, res;
+} ScSplatParams;
+
+typedef struct {
+    int32_t nw, nh;
+    int32_t camera;          /* SC_CAM_*                                                   */
+    int32_t exact;           /* 1: FP64 ADC arithmetic identical to the reference           */
+    int32_t rounding;        /* 1: rint the ADC output                                     */
+    int32_t bit;
+    double qe, background, readout_noise, emgain, fullwell;
+    double offset0, gain0;   /* used when the offset / gain maps are NULL                   */
+    int32_t table_n;         /* CMOS noise table length                                    */
+    uint64_t seed;           /* Philox key for native draws                                */
+    uint64_t counter;        /* Philox counter base (e.g. frame index)                     */
+} ScCameraParams;
+
+int sc_get_version(void);
+const char *sc_last_error(void);
+
+/* Radial PSF tables for n_keys depths, n_r radii each (r_i = i * res).
+ * Replaces PointSpreadingFunction.get_born_wolf_distribution /
+ * get_gaussian_distribution (src/scopyon/_epifm.py:136-213).               */
+int sc_psf_radial(int kind, double wavelength, double na, double sigma,
+                  const double *d_depths, int n_keys, int n_r, double res,
+                  double *d_radial, void *stream);
+
+/* Quadrant summed-area tables (double-float pairs) of the cartesian PSF grid,
+ * one per radial table.  Replaces PointSpreadingFunction.radial_to_cartesian
+ * (src/scopyon/_epifm.py:99-126) and the per-pixel slice sums of
+ * overlay_signal_ (src/scopyon/_epifm.py:277-282).                          */
+int sc_psf_quadrant_sat(const double *d_radial, int n_keys, int n_r, double res,
+                        float *d_sat, int sat_pitch, void *stream);
+
+/* Emitter physics for one frame: excitation, emitted photons, photon-budget
+ * bleaching, normalisation, depth key and footprint origin per particle and
+ * sub-step.  d_particles is [n_sub][n_particles][5] (depth, x, y, m_id,
+ * p_state) as formatted by EPIFMSimulator.__format_data; d_present
+ * ([n_sub][n_particles] bytes, NULL = all present) marks particle slots
+ * absent at a sub-step; d_budget holds the
+ * photon budget per particle slot (initialised by the caller at first sight,
+ * carried across frames); d_optinfo receives the per-slot 8-vector sums of
+ * the frame (may be NULL when with_optinfo is 0).  Replaces
+ * _EPIFMSimulator.__overlay_molecule_plane and get_emit_photons
+ * (src/scopyon/_epifm.py:1267-1360).                                       */
+int sc_emitter_steps(const ScStepParams *p, const double *d_particles,
+                     const double *d_unit_time, const uint8_t *d_present,
+                     const int32_t *d_key_slot,
+                     double *d_budget, double *d_optinfo, ScStepRec *d_recs,
+                     int32_t *d_status, void *stream);
+
+/* Bytes of scratch sc_bin_steps needs for n_rec records on a tile grid. */
+size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total);
+/* Upper bound of bin entries (record, tile) for n_rec records. */
+int64_t sc_bin_capacity(int n_rec, double px, double res, int n_signal, int tile);
+
+/* Deterministic counting sort of records by output tile (new; the reference
+ * splats particle by particle, src/scopyon/_epifm.py:1262-1264).           */
+int sc_bin_steps(const ScStepRec *d_recs, int n_rec,
+                 const ScSplatParams *p, void *d_ws, size_t ws_bytes,
+                 int32_t *d_tile_start, int32_t *d_items, int64_t capacity,
+                 int32_t *d_status, void *stream);
+
+/* Tile splat: each CTA owns one output tile and sums the footprint integrals
+ * of the records binned to it.  Replaces overlay_signal_
+ * (src/scopyon/_epifm.py:224-282) for every particle and sub-step.          */
+int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
+             const int32_t *d_items, const float *d_sat, const ScSplatParams *p,
+             float *d_image, int32_t *d_status, void *stream);
+
+/* Camera model and ADC.  Replaces _EPIFMSimulator.__detector_output, the
+ * EMCCD / CCD / CMOS classes and __get_analog_to_digital_converter_counts
+ * (src/scopyon/_epifm.py:329-433, :1430-1484).
+ * Native mode (p->exact == 0): Philox draws, FP32 arithmetic with the float
+ * maps d_offset_f / d_inv_gain_f (NULL: constants offset0 / 1/gain0).
+ * Exact mode (p->exact == 1): draws injected by the caller — d_inj_signal
+ * (electrons) and d_inj_noise (electrons) or, for the CMOS table,
+ * d_inj_uniform — and the reference's FP64 ADC sequence with d_offset /
+ * d_gain.  Writes the expectation QE*(photons+background) to d_expect and
+ * the ADC image to d_adc64 and/or d_adc32.                                  */
+int sc_camera(const ScCameraParams *p, const float *d_photons,
+              const double *d_offset, const double *d_gain,
+              const float *d_offset_f, const float *d_inv_gain_f, const float *d_sigma,
+              const double *d_table_value, const double *d_table_cdf,
+              const double *d_inj_noise, const double *d_inj_signal,
+              const double *d_inj_uniform, float *d_expect, double *d_adc64,
+              float *d_adc32, int32_t *d_status, void *stream);
+
+/* Exact EMCCD draw: the reference's discrete distribution over integer
+ * output electrons, inverse CDF at the given uniform, per pixel
+ * (EMCCD.probability_distribution / draw_signal, src/scopyon/_epifm.py:365-400). */
+int sc_emccd_exact(const float *d_photons, double qe, double background,
+                   const double *d_uniform, int n_pixels, double emgain,
+                   double *d_signal, int32_t *d_status, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCOPYON_GB300_H */

@@ -1,0 +1,137 @@
+"""ctypes binding of ``libscopyon_gb300.so`` (declarations in include/scopyon_gb300.h).
+
+The library is the only compute path: if it is missing this module raises on
+first use; there is no CPU fallback.
+"""
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libscopyon_gb300.so")
+
+SC_OK, SC_ERR_ARG, SC_ERR_CUDA, SC_ERR_TIMEOUT, SC_ERR_NAN, SC_ERR_CAPACITY = 0, -1, -2, -3, -4, -5
+PSF_BORN_WOLF, PSF_GAUSSIAN = 0, 1
+CAM_EMCCD, CAM_CCD, CAM_CMOS_TABLE, CAM_SCMOS = 0, 1, 2, 3
+STEP_REC_BYTES = 48
+STATUS_WORDS = 4
+
+c_double_p = ctypes.c_void_p  # device pointers travel as integers
+
+
+class StepParams(ctypes.Structure):
+    _fields_ = [("px", ctypes.c_double), ("res", ctypes.c_double),
+                ("depth_cutoff", ctypes.c_double), ("focal", ctypes.c_double * 3),
+                ("nw", ctypes.c_int32), ("nh", ctypes.c_int32), ("n_signal", ctypes.c_int32),
+                ("n_sub", ctypes.c_int32), ("n_particles", ctypes.c_int32),
+                ("max_key", ctypes.c_int32),
+                ("amplitude0", ctypes.c_double), ("penetration", ctypes.c_double),
+                ("x_sec", ctypes.c_double), ("qy", ctypes.c_double), ("beer", ctypes.c_double),
+                ("norm_coeff", ctypes.c_double),
+                ("bleaching", ctypes.c_int32), ("with_optinfo", ctypes.c_int32)]
+
+
+class SplatParams(ctypes.Structure):
+    _fields_ = [("nw", ctypes.c_int32), ("nh", ctypes.c_int32), ("tile", ctypes.c_int32),
+                ("tiles_x", ctypes.c_int32), ("tiles_y", ctypes.c_int32),
+                ("n_r", ctypes.c_int32), ("sat_pitch", ctypes.c_int32),
+                ("n_images", ctypes.c_int32), ("rec_per_image", ctypes.c_int32),
+                ("px", ctypes.c_double), ("res", ctypes.c_double)]
+
+
+class CameraParams(ctypes.Structure):
+    _fields_ = [("nw", ctypes.c_int32), ("nh", ctypes.c_int32), ("camera", ctypes.c_int32),
+                ("exact", ctypes.c_int32), ("rounding", ctypes.c_int32), ("bit", ctypes.c_int32),
+                ("qe", ctypes.c_double), ("background", ctypes.c_double),
+                ("readout_noise", ctypes.c_double), ("emgain", ctypes.c_double),
+                ("fullwell", ctypes.c_double), ("offset0", ctypes.c_double),
+                ("gain0", ctypes.c_double), ("table_n", ctypes.c_int32),
+                ("seed", ctypes.c_uint64), ("counter", ctypes.c_uint64)]
+
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_SIG = {
+    "sc_get_version": (_I, []),
+    "sc_last_error": (ctypes.c_char_p, []),
+    "sc_psf_radial": (_I, [_I, _D, _D, _D, _P, _I, _I, _D, _P, _P]),
+    "sc_psf_quadrant_sat": (_I, [_P, _I, _I, _D, _P, _I, _P]),
+    "sc_emitter_steps": (_I, [ctypes.POINTER(StepParams), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sc_bin_workspace_bytes": (ctypes.c_size_t, [_I, _I]),
+    "sc_bin_capacity": (ctypes.c_int64, [_I, _D, _D, _I, _I]),
+    "sc_bin_steps": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P, _P,
+                          ctypes.c_int64, _P, _P]),
+    "sc_splat": (_I, [_P, _P, _P, _P, ctypes.POINTER(SplatParams), _P, _P, _P]),
+    "sc_camera": (_I, [ctypes.POINTER(CameraParams), _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                       _P, _P, _P, _P, _P]),
+    "sc_emccd_exact": (_I, [_P, _D, _D, _P, _I, _D, _P, _P, _P]),
+}
+
+
+class ScopyonGPUError(RuntimeError):
+    """A library call failed; ``code`` is the SC_ERR_* value."""
+
+    def __init__(self, code, message):
+        super().__init__(message)
+        self.code = code
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def declared_symbols():
+    return sorted(_SIG)
+
+
+def load():
+    """Load the library (once) and attach prototypes; raise if it is not built."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                "libscopyon_gb300.so is not built (%s); run "
+                "`python -c 'import __graft_entry__ as g; g.build()'` first" % LIB_PATH)
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIG.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(rc, what=""):
+    """Map a library return code to an exception."""
+    if rc == SC_OK:
+        return
+    msg = load().sc_last_error().decode(errors="replace")
+    text = "%s failed (%d): %s" % (what or "scopyon_gb300", rc, msg)
+    if rc == SC_ERR_ARG:
+        raise ValueError(text)
+    if rc == SC_ERR_TIMEOUT:
+        raise TimeoutError(text)
+    if rc == SC_ERR_NAN:
+        raise ValueError(text)
+    raise ScopyonGPUError(rc, text)
+
+
+def call(name, *args):
+    rc = getattr(load(), name)(*args)
+    check(rc, name)
+    return rc
+
+
+def ptr(t):
+    """Device address of a torch tensor (None -> NULL)."""
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)

@@ -1,0 +1,277 @@
+"""Public API, a drop-in for ``scopyon.form_image`` / ``scopyon.generate_images``.
+
+Signatures, input layouts, return values and errors follow the reference
+(src/scopyon/base.py:28-294).  Extensions, all keyword-only and optional:
+``device`` (CUDA device), ``draws`` (an ``InjectedDraws`` replacing the
+camera / bleaching random draws, the reference-parity mode).
+
+Random numbers: the caller's ``rng`` (a numpy RandomState) supplies, in the
+reference's order, the fixed-pattern-noise offsets and the photobleaching
+budgets; the camera noise of each frame comes from on-device Philox streams
+keyed by one 64-bit seed drawn from ``rng`` per frame.  Pixel statistics
+match the reference's models; the individual draws differ unless ``draws``
+is given.
+"""
+
+import collections.abc
+import numbers
+import warnings
+
+import numpy
+
+from . import config as _config
+from .epifm import EngineConfig, FramePipeline, InjectedDraws, PSFTables, frame_windows
+from .image import Image
+
+__all__ = ["EPIFMSimulator", "create_simulator", "form_image", "generate_images",
+           "EnvironSettings", "InjectedDraws"]
+
+
+class EnvironSettings:
+    """``environ`` sub-tree (reference base.py:20-26); ``processes`` is accepted and unused."""
+
+    def __init__(self, config):
+        self.processes = config.processes
+
+
+def _as_config(config):
+    if config is None:
+        return _config.DefaultConfiguration()
+    if isinstance(config, str):
+        return _config.Configuration(filename=config)
+    if isinstance(config, _config.Configuration):
+        return config
+    if hasattr(config, "yaml") and isinstance(getattr(config, "yaml"), dict):
+        return _config.Configuration.from_reference(config)
+    raise TypeError("Configuration or str must be given [{}].".format(type(config)))
+
+
+# PSF tables and device buffers survive across calls with the same optics
+_PSF_CACHE = {}
+
+
+def _psf_for(cfg, device):
+    key = (str(device), cfg.fluorophore_type, float(cfg.psf_wavelength), cfg.na,
+           float(cfg.radial_width or 0.0), float(cfg.radial_cutoff), float(cfg.depth_cutoff))
+    tables = _PSF_CACHE.get(key)
+    if tables is None:
+        tables = _PSF_CACHE[key] = PSFTables(cfg, device)
+    return tables
+
+
+class EPIFMSimulator:
+
+    def __init__(self, config=None, method=None, rng=None, device=None):
+        config = _as_config(config)
+        if rng is None:
+            warnings.warn("A random number generator is not given.")
+            rng = numpy.random.RandomState()
+        self.__config = config
+        self.__method = (method or config.get("method", "default")).lower()
+        self.__rng = rng
+        self.__device = device or "cuda"
+
+    @property
+    def config(self):
+        return self.__config
+
+    @property
+    def method(self):
+        return self.__method
+
+    def base(self):
+        """Engine configuration of the method sub-tree (draws FPN offsets from rng)."""
+        return EngineConfig(self.__config[self.__method], rng=self.__rng)
+
+    def _format_data(self, inputs):
+        """Columns -> [depth, x, y, m_id, p_state] (reference base.py:61-110)."""
+        if not isinstance(inputs, numpy.ndarray):
+            raise TypeError("a numpy.ndarray is expected")
+        if inputs.ndim != 2:
+            raise ValueError("The given 'inputs' has wrong dimension.")
+        pre = self.__config.preprocessing
+        k = inputs.shape[1]
+        n = inputs.shape[0]
+        if k == 2:
+            data = numpy.hstack((numpy.zeros((n, 1)), inputs * pre.scale))
+            data = numpy.hstack((data, numpy.zeros((n, 2))))
+            data[:, 3] = numpy.arange(n)
+            data[:, 4] = 1.0
+        elif k in (3, 5):
+            origin = numpy.array(pre.origin)
+            pos = inputs[:, :3] * pre.scale - origin
+            unit_z = numpy.cross(pre.unit_x, pre.unit_y)
+            data = numpy.hstack((numpy.dot(pos, unit_z).reshape((-1, 1)),
+                                 numpy.dot(pos, pre.unit_x).reshape((-1, 1)),
+                                 numpy.dot(pos, pre.unit_y).reshape((-1, 1))))
+            if k == 3:
+                data = numpy.hstack((data, numpy.zeros((n, 2))))
+                data[:, 3] = numpy.arange(n)
+                data[:, 4] = 1.0
+            else:
+                data = numpy.hstack((data, inputs[:, 3:]))
+        elif k == 4:
+            data = numpy.hstack((numpy.zeros((n, 1)), inputs[:, :2] * pre.scale, inputs[:, 2:]))
+        else:
+            raise ValueError("The given 'inputs' has wrong shape.")
+        return data
+
+    def _format_inputs(self, inputs):
+        if isinstance(inputs, numpy.ndarray):
+            return ((0.0, self._format_data(inputs)),)
+        if isinstance(inputs, collections.abc.Iterable):
+            data = []
+            for elem in inputs:
+                if not (isinstance(elem, (tuple, list)) and len(elem) == 2
+                        and isinstance(elem[0], numbers.Real) and isinstance(elem[1], numpy.ndarray)):
+                    raise ValueError("The given 'inputs' has wrong type.")
+                data.append((elem[0], self._format_data(elem[1])))
+            return data
+        raise TypeError("Invalid argument was given [{}]. A ndarray is expected.".format(type(inputs)))
+
+    def form_image(self, inputs, start_time=0.0, exposure_time=None, full_output=False, *,
+                   draws=None):
+        """Form one image; returns ``Image`` or ``(Image, infodict)`` like scopyon."""
+        data = self._format_inputs(inputs)
+        cfg = self.base()
+        img, info = next(_Frames(self, cfg, data, 1, start_time, exposure_time, False, draws))
+        if full_output:
+            return img, info
+        return img
+
+    def generate_images(self, inputs, num_frames, start_time=0.0, exposure_time=None,
+                        full_output=False, *, draws=None):
+        """Yield ``num_frames`` images (with infodicts if ``full_output``)."""
+        data = self._format_inputs(inputs)
+        cfg = self.base()
+        for img, info in _Frames(self, cfg, data, num_frames, start_time, exposure_time,
+                                 cfg.bleaching, draws):
+            yield (img, info) if full_output else img
+
+    # access for _Frames
+    def _rng(self):
+        return self.__rng
+
+    def _device(self):
+        return self.__device
+
+
+def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, draws):
+    """Frame generator: host bookkeeping around FramePipeline.run_frame."""
+    import torch
+    rng = sim._rng()
+    device = torch.device(sim._device())
+    pipe = FramePipeline(cfg, device, psf=_psf_for(cfg, device))
+    exposure = exposure_time or cfg.exposure_time
+    times = numpy.array([t for t, _ in data])
+    shutter = (cfg.shutter_start, cfg.shutter_end) if cfg.shutter_switch else None
+    slots = {}
+    slot_ids = []
+    slot_arr = numpy.zeros(0, dtype=numpy.int64)
+    beta = cfg.half_life / numpy.log(2.0) if bleaching else None
+    focal0 = cfg.focal_point[0]
+    nw, nh = cfg.image_size
+    for f in range(num_frames):
+        windows, exp_eff = frame_windows(times, len(data), start_time, exposure, f, shutter)
+        arrays = [data[i][1] for i, _ in windows]
+        uts = numpy.array([ut for _, ut in windows], dtype=float)
+        new_ids = []
+        id_cols = [a[:, 3].astype(numpy.int64) for a in arrays]
+        same = len(arrays) > 0 and all(ids.shape == id_cols[0].shape and numpy.array_equal(ids, id_cols[0])
+                                       for ids in id_cols)
+        known = same and slot_arr.shape == id_cols[0].shape and numpy.array_equal(slot_arr, id_cols[0])
+        if not known:
+            for ids in (id_cols[:1] if same else id_cols):
+                for m in ids.tolist():
+                    if m not in slots:
+                        slots[m] = len(slots)
+                        slot_ids.append(m)
+                        new_ids.append(m)
+            slot_arr = numpy.array(slot_ids, dtype=numpy.int64)
+        n_slots = len(slots)
+        pipe.ensure_slots(n_slots)
+        if bleaching and new_ids:
+            times_b = numpy.empty(len(new_ids))
+            todo = [k for k, m in enumerate(new_ids) if not (draws and m in draws.bleach)]
+            if todo:
+                times_b[todo] = rng.exponential(scale=beta, size=len(todo))
+            for k, m in enumerate(new_ids):
+                if draws and m in draws.bleach:
+                    times_b[k] = draws.bleach[m]
+            idx = torch.tensor([slots[m] for m in new_ids], dtype=torch.int64, device=device)
+            pipe.budget.index_copy_(0, idx, torch.from_numpy(times_b * cfg.n_emit0).to(device))
+        s_count = len(arrays)
+        present = None
+        if s_count == 0:
+            particles = numpy.zeros((0, n_slots, 5))
+        elif same and slot_arr.shape == id_cols[0].shape and numpy.array_equal(slot_arr, id_cols[0]):
+            particles = numpy.stack(arrays)
+        else:
+            particles = numpy.zeros((s_count, n_slots, 5))
+            present = numpy.zeros((s_count, n_slots), dtype=numpy.uint8)
+            for s_i, a in enumerate(arrays):
+                sl = numpy.array([slots[m] for m in id_cols[s_i].tolist()], dtype=numpy.int64)
+                particles[s_i, sl] = a
+                present[s_i, sl] = 1
+        if s_count:
+            pipe.psf.ensure(cfg.depth_keys(particles[:, :, 0].ravel() - focal0))
+        frame_draws = draws.next_frame() if draws is not None and draws.frames else None
+        seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | int(rng.randint(0, 2 ** 31 - 1)) \
+            if frame_draws is None else 0
+        expect, adc, opt = pipe.run_frame(particles, uts, with_optinfo=True, draws=frame_draws,
+                                          seed=seed, counter=f, present=present,
+                                          bleaching=bleaching)
+        pipe.check_status()
+        adc_np = adc.cpu().numpy().reshape(nw, nh).copy()
+        info = {"expectation": expect.cpu().numpy().astype(float).reshape(nw, nh)}
+        info["true_data"] = _true_data(cfg, opt, slots, id_cols, exp_eff, nw, nh)
+        if bleaching:
+            b = pipe.budget[:n_slots].cpu().numpy()
+            info["fluorescence_states"] = {m: float(b[slots[m]]) for m in slot_ids}
+        yield Image(adc_np), info
+
+
+def _true_data(cfg, opt, slots, id_cols, exposure, nw, nh):
+    """Per-molecule 8-vectors of the frame (_epifm.py:1207-1216, :1322-1333)."""
+    if opt is None or not id_cols:
+        return {}
+    seen = []
+    mark = set()
+    for ids in id_cols:
+        for m in ids.tolist():
+            if m not in mark:
+                mark.add(m)
+                seen.append(m)
+    o = opt.cpu().numpy()[[slots[m] for m in seen]].copy()
+    p0 = cfg.focal_point
+    px = cfg.px
+    o[:, 1] /= exposure
+    o[:, 2:6] /= o[:, 0:1]
+    o[:, 2] = (o[:, 2] - p0[1]) / px + (nw - 1) * 0.5
+    o[:, 3] = (o[:, 3] - p0[2]) / px + (nh - 1) * 0.5
+    return {m: o[k] for k, m in enumerate(seen)}
+
+
+def create_simulator(config=None, method=None, rng=None, device=None):
+    """Return a simulator for ``config[method].type`` (reference base.py:203-225)."""
+    config = _as_config(config)
+    method = (method or config.get("method", "default")).lower()
+    kind = str(config[method].type).lower()
+    if kind in ("epifm", "epifm_gpu"):
+        return EPIFMSimulator(config=config, method=method, rng=rng, device=device)
+    raise ValueError(f"An unknown type [{kind}] was given.")
+
+
+def form_image(inputs, start_time=0.0, exposure_time=None, *, method=None, config=None, rng=None,
+               full_output=False, device=None, draws=None):
+    """Form one image (reference base.py:227-258)."""
+    sim = create_simulator(config, method=method, rng=rng, device=device)
+    return sim.form_image(inputs, start_time, exposure_time, full_output=full_output, draws=draws)
+
+
+def generate_images(inputs, num_frames, start_time=0.0, exposure_time=None, *, method=None,
+                    config=None, rng=None, full_output=False, device=None, draws=None):
+    """Generate images frame by frame (reference base.py:260-294)."""
+    sim = create_simulator(config, method=method, rng=rng, device=device)
+    return sim.generate_images(inputs, num_frames, start_time, exposure_time,
+                               full_output=full_output, draws=draws)

@@ -1,0 +1,309 @@
+// Camera models and analog-to-digital conversion, one pass over the frame.
+//
+// Reference: _EPIFMSimulator.__detector_output and
+// __get_analog_to_digital_converter_counts (src/scopyon/_epifm.py:1430-1484),
+// with the detector classes EMCCD / CCD / CMOS (:329-433):
+//   expected = QE * (photons + background)
+//   EMCCD: signal ~ compound Poisson-Gamma (EM gain), noise ~ N(0, readout)
+//   CCD:   signal ~ Poisson(expected), noise ~ N(0, readout)
+//   CMOS:  signal ~ Poisson(expected), noise ~ tabulated distribution (additive)
+//   sCMOS (this engine only): noise ~ N(0, sigma_ij) with a per-pixel sigma map
+//   ADC = clip(min(signal + noise, fullwell) / gain + offset, 0, 2^bit - 1)
+// Draws come either from Philox4x32-10 (native, one counter stream per pixel)
+// or from caller arrays recorded from the reference (injected), in which case
+// the ADC arithmetic is the reference's FP64 sequence.
+#include "sc_common.cuh"
+
+namespace {
+
+struct CamConsts {
+    int n, camera, exact, rounding, table_n;
+    double qe, background, readout, emgain, fullwell, adc_max, offset0, gain0;
+    float qe_f, background_f, readout_f, emgain_f, fullwell_f, adc_max_f, offset0_f, inv_gain0_f;
+    uint64_t seed, counter;
+};
+
+// Poisson variate.  Small means: sequential inversion.  Large means: the
+// transformed rejection method PTRS (W. Hormann, "The transformed rejection
+// method for generating Poisson random variables", Insurance: Mathematics and
+// Economics 12 (1993) 39-45), with log(k!) from Stirling's series.
+__device__ float poisson(sc::rng_stream &rs, float lam, int32_t *status) {
+    if (!(lam > 0.f)) return 0.f;
+    if (lam < 12.f) {
+        const float u = rs.uniform();
+        float p = expf(-lam), s = p;
+        int k = 0;
+        while (u > s && k < 200) {
+            ++k;
+            p *= lam / (float)k;
+            s += p;
+        }
+        return (float)k;
+    }
+    const float slam = sqrtf(lam), loglam = logf(lam);
+    const float b = 0.931f + 2.53f * slam;
+    const float a = -0.059f + 0.02483f * b;
+    const float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
+    const float vr = 0.9277f - 3.6224f / (b - 2.f);
+    for (int it = 0; it < 64; ++it) {
+        const float U = rs.uniform() - 0.5f;
+        const float V = rs.uniform();
+        const float us = 0.5f - fabsf(U);
+        const float k = floorf((2.f * a / us + b) * U + lam + 0.43f);
+        if (us >= 0.07f && V <= vr) return k;
+        if (k < 0.f || (us < 0.013f && V > us)) continue;
+        // -lam + k log(lam) - log(k!) via Stirling, written relative to k - lam
+        const float kk = fmaxf(k, 1.f);
+        const float d = (k - lam) / lam;
+        const float lfact_rel = (k - lam) - k * log1pf(d) - 0.5f * logf(6.2831853f * kk) -
+                                1.f / (12.f * kk) + 1.f / (360.f * kk * kk * kk);
+        const float rhs = k == 0.f ? -lam : lfact_rel;
+        if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <= rhs) return k;
+    }
+    sc::flag_status(status, 3, 0, 0, 0);
+    return rintf(lam);
+}
+
+// Gamma(shape, 1) for shape >= 1: G. Marsaglia and W. W. Tsang, "A simple
+// method for generating gamma variables", ACM TOMS 26 (2000) 363-372.
+__device__ float gamma_ge1(sc::rng_stream &rs, float shape, int32_t *status) {
+    const float d = shape - 1.f / 3.f;
+    const float c = rsqrtf(9.f * d);
+    for (int it = 0; it < 64; ++it) {
+        const float x = rs.normal();
+        const float t = c * x;
+        if (t <= -1.f) continue;
+        const float u = rs.uniform();
+        const float vm1 = t * (3.f + t * (3.f + t));  // (1 + t)^3 - 1
+        const float x2 = x * x;
+        if (u < 1.f - 0.0331f * x2 * x2) return d * (1.f + vm1);
+        if (logf(u) < 0.5f * x2 + d * (3.f * log1pf(t) - vm1)) return d * (1.f + vm1);
+    }
+    sc::flag_status(status, 3, 1, 0, 0);
+    return shape;
+}
+
+__device__ __forceinline__ int table_index(const double *cdf, int n, double u) {
+    // searchsorted(cdf, u, side='right')
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cdf[mid] <= u) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < n ? lo : n - 1;
+}
+
+__global__ void camera_kernel(CamConsts c, const float *__restrict__ photons,
+                              const double *__restrict__ offset, const double *__restrict__ gain,
+                              const float *__restrict__ offset_f, const float *__restrict__ inv_gain_f,
+                              const float *__restrict__ sigma, const double *__restrict__ table_value,
+                              const double *__restrict__ table_cdf, const double *__restrict__ inj_noise,
+                              const double *__restrict__ inj_signal, const double *__restrict__ inj_uniform,
+                              float *__restrict__ expect, double *__restrict__ adc64,
+                              float *__restrict__ adc32, int32_t *status) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.n; p += stride) {
+        const double ph = (double)photons[p] + c.background;
+        const double e = c.qe * ph;
+        if (expect) expect[p] = (float)e;
+        if (c.exact) {
+            double noise, signal;
+            if (c.camera == SC_CAM_CMOS_TABLE && inj_uniform)
+                noise = table_value[table_index(table_cdf, c.table_n, inj_uniform[p])];
+            else
+                noise = inj_noise ? inj_noise[p] : 0.0;
+            signal = inj_signal ? inj_signal[p] : 0.0;
+            double v = signal + noise;
+            if (v > c.fullwell) v = c.fullwell;
+            v /= gain ? gain[p] : c.gain0;
+            v += offset ? offset[p] : c.offset0;
+            if (v > c.adc_max) v = c.adc_max;
+            if (v < 0) v = 0;
+            if (c.rounding) v = rint(v);
+            if (adc64) adc64[p] = v;
+            if (adc32) adc32[p] = (float)v;
+            continue;
+        }
+        sc::rng_stream rs(c.seed, (uint32_t)p, (uint32_t)c.counter, (uint32_t)(c.counter >> 32));
+        const float ef = (float)e;
+        float signal, noise;
+        switch (c.camera) {
+            case SC_CAM_EMCCD: {
+                const float n_in = poisson(rs, ef, status);
+                signal = n_in > 0.f ? rintf(c.emgain_f * gamma_ge1(rs, n_in, status)) : 0.f;
+                noise = c.readout_f > 0.f ? c.readout_f * rs.normal() : 0.f;
+                break;
+            }
+            case SC_CAM_CCD:
+                signal = poisson(rs, ef, status);
+                noise = c.readout_f > 0.f ? c.readout_f * rs.normal() : 0.f;
+                break;
+            case SC_CAM_CMOS_TABLE:
+                noise = (float)table_value[table_index(table_cdf, c.table_n, rs.uniform_d())];
+                signal = poisson(rs, ef, status);
+                break;
+            default:  // SC_CAM_SCMOS
+                signal = poisson(rs, ef, status);
+                noise = (sigma ? sigma[p] : c.readout_f) * rs.normal();
+                break;
+        }
+        float v = fminf(signal + noise, c.fullwell_f);
+        v = v * (inv_gain_f ? inv_gain_f[p] : c.inv_gain0_f) + (offset_f ? offset_f[p] : c.offset0_f);
+        v = fminf(fmaxf(v, 0.f), c.adc_max_f);
+        if (c.rounding) v = rintf(v);
+        if (adc32) adc32[p] = v;
+        if (adc64) adc64[p] = (double)v;
+    }
+}
+
+// ---------------------------------------------------------------- exact EMCCD
+// i1e(y) = I1(y) exp(-y).  CUDA's cyl_bessel_i1 is finite below ~710; above
+// 600 the asymptotic expansion (Abramowitz & Stegun 9.7.1, nu = 1) is used.
+__device__ double i1e_d(double y) {
+    if (y < 600.0) return cyl_bessel_i1(y) * exp(-y);
+    const double mu = 4.0;
+    double term = 1.0, sum = 1.0;
+    for (int k = 1; k <= 10; ++k) {
+        const double odd = (double)(2 * k - 1);
+        term *= -(mu - odd * odd) / ((double)k * 8.0 * y);
+        sum += term;
+    }
+    return sum / sqrt(2.0 * M_PI * y);
+}
+
+// One warp per pixel: support [s_min, s_max), weights p(S) with the exponent
+// shifted by E (the continuous maximum, so nothing overflows), total, then
+// the first S whose cumulative weight exceeds u * total.
+__global__ void emccd_exact_kernel(const float *photons, double qe, double background,
+                                   const double *uniform, int n, double g, double *signal,
+                                   int32_t *status) {
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < n; p += warps) {
+        const double e = qe * ((double)photons[p] + background);
+        if (!(e > 0.0)) {
+            if (lane == 0) signal[p] = 0.0;
+            continue;
+        }
+        const double sig = sqrt(e) * 5 + 10;
+        const double smin_d = fmax(0.0, g * trunc(e - sig));
+        const double smax_d = g * trunc(e + sig);
+        const int64_t s_min = (int64_t)smin_d, count = (int64_t)smax_d - s_min;
+        if (count <= 0) {
+            if (lane == 0) {
+                signal[p] = 0.0;
+                sc::flag_status(status, 2, p, 0, 0);
+            }
+            continue;
+        }
+        const double a = 1.0 / g;
+        auto weight = [&](int64_t idx) -> double {
+            const double S = (double)(s_min + idx);
+            if (S <= 0.0) return 1.0 / (2 * a * e) * exp(-e);
+            const double X = a * S;
+            const double Y = 2 * sqrt(e * X);
+            return 1.0 / Y * exp(-X + Y - e) * i1e_d(Y);
+        };
+        double total = 0.0;
+        for (int64_t base = 0; base < count; base += 32) {
+            const int64_t idx = base + lane;
+            double w = idx < count ? weight(idx) : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+            total += w;
+        }
+        const double target = uniform[p] * total;
+        double run = 0.0;
+        int64_t found = count - 1;
+        for (int64_t base = 0; base < count; base += 32) {
+            const int64_t idx = base + lane;
+            double w = idx < count ? weight(idx) : 0.0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double nb = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += nb;
+            }
+            const unsigned hit = __ballot_sync(0xffffffffu, idx < count && run + w > target);
+            if (hit) {
+                found = base + (__ffs(hit) - 1);
+                break;
+            }
+            run += __shfl_sync(0xffffffffu, w, 31);
+        }
+        if (lane == 0) signal[p] = (double)(s_min + found);
+    }
+}
+
+}  // namespace
+
+extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const double *d_offset,
+                         const double *d_gain, const float *d_offset_f, const float *d_inv_gain_f,
+                         const float *d_sigma, const double *d_table_value,
+                         const double *d_table_cdf, const double *d_inj_noise,
+                         const double *d_inj_signal, const double *d_inj_uniform, float *d_expect,
+                         double *d_adc64, float *d_adc32, int32_t *d_status, void *stream) {
+    SC_REQUIRE(p != nullptr, "sc_camera: params are NULL");
+    SC_REQUIRE(p->nw > 0 && p->nh > 0, "sc_camera: image %dx%d", p->nw, p->nh);
+    SC_REQUIRE(p->camera >= SC_CAM_EMCCD && p->camera <= SC_CAM_SCMOS, "sc_camera: camera %d",
+               p->camera);
+    SC_REQUIRE(p->bit > 0 && p->bit <= 32, "sc_camera: bit=%d", p->bit);
+    SC_REQUIRE(d_photons != nullptr && (d_adc64 || d_adc32), "sc_camera: NULL input/output");
+    if (p->camera == SC_CAM_CMOS_TABLE)
+        SC_REQUIRE(p->table_n > 0 && d_table_value && d_table_cdf,
+                   "sc_camera: CMOS table mode needs the noise table");
+    if (p->exact) {
+        SC_REQUIRE(d_inj_signal != nullptr, "sc_camera: exact mode needs injected signal");
+        SC_REQUIRE(p->camera == SC_CAM_CMOS_TABLE ? (d_inj_uniform || d_inj_noise) : true,
+                   "sc_camera: CMOS exact mode needs injected uniforms or noise");
+    }
+    CamConsts c;
+    c.n = p->nw * p->nh;
+    c.camera = p->camera;
+    c.exact = p->exact;
+    c.rounding = p->rounding;
+    c.table_n = p->table_n;
+    c.qe = p->qe;
+    c.background = p->background;
+    c.readout = p->readout_noise;
+    c.emgain = p->emgain;
+    c.fullwell = p->fullwell;
+    c.adc_max = (double)((1ull << p->bit) - 1);
+    c.offset0 = p->offset0;
+    c.gain0 = p->gain0;
+    c.qe_f = (float)p->qe;
+    c.background_f = (float)p->background;
+    c.readout_f = (float)p->readout_noise;
+    c.emgain_f = (float)p->emgain;
+    c.fullwell_f = (float)p->fullwell;
+    c.adc_max_f = (float)c.adc_max;
+    c.offset0_f = (float)p->offset0;
+    c.inv_gain0_f = (float)(1.0 / p->gain0);
+    c.seed = p->seed;
+    c.counter = p->counter;
+    const int block = 256;
+    int grid = (c.n + block - 1) / block;
+    if (grid > 152 * 16) grid = 152 * 16;
+    camera_kernel<<<grid, block, 0, sc::as_stream(stream)>>>(
+        c, d_photons, d_offset, d_gain, d_offset_f, d_inv_gain_f, d_sigma, d_table_value,
+        d_table_cdf, d_inj_noise, d_inj_signal, d_inj_uniform, d_expect, d_adc64, d_adc32,
+        d_status);
+    return sc::launch_status("sc_camera");
+}
+
+extern "C" int sc_emccd_exact(const float *d_photons, double qe, double background,
+                              const double *d_uniform, int n_pixels, double emgain,
+                              double *d_signal, int32_t *d_status, void *stream) {
+    SC_REQUIRE(n_pixels >= 0, "sc_emccd_exact: n_pixels=%d", n_pixels);
+    SC_REQUIRE(emgain >= 1 && emgain == floor(emgain),
+               "sc_emccd_exact: emgain must be a positive integer (got %g)", emgain);
+    if (n_pixels == 0) return SC_OK;
+    SC_REQUIRE(d_photons && d_uniform && d_signal, "sc_emccd_exact: NULL pointer");
+    const int block = 256;
+    int grid = (n_pixels * 32 + block - 1) / block;
+    if (grid > 152 * 8) grid = 152 * 8;
+    emccd_exact_kernel<<<grid, block, 0, sc::as_stream(stream)>>>(d_photons, qe, background,
+                                                                  d_uniform, n_pixels, emgain,
+                                                                  d_signal, d_status);
+    return sc::launch_status("sc_emccd_exact");
+}

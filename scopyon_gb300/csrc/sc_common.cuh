@@ -1,0 +1,135 @@
+// Shared device helpers for the scopyon_gb300 kernels: error reporting,
+// double-float (hi + lo FP32 pair) arithmetic, and the Philox4x32-10
+// counter-based generator (Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC'11).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+
+#include "../../include/scopyon_gb300.h"
+
+namespace sc {
+
+// ------------------------------------------------------------------ errors
+void set_error(const char *fmt, ...);
+int cuda_status(cudaError_t err, const char *what);
+int launch_status(const char *what);
+
+#define SC_REQUIRE(cond, ...)            \
+    do {                                 \
+        if (!(cond)) {                   \
+            ::sc::set_error(__VA_ARGS__); \
+            return SC_ERR_ARG;           \
+        }                                \
+    } while (0)
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// status word helpers (device): first error wins the index slots
+__device__ __forceinline__ void flag_status(int32_t *status, int bit, int a, int b, int c) {
+    if (status == nullptr) return;
+    int old = atomicOr(status, 1 << bit);
+    if (old == 0) {
+        status[1] = a;
+        status[2] = b;
+        status[3] = c;
+    }
+}
+
+// ------------------------------------------------------------ double-float
+// A value v is held as hi + lo with hi = fl32(v) and lo = fl32(v - hi).
+struct df {
+    float hi, lo;
+};
+
+// Error-free sum of two floats (Knuth TwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// acc += sign * (hi + lo), keeping acc as an unnormalised (s, e) pair.
+__device__ __forceinline__ void df_acc(float &s, float &e, float hi, float lo, float sign) {
+    float t, err;
+    two_sum(s, sign * hi, t, err);
+    s = t;
+    e += err + sign * lo;
+}
+
+// ------------------------------------------------------------------ Philox
+struct u4 {
+    uint32_t x, y, z, w;
+};
+
+__device__ __forceinline__ u4 philox4x32_10(u4 ctr, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
+        uint32_t hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
+        u4 n;
+        n.x = hi1 ^ ctr.y ^ k0;
+        n.y = lo1;
+        n.z = hi0 ^ ctr.w ^ k1;
+        n.w = lo0;
+        ctr = n;
+        k0 += W0;
+        k1 += W1;
+    }
+    return ctr;
+}
+
+// uniform in (0, 1) from 32 bits
+__device__ __forceinline__ float u01f(uint32_t x) {
+    return (float)(x >> 8) * (1.0f / 16777216.0f) + (0.5f / 16777216.0f);
+}
+
+// uniform in (0, 1) from 64 bits, double precision
+__device__ __forceinline__ double u01d(uint32_t a, uint32_t b) {
+    uint64_t v = ((uint64_t)a << 21) ^ (uint64_t)(b >> 11);
+    return ((double)(v & ((1ull << 53) - 1)) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+// A stream of Philox outputs for one (key, counter) pair: counter.w advances.
+struct rng_stream {
+    uint32_t k0, k1;
+    u4 ctr;
+    u4 buf;
+    int left;
+    __device__ rng_stream(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2)
+        : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), left(0) {
+        ctr.x = c0;
+        ctr.y = c1;
+        ctr.z = c2;
+        ctr.w = 0;
+    }
+    __device__ uint32_t next() {
+        if (left == 0) {
+            buf = philox4x32_10(ctr, k0, k1);
+            ctr.w += 1;
+            left = 4;
+        }
+        uint32_t v = left == 4 ? buf.x : left == 3 ? buf.y : left == 2 ? buf.z : buf.w;
+        --left;
+        return v;
+    }
+    __device__ float uniform() { return u01f(next()); }
+    __device__ double uniform_d() {
+        uint32_t a = next();
+        return u01d(a, next());
+    }
+    // standard normal, Box-Muller on two uniforms
+    __device__ float normal() {
+        float u1 = uniform(), u2 = uniform();
+        float r = sqrtf(-2.0f * logf(u1));
+        float s, c;
+        sincospif(2.0f * u2, &s, &c);
+        return r * c;
+    }
+};
+
+}  // namespace sc

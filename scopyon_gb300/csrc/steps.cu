@@ -1,0 +1,129 @@
+// Emitter physics per particle and exposure sub-step -> splat records.
+//
+// One thread owns one particle slot and walks the frame's sub-steps in order,
+// so the photon budget (bleaching) and the true_data sums are accumulated in
+// exactly the reference's sequence:
+//   amplitude  = amplitude0 * exp(-|depth| / penetration)     _epifm.py:1281-1289
+//   n_emit     = QY * (amplitude * x_sec * dt) * (1 - 10^-A)   _epifm.py:1344-1360
+//   budget    -= n_emit; <= 0 -> p_state = 0                   _epifm.py:1294-1306
+//   norm       = norm_coeff * (p_state * n_emit / 4 pi)        _epifm.py:1309-1315
+//   depth key  = int(|depth| / res) or -1 past the cutoff      _epifm.py:76-88
+//   footprint  = pixel range and grid origin along x and y    _epifm.py:224-258
+// All of it is FP64 (a few dozen flops per record) so that keys, footprint
+// bounds and bleaching decisions are the reference's.
+#include "sc_common.cuh"
+#include "steps.cuh"
+
+namespace {
+
+__global__ void emitter_steps_kernel(sc::StepConsts c, const double *particles,
+                                     const double *unit_time, const uint8_t *present,
+                                     const int32_t *key_slot, double *budget, double *optinfo,
+                                     ScStepRec *recs, int32_t *status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c.n_particles) return;
+    double b = c.bleaching ? budget[i] : 0.0;
+    double acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = 0.0;
+    for (int s = 0; s < c.n_sub; ++s) {
+        const double *q = particles + ((size_t)s * c.n_particles + i) * 5;
+        ScStepRec *out = recs + (size_t)s * c.n_particles + i;
+        if (present && !present[(size_t)s * c.n_particles + i]) {
+            out->n_i = out->n_j = 0;  // absent at this sub-step: no record, no state change
+            continue;
+        }
+        const double ut = unit_time[s];
+        double p_state = q[4];
+        const double rel0 = q[0] - c.focal[0];
+        const double rel1 = q[1] - c.focal[1];
+        const double rel2 = q[2] - c.focal[2];
+        const double amp = c.amplitude0 * exp(-fabs(rel0) / c.penetration);
+        const double n_emit = sc::emit_photons(c, amp, ut);
+        if (c.bleaching) {
+            double nb = b - n_emit;
+            if (nb <= 0) {
+                nb = 0;
+                p_state = 0.0;
+            }
+            b = nb;
+        }
+        const double norm = c.norm_coeff * (p_state * n_emit / (4.0 * M_PI));
+        ScStepRec rec;
+        sc::make_record(c, rel0, rel1, rel2, norm, key_slot, status, i, s, rec);
+        *out = rec;
+        if (c.with_optinfo) {
+            acc[0] += ut;
+            acc[1] += ut * p_state;
+            acc[2] += ut * q[1];
+            acc[3] += ut * q[2];
+            acc[4] += ut * q[1];
+            acc[5] += ut * q[2];
+            acc[6] += ut * rel0;
+            acc[7] += norm;
+        }
+    }
+    if (c.bleaching) budget[i] = b;
+    if (c.with_optinfo) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) optinfo[(size_t)i * 8 + k] = acc[k];
+    }
+}
+
+}  // namespace
+
+namespace sc {
+
+int step_consts(const ScStepParams *p, StepConsts &c) {
+    SC_REQUIRE(p != nullptr, "step params are NULL");
+    SC_REQUIRE(p->px > 0 && p->res > 0, "px and res must be positive");
+    SC_REQUIRE(p->nw > 0 && p->nh > 0 && p->nw < 32767 && p->nh < 32767,
+               "image size %dx%d out of range", p->nw, p->nh);
+    SC_REQUIRE(p->n_signal >= 3, "n_signal=%d too small", p->n_signal);
+    SC_REQUIRE(p->max_key >= 0, "max_key=%d", p->max_key);
+    SC_REQUIRE(p->n_particles >= 0 && p->n_sub >= 0, "negative sizes");
+    c.px = p->px;
+    c.res = p->res;
+    c.depth_cutoff = p->depth_cutoff;
+    for (int k = 0; k < 3; ++k) c.focal[k] = p->focal[k];
+    c.nw = p->nw;
+    c.nh = p->nh;
+    c.n_signal = p->n_signal;
+    c.n_sub = p->n_sub;
+    c.n_particles = p->n_particles;
+    c.max_key = p->max_key;
+    c.amplitude0 = p->amplitude0;
+    c.penetration = p->penetration;
+    c.x_sec = p->x_sec;
+    c.qy = p->qy;
+    c.beer = p->beer;
+    c.norm_coeff = p->norm_coeff;
+    c.bleaching = p->bleaching;
+    c.with_optinfo = p->with_optinfo;
+    c.half_w = (double)p->nw * p->px * 0.5;
+    c.half_h = (double)p->nh * p->px * 0.5;
+    c.half_sig = p->res * (double)(p->n_signal - 1) * 0.5;
+    c.inv_res_hi = 0.0;
+    return SC_OK;
+}
+
+}  // namespace sc
+
+extern "C" int sc_emitter_steps(const ScStepParams *p, const double *d_particles,
+                                const double *d_unit_time, const uint8_t *d_present,
+                                const int32_t *d_key_slot,
+                                double *d_budget, double *d_optinfo, ScStepRec *d_recs,
+                                int32_t *d_status, void *stream) {
+    sc::StepConsts c;
+    int rc = sc::step_consts(p, c);
+    if (rc) return rc;
+    if (c.n_particles == 0 || c.n_sub == 0) return SC_OK;
+    SC_REQUIRE(d_particles && d_unit_time && d_key_slot && d_recs,
+               "sc_emitter_steps: NULL input/output pointer");
+    SC_REQUIRE(!c.bleaching || d_budget, "sc_emitter_steps: bleaching needs a budget array");
+    SC_REQUIRE(!c.with_optinfo || d_optinfo, "sc_emitter_steps: optinfo output is NULL");
+    const int block = 128;
+    emitter_steps_kernel<<<(c.n_particles + block - 1) / block, block, 0, sc::as_stream(stream)>>>(
+        c, d_particles, d_unit_time, d_present, d_key_slot, d_budget, d_optinfo, d_recs, d_status);
+    return sc::launch_status("sc_emitter_steps");
+}

@@ -1,0 +1,98 @@
+// Per-record emitter physics shared by the trajectory-driven and the
+// on-device-diffusion step kernels.
+#pragma once
+
+#include "sc_common.cuh"
+
+namespace sc {
+
+struct StepConsts {
+    double px, res, depth_cutoff;
+    double focal[3];
+    int nw, nh, n_signal, n_sub, n_particles, max_key;
+    double amplitude0, penetration, x_sec, qy, beer, norm_coeff;
+    int bleaching, with_optinfo;
+    double half_w, half_h, half_sig, inv_res_hi;
+};
+
+int step_consts(const ScStepParams *p, StepConsts &c);
+
+// n_emit = QY * (amplitude * x_sec * dt) * (1 - 10^-A)   (_epifm.py:1344-1360)
+__device__ __forceinline__ double emit_photons(const StepConsts &c, double amplitude, double dt) {
+    const double n_abs = amplitude * c.x_sec * dt;
+    return c.qy * n_abs * c.beer;
+}
+
+// Footprint of one axis (_epifm.py:233-258): first pixel, number of bounds,
+// the exact FP64 origin and the first bound's unrounded value as a double-float.
+__device__ __forceinline__ void axis_footprint(double half_len, double coord, double half_sig,
+                                               double px, double res, int n_pix, double &origin,
+                                               int16_t &start, int16_t &count, float &a_hi,
+                                               float &a_lo) {
+    origin = (half_len + coord) - half_sig;
+    const double lo = floor(origin / px);
+    const double hi = ceil(((half_len + coord) + half_sig) / px);
+    const double lo_c = fmax(lo, 0.0);
+    const double hi_c = fmin(hi, (double)n_pix);
+    start = 0;
+    count = 0;
+    a_hi = a_lo = 0.f;
+    if (!(hi_c >= lo_c)) return;
+    const int i0 = (int)lo_c;
+    const int n = (int)hi_c - i0 + 1;
+    start = (int16_t)i0;
+    count = (int16_t)n;
+    const double a = ((double)i0 * px - origin) / res;
+    a_hi = (float)a;
+    a_lo = (float)(a - (double)a_hi);
+}
+
+__device__ __forceinline__ void make_record(const StepConsts &c, double rel0, double rel1,
+                                            double rel2, double norm, const int32_t *key_slot,
+                                            int32_t *status, int i, int s, ScStepRec &rec) {
+    rec.x0 = rec.y0 = 0.0;
+    rec.ax_hi = rec.ax_lo = rec.ay_hi = rec.ay_lo = 0.f;
+    rec.i_start = rec.j_start = 0;
+    rec.n_i = rec.n_j = 0;
+    rec.slot = -1;
+    rec.w = 0.f;
+    if (norm <= 0.0) return;  // overlay_signal returns early (_epifm.py:216-217)
+    const double depth = fabs(rel0);
+    int key;
+    if (depth < c.depth_cutoff + c.res) {
+        const double kd = depth / c.res;
+        if (kd > (double)c.max_key) {
+            flag_status(status, 0, i, s, 0);
+            return;
+        }
+        key = (int)kd;
+    } else {
+        key = -1;
+    }
+    const int idx = key >= 0 ? key : c.max_key + 1;
+    const int slot = key_slot[idx];
+    if (slot < 0) {
+        flag_status(status, 1, i, s, key);
+        return;
+    }
+    int16_t si, ni, sj, nj;
+    float axh, axl, ayh, ayl;
+    double x0, y0;
+    axis_footprint(c.half_w, rel1, c.half_sig, c.px, c.res, c.nw, x0, si, ni, axh, axl);
+    axis_footprint(c.half_h, rel2, c.half_sig, c.px, c.res, c.nh, y0, sj, nj, ayh, ayl);
+    if (ni < 2 || nj < 2) return;
+    rec.x0 = x0;
+    rec.y0 = y0;
+    rec.ax_hi = axh;
+    rec.ax_lo = axl;
+    rec.ay_hi = ayh;
+    rec.ay_lo = ayl;
+    rec.i_start = si;
+    rec.n_i = ni;
+    rec.j_start = sj;
+    rec.n_j = nj;
+    rec.slot = slot;
+    rec.w = (float)(norm * (c.res * c.res));
+}
+
+}  // namespace sc

@@ -1,0 +1,494 @@
+"""Image-formation engine: configuration, PSF tables and the frame pipeline.
+
+Host code mirrors the reference's ``EPIFMConfigs`` / ``_EPIFMSimulator``
+(src/scopyon/_epifm.py:757-1225) for everything that is set-up or
+bookkeeping (frame windows, molecule ids, random draws taken from the caller's
+``rng``); every per-particle, per-pixel operation runs in the CUDA library.
+Device buffers are torch CUDA tensors, reused across frames.
+"""
+
+import math
+import warnings
+
+import numpy
+import torch
+
+from . import _catalog, _lib
+from ._lib import call, ptr, stream_ptr
+from .physics import absorption_terms, snells_law
+
+__all__ = ["EngineConfig", "PSFTables", "FramePipeline", "InjectedDraws", "frame_windows"]
+
+PSF_RES = 1e-9  # radial and depth resolution of the PSF tables (_epifm.py:61-62)
+
+
+def _gpu_opt(tree, key, default=None):
+    gpu = tree.get("gpu") if isinstance(tree, dict) else None
+    if not isinstance(gpu, dict):
+        return default
+    v = gpu.get(key, default)
+    return default if v is None else v
+
+
+class EngineConfig:
+    """Numbers of one method sub-tree (what ``EPIFMConfigs.initialize`` reads).
+
+    ``conf`` is a ``Configuration`` of the method sub-tree; ``rng`` is used only
+    for fixed-pattern-noise offsets, drawn exactly as the reference does
+    (``_epifm.py:926-963``).
+    """
+
+    def __init__(self, conf, rng=None):
+        if str(conf.type).lower() != "epifm":
+            raise ValueError("An invalid type [%s] was given. 'epifm' is required." % conf.type)
+        raw = conf.yaml
+        fl = conf.fluorophore
+        self.fluorophore_type = fl.type
+        self.radius = fl.radius
+        self.psf_normalization = fl.normalization
+        self.radial_width = fl.radial_width if "radial_width" in fl else None
+        self.radial_cutoff = fl.radial_cutoff
+        self.depth_cutoff = fl.depth_cutoff
+        min_wl, max_wl = fl.min_wave_length, fl.max_wave_length
+        fl_wl = fl.wave_length if "wave_length" in fl else None
+        self.psf_wavelength, fl_norm_sum = _catalog.psf_wavelength_and_norm(
+            self.fluorophore_type, min_wl, max_wl, fl_wl,
+            catalog_dir=_gpu_opt(raw, "catalog_dir"), override=_gpu_opt(raw, "psf_wavelength"))
+        if self.fluorophore_type == "Gaussian" and self.radial_width is None:
+            raise ValueError("fluorophore.radial_width must be given for Gaussian type fluorophore.")
+        self.na = float(_gpu_opt(raw, "NA", 1.4))
+
+        src = conf.light_source
+        self.source_wavelength = src.wave_length
+        self.flux_density = src.flux_density
+        self.angle = src.angle
+        self.amplitude0, self.penetration = snells_law(self.flux_density, self.source_wavelength,
+                                                       self.angle)
+        self.magnification = conf.magnification
+
+        det = conf.detector
+        self.detector_type = det.type
+        if self.detector_type not in ("EMCCD", "CCD", "CMOS"):
+            raise RuntimeError("Unknown detector type was given [%s]. Use either one of 'CMOS', "
+                               "'CCD' or 'EMCCD'." % self.detector_type)
+        self.image_size = tuple(int(v) for v in det.image_size)
+        self.pixel_length = det.pixel_length
+        self.exposure_time = det.exposure_time
+        self.focal_point = numpy.asarray(det.focal_point, dtype=float)
+        self.qe = det.QE
+        self.readout_noise = det.readout_noise
+        self.emgain = det.emgain
+
+        adc = conf.analog_to_digital_converter
+        self.bit = int(adc.bit)
+        self.fullwell = adc.fullwell
+        self.fpn_type, self.fpn_count = adc.type, adc.count
+        self.offset, self.gain = self._adc_maps(adc.offset, rng)
+
+        eff = conf.effects
+        self.background_switch = bool(eff.background.switch)
+        self.background_mean = eff.background.mean
+        self.qy = eff.fluorescence.quantum_yield
+        self.abs_coeff = eff.fluorescence.abs_coefficient
+        pb = eff.photo_bleaching
+        self.bleaching = bool(pb.switch)
+        self.half_life = pb.half_life
+        self.x_sec, self.beer = absorption_terms(self.abs_coeff, self.radius)
+        # photons per second at the unattenuated amplitude: the budget unit
+        self.n_emit0 = self.qy * (self.amplitude0 * self.x_sec * 1.0) * self.beer
+
+        sh = conf.shutter if "shutter" in conf else None
+        self.shutter_switch = bool(sh.switch) if sh is not None else False
+        self.shutter_start = sh.start_time if sh is not None else None
+        self.shutter_end = sh.end_time if sh is not None else None
+
+        norm = fl_norm_sum
+        for name in ("dichroic_mirror", "emission_filter"):
+            if name in conf and conf[name].switch:
+                warnings.warn("%s is on: the spectral efficiency is applied once per configuration "
+                              "(the reference compounds it per particle)" % name)
+                norm = self._filtered_norm(conf, name, min_wl, max_wl)
+        self.norm_coeff = norm * self.psf_normalization
+
+        self.cmos_noise = str(_gpu_opt(raw, "cmos_noise", "table"))
+        self.scmos_median = float(_gpu_opt(raw, "scmos_readout_median", 1.5))
+        self.scmos_sigma = float(_gpu_opt(raw, "scmos_readout_sigma", 0.4))
+        self.adc_rounding = str(_gpu_opt(raw, "adc_rounding", "none")) == "round"
+        self.boundary = str(_gpu_opt(raw, "boundary", "none"))
+        self.tile = int(_gpu_opt(raw, "tile", 0))
+        self.catalog_dir = _gpu_opt(raw, "catalog_dir")
+        table = _gpu_opt(raw, "cmos_table")
+        self.cmos_table = None if table is None else numpy.asarray(table, dtype=float)
+
+    @property
+    def px(self):
+        return self.pixel_length / self.magnification
+
+    def _adc_maps(self, offset0, rng):
+        nw, nh = self.image_size
+        if self.fpn_type == "none":
+            offset = numpy.full(nw * nh, offset0)
+        elif self.fpn_type == "pixel":
+            if rng is None:
+                raise RuntimeError("A random number generator is required.")
+            offset = numpy.rint(rng.normal(offset0, self.fpn_count, nw * nh))
+        elif self.fpn_type == "column":
+            if rng is None:
+                raise RuntimeError("A random number generator is required.")
+            column = rng.normal(offset0, self.fpn_count, nh)
+            offset = numpy.rint(numpy.tile(column, (1, nw)).reshape(nh * nw))
+        else:
+            raise ValueError("FPN type [%s] is invalid ['pixel', 'column' or 'none']"
+                             % self.fpn_type)
+        gain = (self.fullwell - 0.0) / (pow(2.0, self.bit) - offset)
+        return (numpy.asarray(offset, dtype=float).reshape(nw, nh),
+                numpy.asarray(gain, dtype=float).reshape(nw, nh))
+
+    def _filtered_norm(self, conf, name, min_wl, max_wl):
+        cdir = _catalog.find_catalog_dir(self.catalog_dir)
+        if cdir is None:
+            raise FileNotFoundError("%s needs the scopyon catalog (gpu.catalog_dir)" % name)
+        grid = numpy.arange(min_wl, max_wl, 1e-9, dtype=float)
+        sections = _catalog.read_catalog(
+            "%s/fluorophore/%s.csv" % (cdir, self.fluorophore_type))
+        em = _catalog._efficiency(sections["Emission"], grid)
+        em[int(em.argmax())] = 100
+        em /= sum(em)
+        sub = {"dichroic_mirror": "dichroic", "emission_filter": "emission"}[name]
+        spec = _catalog.read_catalog("%s/%s/%s.csv" % (cdir, sub, conf[name].type))["wavedataset"]
+        return float(numpy.sum(em * 0.01 * _catalog._efficiency(spec, grid)))
+
+    # -- PSF geometry ----------------------------------------------------
+    @property
+    def n_r(self):
+        return len(numpy.arange(0.0, self.radial_cutoff, PSF_RES, dtype=float))
+
+    @property
+    def max_key(self):
+        return int((self.depth_cutoff + PSF_RES) / PSF_RES) + 1
+
+    def depth_keys(self, depths):
+        """Depth keys of ``PointSpreadingFunction.get`` (_epifm.py:76-88), vectorised."""
+        d = numpy.abs(numpy.asarray(depths, dtype=float))
+        inside = d < self.depth_cutoff + PSF_RES
+        keys = numpy.full(d.shape, -1, dtype=numpy.int64)
+        keys[inside] = (d[inside] / PSF_RES).astype(numpy.int64)
+        return keys
+
+
+class PSFTables:
+    """Device cache of quadrant summed-area tables, one per 1-nm depth key."""
+
+    def __init__(self, cfg, device):
+        self.cfg = cfg
+        self.device = device
+        self.n_r = cfg.n_r
+        self.pitch = ((self.n_r + 1 + 3) // 4) * 4
+        self.table_floats = (self.n_r + 1) * self.pitch * 2
+        self.max_key = cfg.max_key
+        self.slot_of = {}
+        self.key_slot_host = numpy.full(self.max_key + 2, -1, dtype=numpy.int32)
+        self.key_slot = torch.full((self.max_key + 2,), -1, dtype=torch.int32, device=device)
+        self.tables = torch.empty(0, dtype=torch.float32, device=device)
+        self.capacity = 0
+
+    def _depth_of_key(self, key):
+        return self.cfg.depth_cutoff if key < 0 else key * PSF_RES
+
+    def _grow(self, need):
+        if need <= self.capacity:
+            return
+        cap = max(need, min(2 * self.capacity, self.max_key + 2), 1)
+        new = torch.empty(cap * self.table_floats, dtype=torch.float32, device=self.device)
+        if self.capacity:
+            new[: self.capacity * self.table_floats].copy_(self.tables)
+        self.tables, self.capacity = new, cap
+
+    def ensure(self, keys, stream=None):
+        """Build the tables of any keys not cached yet."""
+        keys = numpy.unique(numpy.asarray(keys, dtype=numpy.int64))
+        missing = [int(k) for k in keys if int(k) not in self.slot_of]
+        if not missing:
+            return
+        if any(k > self.max_key for k in missing):
+            raise ValueError("depth key beyond the table range")
+        self._grow(len(self.slot_of) + len(missing))
+        kind = _lib.PSF_GAUSSIAN if self.cfg.fluorophore_type == "Gaussian" else _lib.PSF_BORN_WOLF
+        sigma = float(self.cfg.radial_width or 0.0)
+        batch = 64
+        s = stream_ptr(stream)
+        for b0 in range(0, len(missing), batch):
+            chunk = missing[b0: b0 + batch]
+            depths = torch.tensor([self._depth_of_key(k) for k in chunk], dtype=torch.float64,
+                                  device=self.device)
+            radial = torch.empty((len(chunk), self.n_r), dtype=torch.float64, device=self.device)
+            call("sc_psf_radial", kind, float(self.cfg.psf_wavelength), self.cfg.na, sigma,
+                 ptr(depths), len(chunk), self.n_r, PSF_RES, ptr(radial), s)
+            first = len(self.slot_of)
+            out = self.tables[first * self.table_floats: (first + len(chunk)) * self.table_floats]
+            call("sc_psf_quadrant_sat", ptr(radial), len(chunk), self.n_r, PSF_RES, ptr(out),
+                 self.pitch, s)
+            for j, k in enumerate(chunk):
+                self.slot_of[k] = first + j
+                self.key_slot_host[k if k >= 0 else self.max_key + 1] = first + j
+        self.key_slot.copy_(torch.from_numpy(self.key_slot_host))
+
+    def ensure_all(self, stream=None):
+        self.ensure(list(range(0, self.max_key + 1)) + [-1], stream)
+
+
+class InjectedDraws:
+    """Random draws supplied by the caller instead of the engine's Philox streams.
+
+    ``bleach``: {m_id: bleaching time in seconds}, used at a molecule's first
+    sight in place of ``rng.exponential``.  ``frames``: one dict per frame with
+    ``noise`` (electrons, W x H) and ``signal`` (electrons, W x H), or for the
+    EMCCD exact draw ``uniform`` (W x H) instead of ``signal``, or for the
+    CMOS table ``uniform`` (noise index draw) and ``signal``.  This is the mode
+    in which the engine reproduces the reference's output for recorded draws.
+    """
+
+    def __init__(self, bleach=None, frames=None):
+        self.bleach = dict(bleach or {})
+        self.frames = list(frames or [])
+        self.index = 0
+
+    def next_frame(self):
+        d = self.frames[self.index]
+        self.index += 1
+        return d
+
+
+def frame_windows(times, num, start_time, exposure_time, frame_index, shutter=None):
+    """Sub-step slices and unit times of one frame (_epifm.py:1146-1193)."""
+    t = start_time + exposure_time * frame_index
+    if shutter is not None:
+        t = max(t, shutter[0])
+        exposure_time = max(0.0, min(t + exposure_time, shutter[1]))
+    start = numpy.searchsorted(times, t, side="right")
+    if start != 0:
+        start -= 1
+    stop = numpy.searchsorted(times, t + exposure_time, side="left")
+    if len(times) and times[start] > t:
+        warnings.warn("No data input for interval [{}, {}]".format(t, times[start]))
+    idx = list(range(start, stop))
+    out = []
+    for k, i in enumerate(idx):
+        current = times[i] if k != 0 else t
+        nxt = times[idx[k + 1]] if k + 1 < len(idx) else t + exposure_time
+        unit_time = nxt - current
+        if unit_time < 1e-13:
+            continue
+        out.append((i, unit_time))
+    return out, exposure_time
+
+
+class FramePipeline:
+    """Device buffers and kernel sequence for frames of one configuration."""
+
+    def __init__(self, cfg, device=None, psf=None):
+        self.cfg = cfg
+        self.device = torch.device(device or "cuda")
+        _lib.load()
+        self.psf = psf or PSFTables(cfg, self.device)
+        nw, nh = cfg.image_size
+        self.nw, self.nh = nw, nh
+        self.n_pix = nw * nh
+        dev = self.device
+        self.status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
+        self.image = torch.empty(self.n_pix, dtype=torch.float32, device=dev)
+        self.expect = torch.empty(self.n_pix, dtype=torch.float32, device=dev)
+        self.adc = torch.empty(self.n_pix, dtype=torch.float64, device=dev)
+        self.offset = torch.from_numpy(numpy.ascontiguousarray(cfg.offset, dtype=float)).to(dev).reshape(-1)
+        self.gain = torch.from_numpy(numpy.ascontiguousarray(cfg.gain, dtype=float)).to(dev).reshape(-1)
+        self.offset_f = self.offset.float()
+        self.inv_gain_f = (1.0 / self.gain).float()
+        self.sigma = None
+        self.table_value = self.table_cdf = None
+        self.tile = cfg.tile or self._pick_tile()
+        self.tiles_x = (nw + self.tile - 1) // self.tile
+        self.tiles_y = (nh + self.tile - 1) // self.tile
+        self._cap = {}
+        self.budget = torch.zeros(0, dtype=torch.float64, device=dev)
+        self.camera_kind = self._camera_kind()
+
+    def _pick_tile(self):
+        return 32 if self.cfg.px >= 90e-9 else 64
+
+    def _camera_kind(self):
+        t = self.cfg.detector_type
+        if t == "EMCCD":
+            return _lib.CAM_EMCCD
+        if t == "CCD":
+            return _lib.CAM_CCD
+        if self.cfg.cmos_noise == "scmos":
+            return _lib.CAM_SCMOS
+        return _lib.CAM_CMOS_TABLE
+
+    def scmos_sigma_map(self, rng):
+        """Per-pixel readout sigma ~ lognormal(log(median), sigma) (sCMOS mode)."""
+        sig = rng.lognormal(math.log(self.cfg.scmos_median), self.cfg.scmos_sigma,
+                            size=self.n_pix)
+        self.sigma = torch.from_numpy(sig.astype(numpy.float32)).to(self.device)
+
+    def load_cmos_table(self, table=None):
+        if table is None:
+            table = _catalog.cmos_noise_table(self.cfg.catalog_dir)
+        table = numpy.asarray(table, dtype=float)
+        prob = table[:, 1] / table[:, 1].sum()
+        cdf = prob.cumsum()
+        cdf /= cdf[-1]
+        self.table_value = torch.from_numpy(numpy.ascontiguousarray(table[:, 0])).to(self.device)
+        self.table_cdf = torch.from_numpy(cdf).to(self.device)
+
+    # -- scratch buffers sized on demand, reused across frames -------------
+    def _buf(self, name, numel, dtype):
+        t = self._cap.get(name)
+        if t is None or t.numel() < numel or t.dtype != dtype:
+            t = torch.empty(max(numel, 1), dtype=dtype, device=self.device)
+            self._cap[name] = t
+        return t
+
+    def ensure_slots(self, n_slots, initial=None):
+        if self.budget.numel() < n_slots:
+            grown = torch.zeros(n_slots, dtype=torch.float64, device=self.device)
+            if self.budget.numel():
+                grown[: self.budget.numel()].copy_(self.budget)
+            self.budget = grown
+
+    def step_params(self, n_sub, n_particles, with_optinfo):
+        cfg = self.cfg
+        p = _lib.StepParams()
+        p.px, p.res, p.depth_cutoff = cfg.px, PSF_RES, cfg.depth_cutoff
+        for k in range(3):
+            p.focal[k] = float(cfg.focal_point[k])
+        p.nw, p.nh = self.nw, self.nh
+        p.n_signal = 2 * self.psf.n_r - 1
+        p.n_sub, p.n_particles = n_sub, n_particles
+        p.max_key = self.psf.max_key
+        p.amplitude0, p.penetration = float(cfg.amplitude0), float(cfg.penetration)
+        p.x_sec, p.qy, p.beer = float(cfg.x_sec), float(cfg.qy), float(cfg.beer)
+        p.norm_coeff = float(cfg.norm_coeff)
+        p.bleaching = 1 if cfg.bleaching else 0
+        p.with_optinfo = 1 if with_optinfo else 0
+        return p
+
+    def splat_params(self, n_images=1, rec_per_image=0):
+        p = _lib.SplatParams()
+        p.nw, p.nh, p.tile = self.nw, self.nh, self.tile
+        p.tiles_x, p.tiles_y = self.tiles_x, self.tiles_y
+        p.n_r, p.sat_pitch = self.psf.n_r, self.psf.pitch
+        p.n_images, p.rec_per_image = n_images, rec_per_image
+        p.px, p.res = self.cfg.px, PSF_RES
+        return p
+
+    def splat_records(self, recs, n_rec, image, n_images=1, rec_per_image=0, stream=None):
+        """Bin records by tile and splat them into ``image`` (n_images x W x H, float32)."""
+        s = stream_ptr(stream)
+        sp = self.splat_params(n_images, rec_per_image)
+        n_tiles = self.tiles_x * self.tiles_y * n_images
+        ws_bytes = _lib.load().sc_bin_workspace_bytes(n_rec, n_tiles)
+        ws = self._buf("ws", (ws_bytes + 3) // 4, torch.int32)
+        cap = _lib.load().sc_bin_capacity(n_rec, self.cfg.px, PSF_RES, 2 * self.psf.n_r - 1,
+                                          self.tile)
+        items = self._buf("items", cap, torch.int32)
+        tile_start = self._buf("tile_start", n_tiles + 1, torch.int32)
+        call("sc_bin_steps", ptr(recs), n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items),
+             cap, ptr(self.status), s)
+        call("sc_splat", ptr(recs), ptr(tile_start), ptr(items), ptr(self.psf.tables), sp,
+             ptr(image), ptr(self.status), s)
+
+    def camera(self, photons, expect, adc64, adc32=None, seed=0, counter=0, draws=None,
+               stream=None):
+        """Camera model + ADC on one frame (photons: float32 W*H on the device)."""
+        cfg = self.cfg
+        s = stream_ptr(stream)
+        cp = _lib.CameraParams()
+        cp.nw, cp.nh, cp.camera = self.nw, self.nh, self.camera_kind
+        cp.exact = 1 if draws is not None else 0
+        cp.rounding = 1 if cfg.adc_rounding else 0
+        cp.bit = cfg.bit
+        cp.qe = float(cfg.qe)
+        cp.background = float(cfg.background_mean) if cfg.background_switch else 0.0
+        cp.readout_noise = float(cfg.readout_noise or 0.0)
+        cp.emgain = float(cfg.emgain or 1.0)
+        cp.fullwell = float(cfg.fullwell)
+        cp.offset0, cp.gain0 = float(cfg.offset.flat[0]), float(cfg.gain.flat[0])
+        cp.table_n = 0 if self.table_value is None else self.table_value.numel()
+        cp.seed, cp.counter = int(seed) & (2 ** 64 - 1), int(counter) & (2 ** 64 - 1)
+        inj_noise = inj_signal = inj_uniform = None
+        if draws is not None:
+            dev = self.device
+
+            def dev64(a):
+                return torch.from_numpy(numpy.ascontiguousarray(a, dtype=float).reshape(-1)).to(dev)
+
+            inj_noise = dev64(draws["noise"]) if "noise" in draws else None
+            if "signal" in draws:
+                inj_signal = dev64(draws["signal"])
+            if "uniform" in draws:
+                inj_uniform = dev64(numpy.nan_to_num(numpy.asarray(draws["uniform"], float)))
+            if inj_signal is None and self.camera_kind == _lib.CAM_EMCCD:
+                inj_signal = self._buf("emccd_sig", self.n_pix, torch.float64)
+                call("sc_emccd_exact", ptr(photons), float(cfg.qe), cp.background,
+                     ptr(inj_uniform), self.n_pix, float(cfg.emgain), ptr(inj_signal),
+                     ptr(self.status), s)
+                inj_uniform = None
+        if self.camera_kind == _lib.CAM_CMOS_TABLE and self.table_value is None:
+            self.load_cmos_table(self.cfg.cmos_table)
+            cp.table_n = self.table_value.numel()
+        call("sc_camera", cp, ptr(photons), ptr(self.offset), ptr(self.gain), ptr(self.offset_f),
+             ptr(self.inv_gain_f), ptr(self.sigma), ptr(self.table_value), ptr(self.table_cdf),
+             ptr(inj_noise), ptr(inj_signal), ptr(inj_uniform), ptr(expect), ptr(adc64),
+             ptr(adc32), ptr(self.status), s)
+
+    def check_status(self):
+        st = self.status.cpu().numpy()
+        if st[0]:
+            self.status.zero_()
+            bits = int(st[0])
+            msgs = []
+            if bits & 1:
+                msgs.append("depth key beyond table range (particle %d, sub-step %d)" % (st[1], st[2]))
+            if bits & 2:
+                msgs.append("PSF table missing for key %d" % st[3])
+            if bits & 4:
+                msgs.append("EMCCD support empty")
+            if bits & 8:
+                msgs.append("random-variate loop bound reached")
+            if bits & 16:
+                msgs.append("bin capacity exceeded (%d entries)" % st[1])
+            raise _lib.ScopyonGPUError(_lib.SC_ERR_CAPACITY, "; ".join(msgs))
+
+    def run_frame(self, particles, unit_times, with_optinfo=True, draws=None, seed=0, counter=0,
+                  present=None, bleaching=None, stream=None):
+        """One frame from host arrays.
+
+        particles: (S, N, 5) float64 [depth, x, y, m_id, p_state] per sub-step,
+        column n holding particle slot n; unit_times: (S,) float64.
+        Returns device tensors (expect f32, adc f64, optinfo f64 (N, 8) or None).
+        """
+        s = stream_ptr(stream)
+        n_sub, n = particles.shape[0], particles.shape[1]
+        dev = self.device
+        self.ensure_slots(n)
+        part = self._buf("particles", n_sub * n * 5, torch.float64)[: n_sub * n * 5]
+        part.copy_(torch.from_numpy(numpy.ascontiguousarray(particles, dtype=float).reshape(-1)),
+                   non_blocking=False)
+        ut = torch.from_numpy(numpy.ascontiguousarray(unit_times, dtype=float)).to(dev)
+        n_rec = n_sub * n
+        recs = self._buf("recs", max(n_rec, 1) * (_lib.STEP_REC_BYTES // 4), torch.int32)
+        optinfo = self._buf("optinfo", n * 8, torch.float64) if with_optinfo else None
+        pres = None
+        if present is not None:
+            pres = torch.from_numpy(numpy.ascontiguousarray(present, dtype=numpy.uint8).reshape(-1)).to(dev)
+        if n_rec:
+            sp = self.step_params(n_sub, n, with_optinfo)
+            if bleaching is not None:
+                sp.bleaching = 1 if bleaching else 0
+            call("sc_emitter_steps", sp, ptr(part), ptr(ut), ptr(pres), ptr(self.psf.key_slot),
+                 ptr(self.budget), ptr(optinfo), ptr(recs), ptr(self.status), s)
+        self.splat_records(recs, n_rec, self.image, stream=stream)
+        self.camera(self.image, self.expect, self.adc, seed=seed, counter=counter, draws=draws,
+                    stream=stream)
+        return self.expect, self.adc, (optinfo[: n * 8].view(n, 8) if with_optinfo else None)

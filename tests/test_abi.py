@@ -1,0 +1,67 @@
+"""The C ABI library builds for sm_103a, loads, and exports every declared symbol.
+
+No compute call is made here (this runs without a GPU)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for fname in os.listdir(os.path.join(ROOT, "include")):
+        if fname.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fname)).read()
+            names |= set(re.findall(r"^[A-Za-z_][\w \*]*?\b(sc_\w+)\s*\(", text, re.M))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from scopyon_gb300 import _build
+    path = _build.build()
+    return ctypes.CDLL(path)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) >= 10
+    for name in sorted(names):
+        assert hasattr(lib, name), name
+
+
+def test_binding_covers_header():
+    from scopyon_gb300 import _lib
+    assert set(_lib.declared_symbols()) == _declared()
+
+
+def test_version_and_error_string(lib):
+    lib.sc_get_version.restype = ctypes.c_int
+    lib.sc_last_error.restype = ctypes.c_char_p
+    assert lib.sc_get_version() >= 1
+    assert isinstance(lib.sc_last_error(), bytes)
+
+
+def test_host_side_validation_needs_no_gpu():
+    # argument checks run before any CUDA call and return SC_ERR_ARG
+    from scopyon_gb300 import _build, _lib
+    _build.build()
+    L = _lib.load()
+    assert L.sc_psf_radial(0, 5e-7, 1.4, 0.0, None, 0, 1000, 1e-9, None, None) == _lib.SC_ERR_ARG
+    assert b"n_keys" in L.sc_last_error()
+    p = _lib.SplatParams(nw=64, nh=64, tile=12, tiles_x=6, tiles_y=6, n_r=1000, sat_pitch=1004,
+                         n_images=1, rec_per_image=0, px=1.6e-7, res=1e-9)
+    assert L.sc_splat(None, None, None, None, ctypes.byref(p), None, None, None) == _lib.SC_ERR_ARG
+    assert L.sc_bin_workspace_bytes(0, 16) == 0
+    assert L.sc_bin_capacity(100, 1.6e-7, 1e-9, 1999, 32) == 100 * 4
+
+
+def test_struct_sizes_match_c_layout():
+    from scopyon_gb300 import _lib
+    assert ctypes.sizeof(_lib.StepParams) == 128
+    assert ctypes.sizeof(_lib.SplatParams) == 56
+    assert ctypes.sizeof(_lib.CameraParams) == 104

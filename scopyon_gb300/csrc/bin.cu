@@ -76,13 +76,14 @@ __global__ void bin_tile_scan_kernel(const int32_t *tile_total, int n_tiles, int
         __syncthreads();
         const int32_t carry = carry_s;
         const int32_t incl = x + (warp > 0 ? warp_tot[warp - 1] : 0) + carry;
-        if (t < n_tiles) tile_start[t] = incl - v;
+        // clamped so that a consumer never reads item slots past the buffer
+        if (t < n_tiles) tile_start[t] = (int32_t)min((int64_t)(incl - v), capacity);
         __syncthreads();
         if (threadIdx.x == blockDim.x - 1) carry_s = incl;
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        tile_start[n_tiles] = carry_s;
+        tile_start[n_tiles] = (int32_t)min((int64_t)carry_s, capacity);
         if ((int64_t)carry_s > capacity) sc::flag_status(status, 4, carry_s, 0, 0);
     }
 }

@@ -1,0 +1,407 @@
+#!/usr/bin/env python
+"""Frames/s of the image-formation path on the EPIFM-defocus workload.
+
+Workload (one step = one camera frame): 20,000 emitters with x, y uniform over
+a 512 x 512 field of 160 nm pixels (81.92 um) and z uniform in [-1, 1] um, half
+diffusing at D = 0.01 um^2/s and half at 1.0 um^2/s; EPI illumination; 10 ms
+exposure in 20 sub-steps; photobleaching with a 2 s mean lifetime; sCMOS camera
+with per-pixel readout sigma ~ lognormal(ln 1.5 e-, 0.4) and per-pixel offset
+~ N(100, 5); 12-bit ADC.  Synthetic, seeded inputs of these shapes.
+
+``value``: frames/s with trajectories resident in HBM (sub-step records, tile
+binning, splat, camera + ADC per frame; outputs stay on the device).
+``e2e``: frames/s through ``scopyon_gb300.generate_images`` with host
+trajectories (pinned H2D of each frame's sub-steps, D2H of the ADC frame).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_EMIT = 20000
+IMAGE = 512
+SUBSTEPS = 20
+EXPOSURE = 0.010
+PX = 16e-6 / 100
+HALF = IMAGE * PX / 2
+METRIC = "frames/s, 512^2 px 20k emitters (EPIFM defocus, sCMOS)"
+WORKLOAD = "epifm_defocus_512px_20k_emitters_20substeps_scmos"
+
+
+def workload_config():
+    import scopyon_gb300 as sg
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {
+        "magnification": 100,
+        "light_source": {"angle": 0.0},
+        "detector": {"type": "CMOS", "image_size": [IMAGE, IMAGE], "exposure_time": EXPOSURE},
+        "analog_to_digital_converter": {"bit": 12, "offset": 100, "type": "pixel", "count": 5.0,
+                                        "fullwell": 30000},
+        "effects": {"photo_bleaching": {"switch": True, "half_life": 2.0 * math.log(2.0)}},
+        "gpu": {"cmos_noise": "scmos", "scmos_readout_median": 1.5, "scmos_readout_sigma": 0.4}}})
+    return cfg
+
+
+def trajectories(n_frames, seed=7):
+    """(n_frames*SUBSTEPS + 1, N, 5) formatted [depth, x, y, m_id, p_state] and raw inputs."""
+    rng = numpy.random.RandomState(seed)
+    steps = n_frames * SUBSTEPS
+    dt = EXPOSURE / SUBSTEPS
+    pos = numpy.empty((steps + 1, N_EMIT, 3))
+    pos[0, :, 0] = rng.uniform(-HALF, HALF, N_EMIT)
+    pos[0, :, 1] = rng.uniform(-HALF, HALF, N_EMIT)
+    pos[0, :, 2] = rng.uniform(-1e-6, 1e-6, N_EMIT)
+    d = numpy.where(numpy.arange(N_EMIT) < N_EMIT // 2, 0.01e-12, 1.0e-12)
+    scale = numpy.sqrt(2 * d * dt)[:, None]
+    for t in range(steps):
+        pos[t + 1] = pos[t] + scale * rng.standard_normal((N_EMIT, 3))
+    times = numpy.arange(steps + 1) * dt
+    return times, pos
+
+
+def formatted(pos):
+    out = numpy.empty(pos.shape[:2] + (5,))
+    out[..., 0] = pos[..., 2]
+    out[..., 1] = pos[..., 0]
+    out[..., 2] = pos[..., 1]
+    out[..., 3] = numpy.arange(pos.shape[1])
+    out[..., 4] = 1.0
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = [r.split(",") for r in open(self.file.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.strip() == "Active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def splat_algorithmic_bytes(n_rec):
+    """Bytes one splat launch must move: records, quadrant-table entries, image.
+
+    Per emitter-step: its 48-byte record, and the (n_b + 2)^2 distinct 8-byte
+    quadrant-table entries of its footprint, n_b = ceil(1999 nm / px) + 1
+    bounds per axis (the +2: the fold's centre knots).  Plus one float write
+    per image pixel.
+    """
+    n_b = math.ceil(1999e-9 / PX) + 1
+    return n_rec * (48 + 8 * (n_b + 2) ** 2) + 4 * IMAGE * IMAGE
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def gb300_arm(args, rank, world):
+    import torch
+    import scopyon_gb300 as sg
+    from scopyon_gb300 import _lib
+    from scopyon_gb300.epifm import EngineConfig, FramePipeline
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    cfg = workload_config()
+    rng = numpy.random.RandomState(11 + rank)
+    eng = EngineConfig(cfg["default"], rng=rng)
+    from scopyon_gb300.base import _psf_for
+    pipe = FramePipeline(eng, dev, psf=_psf_for(eng, dev))
+    pipe.scmos_sigma_map(rng)
+    t0 = time.time()
+    pipe.psf.ensure_all()
+    torch.cuda.synchronize()
+    psf_build_s = time.time() - t0
+
+    n_frames = args.warmup + args.steps
+    times, pos = trajectories(n_frames, seed=7 + rank)
+    traj = torch.from_numpy(formatted(pos)).to(dev)
+    ut = torch.full((SUBSTEPS,), EXPOSURE / SUBSTEPS, dtype=torch.float64, device=dev)
+    pipe.ensure_slots(N_EMIT)
+    beta = eng.half_life / math.log(2.0)
+    pipe.budget[:N_EMIT].copy_(torch.from_numpy(rng.exponential(beta, N_EMIT) * eng.n_emit0))
+    frame_stride = SUBSTEPS * N_EMIT * 5
+
+    def frame(f):
+        part = traj.view(-1)[f * frame_stride: (f + 1) * frame_stride]
+        return pipe.run_frame_device(part, ut, SUBSTEPS, N_EMIT, with_optinfo=False,
+                                     seed=1234 + rank, counter=f)
+
+    for f in range(args.warmup):
+        frame(f)
+    pipe.check_status()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    pipe.kernel_events = {}
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record()
+    for f in range(args.warmup, n_frames):
+        frame(f)
+    end.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    elapsed_ms = start.elapsed_time(end)
+    clk = clocks.stop()
+    pipe.check_status()
+    splat_ms = [a.elapsed_time(b) for a, b in pipe.kernel_events["splat"]]
+    pipe.kernel_events = None
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    ms_per_step = elapsed_ms / args.steps
+    value = world * args.steps / (elapsed_ms / 1e3)
+
+    e2e = e2e_arm(args, cfg, dev, rank, world)
+
+    splat_avg_ms = sum(splat_ms) / len(splat_ms)
+    n_rec = SUBSTEPS * N_EMIT
+    alg = splat_algorithmic_bytes(n_rec)
+    peak, peak_kind = load_peaks()
+    achieved = alg / (splat_avg_ms / 1e3) / 1e9
+    traffic = os.environ.get("SC_SPLAT_TRAFFIC_BYTES")
+    result = {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded uniform positions, Gaussian Brownian steps)",
+        "config": {"workload": WORKLOAD, "n_emitters": N_EMIT, "image": [IMAGE, IMAGE],
+                   "substeps": SUBSTEPS, "exposure_s": EXPOSURE, "pixel_nm": PX * 1e9,
+                   "camera": "sCMOS per-pixel sigma, 12-bit", "psf": "Born-Wolf TRITC, 1002 depth keys",
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (PSF tables %.1f GB)" % (
+                       pipe.psf.tables.numel() * 4 / 1e9),
+                   "psf_build_s": round(psf_build_s, 3)},
+        "e2e": e2e,
+        "gpu_launches": 7 * args.steps,
+        "clocks": clk,
+        "roofline": {"kernel": "splat_tile_kernel", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind,
+                     "traffic": float(traffic) if traffic else None,
+                     "algorithmic_bytes": alg, "avg_launch_ms": splat_avg_ms},
+    }
+    if rank == 0 and not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline()
+    return result
+
+
+def e2e_arm(args, cfg, dev, rank, world):
+    """Frames/s through the public API with host trajectories."""
+    import torch
+    import scopyon_gb300 as sg
+    n_frames = args.warmup + args.steps
+    times, pos = trajectories(n_frames, seed=21 + rank)
+    ids = numpy.arange(N_EMIT, dtype=float)
+    inputs = [(float(t), numpy.hstack([pos[k], ids[:, None], numpy.ones((N_EMIT, 1))]))
+              for k, t in enumerate(times)]
+    gen = sg.generate_images(inputs, n_frames, config=cfg, rng=numpy.random.RandomState(3 + rank),
+                             device=dev)
+    for _ in range(args.warmup):
+        next(gen)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        img = next(gen)
+        img.as_array()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([dt], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dt = float(t.item())
+    return {"value": world * args.steps / dt, "unit": "frames/s",
+            "h2d_bytes_per_step": SUBSTEPS * N_EMIT * 5 * 8 + SUBSTEPS * 8,
+            "d2h_bytes_per_step": IMAGE * IMAGE * 8 + 16}
+
+
+# ---------------------------------------------------------------- CPU baseline
+_WORKER_PSF = {}
+
+
+def _cpu_worker(job):
+    """Times the oracle on one bounded sample: footprint sums of ``n_steps``
+    emitter-steps over ``n_keys`` depth keys (tables built once per process,
+    untimed) and the CMOS camera on a 64 x 64 patch (per-pixel table choice
+    plus Poisson draw, the reference's CMOS loop)."""
+    n_steps, n_keys, seed = job
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    import oracle as O
+    from scopyon_gb300._catalog import psf_wavelength_and_norm
+    rng = numpy.random.RandomState(seed)
+    z = numpy.random.RandomState(seed % 1000).uniform(-1e-6, 1e-6, size=n_keys)
+    psf = _WORKER_PSF.get("psf")
+    if psf is None:
+        wl, _ = psf_wavelength_and_norm("Tetramethylrhodamine(TRITC)")
+        psf = _WORKER_PSF["psf"] = O.PSFCache("Born-Wolf", wl)
+    for d in z:
+        psf.get(d)
+    xy = rng.uniform(-HALF, HALF, size=(n_steps, 2))
+    img = numpy.zeros((IMAGE, IMAGE))
+    t0 = time.perf_counter()
+    for k in range(n_steps):
+        O.overlay_signal(img, psf.get(z[k % n_keys]), [0.0, xy[k, 0], xy[k, 1]], PX, 1.0)
+    t_splat = (time.perf_counter() - t0) / n_steps
+    table = numpy.column_stack([numpy.linspace(0.6, 19.9, 194),
+                                numpy.exp(-numpy.linspace(0, 8, 194))])
+
+    class P:
+        detector_type = "CMOS"
+        cmos_table = table
+
+    patch = rng.uniform(0, 20, size=(64, 64))
+    t0 = time.perf_counter()
+    O.NumpyDraws(rng).camera(P, patch)
+    t_cam = (time.perf_counter() - t0) / patch.size
+    return t_splat, t_cam
+
+
+def _rate(res, threads):
+    t_splat = statistics.mean(r[0] for r in res)
+    t_cam = statistics.mean(r[1] for r in res)
+    sec_per_frame = (t_splat * SUBSTEPS * N_EMIT + t_cam * IMAGE * IMAGE) / threads
+    return 1.0 / sec_per_frame, t_splat, t_cam
+
+
+def cpu_baseline(n_steps=300, n_keys=6):
+    """Oracle frames/s on one host core (bounded sample, extrapolated)."""
+    t0 = time.perf_counter()
+    res = [_cpu_worker((n_steps, n_keys, 100))]
+    wall = time.perf_counter() - t0
+    value, t_splat, t_cam = _rate(res, 1)
+    return {"value": value, "unit": "frames/s", "cores": 1, "kind": "port",
+            "sample": "%d emitter-step footprint sums (exact 1-nm slice sums over %d depth "
+                      "keys, tables built untimed) + CMOS table/Poisson camera on 64x64 px, "
+                      "extrapolated linearly to 400k emitter-steps and 512^2 px per frame "
+                      "(%.2f ms/step, %.1f us/px; %.1f s wall)"
+                      % (n_steps, n_keys, t_splat * 1e3, t_cam * 1e6, wall)}
+
+
+def reference_arm(args, rank, world):
+    """The oracle port on all host cores; each step is one bounded sample."""
+    if rank != 0:
+        return None
+    import multiprocessing as mp
+    threads = max(1, min(os.cpu_count() or 1, 64))
+    n_steps, n_keys = 40, 2
+    times_ = []
+    with mp.get_context("spawn").Pool(threads) as pool:
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_worker, [(n_steps, n_keys, 1000 * k + w) for w in range(threads)])
+            if k >= args.warmup:
+                times_.append((res, time.perf_counter() - t0))
+    all_res = [r for res, _ in times_ for r in res]
+    value, t_splat, t_cam = _rate(all_res, threads)
+    sample = ("%d processes x %d emitter-step footprint sums (%d depth keys) + 64x64 px CMOS "
+              "camera per step; extrapolated to 400k emitter-steps and 512^2 px per frame "
+              "(%.2f ms/step, %.1f us/px per process)" % (threads, n_steps, n_keys,
+                                                         t_splat * 1e3, t_cam * 1e6))
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_emitters": N_EMIT, "image": [IMAGE, IMAGE],
+                       "substeps": SUBSTEPS},
+            "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        res = reference_arm(args, rank, world)
+        if res is not None:
+            print(json.dumps(res), flush=True)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    res = gb300_arm(args, rank, world)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

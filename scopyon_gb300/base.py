@@ -19,6 +19,7 @@ import warnings
 
 import numpy
 
+from . import _lib
 from . import config as _config
 from .epifm import EngineConfig, FramePipeline, InjectedDraws, PSFTables, frame_windows
 from .image import Image
@@ -134,7 +135,8 @@ class EPIFMSimulator:
         """Form one image; returns ``Image`` or ``(Image, infodict)`` like scopyon."""
         data = self._format_inputs(inputs)
         cfg = self.base()
-        img, info = next(_Frames(self, cfg, data, 1, start_time, exposure_time, False, draws))
+        img, info = next(_Frames(self, cfg, data, 1, start_time, exposure_time, False, draws,
+                                 full_output))
         if full_output:
             return img, info
         return img
@@ -145,7 +147,7 @@ class EPIFMSimulator:
         data = self._format_inputs(inputs)
         cfg = self.base()
         for img, info in _Frames(self, cfg, data, num_frames, start_time, exposure_time,
-                                 cfg.bleaching, draws):
+                                 cfg.bleaching, draws, full_output):
             yield (img, info) if full_output else img
 
     # access for _Frames
@@ -156,12 +158,15 @@ class EPIFMSimulator:
         return self.__device
 
 
-def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, draws):
+def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, draws,
+            full_output=True):
     """Frame generator: host bookkeeping around FramePipeline.run_frame."""
     import torch
     rng = sim._rng()
     device = torch.device(sim._device())
     pipe = FramePipeline(cfg, device, psf=_psf_for(cfg, device))
+    if pipe.camera_kind == _lib.CAM_SCMOS:
+        pipe.scmos_sigma_map(rng)
     exposure = exposure_time or cfg.exposure_time
     times = numpy.array([t for t, _ in data])
     shutter = (cfg.shutter_start, cfg.shutter_end) if cfg.shutter_switch else None
@@ -205,7 +210,8 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
         if s_count == 0:
             particles = numpy.zeros((0, n_slots, 5))
         elif same and slot_arr.shape == id_cols[0].shape and numpy.array_equal(slot_arr, id_cols[0]):
-            particles = numpy.stack(arrays)
+            particles = pipe.host_staging((s_count, n_slots, 5))
+            numpy.stack(arrays, out=particles)
         else:
             particles = numpy.zeros((s_count, n_slots, 5))
             present = numpy.zeros((s_count, n_slots), dtype=numpy.uint8)
@@ -218,14 +224,16 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
         frame_draws = draws.next_frame() if draws is not None and draws.frames else None
         seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | int(rng.randint(0, 2 ** 31 - 1)) \
             if frame_draws is None else 0
-        expect, adc, opt = pipe.run_frame(particles, uts, with_optinfo=True, draws=frame_draws,
-                                          seed=seed, counter=f, present=present,
-                                          bleaching=bleaching)
+        expect, adc, opt = pipe.run_frame(particles, uts, with_optinfo=full_output,
+                                          draws=frame_draws, seed=seed, counter=f,
+                                          present=present, bleaching=bleaching)
         pipe.check_status()
         adc_np = adc.cpu().numpy().reshape(nw, nh).copy()
-        info = {"expectation": expect.cpu().numpy().astype(float).reshape(nw, nh)}
-        info["true_data"] = _true_data(cfg, opt, slots, id_cols, exp_eff, nw, nh)
-        if bleaching:
+        info = {}
+        if full_output:
+            info["expectation"] = expect.cpu().numpy().astype(float).reshape(nw, nh)
+            info["true_data"] = _true_data(cfg, opt, slots, id_cols, exp_eff, nw, nh)
+        if bleaching and full_output:
             b = pipe.budget[:n_slots].cpu().numpy()
             info["fluorescence_states"] = {m: float(b[slots[m]]) for m in slot_ids}
         yield Image(adc_np), info

@@ -105,7 +105,7 @@ __global__ void camera_kernel(CamConsts c, const float *__restrict__ photons,
     const int stride = gridDim.x * blockDim.x;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.n; p += stride) {
         const double ph = (double)photons[p] + c.background;
-        const double e = c.qe * ph;
+        const double e = __dmul_rn(c.qe, ph);
         if (expect) expect[p] = (float)e;
         if (c.exact) {
             double noise, signal;

@@ -45,7 +45,9 @@ __device__ __forceinline__ int axis_bound(int k, int n, int start, float a_hi, f
     if (fabsf(d) >= 1e-6f) {
         v = (int)r + (d > 0.f ? 1 : 0);
     } else {
-        const double t = ((double)(start + k) * c.px - origin) / c.res;
+        // the reference's FP64 sequence; __dmul_rn keeps the product rounded
+        // (a contracted fma would skip that rounding and can flip the ceil)
+        const double t = (__dmul_rn((double)(start + k), c.px) - origin) / c.res;
         v = (int)ceil(t);
     }
     if (k == 0) v = max(v, 0);

@@ -38,7 +38,7 @@ __global__ void emitter_steps_kernel(sc::StepConsts c, const double *particles,
         const double rel0 = q[0] - c.focal[0];
         const double rel1 = q[1] - c.focal[1];
         const double rel2 = q[2] - c.focal[2];
-        const double amp = c.amplitude0 * exp(-fabs(rel0) / c.penetration);
+        const double amp = __dmul_rn(c.amplitude0, exp(-fabs(rel0) / c.penetration));
         const double n_emit = sc::emit_photons(c, amp, ut);
         if (c.bleaching) {
             double nb = b - n_emit;
@@ -48,18 +48,18 @@ __global__ void emitter_steps_kernel(sc::StepConsts c, const double *particles,
             }
             b = nb;
         }
-        const double norm = c.norm_coeff * (p_state * n_emit / (4.0 * M_PI));
+        const double norm = __dmul_rn(c.norm_coeff, __dmul_rn(p_state, n_emit) / (4.0 * M_PI));
         ScStepRec rec;
         sc::make_record(c, rel0, rel1, rel2, norm, key_slot, status, i, s, rec);
         *out = rec;
         if (c.with_optinfo) {
             acc[0] += ut;
-            acc[1] += ut * p_state;
-            acc[2] += ut * q[1];
-            acc[3] += ut * q[2];
-            acc[4] += ut * q[1];
-            acc[5] += ut * q[2];
-            acc[6] += ut * rel0;
+            acc[1] += __dmul_rn(ut, p_state);
+            acc[2] += __dmul_rn(ut, q[1]);
+            acc[3] += __dmul_rn(ut, q[2]);
+            acc[4] += __dmul_rn(ut, q[1]);
+            acc[5] += __dmul_rn(ut, q[2]);
+            acc[6] += __dmul_rn(ut, rel0);
             acc[7] += norm;
         }
     }

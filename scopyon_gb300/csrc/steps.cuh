@@ -17,10 +17,13 @@ struct StepConsts {
 
 int step_consts(const ScStepParams *p, StepConsts &c);
 
-// n_emit = QY * (amplitude * x_sec * dt) * (1 - 10^-A)   (_epifm.py:1344-1360)
+// n_emit = QY * (amplitude * x_sec * dt) * (1 - 10^-A)   (_epifm.py:1344-1360).
+// Products that feed an addition use __dmul_rn throughout these kernels: a
+// contracted fma would skip the product's rounding, which the reference (numpy,
+// one rounded operation at a time) performs, and flip threshold decisions.
 __device__ __forceinline__ double emit_photons(const StepConsts &c, double amplitude, double dt) {
-    const double n_abs = amplitude * c.x_sec * dt;
-    return c.qy * n_abs * c.beer;
+    const double n_abs = __dmul_rn(__dmul_rn(amplitude, c.x_sec), dt);
+    return __dmul_rn(__dmul_rn(c.qy, n_abs), c.beer);
 }
 
 // Footprint of one axis (_epifm.py:233-258): first pixel, number of bounds,
@@ -42,7 +45,7 @@ __device__ __forceinline__ void axis_footprint(double half_len, double coord, do
     const int n = (int)hi_c - i0 + 1;
     start = (int16_t)i0;
     count = (int16_t)n;
-    const double a = ((double)i0 * px - origin) / res;
+    const double a = (__dmul_rn((double)i0, px) - origin) / res;
     a_hi = (float)a;
     a_lo = (float)(a - (double)a_hi);
 }

@@ -311,6 +311,8 @@ class FramePipeline:
         self._cap = {}
         self.budget = torch.zeros(0, dtype=torch.float64, device=dev)
         self.camera_kind = self._camera_kind()
+        # name -> [(start, end) CUDA events]; set to a dict to time kernels in place
+        self.kernel_events = None
 
     def _pick_tile(self):
         return 32 if self.cfg.px >= 90e-9 else 64
@@ -348,6 +350,18 @@ class FramePipeline:
             t = torch.empty(max(numel, 1), dtype=dtype, device=self.device)
             self._cap[name] = t
         return t
+
+    def host_staging(self, shape):
+        """A pinned host array of ``shape`` (float64) for the next upload."""
+        numel = int(numpy.prod(shape))
+        ev = self._cap.get("staging_event")
+        if ev is not None:
+            ev.synchronize()  # the previous upload from this buffer has finished
+        t = self._cap.get("staging")
+        if t is None or t.numel() < numel:
+            t = torch.empty(max(numel, 1), dtype=torch.float64, pin_memory=True)
+            self._cap["staging"] = t
+        return t[:numel].numpy().reshape(shape)
 
     def ensure_slots(self, n_slots, initial=None):
         if self.budget.numel() < n_slots:
@@ -395,8 +409,16 @@ class FramePipeline:
         tile_start = self._buf("tile_start", n_tiles + 1, torch.int32)
         call("sc_bin_steps", ptr(recs), n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items),
              cap, ptr(self.status), s)
+        ev = self.kernel_events
+        if ev is not None:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
         call("sc_splat", ptr(recs), ptr(tile_start), ptr(items), ptr(self.psf.tables), sp,
              ptr(image), ptr(self.status), s)
+        if ev is not None:
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record(stream)
+            ev.setdefault("splat", []).append((e0, e1))
 
     def camera(self, photons, expect, adc64, adc32=None, seed=0, counter=0, draws=None,
                stream=None):
@@ -468,25 +490,35 @@ class FramePipeline:
         column n holding particle slot n; unit_times: (S,) float64.
         Returns device tensors (expect f32, adc f64, optinfo f64 (N, 8) or None).
         """
-        s = stream_ptr(stream)
         n_sub, n = particles.shape[0], particles.shape[1]
         dev = self.device
-        self.ensure_slots(n)
         part = self._buf("particles", n_sub * n * 5, torch.float64)[: n_sub * n * 5]
-        part.copy_(torch.from_numpy(numpy.ascontiguousarray(particles, dtype=float).reshape(-1)),
-                   non_blocking=False)
+        host = torch.from_numpy(numpy.ascontiguousarray(particles, dtype=float).reshape(-1))
+        part.copy_(host, non_blocking=host.is_pinned())
+        if host.is_pinned():
+            ev = torch.cuda.Event()
+            ev.record()
+            self._cap["staging_event"] = ev
         ut = torch.from_numpy(numpy.ascontiguousarray(unit_times, dtype=float)).to(dev)
-        n_rec = n_sub * n
-        recs = self._buf("recs", max(n_rec, 1) * (_lib.STEP_REC_BYTES // 4), torch.int32)
-        optinfo = self._buf("optinfo", n * 8, torch.float64) if with_optinfo else None
         pres = None
         if present is not None:
             pres = torch.from_numpy(numpy.ascontiguousarray(present, dtype=numpy.uint8).reshape(-1)).to(dev)
+        return self.run_frame_device(part, ut, n_sub, n, with_optinfo, draws, seed, counter, pres,
+                                     bleaching, stream)
+
+    def run_frame_device(self, part, ut, n_sub, n, with_optinfo=True, draws=None, seed=0,
+                         counter=0, present=None, bleaching=None, stream=None):
+        """One frame from device tensors: part (n_sub*n*5 f64), ut (n_sub f64)."""
+        s = stream_ptr(stream)
+        self.ensure_slots(n)
+        n_rec = n_sub * n
+        recs = self._buf("recs", max(n_rec, 1) * (_lib.STEP_REC_BYTES // 4), torch.int32)
+        optinfo = self._buf("optinfo", n * 8, torch.float64) if with_optinfo else None
         if n_rec:
             sp = self.step_params(n_sub, n, with_optinfo)
             if bleaching is not None:
                 sp.bleaching = 1 if bleaching else 0
-            call("sc_emitter_steps", sp, ptr(part), ptr(ut), ptr(pres), ptr(self.psf.key_slot),
+            call("sc_emitter_steps", sp, ptr(part), ptr(ut), ptr(present), ptr(self.psf.key_slot),
                  ptr(self.budget), ptr(optinfo), ptr(recs), ptr(self.status), s)
         self.splat_records(recs, n_rec, self.image, stream=stream)
         self.camera(self.image, self.expect, self.adc, seed=seed, counter=counter, draws=draws,

@@ -233,7 +233,8 @@ def gb300_arm(args, rank, world):
                    "camera": "sCMOS per-pixel sigma, 12-bit", "psf": "Born-Wolf TRITC, 1002 depth keys",
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (PSF tables %.1f GB)" % (
-                       pipe.psf.tables.numel() * 4 / 1e9),
+                       (pipe.psf.tables.numel() + (pipe.psf.box.numel() if pipe.psf.box is not None
+                                                   else 0)) * 4 / 1e9),
                    "psf_build_s": round(psf_build_s, 3)},
         "e2e": e2e,
         "gpu_launches": 7 * args.steps,

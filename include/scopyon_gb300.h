@@ -40,13 +40,16 @@ extern "C" {
  *     bit3 RNG loop bound hit, bit4 capacity), [1..3] first offending index. */
 #define SC_STATUS_WORDS 4
 
-/* One emitter during one exposure sub-step, ready to be splatted (48 bytes). */
+/* One emitter during one exposure sub-step, ready to be splatted (56 bytes). */
 typedef struct {
     double x0, y0;       /* footprint origin along x / y in metres (exact FP64)      */
     float ax_hi, ax_lo;  /* (i_start*px - x0)/res as a double-float                   */
     float ay_hi, ay_lo;  /* (j_start*px - y0)/res as a double-float                   */
     int16_t i_start, n_i;/* first pixel index and number of footprint bounds along x  */
     int16_t j_start, n_j;/* same along y; n_i < 2 or n_j < 2 means nothing to splat   */
+    int16_t l0x, l0y;    /* first footprint bound along x / y before clamping          */
+    int16_t box;         /* 1: bounds are l0 + P*k exactly, use the box table          */
+    int16_t pad;
     int32_t slot;        /* PSF table slot of the depth key                           */
     float w;             /* normalisation * res^2: photons per unit table sum          */
 } ScStepRec;
@@ -71,6 +74,8 @@ typedef struct {
     double norm_coeff;       /* sum(fluoem_norm) * psf_normalization                       */
     int32_t bleaching;       /* 1: photon-budget bleaching on                              */
     int32_t with_optinfo;    /* 1: accumulate the 8-vector true_data per particle          */
+    int32_t box_p;           /* px / res when it is an integer P (box tables built), else 0 */
+    int32_t pad0;
 } ScStepParams;
 
 typedef struct {
@@ -82,6 +87,7 @@ typedef struct {
     int32_t n_images;        /* frames/images splatted by one launch                        */
     int32_t rec_per_image;   /* records per image (record r is in image r / rec_per_image); */
                              /* 0 means every record belongs to image 0                     */
+    int32_t box_p, box_nq;   /* box tables: P rows per pixel and NQ pixel offsets, or 0     */
     double px, res;
 } ScSplatParams;
 
@@ -114,6 +120,16 @@ int sc_psf_radial(int kind, double wavelength, double na, double sigma,
  * overlay_signal_ (src/scopyon/_epifm.py:277-282).                          */
 int sc_psf_quadrant_sat(const double *d_radial, int n_keys, int n_r, double res,
                         float *d_sat, int sat_pitch, void *stream);
+
+/* Box-integrated PSF tables for an integer pixel pitch of P grid rows: for
+ * every pixel start row m_x, m_y in [-P, NQ*P - P), the sum of the cartesian
+ * grid over [m_x, m_x+P) x [m_y, m_y+P) clipped to the grid, stored as FP32 in
+ * phase-major order [key][m_x mod P][m_y mod P][m_x div P][m_y div P] (with m
+ * shifted by +P), NQ = (2 n_r - 1 + P - 1) / P + 1.  Built from the quadrant
+ * tables of sc_psf_quadrant_sat.  With it, one emitter's footprint is one
+ * contiguous block (the pixel sums of overlay_signal_, src/scopyon/_epifm.py:277-282). */
+int sc_psf_box_table(const float *d_sat, int n_keys, int n_r, int sat_pitch, int box_p,
+                     float *d_box, void *stream);
 
 /* Emitter physics for one frame: excitation, emitted photons, photon-budget
  * bleaching, normalisation, depth key and footprint origin per particle and
@@ -148,8 +164,8 @@ int sc_bin_steps(const ScStepRec *d_recs, int n_rec,
  * of the records binned to it.  Replaces overlay_signal_
  * (src/scopyon/_epifm.py:224-282) for every particle and sub-step.          */
 int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
-             const int32_t *d_items, const float *d_sat, const ScSplatParams *p,
-             float *d_image, int32_t *d_status, void *stream);
+             const int32_t *d_items, const float *d_sat, const float *d_box,
+             const ScSplatParams *p, float *d_image, int32_t *d_status, void *stream);
 
 /* Camera model and ADC.  Replaces _EPIFMSimulator.__detector_output, the
  * EMCCD / CCD / CMOS classes and __get_analog_to_digital_converter_counts

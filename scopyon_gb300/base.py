@@ -53,7 +53,8 @@ _PSF_CACHE = {}
 
 def _psf_for(cfg, device):
     key = (str(device), cfg.fluorophore_type, float(cfg.psf_wavelength), cfg.na,
-           float(cfg.radial_width or 0.0), float(cfg.radial_cutoff), float(cfg.depth_cutoff))
+           float(cfg.radial_width or 0.0), float(cfg.radial_cutoff), float(cfg.depth_cutoff),
+           cfg.box_p)
     tables = _PSF_CACHE.get(key)
     if tables is None:
         tables = _PSF_CACHE[key] = PSFTables(cfg, device)

@@ -9,6 +9,7 @@
 // G[u][v] = sum_{p<u, q<v} Q[p][q]; any footprint rectangle of P is a signed
 // sum of G entries (see splat.cu).
 #include "sc_common.cuh"
+#include "fold.cuh"
 
 namespace {
 
@@ -149,6 +150,45 @@ quadrant_sat_kernel(const double *radial, int n_r, double res, float *sat, int p
     }
 }
 
+// Box table: entry (key, r_x, r_y, q_x, q_y) is the grid sum over rows
+// [m_x, m_x + P) and columns [m_y, m_y + P) clipped to [0, 2n-1), where
+// m = q * P + r - P.  Each sum is a signed combination of quadrant-table
+// entries, accumulated in FP64 and rounded once to FP32.
+__global__ void box_table_kernel(const float2 *__restrict__ sat, int n_r, int pitch, int P,
+                                 int nq, float *__restrict__ box) {
+    const int key = blockIdx.y;
+    const int n_signal = 2 * n_r - 1;
+    const float2 *G = sat + (size_t)key * (n_r + 1) * pitch;
+    const int per_key = P * P * nq * nq;  // < 2^31 for any grid the API accepts
+    float *out = box + (size_t)key * per_key;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < per_key; e += gridDim.x * blockDim.x) {
+        int rest = e;
+        const int qy = rest % nq; rest /= nq;
+        const int qx = rest % nq; rest /= nq;
+        const int ry = rest % P;
+        const int rx = rest / P;
+        int a0 = qx * P + rx - P, b0 = qy * P + ry - P;
+        int a1 = min(a0 + P, n_signal), b1 = min(b0 + P, n_signal);
+        a0 = max(a0, 0);
+        b0 = max(b0, 0);
+        double v = 0.0;
+        if (a1 > a0 && b1 > b0) {
+            int uu[3], vv[3];
+            float us[3], vs[3];
+            const int nu = sc::fold(a0, a1, n_r, uu, us);
+            const int nv = sc::fold(b0, b1, n_r, vv, vs);
+            for (int iu = 0; iu < nu; ++iu) {
+                const float2 *row = G + (size_t)uu[iu] * pitch;
+                for (int iv = 0; iv < nv; ++iv) {
+                    const float2 g = row[vv[iv]];
+                    v += (double)(us[iu] * vs[iv]) * ((double)g.x + (double)g.y);
+                }
+            }
+        }
+        out[e] = (float)v;
+    }
+}
+
 }  // namespace
 
 extern "C" int sc_psf_radial(int kind, double wavelength, double na, double sigma,
@@ -192,4 +232,19 @@ extern "C" int sc_psf_quadrant_sat(const double *d_radial, int n_keys, int n_r, 
     quadrant_sat_kernel<<<n_keys, kSatThreads, smem, sc::as_stream(stream)>>>(d_radial, n_r, res,
                                                                             d_sat, sat_pitch);
     return sc::launch_status("sc_psf_quadrant_sat");
+}
+
+extern "C" int sc_psf_box_table(const float *d_sat, int n_keys, int n_r, int sat_pitch, int box_p,
+                                float *d_box, void *stream) {
+    SC_REQUIRE(n_keys > 0 && n_keys <= 65535, "sc_psf_box_table: n_keys=%d", n_keys);
+    SC_REQUIRE(n_r >= 2 && sat_pitch >= n_r + 1, "sc_psf_box_table: n_r=%d pitch=%d", n_r,
+               sat_pitch);
+    SC_REQUIRE(box_p >= 1 && box_p <= 4096, "sc_psf_box_table: P=%d out of range", box_p);
+    SC_REQUIRE(d_sat && d_box, "sc_psf_box_table: NULL pointer");
+    const int n_signal = 2 * n_r - 1;
+    const int nq = (n_signal + box_p - 1) / box_p + 1;
+    dim3 grid(256, n_keys);
+    box_table_kernel<<<grid, 256, 0, sc::as_stream(stream)>>>(
+        reinterpret_cast<const float2 *>(d_sat), n_r, sat_pitch, box_p, nq, d_box);
+    return sc::launch_status("sc_psf_box_table");
 }

@@ -18,6 +18,7 @@
 // summed in a fixed order at the end, so there are no atomics at all.
 #include "sc_common.cuh"
 #include "bin.cuh"
+#include "fold.cuh"
 
 namespace {
 
@@ -27,6 +28,9 @@ struct SplatConsts {
     int pitch;
     double px, res;
     float b_hi, b_lo;  // px / res as a double-float
+    const float *box;  // box tables (NULL when px / res is not an integer)
+    int box_p, box_nq;
+    int64_t box_stride;  // floats per box table
 };
 
 // Footprint bound k of one axis: ceil(((start + k) * px - origin) / res) with
@@ -53,33 +57,6 @@ __device__ __forceinline__ int axis_bound(int k, int n, int start, float a_hi, f
     if (k == 0) v = max(v, 0);
     if (k == n - 1) v = min(v, c.n_signal);
     return v;
-}
-
-// Python slice semantics of grid[lo:hi] on an axis of length n.
-__device__ __forceinline__ void slice_bounds(int &lo, int &hi, int n) {
-    if (lo < 0) lo = max(lo + n, 0);
-    else if (lo > n) lo = n;
-    if (hi < 0) hi = max(hi + n, 0);
-    else if (hi > n) hi = n;
-}
-
-// Quadrant-table terms of a grid interval [a0, a1): signed row indices u with
-// sum_{x in [a0,a1)} f(|x - c|) = sum_k sign_k * F(u_k), F the exclusive prefix.
-__device__ __forceinline__ int fold(int a0, int a1, int n, int *u, float *sg) {
-    const int c = n - 1;
-    int m = 0;
-    if (a1 <= n) {
-        u[m] = n - a0; sg[m++] = 1.f;
-        if (n - a1 > 0) { u[m] = n - a1; sg[m++] = -1.f; }
-    } else if (a0 >= c) {
-        u[m] = a1 - c; sg[m++] = 1.f;
-        if (a0 - c > 0) { u[m] = a0 - c; sg[m++] = -1.f; }
-    } else {
-        u[m] = n - a0; sg[m++] = 1.f;
-        u[m] = a1 - c; sg[m++] = 1.f;
-        u[m] = 1; sg[m++] = -1.f;
-    }
-    return m;
 }
 
 template <int T, int NW>
@@ -111,6 +88,33 @@ splat_tile_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict_
         const int pj_lo = max((int)rec.j_start, py0);
         const int pj_hi = min(min(rec.j_start + rec.n_j - 2, py0 + T - 1), c.nh - 1);
         if (pi_hi < pi_lo || pj_hi < pj_lo) continue;
+        if (rec.box && c.box != nullptr) {
+            // pixel (i, j) integrates grid rows [l0x + P (i - i_start), + P) and the
+            // same for columns: one entry of the box table, contiguous along j
+            const int P = c.box_p, NQ = c.box_nq;
+            const int mx = rec.l0x + P, my = rec.l0y + P;
+            const int qx0 = mx / P + (pi_lo - rec.i_start);
+            const int qy0 = my / P + (pj_lo - rec.j_start);
+            const float *B = c.box + (int64_t)rec.slot * c.box_stride +
+                             (int64_t)((mx % P) * P + (my % P)) * NQ * NQ;
+            const int npy = pj_hi - pj_lo + 1;
+            const int npix = (pi_hi - pi_lo + 1) * npy;
+            for (int q = lane; q < npix; q += 32) {
+                const int a = q / npy, bj = q - (q / npy) * npy;
+                const int qx = qx0 + a, qy = qy0 + bj;
+                if (qx >= NQ || qy >= NQ) continue;
+                const float val = __ldg(B + qx * NQ + qy);
+                if (val > 0.f) {
+                    const float f = rec.w * val;
+                    const int idx = (pi_lo + a - px0) * T + (pj_lo + bj - py0);
+                    const float y = f - my_cmp[idx];
+                    const float tsum = my_acc[idx] + y;
+                    my_cmp[idx] = (tsum - my_acc[idx]) - y;
+                    my_acc[idx] = tsum;
+                }
+            }
+            continue;
+        }
         const int nbx = pi_hi - pi_lo + 2, nby = pj_hi - pj_lo + 2;
         for (int b = lane; b < nbx + nby; b += 32) {
             if (b < nbx)
@@ -127,13 +131,13 @@ splat_tile_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict_
         for (int q = lane; q < npix; q += 32) {
             const int a = q / npy, bj = q - (q / npy) * npy;
             int a0 = bx[a], a1 = bx[a + 1], b0 = by[bj], b1 = by[bj + 1];
-            slice_bounds(a0, a1, c.n_signal);
-            slice_bounds(b0, b1, c.n_signal);
+            sc::slice_bounds(a0, a1, c.n_signal);
+            sc::slice_bounds(b0, b1, c.n_signal);
             if (a1 <= a0 || b1 <= b0) continue;
             int uu[3], vv[3];
             float us[3], vs[3];
-            const int nu = fold(a0, a1, c.n_r, uu, us);
-            const int nv = fold(b0, b1, c.n_r, vv, vs);
+            const int nu = sc::fold(a0, a1, c.n_r, uu, us);
+            const int nv = sc::fold(b0, b1, c.n_r, vv, vs);
             float s = 0.f, e = 0.f;
             for (int iu = 0; iu < nu; ++iu) {
                 const float2 *row = G + (int64_t)uu[iu] * c.pitch;
@@ -185,8 +189,9 @@ int launch_splat(const ScStepRec *recs, const int32_t *tile_start, const int32_t
 }  // namespace
 
 extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
-                        const int32_t *d_items, const float *d_sat, const ScSplatParams *p,
-                        float *d_image, int32_t *d_status, void *stream) {
+                        const int32_t *d_items, const float *d_sat, const float *d_box,
+                        const ScSplatParams *p, float *d_image, int32_t *d_status,
+                        void *stream) {
     (void)d_status;
     sc::TileGeom g;
     int rc = sc::tile_geom(p, g);
@@ -209,6 +214,14 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
     const double b = p->px / p->res;
     c.b_hi = (float)b;
     c.b_lo = (float)(b - (double)c.b_hi);
+    c.box = d_box;
+    c.box_p = p->box_p;
+    c.box_nq = p->box_nq;
+    c.box_stride = (int64_t)p->box_p * p->box_p * p->box_nq * p->box_nq;
+    if (d_box) {
+        SC_REQUIRE(p->box_p >= 1 && p->box_nq == (c.n_signal + p->box_p - 1) / p->box_p + 1,
+                   "sc_splat: box_p=%d / box_nq=%d inconsistent", p->box_p, p->box_nq);
+    }
     const float2 *sat = reinterpret_cast<const float2 *>(d_sat);
     cudaStream_t s = sc::as_stream(stream);
     switch (g.tile) {

@@ -100,6 +100,8 @@ int step_consts(const ScStepParams *p, StepConsts &c) {
     c.norm_coeff = p->norm_coeff;
     c.bleaching = p->bleaching;
     c.with_optinfo = p->with_optinfo;
+    c.box_p = p->box_p;
+    SC_REQUIRE(p->box_p >= 0 && p->box_p < 16384, "box_p=%d out of range", p->box_p);
     c.half_w = (double)p->nw * p->px * 0.5;
     c.half_h = (double)p->nh * p->px * 0.5;
     c.half_sig = p->res * (double)(p->n_signal - 1) * 0.5;

@@ -11,7 +11,7 @@ struct StepConsts {
     double focal[3];
     int nw, nh, n_signal, n_sub, n_particles, max_key;
     double amplitude0, penetration, x_sec, qy, beer, norm_coeff;
-    int bleaching, with_optinfo;
+    int bleaching, with_optinfo, box_p;
     double half_w, half_h, half_sig, inv_res_hi;
 };
 
@@ -31,7 +31,7 @@ __device__ __forceinline__ double emit_photons(const StepConsts &c, double ampli
 __device__ __forceinline__ void axis_footprint(double half_len, double coord, double half_sig,
                                                double px, double res, int n_pix, double &origin,
                                                int16_t &start, int16_t &count, float &a_hi,
-                                               float &a_lo) {
+                                               float &a_lo, double &a) {
     origin = (half_len + coord) - half_sig;
     const double lo = floor(origin / px);
     const double hi = ceil(((half_len + coord) + half_sig) / px);
@@ -40,12 +40,13 @@ __device__ __forceinline__ void axis_footprint(double half_len, double coord, do
     start = 0;
     count = 0;
     a_hi = a_lo = 0.f;
+    a = 0.0;
     if (!(hi_c >= lo_c)) return;
     const int i0 = (int)lo_c;
     const int n = (int)hi_c - i0 + 1;
     start = (int16_t)i0;
     count = (int16_t)n;
-    const double a = (__dmul_rn((double)i0, px) - origin) / res;
+    a = (__dmul_rn((double)i0, px) - origin) / res;
     a_hi = (float)a;
     a_lo = (float)(a - (double)a_hi);
 }
@@ -57,6 +58,9 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     rec.ax_hi = rec.ax_lo = rec.ay_hi = rec.ay_lo = 0.f;
     rec.i_start = rec.j_start = 0;
     rec.n_i = rec.n_j = 0;
+    rec.l0x = rec.l0y = 0;
+    rec.box = 0;
+    rec.pad = 0;
     rec.slot = -1;
     rec.w = 0.f;
     if (norm <= 0.0) return;  // overlay_signal returns early (_epifm.py:216-217)
@@ -80,10 +84,18 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     }
     int16_t si, ni, sj, nj;
     float axh, axl, ayh, ayl;
-    double x0, y0;
-    axis_footprint(c.half_w, rel1, c.half_sig, c.px, c.res, c.nw, x0, si, ni, axh, axl);
-    axis_footprint(c.half_h, rel2, c.half_sig, c.px, c.res, c.nh, y0, sj, nj, ayh, ayl);
+    double x0, y0, ax, ay;
+    axis_footprint(c.half_w, rel1, c.half_sig, c.px, c.res, c.nw, x0, si, ni, axh, axl, ax);
+    axis_footprint(c.half_h, rel2, c.half_sig, c.px, c.res, c.nh, y0, sj, nj, ayh, ayl, ay);
     if (ni < 2 || nj < 2) return;
+    // Box path: with an integer pitch of P grid rows, bound k is ceil(a) + P k
+    // for every k unless a lies within 1e-9 of an integer (FP64 evaluation
+    // noise is ~1e-12 here); those emitters keep the summed-area path.
+    if (c.box_p > 0 && fabs(ax - rint(ax)) > 1e-9 && fabs(ay - rint(ay)) > 1e-9) {
+        rec.box = 1;
+        rec.l0x = (int16_t)ceil(ax);
+        rec.l0y = (int16_t)ceil(ay);
+    }
     rec.x0 = x0;
     rec.y0 = y0;
     rec.ax_hi = axh;

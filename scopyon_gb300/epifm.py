@@ -116,6 +116,7 @@ class EngineConfig:
         self.adc_rounding = str(_gpu_opt(raw, "adc_rounding", "none")) == "round"
         self.boundary = str(_gpu_opt(raw, "boundary", "none"))
         self.tile = int(_gpu_opt(raw, "tile", 0))
+        self.use_box = bool(_gpu_opt(raw, "box_tables", True))
         self.catalog_dir = _gpu_opt(raw, "catalog_dir")
         table = _gpu_opt(raw, "cmos_table")
         self.cmos_table = None if table is None else numpy.asarray(table, dtype=float)
@@ -164,6 +165,23 @@ class EngineConfig:
         return len(numpy.arange(0.0, self.radial_cutoff, PSF_RES, dtype=float))
 
     @property
+    def box_p(self):
+        """Grid rows per pixel when px / 1 nm is an integer P (box tables apply), else 0.
+
+        The box path needs bound k = ceil(a) + P k for every bound of a
+        footprint; with |px/res - P| * (bounds per footprint) below 1e-10 the
+        drift stays far inside the 1e-9 margin the records test for.
+        """
+        if not self.use_box:
+            return 0
+        b = self.px / PSF_RES
+        p = int(round(b))
+        n_signal = 2 * self.n_r - 1
+        if p < 1 or abs(b - p) * (n_signal / p + 3) >= 1e-10:
+            return 0
+        return p
+
+    @property
     def max_key(self):
         return int((self.depth_cutoff + PSF_RES) / PSF_RES) + 1
 
@@ -191,6 +209,11 @@ class PSFTables:
         self.key_slot = torch.full((self.max_key + 2,), -1, dtype=torch.int32, device=device)
         self.tables = torch.empty(0, dtype=torch.float32, device=device)
         self.capacity = 0
+        self.box_p = cfg.box_p
+        n_signal = 2 * self.n_r - 1
+        self.box_nq = (n_signal + self.box_p - 1) // self.box_p + 1 if self.box_p else 0
+        self.box_floats = self.box_p ** 2 * self.box_nq ** 2
+        self.box = torch.empty(0, dtype=torch.float32, device=device) if self.box_p else None
 
     def _depth_of_key(self, key):
         return self.cfg.depth_cutoff if key < 0 else key * PSF_RES
@@ -202,6 +225,11 @@ class PSFTables:
         new = torch.empty(cap * self.table_floats, dtype=torch.float32, device=self.device)
         if self.capacity:
             new[: self.capacity * self.table_floats].copy_(self.tables)
+        if self.box_p:
+            nbox = torch.empty(cap * self.box_floats, dtype=torch.float32, device=self.device)
+            if self.capacity:
+                nbox[: self.capacity * self.box_floats].copy_(self.box)
+            self.box = nbox
         self.tables, self.capacity = new, cap
 
     def ensure(self, keys, stream=None):
@@ -228,6 +256,10 @@ class PSFTables:
             out = self.tables[first * self.table_floats: (first + len(chunk)) * self.table_floats]
             call("sc_psf_quadrant_sat", ptr(radial), len(chunk), self.n_r, PSF_RES, ptr(out),
                  self.pitch, s)
+            if self.box_p:
+                bout = self.box[first * self.box_floats: (first + len(chunk)) * self.box_floats]
+                call("sc_psf_box_table", ptr(out), len(chunk), self.n_r, self.pitch, self.box_p,
+                     ptr(bout), s)
             for j, k in enumerate(chunk):
                 self.slot_of[k] = first + j
                 self.key_slot_host[k if k >= 0 else self.max_key + 1] = first + j
@@ -385,6 +417,7 @@ class FramePipeline:
         p.norm_coeff = float(cfg.norm_coeff)
         p.bleaching = 1 if cfg.bleaching else 0
         p.with_optinfo = 1 if with_optinfo else 0
+        p.box_p = self.psf.box_p
         return p
 
     def splat_params(self, n_images=1, rec_per_image=0):
@@ -393,6 +426,7 @@ class FramePipeline:
         p.tiles_x, p.tiles_y = self.tiles_x, self.tiles_y
         p.n_r, p.sat_pitch = self.psf.n_r, self.psf.pitch
         p.n_images, p.rec_per_image = n_images, rec_per_image
+        p.box_p, p.box_nq = self.psf.box_p, self.psf.box_nq
         p.px, p.res = self.cfg.px, PSF_RES
         return p
 
@@ -413,8 +447,8 @@ class FramePipeline:
         if ev is not None:
             e0 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-        call("sc_splat", ptr(recs), ptr(tile_start), ptr(items), ptr(self.psf.tables), sp,
-             ptr(image), ptr(self.status), s)
+        call("sc_splat", ptr(recs), ptr(tile_start), ptr(items), ptr(self.psf.tables),
+             ptr(self.psf.box), sp, ptr(image), ptr(self.status), s)
         if ev is not None:
             e1 = torch.cuda.Event(enable_timing=True)
             e1.record(stream)

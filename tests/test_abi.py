@@ -55,13 +55,13 @@ def test_host_side_validation_needs_no_gpu():
     assert b"n_keys" in L.sc_last_error()
     p = _lib.SplatParams(nw=64, nh=64, tile=12, tiles_x=6, tiles_y=6, n_r=1000, sat_pitch=1004,
                          n_images=1, rec_per_image=0, px=1.6e-7, res=1e-9)
-    assert L.sc_splat(None, None, None, None, ctypes.byref(p), None, None, None) == _lib.SC_ERR_ARG
+    assert L.sc_splat(None, None, None, None, None, ctypes.byref(p), None, None, None) == _lib.SC_ERR_ARG
     assert L.sc_bin_workspace_bytes(0, 16) == 0
     assert L.sc_bin_capacity(100, 1.6e-7, 1e-9, 1999, 32) == 100 * 4
 
 
 def test_struct_sizes_match_c_layout():
     from scopyon_gb300 import _lib
-    assert ctypes.sizeof(_lib.StepParams) == 128
-    assert ctypes.sizeof(_lib.SplatParams) == 56
+    assert ctypes.sizeof(_lib.StepParams) == 136
+    assert ctypes.sizeof(_lib.SplatParams) == 64
     assert ctypes.sizeof(_lib.CameraParams) == 104

@@ -69,6 +69,33 @@ def test_quadrant_sat(lib, golden):
         assert numpy.abs(val - ref).max() <= 4 * 2.0 ** -48 * ref.max()
 
 
+def test_box_table(lib, golden):
+    """Box-integrated entries against FP64 sums of the full cartesian grid."""
+    radial = golden["psf_tritc_radial"][[3]]
+    pitch, P = 1004, 160
+    sat = torch.zeros(1001 * pitch * 2, dtype=torch.float32, device="cuda")
+    lib.call("sc_psf_quadrant_sat", lib.ptr(_dev(radial)), 1, 1000, 1e-9, lib.ptr(sat), pitch,
+             lib.stream_ptr())
+    nq = (1999 + P - 1) // P + 1
+    box = torch.zeros(P * P * nq * nq, dtype=torch.float32, device="cuda")
+    lib.call("sc_psf_box_table", lib.ptr(sat), 1, 1000, pitch, P, lib.ptr(box), lib.stream_ptr())
+    got = box.cpu().numpy().reshape(P, P, nq, nq)
+    full = O.radial_to_cartesian(O.radial_grid(), radial[0])
+    csum = numpy.zeros((2000, 2000))
+    csum[1:, 1:] = full.cumsum(0).cumsum(1)
+    rng = numpy.random.RandomState(0)
+    for _ in range(400):
+        rx, ry = rng.randint(P, size=2)
+        qx, qy = rng.randint(nq, size=2)
+        mx, my = qx * P + rx - P, qy * P + ry - P
+        a0, a1 = max(mx, 0), min(mx + P, 1999)
+        b0, b1 = max(my, 0), min(my + P, 1999)
+        ref = 0.0 if a1 <= a0 or b1 <= b0 else (
+            csum[a1, b1] - csum[a0, b1] - csum[a1, b0] + csum[a0, b0])
+        v = got[rx, ry, qx, qy]
+        assert abs(v - ref) <= 2e-7 * abs(ref) + 1e-9 * csum[-1, -1] * 1e-9, (rx, ry, qx, qy)
+
+
 def _config_from_tree(tree, **gpu):
     import scopyon_gb300 as sg
     tree = json.loads(json.dumps(tree))
@@ -76,10 +103,14 @@ def _config_from_tree(tree, **gpu):
     return sg.Configuration(yaml=tree)
 
 
+@pytest.mark.parametrize("box", [True, False])
 @pytest.mark.parametrize("depth_idx", [0, 3])
 @pytest.mark.parametrize("case", ["c40_px160", "c96x64_px66"])
-def test_single_emitter_footprints(lib, golden, case, depth_idx):
-    """One emitter per sub-step through steps -> bin -> splat, against overlay_signal_."""
+def test_single_emitter_footprints(lib, golden, case, depth_idx, box):
+    """One emitter per sub-step through steps -> bin -> splat, against overlay_signal_.
+
+    box=True takes the box-table path where it applies (integer px, generic
+    positions); box=False forces the summed-area path everywhere."""
     from scopyon_gb300.config import DefaultConfiguration
     from scopyon_gb300.epifm import EngineConfig, FramePipeline
     px = float(golden["ov_%s_px" % case])
@@ -88,9 +119,10 @@ def test_single_emitter_footprints(lib, golden, case, depth_idx):
     cfg.update({"default": {
         "magnification": 1.0, "detector": {"pixel_length": px, "image_size": list(shape)},
         "effects": {"photo_bleaching": {"switch": False}},
-        "gpu": {"psf_wavelength": 5.78e-07}}})
+        "gpu": {"psf_wavelength": 5.78e-07, "box_tables": box}}})
     eng = EngineConfig(cfg["default"])
     assert eng.px == px
+    assert eng.box_p == (160 if (box and case == "c40_px160") else 0)
     pipe = FramePipeline(eng, "cuda")
     depth = float(golden["psf_depths"][depth_idx])
     n_emit = eng.qy * (eng.amplitude0 * numpy.exp(-abs(depth) / eng.penetration) * eng.x_sec

@@ -55,16 +55,20 @@ def workload_config():
     return cfg
 
 
+Z_HALF = 1e-6  # depth range [-Z_HALF, Z_HALF]; --small narrows it for profiling
+D_FAST = 1.0e-12  # m^2/s of the faster half of the emitters
+
+
 def trajectories(n_frames, seed=7):
-    """(n_frames*SUBSTEPS + 1, N, 5) formatted [depth, x, y, m_id, p_state] and raw inputs."""
+    """Times and (n_frames*SUBSTEPS + 1, N, 3) Brownian positions (x, y, z)."""
     rng = numpy.random.RandomState(seed)
     steps = n_frames * SUBSTEPS
     dt = EXPOSURE / SUBSTEPS
     pos = numpy.empty((steps + 1, N_EMIT, 3))
     pos[0, :, 0] = rng.uniform(-HALF, HALF, N_EMIT)
     pos[0, :, 1] = rng.uniform(-HALF, HALF, N_EMIT)
-    pos[0, :, 2] = rng.uniform(-1e-6, 1e-6, N_EMIT)
-    d = numpy.where(numpy.arange(N_EMIT) < N_EMIT // 2, 0.01e-12, 1.0e-12)
+    pos[0, :, 2] = rng.uniform(-Z_HALF, Z_HALF, N_EMIT)
+    d = numpy.where(numpy.arange(N_EMIT) < N_EMIT // 2, 0.01e-12, D_FAST)
     scale = numpy.sqrt(2 * d * dt)[:, None]
     for t in range(steps):
         pos[t + 1] = pos[t] + scale * rng.standard_normal((N_EMIT, 3))
@@ -131,16 +135,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def splat_algorithmic_bytes(n_rec):
-    """Bytes one splat launch must move: records, quadrant-table entries, image.
+def splat_algorithmic_bytes(n_rec, tile, halo):
+    """Bytes one splat (halo kernel + merge) must move.
 
-    Per emitter-step: its 48-byte record, and the (n_b + 2)^2 distinct 8-byte
-    quadrant-table entries of its footprint, n_b = ceil(1999 nm / px) + 1
-    bounds per axis (the +2: the fold's centre knots).  Plus one float write
-    per image pixel.
+    Per emitter-step: its item index (4 B), the 32-byte record head, and the
+    footprint's box-table block: (n_px)^2 FP32 pixel sums, n_px =
+    ceil(1998 nm / px) + 1 pixels per axis on average.  Per tile: the FP64
+    (tile + halo)^2 buffer written and read back by the merge; per pixel one
+    FP32 image write.
     """
-    n_b = math.ceil(1999e-9 / PX) + 1
-    return n_rec * (48 + 8 * (n_b + 2) ** 2) + 4 * IMAGE * IMAGE
+    n_px = 1998e-9 / PX + 1
+    n_tiles = (IMAGE // tile) ** 2
+    return (n_rec * (4 + 32 + 4 * n_px * n_px) + n_tiles * (tile + halo) ** 2 * 8 * 2
+            + 4 * IMAGE * IMAGE)
 
 
 def load_peaks():
@@ -167,12 +174,14 @@ def gb300_arm(args, rank, world):
     pipe = FramePipeline(eng, dev, psf=_psf_for(eng, dev))
     pipe.scmos_sigma_map(rng)
     t0 = time.time()
-    pipe.psf.ensure_all()
-    torch.cuda.synchronize()
-    psf_build_s = time.time() - t0
-
     n_frames = args.warmup + args.steps
     times, pos = trajectories(n_frames, seed=7 + rank)
+    if args.small:
+        pipe.psf.ensure(eng.depth_keys(pos[..., 2].ravel() - eng.focal_point[0]))
+    else:
+        pipe.psf.ensure_all()
+    torch.cuda.synchronize()
+    psf_build_s = time.time() - t0
     traj = torch.from_numpy(formatted(pos)).to(dev)
     ut = torch.full((SUBSTEPS,), EXPOSURE / SUBSTEPS, dtype=torch.float64, device=dev)
     pipe.ensure_slots(N_EMIT)
@@ -215,11 +224,11 @@ def gb300_arm(args, rank, world):
     ms_per_step = elapsed_ms / args.steps
     value = world * args.steps / (elapsed_ms / 1e3)
 
-    e2e = e2e_arm(args, cfg, dev, rank, world)
+    e2e = None if args.small else e2e_arm(args, cfg, dev, rank, world)
 
     splat_avg_ms = sum(splat_ms) / len(splat_ms)
     n_rec = SUBSTEPS * N_EMIT
-    alg = splat_algorithmic_bytes(n_rec)
+    alg = splat_algorithmic_bytes(n_rec, pipe.tile, pipe.halo)
     peak, peak_kind = load_peaks()
     achieved = alg / (splat_avg_ms / 1e3) / 1e9
     traffic = os.environ.get("SC_SPLAT_TRAFFIC_BYTES")
@@ -228,9 +237,11 @@ def gb300_arm(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform positions, Gaussian Brownian steps)",
-        "config": {"workload": WORKLOAD, "n_emitters": N_EMIT, "image": [IMAGE, IMAGE],
+        "config": {"workload": WORKLOAD + ("_z0.1um_profiling" if args.small else ""),
+                   "n_emitters": N_EMIT, "image": [IMAGE, IMAGE],
                    "substeps": SUBSTEPS, "exposure_s": EXPOSURE, "pixel_nm": PX * 1e9,
                    "camera": "sCMOS per-pixel sigma, 12-bit", "psf": "Born-Wolf TRITC, 1002 depth keys",
+                   "tile": pipe.tile, "warps_per_tile": pipe.warps,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (PSF tables %.1f GB)" % (
                        (pipe.psf.tables.numel() + (pipe.psf.box.numel() if pipe.psf.box is not None
@@ -239,7 +250,7 @@ def gb300_arm(args, rank, world):
         "e2e": e2e,
         "gpu_launches": 7 * args.steps,
         "clocks": clk,
-        "roofline": {"kernel": "splat_tile_kernel", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": "splat_halo_kernel + splat_merge_kernel", "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
                      "traffic": float(traffic) if traffic else None,
@@ -383,7 +394,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="profiling case: depth range +-0.1 um and D = 0.01 um^2/s for all "
+                         "emitters (about 130 PSF keys, 3.7 GB of tables), no e2e or CPU legs")
     args = ap.parse_args()
+    if args.small:
+        global Z_HALF, D_FAST
+        Z_HALF, D_FAST = 0.1e-6, 0.01e-12
+        args.no_cpu = True
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     world = int(os.environ.get("WORLD_SIZE", "1"))

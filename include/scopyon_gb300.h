@@ -40,18 +40,19 @@ extern "C" {
  *     bit3 RNG loop bound hit, bit4 capacity), [1..3] first offending index. */
 #define SC_STATUS_WORDS 4
 
-/* One emitter during one exposure sub-step, ready to be splatted (56 bytes). */
+/* One emitter during one exposure sub-step, ready to be splatted (64 bytes).
+ * The first 32 bytes are all the box path reads. */
 typedef struct {
+    int64_t box_off;     /* box path: float index of pixel (i_start, j_start)'s entry */
+    int16_t i_start, n_i;/* first pixel index and number of footprint bounds along x  */
+    int16_t j_start, n_j;/* same along y; n_i < 2 or n_j < 2 means nothing to splat   */
+    float w;             /* normalisation * res^2: photons per unit table sum          */
+    int32_t slot;        /* PSF table slot of the depth key; -1: nothing to splat      */
+    int32_t box;         /* 1: bounds are l0 + P*k exactly, use the box table          */
+    int32_t pad;
     double x0, y0;       /* footprint origin along x / y in metres (exact FP64)      */
     float ax_hi, ax_lo;  /* (i_start*px - x0)/res as a double-float                   */
     float ay_hi, ay_lo;  /* (j_start*px - y0)/res as a double-float                   */
-    int16_t i_start, n_i;/* first pixel index and number of footprint bounds along x  */
-    int16_t j_start, n_j;/* same along y; n_i < 2 or n_j < 2 means nothing to splat   */
-    int16_t l0x, l0y;    /* first footprint bound along x / y before clamping          */
-    int16_t box;         /* 1: bounds are l0 + P*k exactly, use the box table          */
-    int16_t pad;
-    int32_t slot;        /* PSF table slot of the depth key                           */
-    float w;             /* normalisation * res^2: photons per unit table sum          */
 } ScStepRec;
 
 typedef struct {
@@ -75,12 +76,14 @@ typedef struct {
     int32_t bleaching;       /* 1: photon-budget bleaching on                              */
     int32_t with_optinfo;    /* 1: accumulate the 8-vector true_data per particle          */
     int32_t box_p;           /* px / res when it is an integer P (box tables built), else 0 */
-    int32_t pad0;
+    int32_t box_nq;          /* pixel offsets per box-table axis, (n_signal+P-1)/P + 1      */
 } ScStepParams;
 
 typedef struct {
     int32_t nw, nh;          /* image size                                                 */
-    int32_t tile;            /* tile edge in pixels (8..64, multiple of 8)                 */
+    int32_t tile;            /* tile edge in pixels (8, 16 or 32)                          */
+    int32_t halo;            /* pixels a footprint reaches past its first: ceil(sw/px) + 1 */
+    int32_t warps;           /* warps per tile CTA (4 or 8)                                */
     int32_t tiles_x, tiles_y;
     int32_t n_r;             /* radial samples; quadrant table is (n_r+1)^2               */
     int32_t sat_pitch;       /* row pitch of one quadrant table in float2 entries          */
@@ -148,24 +151,29 @@ int sc_emitter_steps(const ScStepParams *p, const double *d_particles,
                      double *d_budget, double *d_optinfo, ScStepRec *d_recs,
                      int32_t *d_status, void *stream);
 
-/* Bytes of scratch sc_bin_steps needs for n_rec records on a tile grid. */
+/* Bytes of scratch sc_bin_steps needs for n_rec records on n_tiles_total tiles. */
 size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total);
-/* Upper bound of bin entries (record, tile) for n_rec records. */
-int64_t sc_bin_capacity(int n_rec, double px, double res, int n_signal, int tile);
 
-/* Deterministic counting sort of records by output tile (new; the reference
- * splats particle by particle, src/scopyon/_epifm.py:1262-1264).           */
+/* Deterministic counting sort of records by the tile that holds their first
+ * footprint pixel; d_items receives n_rec record indices grouped by tile,
+ * d_tile_start (n_tiles + 1) the group offsets.  (New: the reference adds
+ * particle by particle, src/scopyon/_epifm.py:1262-1264.)                  */
 int sc_bin_steps(const ScStepRec *d_recs, int n_rec,
                  const ScSplatParams *p, void *d_ws, size_t ws_bytes,
-                 int32_t *d_tile_start, int32_t *d_items, int64_t capacity,
-                 int32_t *d_status, void *stream);
+                 int32_t *d_tile_start, int32_t *d_items, int32_t *d_status, void *stream);
 
-/* Tile splat: each CTA owns one output tile and sums the footprint integrals
- * of the records binned to it.  Replaces overlay_signal_
- * (src/scopyon/_epifm.py:224-282) for every particle and sub-step.          */
+/* Bytes of scratch sc_splat needs: one FP64 (tile + halo)^2 buffer per tile. */
+size_t sc_splat_workspace_bytes(const ScSplatParams *p);
+
+/* Splat: each CTA sums the whole footprints of the records binned to its
+ * tile into a (tile + halo)^2 buffer in shared memory and stores it in the
+ * workspace; a second pass adds the overlapping buffers into d_image.
+ * Replaces overlay_signal_ (src/scopyon/_epifm.py:224-282) for every
+ * particle and sub-step.                                                    */
 int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
              const int32_t *d_items, const float *d_sat, const float *d_box,
-             const ScSplatParams *p, float *d_image, int32_t *d_status, void *stream);
+             const ScSplatParams *p, void *d_ws, size_t ws_bytes, float *d_image,
+             int32_t *d_status, void *stream);
 
 /* Camera model and ADC.  Replaces _EPIFMSimulator.__detector_output, the
  * EMCCD / CCD / CMOS classes and __get_analog_to_digital_converter_counts

@@ -9,12 +9,12 @@ import os
 import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libscopyon_gb300.so")
+LIB_PATH = os.environ.get("SCOPYON_GB300_LIB") or os.path.join(HERE, "libscopyon_gb300.so")
 
 SC_OK, SC_ERR_ARG, SC_ERR_CUDA, SC_ERR_TIMEOUT, SC_ERR_NAN, SC_ERR_CAPACITY = 0, -1, -2, -3, -4, -5
 PSF_BORN_WOLF, PSF_GAUSSIAN = 0, 1
 CAM_EMCCD, CAM_CCD, CAM_CMOS_TABLE, CAM_SCMOS = 0, 1, 2, 3
-STEP_REC_BYTES = 56
+STEP_REC_BYTES = 64
 STATUS_WORDS = 4
 
 c_double_p = ctypes.c_void_p  # device pointers travel as integers
@@ -30,11 +30,12 @@ class StepParams(ctypes.Structure):
                 ("x_sec", ctypes.c_double), ("qy", ctypes.c_double), ("beer", ctypes.c_double),
                 ("norm_coeff", ctypes.c_double),
                 ("bleaching", ctypes.c_int32), ("with_optinfo", ctypes.c_int32),
-                ("box_p", ctypes.c_int32), ("pad0", ctypes.c_int32)]
+                ("box_p", ctypes.c_int32), ("box_nq", ctypes.c_int32)]
 
 
 class SplatParams(ctypes.Structure):
     _fields_ = [("nw", ctypes.c_int32), ("nh", ctypes.c_int32), ("tile", ctypes.c_int32),
+                ("halo", ctypes.c_int32), ("warps", ctypes.c_int32),
                 ("tiles_x", ctypes.c_int32), ("tiles_y", ctypes.c_int32),
                 ("n_r", ctypes.c_int32), ("sat_pitch", ctypes.c_int32),
                 ("n_images", ctypes.c_int32), ("rec_per_image", ctypes.c_int32),
@@ -63,10 +64,11 @@ _SIG = {
     "sc_psf_box_table": (_I, [_P, _I, _I, _I, _I, _P, _P]),
     "sc_emitter_steps": (_I, [ctypes.POINTER(StepParams), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sc_bin_workspace_bytes": (ctypes.c_size_t, [_I, _I]),
-    "sc_bin_capacity": (ctypes.c_int64, [_I, _D, _D, _I, _I]),
-    "sc_bin_steps": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P, _P,
-                          ctypes.c_int64, _P, _P]),
-    "sc_splat": (_I, [_P, _P, _P, _P, _P, ctypes.POINTER(SplatParams), _P, _P, _P]),
+    "sc_bin_steps": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P, _P, _P,
+                          _P]),
+    "sc_splat_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(SplatParams)]),
+    "sc_splat": (_I, [_P, _P, _P, _P, _P, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P,
+                      _P, _P]),
     "sc_camera": (_I, [ctypes.POINTER(CameraParams), _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                        _P, _P, _P, _P, _P]),
     "sc_emccd_exact": (_I, [_P, _D, _D, _P, _I, _D, _P, _P, _P]),

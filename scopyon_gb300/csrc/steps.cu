@@ -16,29 +16,33 @@
 
 namespace {
 
-__global__ void emitter_steps_kernel(sc::StepConsts c, const double *particles,
-                                     const double *unit_time, const uint8_t *present,
-                                     const int32_t *key_slot, double *budget, double *optinfo,
-                                     ScStepRec *recs, int32_t *status) {
+// Pass 1, one thread per particle slot, sub-steps in order: excitation,
+// emitted photons, the photon-budget chain and the normalisation.  The
+// normalisation of each (sub-step, slot) is parked in its record's x0 field
+// for pass 2 (0: nothing to splat).
+__global__ void emitter_physics_kernel(sc::StepConsts c, const double *particles,
+                                       const double *unit_time, const uint8_t *present,
+                                       double *budget, double *optinfo, ScStepRec *recs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n_particles) return;
     double b = c.bleaching ? budget[i] : 0.0;
     double acc[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) acc[k] = 0.0;
+    const bool epi = isinf(c.penetration);
     for (int s = 0; s < c.n_sub; ++s) {
-        const double *q = particles + ((size_t)s * c.n_particles + i) * 5;
-        ScStepRec *out = recs + (size_t)s * c.n_particles + i;
-        if (present && !present[(size_t)s * c.n_particles + i]) {
-            out->n_i = out->n_j = 0;  // absent at this sub-step: no record, no state change
+        const size_t idx = (size_t)s * c.n_particles + i;
+        const double *q = particles + idx * 5;
+        if (present && !present[idx]) {
+            recs[idx].x0 = 0.0;  // absent at this sub-step: no record, no state change
             continue;
         }
         const double ut = unit_time[s];
         double p_state = q[4];
         const double rel0 = q[0] - c.focal[0];
-        const double rel1 = q[1] - c.focal[1];
-        const double rel2 = q[2] - c.focal[2];
-        const double amp = __dmul_rn(c.amplitude0, exp(-fabs(rel0) / c.penetration));
+        // amplitude0 * exp(-|depth| / inf) is amplitude0 exactly
+        const double amp = epi ? c.amplitude0
+                               : __dmul_rn(c.amplitude0, exp(-fabs(rel0) / c.penetration));
         const double n_emit = sc::emit_photons(c, amp, ut);
         if (c.bleaching) {
             double nb = b - n_emit;
@@ -49,9 +53,7 @@ __global__ void emitter_steps_kernel(sc::StepConsts c, const double *particles,
             b = nb;
         }
         const double norm = __dmul_rn(c.norm_coeff, __dmul_rn(p_state, n_emit) / (4.0 * M_PI));
-        ScStepRec rec;
-        sc::make_record(c, rel0, rel1, rel2, norm, key_slot, status, i, s, rec);
-        *out = rec;
+        recs[idx].x0 = norm;
         if (c.with_optinfo) {
             acc[0] += ut;
             acc[1] += __dmul_rn(ut, p_state);
@@ -68,6 +70,20 @@ __global__ void emitter_steps_kernel(sc::StepConsts c, const double *particles,
 #pragma unroll
         for (int k = 0; k < 8; ++k) optinfo[(size_t)i * 8 + k] = acc[k];
     }
+}
+
+// Pass 2, one thread per (sub-step, slot): depth key and footprint.
+__global__ void emitter_footprint_kernel(sc::StepConsts c, const double *particles,
+                                         const int32_t *key_slot, ScStepRec *recs,
+                                         int32_t *status) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)c.n_sub * c.n_particles) return;
+    const double norm = recs[idx].x0;
+    const double *q = particles + idx * 5;
+    ScStepRec rec;
+    sc::make_record(c, q[0] - c.focal[0], q[1] - c.focal[1], q[2] - c.focal[2], norm, key_slot,
+                    status, (int)(idx % c.n_particles), (int)(idx / c.n_particles), rec);
+    recs[idx] = rec;
 }
 
 }  // namespace
@@ -101,11 +117,15 @@ int step_consts(const ScStepParams *p, StepConsts &c) {
     c.bleaching = p->bleaching;
     c.with_optinfo = p->with_optinfo;
     c.box_p = p->box_p;
+    c.box_nq = p->box_nq;
     SC_REQUIRE(p->box_p >= 0 && p->box_p < 16384, "box_p=%d out of range", p->box_p);
+    SC_REQUIRE(p->box_p == 0 || p->box_nq == (p->n_signal + p->box_p - 1) / p->box_p + 1,
+               "box_nq=%d inconsistent with box_p=%d", p->box_nq, p->box_p);
     c.half_w = (double)p->nw * p->px * 0.5;
     c.half_h = (double)p->nh * p->px * 0.5;
     c.half_sig = p->res * (double)(p->n_signal - 1) * 0.5;
-    c.inv_res_hi = 0.0;
+    c.inv_px = 1.0 / p->px;
+    c.inv_res = 1.0 / p->res;
     return SC_OK;
 }
 
@@ -124,8 +144,11 @@ extern "C" int sc_emitter_steps(const ScStepParams *p, const double *d_particles
                "sc_emitter_steps: NULL input/output pointer");
     SC_REQUIRE(!c.bleaching || d_budget, "sc_emitter_steps: bleaching needs a budget array");
     SC_REQUIRE(!c.with_optinfo || d_optinfo, "sc_emitter_steps: optinfo output is NULL");
-    const int block = 128;
-    emitter_steps_kernel<<<(c.n_particles + block - 1) / block, block, 0, sc::as_stream(stream)>>>(
-        c, d_particles, d_unit_time, d_present, d_key_slot, d_budget, d_optinfo, d_recs, d_status);
+    cudaStream_t st = sc::as_stream(stream);
+    emitter_physics_kernel<<<(c.n_particles + 127) / 128, 128, 0, st>>>(
+        c, d_particles, d_unit_time, d_present, d_budget, d_optinfo, d_recs);
+    const int64_t n_rec = (int64_t)c.n_sub * c.n_particles;
+    emitter_footprint_kernel<<<(unsigned)((n_rec + 255) / 256), 256, 0, st>>>(
+        c, d_particles, d_key_slot, d_recs, d_status);
     return sc::launch_status("sc_emitter_steps");
 }

@@ -11,8 +11,8 @@ struct StepConsts {
     double focal[3];
     int nw, nh, n_signal, n_sub, n_particles, max_key;
     double amplitude0, penetration, x_sec, qy, beer, norm_coeff;
-    int bleaching, with_optinfo, box_p;
-    double half_w, half_h, half_sig, inv_res_hi;
+    int bleaching, with_optinfo, box_p, box_nq;
+    double half_w, half_h, half_sig, inv_px, inv_res;
 };
 
 int step_consts(const ScStepParams *p, StepConsts &c);
@@ -26,15 +26,35 @@ __device__ __forceinline__ double emit_photons(const StepConsts &c, double ampli
     return __dmul_rn(__dmul_rn(c.qy, n_abs), c.beer);
 }
 
+// floor(x / d) and ceil(x / d) as the reference computes them (one correctly
+// rounded FP64 division, then floor / ceil).  The quotient is estimated with a
+// multiplication by 1/d (relative error ~2^-51); only when the estimate lies
+// within 1e-9 of an integer, where the rounding of the true division could
+// decide the result, is the division itself evaluated.  FP64 division costs
+// dozens of instructions on this GPU; the estimate costs one.
+__device__ __forceinline__ double floor_div(double x, double d, double inv_d) {
+    const double q = x * inv_d;
+    if (fabs(q - rint(q)) > 1e-9 * fmax(1.0, fabs(q))) return floor(q);
+    return floor(x / d);
+}
+
+__device__ __forceinline__ double ceil_div(double x, double d, double inv_d) {
+    const double q = x * inv_d;
+    if (fabs(q - rint(q)) > 1e-9 * fmax(1.0, fabs(q))) return ceil(q);
+    return ceil(x / d);
+}
+
 // Footprint of one axis (_epifm.py:233-258): first pixel, number of bounds,
-// the exact FP64 origin and the first bound's unrounded value as a double-float.
+// the exact FP64 origin and the first bound's unrounded value (to ~1e-13),
+// also as a double-float.
 __device__ __forceinline__ void axis_footprint(double half_len, double coord, double half_sig,
-                                               double px, double res, int n_pix, double &origin,
-                                               int16_t &start, int16_t &count, float &a_hi,
-                                               float &a_lo, double &a) {
+                                               double px, double inv_px, double inv_res,
+                                               int n_pix, double &origin, int16_t &start,
+                                               int16_t &count, float &a_hi, float &a_lo,
+                                               double &a) {
     origin = (half_len + coord) - half_sig;
-    const double lo = floor(origin / px);
-    const double hi = ceil(((half_len + coord) + half_sig) / px);
+    const double lo = floor_div(origin, px, inv_px);
+    const double hi = ceil_div((half_len + coord) + half_sig, px, inv_px);
     const double lo_c = fmax(lo, 0.0);
     const double hi_c = fmin(hi, (double)n_pix);
     start = 0;
@@ -46,7 +66,7 @@ __device__ __forceinline__ void axis_footprint(double half_len, double coord, do
     const int n = (int)hi_c - i0 + 1;
     start = (int16_t)i0;
     count = (int16_t)n;
-    a = (__dmul_rn((double)i0, px) - origin) / res;
+    a = (__dmul_rn((double)i0, px) - origin) * inv_res;
     a_hi = (float)a;
     a_lo = (float)(a - (double)a_hi);
 }
@@ -54,11 +74,11 @@ __device__ __forceinline__ void axis_footprint(double half_len, double coord, do
 __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, double rel1,
                                             double rel2, double norm, const int32_t *key_slot,
                                             int32_t *status, int i, int s, ScStepRec &rec) {
+    rec.box_off = 0;
     rec.x0 = rec.y0 = 0.0;
     rec.ax_hi = rec.ax_lo = rec.ay_hi = rec.ay_lo = 0.f;
     rec.i_start = rec.j_start = 0;
     rec.n_i = rec.n_j = 0;
-    rec.l0x = rec.l0y = 0;
     rec.box = 0;
     rec.pad = 0;
     rec.slot = -1;
@@ -67,7 +87,7 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     const double depth = fabs(rel0);
     int key;
     if (depth < c.depth_cutoff + c.res) {
-        const double kd = depth / c.res;
+        const double kd = floor_div(depth, c.res, c.inv_res);  // int() of a non-negative
         if (kd > (double)c.max_key) {
             flag_status(status, 0, i, s, 0);
             return;
@@ -85,16 +105,23 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     int16_t si, ni, sj, nj;
     float axh, axl, ayh, ayl;
     double x0, y0, ax, ay;
-    axis_footprint(c.half_w, rel1, c.half_sig, c.px, c.res, c.nw, x0, si, ni, axh, axl, ax);
-    axis_footprint(c.half_h, rel2, c.half_sig, c.px, c.res, c.nh, y0, sj, nj, ayh, ayl, ay);
+    axis_footprint(c.half_w, rel1, c.half_sig, c.px, c.inv_px, c.inv_res, c.nw, x0, si, ni, axh,
+                   axl, ax);
+    axis_footprint(c.half_h, rel2, c.half_sig, c.px, c.inv_px, c.inv_res, c.nh, y0, sj, nj, ayh,
+                   ayl, ay);
     if (ni < 2 || nj < 2) return;
     // Box path: with an integer pitch of P grid rows, bound k is ceil(a) + P k
     // for every k unless a lies within 1e-9 of an integer (FP64 evaluation
-    // noise is ~1e-12 here); those emitters keep the summed-area path.
+    // noise and the estimate of a are ~1e-12 here); those emitters keep the
+    // summed-area path.
     if (c.box_p > 0 && fabs(ax - rint(ax)) > 1e-9 && fabs(ay - rint(ay)) > 1e-9) {
+        // entry of pixel (i_start, j_start) in the phase-major box table of the
+        // key: first rows m = l0 + P >= 1 split as (m mod P, m div P)
+        const int P = c.box_p, NQ = c.box_nq;
+        const int mx = (int)ceil(ax) + P, my = (int)ceil(ay) + P;
         rec.box = 1;
-        rec.l0x = (int16_t)ceil(ax);
-        rec.l0y = (int16_t)ceil(ay);
+        rec.box_off = (int64_t)slot * ((int64_t)P * P * NQ * NQ) +
+                      ((int64_t)((mx % P) * P + (my % P)) * NQ + mx / P) * NQ + my / P;
     }
     rec.x0 = x0;
     rec.y0 = y0;

@@ -337,7 +337,12 @@ class FramePipeline:
         self.inv_gain_f = (1.0 / self.gain).float()
         self.sigma = None
         self.table_value = self.table_cdf = None
-        self.tile = cfg.tile or self._pick_tile()
+        n_signal = 2 * self.psf.n_r - 1
+        # pixels a footprint reaches past its first one
+        self.halo = int(math.ceil(PSF_RES * (n_signal - 1) / cfg.px)) + 1
+        self.tile, self.warps = self._pick_tile()
+        if cfg.tile:
+            self.tile = cfg.tile
         self.tiles_x = (nw + self.tile - 1) // self.tile
         self.tiles_y = (nh + self.tile - 1) // self.tile
         self._cap = {}
@@ -347,7 +352,12 @@ class FramePipeline:
         self.kernel_events = None
 
     def _pick_tile(self):
-        return 32 if self.cfg.px >= 90e-9 else 64
+        """(tile edge, warps per tile CTA) that fit shared memory; see tune_tiles."""
+        for tile, warps in ((16, 4), (8, 4), (8, 2), (8, 1)):
+            edge = tile + self.halo
+            if 2 * warps * edge * edge * 4 + warps * 2 * (edge + 2) * 4 <= 200 * 1024:
+                return tile, warps
+        raise ValueError("pixel size %g m is too small for the splat's shared memory" % self.cfg.px)
 
     def _camera_kind(self):
         t = self.cfg.detector_type
@@ -417,12 +427,13 @@ class FramePipeline:
         p.norm_coeff = float(cfg.norm_coeff)
         p.bleaching = 1 if cfg.bleaching else 0
         p.with_optinfo = 1 if with_optinfo else 0
-        p.box_p = self.psf.box_p
+        p.box_p, p.box_nq = self.psf.box_p, self.psf.box_nq
         return p
 
     def splat_params(self, n_images=1, rec_per_image=0):
         p = _lib.SplatParams()
         p.nw, p.nh, p.tile = self.nw, self.nh, self.tile
+        p.halo, p.warps = self.halo, self.warps
         p.tiles_x, p.tiles_y = self.tiles_x, self.tiles_y
         p.n_r, p.sat_pitch = self.psf.n_r, self.psf.pitch
         p.n_images, p.rec_per_image = n_images, rec_per_image
@@ -435,20 +446,21 @@ class FramePipeline:
         s = stream_ptr(stream)
         sp = self.splat_params(n_images, rec_per_image)
         n_tiles = self.tiles_x * self.tiles_y * n_images
-        ws_bytes = _lib.load().sc_bin_workspace_bytes(n_rec, n_tiles)
+        L = _lib.load()
+        ws_bytes = L.sc_bin_workspace_bytes(n_rec, n_tiles)
         ws = self._buf("ws", (ws_bytes + 3) // 4, torch.int32)
-        cap = _lib.load().sc_bin_capacity(n_rec, self.cfg.px, PSF_RES, 2 * self.psf.n_r - 1,
-                                          self.tile)
-        items = self._buf("items", cap, torch.int32)
+        items = self._buf("items", n_rec, torch.int32)
         tile_start = self._buf("tile_start", n_tiles + 1, torch.int32)
         call("sc_bin_steps", ptr(recs), n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items),
-             cap, ptr(self.status), s)
+             ptr(self.status), s)
+        sws_bytes = L.sc_splat_workspace_bytes(sp)
+        sws = self._buf("splat_ws", (sws_bytes + 7) // 8, torch.float64)
         ev = self.kernel_events
         if ev is not None:
             e0 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
         call("sc_splat", ptr(recs), ptr(tile_start), ptr(items), ptr(self.psf.tables),
-             ptr(self.psf.box), sp, ptr(image), ptr(self.status), s)
+             ptr(self.psf.box), sp, ptr(sws), sws_bytes, ptr(image), ptr(self.status), s)
         if ev is not None:
             e1 = torch.cuda.Event(enable_timing=True)
             e1.record(stream)
@@ -509,7 +521,8 @@ class FramePipeline:
             if bits & 2:
                 msgs.append("PSF table missing for key %d" % st[3])
             if bits & 4:
-                msgs.append("EMCCD support empty")
+                msgs.append("footprint outside its tile buffer or EMCCD support empty "
+                            "(%d, %d, %d)" % (st[1], st[2], st[3]))
             if bits & 8:
                 msgs.append("random-variate loop bound reached")
             if bits & 16:

@@ -53,15 +53,18 @@ def test_host_side_validation_needs_no_gpu():
     L = _lib.load()
     assert L.sc_psf_radial(0, 5e-7, 1.4, 0.0, None, 0, 1000, 1e-9, None, None) == _lib.SC_ERR_ARG
     assert b"n_keys" in L.sc_last_error()
-    p = _lib.SplatParams(nw=64, nh=64, tile=12, tiles_x=6, tiles_y=6, n_r=1000, sat_pitch=1004,
-                         n_images=1, rec_per_image=0, px=1.6e-7, res=1e-9)
-    assert L.sc_splat(None, None, None, None, None, ctypes.byref(p), None, None, None) == _lib.SC_ERR_ARG
+    p = _lib.SplatParams(nw=64, nh=64, tile=12, halo=14, warps=4, tiles_x=6, tiles_y=6, n_r=1000,
+                         sat_pitch=1004, n_images=1, rec_per_image=0, px=1.6e-7, res=1e-9)
+    assert L.sc_splat(None, None, None, None, None, ctypes.byref(p), None, 0, None, None,
+                      None) == _lib.SC_ERR_ARG
+    assert b"tile=12" in L.sc_last_error()
     assert L.sc_bin_workspace_bytes(0, 16) == 0
-    assert L.sc_bin_capacity(100, 1.6e-7, 1e-9, 1999, 32) == 100 * 4
+    p.tile, p.tiles_x, p.tiles_y = 16, 4, 4
+    assert L.sc_splat_workspace_bytes(ctypes.byref(p)) == 16 * 30 * 30 * 8
 
 
 def test_struct_sizes_match_c_layout():
     from scopyon_gb300 import _lib
     assert ctypes.sizeof(_lib.StepParams) == 136
-    assert ctypes.sizeof(_lib.SplatParams) == 64
+    assert ctypes.sizeof(_lib.SplatParams) == 72
     assert ctypes.sizeof(_lib.CameraParams) == 104

@@ -107,6 +107,18 @@ typedef struct {
     uint64_t counter;        /* Philox counter base (e.g. frame index)                     */
 } ScCameraParams;
 
+typedef struct {
+    int32_t n_particles, n_sub;
+    int32_t ndim;            /* 2: (x, y) inputs, depth 0; 3: (x, y, z)                    */
+    int32_t boundary;        /* 0 none (reference), 1 periodic, 2 reflecting               */
+    int32_t n_class;         /* diffusion classes in d_sigma                                */
+    int32_t pad;
+    int64_t step0;           /* global index of the frame's first sub-step (Philox counter) */
+    uint64_t seed;           /* Philox key                                                  */
+    double lower[3], upper[3];        /* box of the periodic / reflecting boundary          */
+    double scale, origin[3], unit_x[3], unit_y[3], unit_z[3];  /* preprocessing transform  */
+} ScDiffuseParams;
+
 int sc_get_version(void);
 const char *sc_last_error(void);
 
@@ -123,6 +135,20 @@ int sc_psf_radial(int kind, double wavelength, double na, double sigma,
  * overlay_signal_ (src/scopyon/_epifm.py:277-282).                          */
 int sc_psf_quadrant_sat(const double *d_radial, int n_keys, int n_r, double res,
                         float *d_sat, int sat_pitch, void *stream);
+
+/* Brownian sub-steps of one frame on the device.  d_pos (n x 3, sampling
+ * frame, updated in place) holds the positions at the frame's first time
+ * point; for each sub-step the formatted position [depth, x, y, id, 1] goes to
+ * d_particles ([n_sub][n][5], the layout sc_emitter_steps reads) and the
+ * particle then moves by sigma * N(0, 1) per axis, with d_sigma
+ * [n_sub][n_class][3] (sqrt(2 D dt) per step, class and axis) and d_class
+ * (n, NULL = class 0).  Normals from Philox, or from d_normals
+ * ([n_sub][n][ndim]) when given.  Replaces move_points / sample_inputs
+ * (src/scopyon/sampling.py:88-162) and the periodic wrap of
+ * sampling2.__move_points (src/scopyon/sampling2.py:33-50).               */
+int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, const int32_t *d_class,
+                     const double *d_sigma, const double *d_normals, double *d_particles,
+                     void *stream);
 
 /* Box-integrated PSF tables for an integer pixel pitch of P grid rows: for
  * every pixel start row m_x, m_y in [-P, NQ*P - P), the sum of the cartesian
@@ -155,14 +181,16 @@ int sc_emitter_steps(const ScStepParams *p, const double *d_particles,
 size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total);
 
 /* Deterministic counting sort of records by the tile that holds their first
- * footprint pixel; d_items receives n_rec record indices grouped by tile,
- * d_tile_start (n_tiles + 1) the group offsets.  (New: the reference adds
- * particle by particle, src/scopyon/_epifm.py:1262-1264.)                  */
+ * footprint pixel, box-path records in bins [0, n_tiles) and summed-area-path
+ * records in bins [n_tiles, 2 n_tiles); d_items receives the record indices
+ * grouped by bin (ascending within a bin), d_tile_start (2 n_tiles + 1) the
+ * bin offsets.  (New: the reference adds particle by particle,
+ * src/scopyon/_epifm.py:1262-1264.)                                        */
 int sc_bin_steps(const ScStepRec *d_recs, int n_rec,
                  const ScSplatParams *p, void *d_ws, size_t ws_bytes,
                  int32_t *d_tile_start, int32_t *d_items, int32_t *d_status, void *stream);
 
-/* Bytes of scratch sc_splat needs: one FP64 (tile + halo)^2 buffer per tile. */
+/* Bytes of scratch sc_splat needs: one FP32 (tile + halo)^2 buffer per tile. */
 size_t sc_splat_workspace_bytes(const ScSplatParams *p);
 
 /* Splat: each CTA sums the whole footprints of the records binned to its

@@ -10,9 +10,11 @@ from .config import Configuration, DefaultConfiguration, Quantity, Dimensionalit
 from .image import Image
 from .base import (EPIFMSimulator, EnvironSettings, InjectedDraws, create_simulator, form_image,
                    generate_images)
+from .sampling import DeviceTrajectories, concatenate, sample_inputs, sample_points
 
 __all__ = ["Configuration", "DefaultConfiguration", "Quantity", "DimensionalityError", "Image",
            "EPIFMSimulator", "EnvironSettings", "InjectedDraws", "create_simulator", "form_image",
-           "generate_images"]
+           "generate_images", "sample_inputs", "sample_points", "DeviceTrajectories",
+           "concatenate"]
 
 __version__ = "0.1.0"

@@ -23,6 +23,7 @@ from . import _lib
 from . import config as _config
 from .epifm import EngineConfig, FramePipeline, InjectedDraws, PSFTables, frame_windows
 from .image import Image
+from .sampling import DeviceTrajectories
 
 __all__ = ["EPIFMSimulator", "create_simulator", "form_image", "generate_images",
            "EnvironSettings", "InjectedDraws"]
@@ -119,6 +120,8 @@ class EPIFMSimulator:
         return data
 
     def _format_inputs(self, inputs):
+        if isinstance(inputs, DeviceTrajectories):
+            return inputs
         if isinstance(inputs, numpy.ndarray):
             return ((0.0, self._format_data(inputs)),)
         if isinstance(inputs, collections.abc.Iterable):
@@ -168,6 +171,10 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
     pipe = FramePipeline(cfg, device, psf=_psf_for(cfg, device))
     if pipe.camera_kind == _lib.CAM_SCMOS:
         pipe.scmos_sigma_map(rng)
+    if isinstance(data, DeviceTrajectories):
+        yield from _DeviceFrames(sim, cfg, pipe, data, num_frames, start_time, exposure_time,
+                                 bleaching, draws, full_output)
+        return
     exposure = exposure_time or cfg.exposure_time
     times = numpy.array([t for t, _ in data])
     shutter = (cfg.shutter_start, cfg.shutter_end) if cfg.shutter_switch else None
@@ -238,6 +245,79 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
             b = pipe.budget[:n_slots].cpu().numpy()
             info["fluorescence_states"] = {m: float(b[slots[m]]) for m in slot_ids}
         yield Image(adc_np), info
+
+
+def _DeviceFrames(sim, cfg, pipe, traj, num_frames, start_time, exposure_time, bleaching, draws,
+                  full_output):
+    """Frames from device-resident trajectories: diffusion, physics, splat and camera
+    all on the GPU; the host only picks each frame's time window."""
+    import torch
+    rng = sim._rng()
+    device = pipe.device
+    pre = sim.config.preprocessing
+    transform = {}
+    if traj.ndim == 3:
+        transform = dict(scale=pre.scale, origin=pre.origin, unit_x=pre.unit_x, unit_y=pre.unit_y)
+    else:
+        transform = dict(scale=pre.scale)
+    exposure = exposure_time or cfg.exposure_time
+    shutter = (cfg.shutter_start, cfg.shutter_end) if cfg.shutter_switch else None
+    n = traj.n_particles
+    ids = traj.ids().astype(numpy.int64)
+    nw, nh = cfg.image_size
+    pipe.ensure_slots(n)
+    if bleaching:
+        beta = cfg.half_life / numpy.log(2.0)
+        times_b = numpy.empty(n)
+        todo = [k for k in range(n) if not (draws and int(ids[k]) in draws.bleach)]
+        if todo:
+            times_b[todo] = rng.exponential(scale=beta, size=len(todo))
+        for k in range(n):
+            if draws and int(ids[k]) in draws.bleach:
+                times_b[k] = draws.bleach[int(ids[k])]
+        pipe.budget[:n].copy_(torch.from_numpy(times_b * cfg.n_emit0))
+    slots = {int(m): k for k, m in enumerate(ids)}
+    for f in range(num_frames):
+        windows, exp_eff = frame_windows(traj.times, len(traj), start_time, exposure, f, shutter)
+        if windows:
+            g0, g1 = windows[0][0], windows[-1][0]
+        else:
+            g0 = g1 = None
+        n_sub = 0 if g0 is None else g1 - g0 + 1
+        uts = numpy.zeros(n_sub)
+        for i, ut in windows:
+            uts[i - g0] = ut
+        part = pipe._buf("particles", max(n_sub, 1) * n * 5, torch.float64)
+        if n_sub:
+            traj.run(g0, n_sub, part, transform)
+            if len(pipe.psf.slot_of) < pipe.psf.max_key + 2:
+                pipe.psf.ensure(_device_depth_keys(cfg, part[: n_sub * n * 5].view(n_sub, n, 5)))
+        ut_dev = torch.from_numpy(uts).to(device)
+        frame_draws = draws.next_frame() if draws is not None and draws.frames else None
+        seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | int(rng.randint(0, 2 ** 31 - 1)) \
+            if frame_draws is None else 0
+        expect, adc, opt = pipe.run_frame_device(part, ut_dev, n_sub, n, with_optinfo=full_output,
+                                                 draws=frame_draws, seed=seed, counter=f,
+                                                 bleaching=bleaching)
+        pipe.check_status()
+        adc_np = adc.cpu().numpy().reshape(nw, nh).copy()
+        info = {}
+        if full_output:
+            info["expectation"] = expect.cpu().numpy().astype(float).reshape(nw, nh)
+            info["true_data"] = _true_data(cfg, opt, slots, [ids] if n_sub else [], exp_eff, nw, nh)
+            if bleaching:
+                b = pipe.budget[:n].cpu().numpy()
+                info["fluorescence_states"] = {int(m): float(b[k]) for k, m in enumerate(ids)}
+        yield Image(adc_np), info
+
+
+def _device_depth_keys(cfg, part):
+    """Distinct PSF depth keys of formatted device particles (same rule as depth_keys)."""
+    import torch
+    d = (part[:, :, 0] - float(cfg.focal_point[0])).abs().reshape(-1)
+    inside = d < cfg.depth_cutoff + 1e-9
+    keys = torch.where(inside, torch.floor(d / 1e-9), torch.full_like(d, -1.0))
+    return torch.unique(keys).cpu().numpy().astype(numpy.int64)
 
 
 def _true_data(cfg, opt, slots, id_cols, exposure, nw, nh):

@@ -4,11 +4,12 @@
 // (src/scopyon/_epifm.py:1262-1264, :277-282).  Here each record is filed
 // under the tile that holds its first footprint pixel, so one CTA can sum all
 // of a tile's footprints (which reach into a halo past the tile) in shared
-// memory with no global atomics on pixels.  Records are counted per tile,
-// scattered with one atomic cursor per tile, and each tile's list is then
-// sorted by record index: the final order is the reference's own
-// accumulation order (sub-step, then particle) and does not depend on
-// scheduling.
+// memory with no global atomics on pixels.  Box-path and summed-area-path
+// records go to separate bins (bin t and n_tiles + t for tile t).  Records
+// are counted per bin, scattered with one atomic cursor per bin, and each
+// bin's list is then sorted by record index: the final order is the
+// reference's own accumulation order (sub-step, then particle) and does not
+// depend on scheduling.
 #include "sc_common.cuh"
 #include "bin.cuh"
 
@@ -16,18 +17,24 @@ namespace {
 
 constexpr int kSortSmem = 4096;  // tile lists up to this length are sorted in shared memory
 
-__global__ void bin_count_kernel(const ScStepRec *recs, int n_rec, sc::TileGeom g,
-                                 int32_t *tile_count) {
+// Per-bin counts: a shared-memory histogram per CTA when the bins fit, else
+// global atomics directly.
+__global__ void bin_count_kernel(const ScStepRec *recs, int n_rec, sc::TileGeom g, int n_bins,
+                                 int use_smem, int32_t *tile_count) {
     extern __shared__ int32_t hist[];
-    for (int t = threadIdx.x; t < g.n_tiles; t += blockDim.x) hist[t] = 0;
-    __syncthreads();
+    if (use_smem) {
+        for (int t = threadIdx.x; t < n_bins; t += blockDim.x) hist[t] = 0;
+        __syncthreads();
+    }
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rec; r += gridDim.x * blockDim.x) {
         const int t = sc::record_tile(recs[r], r, g);
-        if (t >= 0) atomicAdd(&hist[t], 1);
+        if (t >= 0) atomicAdd(use_smem ? &hist[t] : &tile_count[t], 1);
     }
-    __syncthreads();
-    for (int t = threadIdx.x; t < g.n_tiles; t += blockDim.x)
-        if (hist[t]) atomicAdd(&tile_count[t], hist[t]);
+    if (use_smem) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < n_bins; t += blockDim.x)
+            if (hist[t]) atomicAdd(&tile_count[t], hist[t]);
+    }
 }
 
 // Single-CTA exclusive scan of per-tile counts -> tile_start[0..n_tiles]; the
@@ -160,7 +167,7 @@ int tile_geom(const ScSplatParams *p, TileGeom &g) {
     g.nh = p->nh;
     g.rec_per_image = p->rec_per_image;
     g.n_images = p->n_images;
-    SC_REQUIRE((size_t)g.n_tiles * 4 <= 200 * 1024, "too many tiles (%d) in one launch", g.n_tiles);
+    SC_REQUIRE(g.n_tiles <= (1 << 24), "too many tiles (%d) in one launch", g.n_tiles);
     return SC_OK;
 }
 
@@ -168,7 +175,7 @@ int tile_geom(const ScSplatParams *p, TileGeom &g) {
 
 extern "C" size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total) {
     if (n_rec <= 0 || n_tiles_total <= 0) return 0;
-    return (size_t)2 * n_tiles_total * sizeof(int32_t);
+    return (size_t)4 * n_tiles_total * sizeof(int32_t);  // counts and cursors of 2 bins per tile
 }
 
 extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatParams *p,
@@ -183,7 +190,8 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
     cudaStream_t s = sc::as_stream(stream);
     if (n_rec == 0) {
         return sc::cuda_status(
-            cudaMemsetAsync(d_tile_start, 0, sizeof(int32_t) * (g.n_tiles + 1), s), "sc_bin_steps");
+            cudaMemsetAsync(d_tile_start, 0, sizeof(int32_t) * (2 * g.n_tiles + 1), s),
+            "sc_bin_steps");
     }
     SC_REQUIRE(d_recs && d_items && d_ws, "sc_bin_steps: NULL pointer");
     SC_REQUIRE(ws_bytes >= sc_bin_workspace_bytes(n_rec, g.n_tiles),
@@ -191,21 +199,24 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
                sc_bin_workspace_bytes(n_rec, g.n_tiles));
     SC_REQUIRE(g.rec_per_image == 0 || (int64_t)g.rec_per_image * g.n_images >= n_rec,
                "sc_bin_steps: rec_per_image too small for n_rec");
+    const int n_bins = 2 * g.n_tiles;
     int32_t *tile_count = static_cast<int32_t *>(d_ws);
-    int32_t *cursor = tile_count + g.n_tiles;
-    rc = sc::cuda_status(cudaMemsetAsync(tile_count, 0, sizeof(int32_t) * g.n_tiles, s),
+    int32_t *cursor = tile_count + n_bins;
+    rc = sc::cuda_status(cudaMemsetAsync(tile_count, 0, sizeof(int32_t) * n_bins, s),
                          "sc_bin_steps memset");
     if (rc) return rc;
-    const size_t smem = (size_t)g.n_tiles * sizeof(int32_t);
-    if (smem > 48 * 1024)
+    const size_t smem = (size_t)n_bins * sizeof(int32_t);
+    const int use_smem = smem <= 96 * 1024;
+    if (use_smem && smem > 48 * 1024)
         cudaFuncSetAttribute(bin_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int grid = (n_rec + 1023) / 1024;
     if (grid > 152 * 4) grid = 152 * 4;
-    bin_count_kernel<<<grid, 256, smem, s>>>(d_recs, n_rec, g, tile_count);
-    bin_tile_scan_kernel<<<1, 1024, 0, s>>>(tile_count, g.n_tiles, d_tile_start, cursor);
+    bin_count_kernel<<<grid, 256, use_smem ? smem : 0, s>>>(d_recs, n_rec, g, n_bins, use_smem,
+                                                           tile_count);
+    bin_tile_scan_kernel<<<1, 1024, 0, s>>>(tile_count, n_bins, d_tile_start, cursor);
     int sgrid = (n_rec + 255) / 256;
     if (sgrid > 152 * 16) sgrid = 152 * 16;
     bin_scatter_kernel<<<sgrid, 256, 0, s>>>(d_recs, n_rec, g, cursor, d_items);
-    bin_sort_kernel<<<g.n_tiles, 256, 0, s>>>(d_tile_start, d_items);
+    bin_sort_kernel<<<n_bins, 256, 0, s>>>(d_tile_start, d_items);
     return sc::launch_status("sc_bin_steps");
 }

@@ -13,12 +13,14 @@ struct TileGeom {
 int tile_geom(const ScSplatParams *p, TileGeom &g);
 int bin_chunk(int n_rec, int n_tiles);
 
-// Tile holding a record's first footprint pixel; -1 when it has no pixels.
+// Bin of a record: the tile holding its first footprint pixel, plus n_tiles
+// for records that take the summed-area path; -1 when it has no pixels.
 __device__ __forceinline__ int record_tile(const ScStepRec &rec, int r, const TileGeom &g) {
     if (rec.n_i < 2 || rec.n_j < 2 || rec.slot < 0) return -1;
     const int img = g.rec_per_image > 0 ? r / g.rec_per_image : 0;
     if (img >= g.n_images || rec.i_start >= g.nw || rec.j_start >= g.nh) return -1;
-    return img * g.tiles_per_image + (rec.i_start / g.tile) * g.tiles_y + rec.j_start / g.tile;
+    const int t = img * g.tiles_per_image + (rec.i_start / g.tile) * g.tiles_y + rec.j_start / g.tile;
+    return rec.box ? t : t + g.n_tiles;
 }
 
 }  // namespace sc

@@ -7,8 +7,8 @@
 //
 // Records are filed under the tile of their first pixel (bin.cu).  One CTA per
 // tile sums the whole footprints of its records into a (tile + halo)^2 buffer
-// in shared memory, one FP32 copy per warp, then stores the sum over warps in
-// FP64 to the workspace; a merge pass adds, per pixel, the up to
+// in shared memory, one FP32 copy per half-warp, then stores the sum over the
+// copies to the workspace; a merge pass adds, per pixel, the up to
 // (1 + halo/tile)^2 buffers that cover it, in a fixed order.  No atomics, and
 // every record is read and processed exactly once.
 //
@@ -25,9 +25,6 @@
 #include "bin.cuh"
 #include "fold.cuh"
 
-#ifndef SC_SPLAT_ROWS
-#define SC_SPLAT_ROWS 8  // footprint rows per lane loaded in one round trip (2 rows per step)
-#endif
 
 namespace {
 
@@ -67,52 +64,21 @@ __device__ __forceinline__ int axis_bound(int k, int n, int start, float a_hi, f
 }
 
 
-// The first 32 bytes of a ScStepRec: everything the box path reads.
-struct RecHead {
-    int off_lo, off_hi, ij0, ij1, w_bits, slot, box;
-};
-
-__device__ __forceinline__ RecHead load_head(const ScStepRec *rec) {
-    const int4 *p = reinterpret_cast<const int4 *>(rec);
-    const int4 a = __ldg(p), b = __ldg(p + 1);
-    RecHead h;
-    h.off_lo = a.x;
-    h.off_hi = a.y;
-    h.ij0 = a.z;
-    h.ij1 = a.w;
-    h.w_bits = b.x;
-    h.slot = b.y;
-    h.box = b.z;
-    return h;
-}
-
-__device__ __forceinline__ RecHead shfl_head(const RecHead &h, int src) {
-    RecHead o;
-    o.off_lo = __shfl_sync(0xffffffffu, h.off_lo, src);
-    o.off_hi = __shfl_sync(0xffffffffu, h.off_hi, src);
-    o.ij0 = __shfl_sync(0xffffffffu, h.ij0, src);
-    o.ij1 = __shfl_sync(0xffffffffu, h.ij1, src);
-    o.w_bits = __shfl_sync(0xffffffffu, h.w_bits, src);
-    o.slot = __shfl_sync(0xffffffffu, h.slot, src);
-    o.box = __shfl_sync(0xffffffffu, h.box, src);
-    return o;
-}
-
-// One summed-area-path record over its whole footprint.  Kept out of line so
-// that the box path, which most records take, keeps a small register footprint.
-__device__ __noinline__ void splat_sat_record(const ScStepRec *rp, int i_start, int n_i,
-                                              int j_start, int n_j, int slot, float w, int base,
-                                              const float2 *__restrict__ sat, const SplatConsts &c,
-                                              int *bx, int *by, float *my_acc, int lane) {
-    const ScStepRec &rec = *rp;
+// One summed-area-path record over its whole footprint, by a whole warp:
+// bounds from the exact footprint arithmetic (bx, by: per-warp scratch), each
+// pixel from folded quadrant-table sums.
+__device__ void splat_sat_record(const ScStepRec &rec, int base, const float2 *__restrict__ sat,
+                                 const SplatConsts &c, int *bx, int *by, float *my_acc, int lane) {
+    const int i_start = rec.i_start, n_i = rec.n_i, j_start = rec.j_start, n_j = rec.n_j;
     const double x0 = rec.x0, y0 = rec.y0;
     const float axh = rec.ax_hi, axl = rec.ax_lo, ayh = rec.ay_hi, ayl = rec.ay_lo;
+    const float w = rec.w;
     for (int b = lane; b < n_i + n_j; b += 32) {
         if (b < n_i) bx[b] = axis_bound(b, n_i, i_start, axh, axl, x0, c);
         else by[b - n_i] = axis_bound(b - n_i, n_j, j_start, ayh, ayl, y0, c);
     }
     __syncwarp();
-    const float2 *G = sat + (int64_t)slot * c.table_stride;
+    const float2 *G = sat + (int64_t)rec.slot * c.table_stride;
     const int ni = n_i - 1, nj = n_j - 1;
     for (int q = lane; q < ni * nj; q += 32) {
         const int a = q / nj, bj = q - (q / nj) * nj;
@@ -138,119 +104,149 @@ __device__ __noinline__ void splat_sat_record(const ScStepRec *rp, int i_start, 
     __syncwarp();
 }
 
-// Box-path values of one record for this lane: rows row0 + 2u of column
-// block cb (16 columns), all issued before any is used.
-struct BoxVals {
-    float v[SC_SPLAT_ROWS];
-};
-
-__device__ __forceinline__ void load_box(const float *B, int nq, int ni, int nj, int cb, int col,
-                                         int row0, int a0, BoxVals &bv) {
-    const int b = cb + col;
-#pragma unroll
-    for (int u = 0; u < SC_SPLAT_ROWS; ++u) {
-        const int a = a0 + row0 + 2 * u;
-        bv.v[u] = (a < ni && b < nj) ? __ldg(B + a * nq + b) : 0.f;
-    }
+// Tile geometry of a CTA; false (after flagging) when a footprint does not
+// fit its tile buffer.
+__device__ __forceinline__ bool in_buffer(int ox, int oy, int ni, int nj, int E) {
+    return ox >= 0 && oy >= 0 && ox + ni <= E && oy + nj <= E;
 }
 
-// Per-warp partial sums are plain FP32: a warp adds at most a few dozen
-// footprints to one pixel (error <~ 1e-6 relative), and the sums across warps
-// and across tiles are FP64.
+// Box path.  Sums are plain FP32: one warp buffer receives at most a few
+// dozen footprints per pixel, and a pixel's value is then the sum of NW warp
+// buffers and of at most (1 + halo/tile)^2 tile buffers, so each chain of
+// roundings is short (about 1e-6 relative at the densities the engine
+// targets; the tests hold 1e-5).
+//
+// Record m of the tile's box list goes to warp m mod NW, so the warps of a
+// CTA finish together.  A warp stages the 32-byte heads of its next 32
+// records in shared memory, then takes them one at a time: lane (row0 =
+// lane / 16, col = lane % 16) loads rows row0, row0 + 2, ... of footprint
+// column col (eight loads in flight), reads the eight buffer values, then
+// writes the eight sums.  Footprints wider or taller than 16 pixels take
+// further passes.
 template <int NW>
-__global__ void __launch_bounds__(NW * 32)
-splat_halo_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
-                  const int32_t *__restrict__ items, const float2 *__restrict__ sat,
-                  SplatConsts c, double *__restrict__ ws, int32_t *status) {
+__global__ void __launch_bounds__(NW * 32, 32 / NW)
+splat_box_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
+                 const int32_t *__restrict__ items, SplatConsts c, float *__restrict__ ws,
+                 int32_t *status) {
     extern __shared__ float sm[];
     const int E = c.edge, EE = c.edge * c.edge;
-    float *acc = sm;
-    int *bnd = reinterpret_cast<int *>(acc + NW * EE);
+    const int BS = (EE + 31) & ~31;
+    float *acc = sm;                                          // [NW][BS]
+    int4 *heads = reinterpret_cast<int4 *>(acc + NW * BS);    // [NW][32][2]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile = blockIdx.x;
     const int t = tile % c.tiles_per_image;
     const int x0 = (t / c.tiles_y) * c.tile, y0 = (t % c.tiles_y) * c.tile;
-    for (int i = threadIdx.x; i < NW * EE; i += blockDim.x) sm[i] = 0.f;
+    for (int i = threadIdx.x; i < NW * BS; i += blockDim.x) sm[i] = 0.f;
     __syncthreads();
-    float *my_acc = acc + warp * EE;
-    int *bx = bnd + warp * 2 * (E + 2);
-    int *by = bx + (E + 2);
+    float *my_acc = acc + warp * BS;
+    int4 *my_heads = heads + warp * 64;
     const int col = lane & 15, row0 = lane >> 4;
+    const int nq = c.box_nq;
     const int it0 = tile_start[tile], it1 = tile_start[tile + 1];
-    for (int base = it0 + warp * 32; base < it1; base += NW * 32) {
-        // 32 records per batch: item index and header loaded lane-parallel
-        int my_item = 0;
-        RecHead my_head = {0, 0, 0, 0, 0, -1, 0};
-        if (base + lane < it1) {
-            my_item = __ldg(items + base + lane);
-            my_head = load_head(recs + my_item);
+    for (int base = it0 + warp; base < it1; base += NW * 32) {
+        const int mine = base + NW * lane;
+        if (mine < it1) {
+            const int4 *src = reinterpret_cast<const int4 *>(recs + __ldg(items + mine));
+            my_heads[2 * lane] = __ldg(src);
+            my_heads[2 * lane + 1] = __ldg(src + 1);
         }
-        const int cnt = min(32, it1 - base);
-        // software pipeline over the batch: the next box record's first rows
-        // are in flight while the current one is accumulated
-        BoxVals next;
-        int next_k = -1;
+        __syncwarp();
+        const int cnt = min(32, (it1 - base + NW - 1) / NW);
         for (int k = 0; k < cnt; ++k) {
-            const RecHead h = shfl_head(my_head, k);
-            const int i_start = (int)(int16_t)(h.ij0 & 0xffff), n_i = h.ij0 >> 16;
-            const int j_start = (int)(int16_t)(h.ij1 & 0xffff), n_j = h.ij1 >> 16;
-            const int ni = n_i - 1, nj = n_j - 1;
+            const int4 ha = my_heads[2 * k], hb = my_heads[2 * k + 1];
+            const int i_start = (int)(int16_t)(ha.z & 0xffff), ni = (ha.z >> 16) - 1;
+            const int j_start = (int)(int16_t)(ha.w & 0xffff), nj = (ha.w >> 16) - 1;
             const int ox = i_start - x0, oy = j_start - y0;
-            const bool ok = ni >= 1 && nj >= 1 && h.slot >= 0;
-            if (ok && (ox < 0 || oy < 0 || ox + ni > E || oy + nj > E)) {
+            if (!in_buffer(ox, oy, ni, nj, E)) {
                 if (lane == 0) sc::flag_status(status, 2, i_start, j_start, tile);
                 continue;
             }
-            if (!ok) continue;
-            const float w = __int_as_float(h.w_bits);
-            const int buf0 = ox * E + oy;
-            if (h.box && c.box != nullptr) {
-                // pixel (i_start + a, j_start + b) is entry box_off + a * NQ + b
-                const float *B = c.box + (((int64_t)h.off_hi << 32) | (uint32_t)h.off_lo);
-                BoxVals cur;
-                if (next_k == k) cur = next;
-                else load_box(B, c.box_nq, ni, nj, 0, col, row0, 0, cur);
-                // prefetch the following record's first block when it is a box record
-                next_k = -1;
-                if (k + 1 < cnt) {
-                    const RecHead hn = shfl_head(my_head, k + 1);
-                    if (hn.box && hn.slot >= 0) {
-                        const int nin = (hn.ij0 >> 16) - 1, njn = (hn.ij1 >> 16) - 1;
-                        const float *Bn = c.box + (((int64_t)hn.off_hi << 32) | (uint32_t)hn.off_lo);
-                        load_box(Bn, c.box_nq, nin, njn, 0, col, row0, 0, next);
-                        next_k = k + 1;
-                    }
-                }
-                for (int cb = 0; cb < nj; cb += 16) {
-                    for (int a0 = 0; a0 < ni; a0 += 2 * SC_SPLAT_ROWS) {
-                        if (cb > 0 || a0 > 0) load_box(B, c.box_nq, ni, nj, cb, col, row0, a0, cur);
-                        const int b = cb + col;
+            const float w = __int_as_float(hb.x);
+            // pixel (i_start + a, j_start + b) is entry box_off + a * NQ + b
+            const float *B = c.box + (((int64_t)ha.y << 32) | (uint32_t)ha.x);
+            float *D = my_acc + ox * E + oy;
+            for (int cb = 0; cb < nj; cb += 16) {
+                const int b = cb + col;
+                const bool cok = b < nj;
+                for (int a0 = row0; a0 < ni; a0 += 16) {
+                    const float *src = B + a0 * nq + b;
+                    float *dst = D + a0 * E + b;
+                    float v[8], o[8];
 #pragma unroll
-                        for (int u = 0; u < SC_SPLAT_ROWS; ++u) {
-                            const int a = a0 + row0 + 2 * u;
-                            if (a < ni && b < nj && cur.v[u] > 0.f)
-                                my_acc[buf0 + a * E + b] += w * cur.v[u];
-                        }
-                    }
+                    for (int u = 0; u < 8; ++u)
+                        v[u] = (cok && a0 + 2 * u < ni) ? __ldg(src + 2 * u * nq) : 0.f;
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+                        o[u] = (cok && a0 + 2 * u < ni) ? dst[2 * u * E] : 0.f;
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+                        if (cok && a0 + 2 * u < ni) dst[2 * u * E] = fmaf(w, v[u], o[u]);
                 }
-                continue;
             }
-            splat_sat_record(recs + __shfl_sync(0xffffffffu, my_item, k), i_start, n_i, j_start,
-                             n_j, h.slot, w, buf0, sat, c, bx, by, my_acc, lane);
         }
+        __syncwarp();
     }
     __syncthreads();
-    double *out = ws + (size_t)tile * EE;
+    float *out = ws + (size_t)tile * EE;
     for (int p = threadIdx.x; p < EE; p += blockDim.x) {
-        double sum = 0.0;
+        float sum = 0.f;
 #pragma unroll
-        for (int w = 0; w < NW; ++w) sum += (double)acc[w * EE + p];
+        for (int w = 0; w < NW; ++w) sum += acc[w * BS + p];
         out[p] = sum;
     }
 }
 
+// Summed-area path: the tile's second bin.  Adds into the tile buffer the box
+// kernel wrote (accumulate = 1) or writes it (accumulate = 0, no box tables).
+template <int NW>
+__global__ void __launch_bounds__(NW * 32)
+splat_sat_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
+                 const int32_t *__restrict__ items, const float2 *__restrict__ sat,
+                 SplatConsts c, int n_tiles, int accumulate, float *__restrict__ ws,
+                 int32_t *status) {
+    extern __shared__ float sm[];
+    const int E = c.edge, EE = c.edge * c.edge;
+    const int BS = (EE + 31) & ~31;
+    const int tile = blockIdx.x;
+    const int it0 = tile_start[n_tiles + tile], it1 = tile_start[n_tiles + tile + 1];
+    float *out = ws + (size_t)tile * EE;
+    if (it0 == it1) {
+        if (!accumulate)
+            for (int p = threadIdx.x; p < EE; p += blockDim.x) out[p] = 0.f;
+        return;
+    }
+    float *acc = sm;
+    int *bnd = reinterpret_cast<int *>(acc + NW * BS);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = tile % c.tiles_per_image;
+    const int x0 = (t / c.tiles_y) * c.tile, y0 = (t % c.tiles_y) * c.tile;
+    for (int i = threadIdx.x; i < NW * BS; i += blockDim.x) sm[i] = 0.f;
+    __syncthreads();
+    float *my_acc = acc + warp * BS;
+    int *bx = bnd + warp * 2 * (E + 2);
+    int *by = bx + (E + 2);
+    for (int m = it0 + warp; m < it1; m += NW) {
+        const ScStepRec &rec = recs[__ldg(items + m)];
+        const int ni = rec.n_i - 1, nj = rec.n_j - 1;
+        const int ox = rec.i_start - x0, oy = rec.j_start - y0;
+        if (!in_buffer(ox, oy, ni, nj, E)) {
+            if (lane == 0) sc::flag_status(status, 2, rec.i_start, rec.j_start, tile);
+            continue;
+        }
+        splat_sat_record(rec, ox * E + oy, sat, c, bx, by, my_acc, lane);
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < EE; p += blockDim.x) {
+        float sum = 0.f;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) sum += acc[w * BS + p];
+        out[p] = accumulate ? out[p] + sum : sum;
+    }
+}
+
 // Per pixel: the tile buffers that cover it, summed in a fixed order.
-__global__ void splat_merge_kernel(const double *__restrict__ ws, SplatConsts c, int n_images,
+__global__ void splat_merge_kernel(const float *__restrict__ ws, SplatConsts c, int n_images,
                                    float *__restrict__ image) {
     const int n = c.nw * c.nh;
     const int E = c.edge, EE = c.edge * c.edge;
@@ -260,8 +256,8 @@ __global__ void splat_merge_kernel(const double *__restrict__ ws, SplatConsts c,
         const int p = (int)(g - (int64_t)img * n);
         const int i = p / c.nh, j = p - (p / c.nh) * c.nh;
         const int tx = i / c.tile, ty = j / c.tile;
-        const double *tiles = ws + (size_t)img * c.tiles_per_image * EE;
-        double sum = 0.0;
+        const float *tiles = ws + (size_t)img * c.tiles_per_image * EE;
+        float sum = 0.f;
         for (int a = 0; a <= tx; ++a) {
             const int li = i - (tx - a) * c.tile;
             if (li >= E) break;
@@ -271,26 +267,40 @@ __global__ void splat_merge_kernel(const double *__restrict__ ws, SplatConsts c,
                 sum += tiles[(size_t)((tx - a) * c.tiles_y + (ty - b)) * EE + li * E + lj];
             }
         }
-        image[g] = (float)sum;
+        image[g] = sum;
     }
 }
 
 template <int NW>
-int launch_halo(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
-                const float2 *sat, const SplatConsts &c, int n_tiles, double *ws, int32_t *status,
-                cudaStream_t s) {
-    const size_t smem = (size_t)NW * c.edge * c.edge * sizeof(float) +
-                        (size_t)NW * 2 * (c.edge + 2) * sizeof(int);
+int launch_splat(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
+                 const float2 *sat, const SplatConsts &c, int n_tiles, bool box, float *ws,
+                 int32_t *status, cudaStream_t s) {
+    const int ee = c.edge * c.edge;
+    const int bs = (ee + 31) & ~31;
+    if (box) {
+        const size_t smem = (size_t)NW * bs * sizeof(float) + (size_t)NW * 64 * sizeof(int4);
+        SC_REQUIRE(smem <= 227 * 1024, "sc_splat: tile %d + halo %d needs %zu bytes of shared "
+                   "memory with %d warps", c.tile, c.halo, smem, NW);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(splat_box_kernel<NW>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return sc::cuda_status(e, "sc_splat: smem attribute");
+        }
+        splat_box_kernel<NW><<<n_tiles, NW * 32, smem, s>>>(recs, tile_start, items, c, ws, status);
+        int rc = sc::launch_status("sc_splat box");
+        if (rc) return rc;
+    }
+    const size_t smem = (size_t)NW * bs * sizeof(float) + (size_t)NW * 2 * (c.edge + 2) * sizeof(int);
     SC_REQUIRE(smem <= 227 * 1024, "sc_splat: tile %d + halo %d needs %zu bytes of shared memory "
                "with %d warps", c.tile, c.halo, smem, NW);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(splat_halo_kernel<NW>,
+        cudaError_t e = cudaFuncSetAttribute(splat_sat_kernel<NW>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return sc::cuda_status(e, "sc_splat: smem attribute");
     }
-    splat_halo_kernel<NW><<<n_tiles, NW * 32, smem, s>>>(recs, tile_start, items, sat, c, ws,
-                                                         status);
-    return sc::launch_status("sc_splat");
+    splat_sat_kernel<NW><<<n_tiles, NW * 32, smem, s>>>(recs, tile_start, items, sat, c, n_tiles,
+                                                        box ? 1 : 0, ws, status);
+    return sc::launch_status("sc_splat summed-area");
 }
 
 int splat_consts(const ScSplatParams *p, const sc::TileGeom &g, SplatConsts &c) {
@@ -323,7 +333,7 @@ int splat_consts(const ScSplatParams *p, const sc::TileGeom &g, SplatConsts &c) 
 extern "C" size_t sc_splat_workspace_bytes(const ScSplatParams *p) {
     sc::TileGeom g;
     if (!p || sc::tile_geom(p, g) != SC_OK) return 0;
-    return (size_t)g.n_tiles * g.edge * g.edge * sizeof(double);
+    return (size_t)g.n_tiles * g.edge * g.edge * sizeof(float);
 }
 
 extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
@@ -347,12 +357,13 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
     }
     const float2 *sat = reinterpret_cast<const float2 *>(d_sat);
     cudaStream_t s = sc::as_stream(stream);
-    double *ws = static_cast<double *>(d_ws);
+    float *ws = static_cast<float *>(d_ws);
+    const bool box = d_box != nullptr;
     switch (g.warps) {
-        case 1: rc = launch_halo<1>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, ws, d_status, s); break;
-        case 2: rc = launch_halo<2>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, ws, d_status, s); break;
-        case 4: rc = launch_halo<4>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, ws, d_status, s); break;
-        default: rc = launch_halo<8>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, ws, d_status, s); break;
+        case 1: rc = launch_splat<1>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, box, ws, d_status, s); break;
+        case 2: rc = launch_splat<2>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, box, ws, d_status, s); break;
+        case 4: rc = launch_splat<4>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, box, ws, d_status, s); break;
+        default: rc = launch_splat<8>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, box, ws, d_status, s); break;
     }
     if (rc) return rc;
     const int64_t total = (int64_t)g.nw * g.nh * g.n_images;

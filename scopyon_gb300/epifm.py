@@ -353,9 +353,10 @@ class FramePipeline:
 
     def _pick_tile(self):
         """(tile edge, warps per tile CTA) that fit shared memory; see tune_tiles."""
-        for tile, warps in ((16, 4), (8, 4), (8, 2), (8, 1)):
+        for tile, warps in ((8, 4), (8, 2), (8, 1)):
             edge = tile + self.halo
-            if 2 * warps * edge * edge * 4 + warps * 2 * (edge + 2) * 4 <= 200 * 1024:
+            stride = ((edge * edge + 31) // 32) * 32 + 16
+            if 2 * warps * stride * 4 + warps * 2 * (edge + 2) * 4 <= 200 * 1024:
                 return tile, warps
         raise ValueError("pixel size %g m is too small for the splat's shared memory" % self.cfg.px)
 
@@ -450,11 +451,11 @@ class FramePipeline:
         ws_bytes = L.sc_bin_workspace_bytes(n_rec, n_tiles)
         ws = self._buf("ws", (ws_bytes + 3) // 4, torch.int32)
         items = self._buf("items", n_rec, torch.int32)
-        tile_start = self._buf("tile_start", n_tiles + 1, torch.int32)
+        tile_start = self._buf("tile_start", 2 * n_tiles + 1, torch.int32)
         call("sc_bin_steps", ptr(recs), n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items),
              ptr(self.status), s)
         sws_bytes = L.sc_splat_workspace_bytes(sp)
-        sws = self._buf("splat_ws", (sws_bytes + 7) // 8, torch.float64)
+        sws = self._buf("splat_ws", (sws_bytes + 3) // 4, torch.float32)
         ev = self.kernel_events
         if ev is not None:
             e0 = torch.cuda.Event(enable_timing=True)

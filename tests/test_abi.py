@@ -60,7 +60,7 @@ def test_host_side_validation_needs_no_gpu():
     assert b"tile=12" in L.sc_last_error()
     assert L.sc_bin_workspace_bytes(0, 16) == 0
     p.tile, p.tiles_x, p.tiles_y = 16, 4, 4
-    assert L.sc_splat_workspace_bytes(ctypes.byref(p)) == 16 * 30 * 30 * 8
+    assert L.sc_splat_workspace_bytes(ctypes.byref(p)) == 16 * 30 * 30 * 4
 
 
 def test_struct_sizes_match_c_layout():

@@ -1,0 +1,181 @@
+"""GPU: device trajectories and the native (Philox) random draws.
+
+* exact-mode trajectories equal the reference's sample_inputs bit for bit;
+* frames from device trajectories equal the reference's frames (injected
+  camera draws), tolerances as in test_gpu_parity;
+* Philox Brownian steps: mean-squared displacement per axis within 4 sigma
+  of 2 D t; reflecting / periodic boundaries keep particles in the box;
+* native camera models: per-pixel mean and variance of the photo-electron
+  signal within 4 standard errors of the model's moments, and a
+  Kolmogorov-Smirnov test of the sCMOS / CCD read noise.
+"""
+
+import json
+
+import numpy
+import pytest
+
+torch = pytest.importorskip("torch")
+from golden_cases import case_frames_draws, case_tree  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sg():
+    from scopyon_gb300 import _build
+    _build.build()
+    import scopyon_gb300
+    return scopyon_gb300
+
+
+def test_exact_trajectories_match_reference(sg, golden):
+    t = numpy.arange(7) * 0.5e-3
+    traj = sg.sample_inputs(t, N=5, lower=[-1e-6, -2e-6, -0.5e-6], upper=[1e-6, 2e-6, 0.5e-6],
+                            D=0.1e-12, ndim=3, rng=numpy.random.RandomState(5), exact=True)
+    pts = numpy.array([p for _, p in traj])
+    numpy.testing.assert_array_equal(pts, golden["samp3_pts"])
+    traj = sg.sample_inputs(t[:4], N=4, lower=-3e-6, upper=3e-6, D=[0.2e-12, 0.05e-12], ndim=2,
+                            rng=numpy.random.RandomState(9), exact=True)
+    numpy.testing.assert_array_equal(numpy.array([p for _, p in traj]), golden["samp2_pts"])
+
+
+@pytest.mark.parametrize("name,nframes,seed,n,lower,upper,D", [
+    ("fb", 3, 3, 9, [-1.5e-6, -1.5e-6, -0.4e-6], [1.5e-6, 1.5e-6, 0.4e-6], 0.2e-12),
+    ("fd", 2, 8, 5, [-1.0e-6, -1.0e-6, 0.0], [1.0e-6, 1.0e-6, 0.2e-6], 0.5e-12),
+])
+def test_device_frames_match_reference(sg, golden, name, nframes, seed, n, lower, upper, D):
+    tree = json.loads(json.dumps(case_tree(golden, name)))
+    tree["default"]["gpu"] = {"cmos_table": golden["cmos_table"].tolist()}
+    cfg = sg.Configuration(yaml=tree)
+    times = golden["%s_input_t" % name]
+    traj = sg.sample_inputs(times, N=n, lower=lower, upper=upper, D=D, ndim=3,
+                            rng=numpy.random.RandomState(seed), exact=True)
+    ids = [int(i) for i in golden["%s_true_ids" % name]]
+    bleach = dict(zip(ids, golden["%s_bleach_times" % name]))
+    draws = sg.InjectedDraws(bleach=bleach, frames=case_frames_draws(golden, name, nframes))
+    sim = sg.EPIFMSimulator(cfg, method="default", rng=numpy.random.RandomState(0))
+    results = list(sim.generate_images(traj, nframes, full_output=True, draws=draws))
+    for f, (img, info) in enumerate(results):
+        e_ref = golden["%s_expectation" % name][f]
+        big = e_ref > 1e-6 * e_ref.max()
+        assert (numpy.abs(info["expectation"] - e_ref)[big] / e_ref[big]).max() < 1e-5
+        a_ref = golden["%s_adc" % name][f]
+        diff = numpy.abs(img.as_array() - a_ref)
+        if tree["default"]["detector"]["type"] == "EMCCD":
+            assert (diff > 1e-9).sum() <= 1 and diff.max() <= 1.0
+        else:
+            assert diff.max() <= 1e-9 * a_ref.max()
+        td = numpy.array([info["true_data"][m] for m in ids])
+        numpy.testing.assert_allclose(td, golden["%s_true_data" % name][f], rtol=1e-12)
+        st = numpy.array([info["fluorescence_states"][m] for m in ids])
+        numpy.testing.assert_allclose(st, golden["%s_states" % name][f], rtol=1e-12, atol=0)
+
+
+def test_philox_diffusion_msd(sg):
+    n, steps, dt, D = 20000, 50, 1e-3, 0.3e-12
+    traj = sg.sample_inputs(numpy.arange(steps + 1) * dt, N=n, lower=0.0, upper=0.0, D=D, ndim=3,
+                            rng=numpy.random.RandomState(1))
+    end = traj.copy().materialize(steps)
+    disp = end[:, :3]
+    var = 2 * D * steps * dt
+    for d in range(3):
+        msd = (disp[:, d] ** 2).mean()
+        # chi-square with n dof: mean var, sd var * sqrt(2/n)
+        assert abs(msd / var - 1) < 4 * numpy.sqrt(2.0 / n), (d, msd / var)
+        assert abs(disp[:, d].mean()) < 4 * numpy.sqrt(var / n)
+    # consecutive steps are independent
+    a = traj.copy().materialize(1)[:, 0]
+    b = traj.copy().materialize(2)[:, 0] - a
+    assert abs(numpy.corrcoef(a, b)[0, 1]) < 4 / numpy.sqrt(n)
+
+
+@pytest.mark.parametrize("boundary", ["reflecting", "periodic"])
+def test_boundaries_confine(sg, boundary):
+    lo, hi = -0.5e-6, 0.5e-6
+    traj = sg.sample_inputs(numpy.arange(201) * 1e-3, N=4000, lower=lo, upper=hi, D=1e-12, ndim=3,
+                            rng=numpy.random.RandomState(2), boundary=boundary)
+    end = traj.copy().materialize(200)[:, :3]
+    assert end.min() >= lo and end.max() <= hi
+    # after many box-crossing times the density is uniform
+    hist, _ = numpy.histogram(end[:, 0], bins=10, range=(lo, hi))
+    expected = len(end) / 10
+    chi2 = ((hist - expected) ** 2 / expected).sum()
+    assert chi2 < 30  # 9 dof, p ~ 4e-4
+
+
+def _camera_stats(sg, det, gpu, photons, n_frames=40, seed=3):
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {
+        "magnification": 100,
+        "detector": {"type": det, "image_size": [64, 64], "exposure_time": 0.01},
+        "effects": {"background": {"switch": True, "mean": photons},
+                    "photo_bleaching": {"switch": False}},
+        # fullwell = 2^16 - offset makes the ADC gain exactly 1 e- per count
+        "analog_to_digital_converter": {"bit": 16, "offset": 2000, "fullwell": 63536},
+        "gpu": gpu}})
+    sim = sg.EPIFMSimulator(cfg, method="default", rng=numpy.random.RandomState(seed))
+    far = numpy.array([[1.0, 1.0]])  # one emitter far outside the field: background only
+    imgs = [img.as_array() for img in sim.generate_images(far, n_frames)]
+    eng = sim.base()
+    return numpy.array(imgs), eng
+
+
+def test_native_ccd_moments_and_noise(sg):
+    imgs, eng = _camera_stats(sg, "CCD", {}, photons=50.0)
+    e = eng.qe * 50.0
+    electrons = (imgs - eng.offset) * eng.gain
+    m, v = electrons.mean(), electrons.var()
+    n = electrons.size
+    var_model = e + eng.readout_noise ** 2
+    assert abs(m - e) < 4 * numpy.sqrt(var_model / n)
+    assert abs(v / var_model - 1) < 4 * numpy.sqrt(2.0 / n) * 1.5
+
+
+def test_native_emccd_moments(sg):
+    imgs, eng = _camera_stats(sg, "EMCCD", {}, photons=20.0)
+    e, g = eng.qe * 20.0, eng.emgain
+    electrons = (imgs - eng.offset) * eng.gain
+    m, v = electrons.mean(), electrons.var()
+    n = electrons.size
+    var_model = 2 * g * g * e + eng.readout_noise ** 2
+    assert abs(m / (g * e) - 1) < 4 * numpy.sqrt(var_model / n) / (g * e) + 1e-3
+    assert abs(v / var_model - 1) < 0.05
+
+
+def test_native_scmos_per_pixel_sigma(sg):
+    imgs, eng = _camera_stats(sg, "CMOS", {"cmos_noise": "scmos", "scmos_readout_median": 1.5,
+                                           "scmos_readout_sigma": 0.4}, photons=30.0, n_frames=80)
+    e = eng.qe * 30.0
+    electrons = (imgs - eng.offset) * eng.gain
+    m = electrons.mean()
+    assert abs(m - e) < 4 * numpy.sqrt((e + 4) / electrons.size)
+    # per-pixel variance ~ e + sigma_ij^2 with lognormal(ln 1.5, 0.4) sigmas: median excess ~2.25
+    pv = electrons.var(axis=0, ddof=1) - e
+    assert 1.5 < numpy.median(pv) < 3.2
+
+
+def test_poisson_sampler_distribution(sg):
+    """Photo-electron counts of the CCD path (read noise off) follow Poisson(E): chi-square."""
+    from scipy import stats
+    cfg = sg.DefaultConfiguration()
+    for photons in (3.0, 40.0, 400.0):
+        cfg.update({"default": {
+            "magnification": 100,
+            "detector": {"type": "CCD", "image_size": [64, 64], "readout_noise": 0},
+            "effects": {"background": {"switch": True, "mean": photons},
+                        "photo_bleaching": {"switch": False}},
+            "analog_to_digital_converter": {"bit": 16, "offset": 2000, "fullwell": 63536}}})
+        sim = sg.EPIFMSimulator(cfg, method="default", rng=numpy.random.RandomState(4))
+        imgs = numpy.array([i.as_array() for i in sim.generate_images(numpy.array([[1.0, 1.0]]), 10)])
+        eng = sim.base()
+        counts = numpy.rint((imgs - eng.offset) * eng.gain).astype(int).ravel()
+        lam = eng.qe * photons
+        lo, hi = int(max(0, lam - 4 * numpy.sqrt(lam))), int(lam + 4 * numpy.sqrt(lam)) + 1
+        edges = numpy.arange(lo, hi + 1)
+        obs = numpy.array([(counts == k).sum() for k in edges[:-1]])
+        exp = stats.poisson.pmf(edges[:-1], lam) * counts.size
+        keep = exp > 20
+        chi2 = (((obs - exp) ** 2) / exp)[keep].sum()
+        dof = keep.sum() - 1
+        assert stats.chi2.sf(chi2, dof) > 1e-4, (photons, chi2, dof)

@@ -162,52 +162,51 @@ def load_peaks():
 def gb300_arm(args, rank, world):
     import torch
     import scopyon_gb300 as sg
-    from scopyon_gb300 import _lib
-    from scopyon_gb300.epifm import EngineConfig, FramePipeline
+    from scopyon_gb300.base import _psf_for
+    from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     cfg = workload_config()
     rng = numpy.random.RandomState(11 + rank)
     eng = EngineConfig(cfg["default"], rng=rng)
-    from scopyon_gb300.base import _psf_for
     pipe = FramePipeline(eng, dev, psf=_psf_for(eng, dev))
     pipe.scmos_sigma_map(rng)
     t0 = time.time()
-    n_frames = args.warmup + args.steps
-    times, pos = trajectories(n_frames, seed=7 + rank)
     if args.small:
-        pipe.psf.ensure(eng.depth_keys(pos[..., 2].ravel() - eng.focal_point[0]))
+        pipe.psf.ensure(list(range(0, int((Z_HALF + 0.3e-6) / 1e-9))))
     else:
         pipe.psf.ensure_all()
     torch.cuda.synchronize()
     psf_build_s = time.time() - t0
-    traj = torch.from_numpy(formatted(pos)).to(dev)
-    ut = torch.full((SUBSTEPS,), EXPOSURE / SUBSTEPS, dtype=torch.float64, device=dev)
+
+    # trajectories on the device: two populations (D = 0.01 and 1 um^2/s), Philox normals
+    n_timing = 4
+    n_frames = args.warmup + args.steps + n_timing
+    dt = EXPOSURE / SUBSTEPS
+    t = numpy.arange(n_frames * SUBSTEPS + 1) * dt
+    box = dict(lower=[-HALF, -HALF, -Z_HALF], upper=[HALF, HALF, Z_HALF], ndim=3, device=dev)
+    slow = sg.sample_inputs(t, N=N_EMIT // 2, D=0.01e-12, rng=rng, **box)
+    fast = sg.sample_inputs(t, N=N_EMIT - N_EMIT // 2, D=D_FAST, rng=rng, start=N_EMIT // 2, **box)
+    traj = sg.concatenate(slow, fast)
     pipe.ensure_slots(N_EMIT)
     beta = eng.half_life / math.log(2.0)
     pipe.budget[:N_EMIT].copy_(torch.from_numpy(rng.exponential(beta, N_EMIT) * eng.n_emit0))
-    frame_stride = SUBSTEPS * N_EMIT * 5
-
-    def frame(f):
-        part = traj.view(-1)[f * frame_stride: (f + 1) * frame_stride]
-        return pipe.run_frame_device(part, ut, SUBSTEPS, N_EMIT, with_optinfo=False,
-                                     seed=1234 + rank, counter=f)
-
-    for f in range(args.warmup):
-        frame(f)
-    pipe.check_status()
+    fg = FrameGraph(pipe, traj, SUBSTEPS, dt, seed=1234 + rank)
+    fg.capture()
+    for _ in range(args.warmup - 1):
+        fg.step()
     torch.cuda.synchronize()
+    pipe.check_status()
     if world > 1:
         torch.distributed.barrier()
-    pipe.kernel_events = {}
     clocks = ClockSampler(dev.index)
     clocks.start()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     start.record()
-    for f in range(args.warmup, n_frames):
-        frame(f)
+    for _ in range(args.steps):
+        fg.step()
     end.record()
     torch.cuda.synchronize()
     if world > 1:
@@ -215,12 +214,18 @@ def gb300_arm(args, rank, world):
     elapsed_ms = start.elapsed_time(end)
     clk = clocks.stop()
     pipe.check_status()
+    # the splat's own duration: the same frames, launched eagerly with events around it
+    fg.graph, fg.use_graph = None, False
+    pipe.kernel_events = {}
+    for _ in range(n_timing):
+        fg.step()
+    torch.cuda.synchronize()
     splat_ms = [a.elapsed_time(b) for a, b in pipe.kernel_events["splat"]]
     pipe.kernel_events = None
     if world > 1:
-        t = torch.tensor([elapsed_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+        tt = torch.tensor([elapsed_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(tt.item())
     ms_per_step = elapsed_ms / args.steps
     value = world * args.steps / (elapsed_ms / 1e3)
 
@@ -232,29 +237,34 @@ def gb300_arm(args, rank, world):
     peak, peak_kind = load_peaks()
     achieved = alg / (splat_avg_ms / 1e3) / 1e9
     traffic = os.environ.get("SC_SPLAT_TRAFFIC_BYTES")
+    tables_gb = (pipe.psf.tables.numel() + (pipe.psf.box.numel() if pipe.psf.box is not None
+                                            else 0)) * 4 / 1e9
     result = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded uniform positions, Gaussian Brownian steps)",
+        "data": "synthetic (seeded uniform initial positions, Philox Brownian steps on the GPU)",
         "config": {"workload": WORKLOAD + ("_z0.1um_profiling" if args.small else ""),
-                   "n_emitters": N_EMIT, "image": [IMAGE, IMAGE],
-                   "substeps": SUBSTEPS, "exposure_s": EXPOSURE, "pixel_nm": PX * 1e9,
-                   "camera": "sCMOS per-pixel sigma, 12-bit", "psf": "Born-Wolf TRITC, 1002 depth keys",
+                   "n_emitters": N_EMIT, "image": [IMAGE, IMAGE], "substeps": SUBSTEPS,
+                   "exposure_s": EXPOSURE, "pixel_nm": PX * 1e9,
+                   "camera": "sCMOS per-pixel sigma, 12-bit",
+                   "psf": "Born-Wolf TRITC, %d depth keys" % len(pipe.psf.slot_of),
                    "tile": pipe.tile, "warps_per_tile": pipe.warps,
+                   "step": "one frame: Brownian sub-steps, physics, binning, splat, camera "
+                           "(one CUDA graph replay)",
                    "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (PSF tables %.1f GB)" % (
-                       (pipe.psf.tables.numel() + (pipe.psf.box.numel() if pipe.psf.box is not None
-                                                   else 0)) * 4 / 1e9),
+                   "l2": "inputs larger than L2 (PSF tables %.1f GB)" % tables_gb,
                    "psf_build_s": round(psf_build_s, 3)},
         "e2e": e2e,
-        "gpu_launches": 7 * args.steps,
+        "gpu_launches": fg.launches_per_frame * args.steps,
         "clocks": clk,
-        "roofline": {"kernel": "splat_halo_kernel + splat_merge_kernel", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": "splat_box_kernel + splat_sat_kernel + splat_merge_kernel",
+                     "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
                      "traffic": float(traffic) if traffic else None,
-                     "algorithmic_bytes": alg, "avg_launch_ms": splat_avg_ms},
+                     "algorithmic_bytes": alg, "avg_launch_ms": splat_avg_ms,
+                     "timed_on": "%d eager frames after the timed graph replays" % n_timing},
     }
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline()
@@ -268,6 +278,7 @@ def e2e_arm(args, cfg, dev, rank, world):
     n_frames = args.warmup + args.steps
     times, pos = trajectories(n_frames, seed=21 + rank)
     ids = numpy.arange(N_EMIT, dtype=float)
+    # host inputs exactly as scopyon.sample_inputs returns them: [(t, (N, 5) [x, y, z, id, 1])]
     inputs = [(float(t), numpy.hstack([pos[k], ids[:, None], numpy.ones((N_EMIT, 1))]))
               for k, t in enumerate(times)]
     gen = sg.generate_images(inputs, n_frames, config=cfg, rng=numpy.random.RandomState(3 + rank),

@@ -105,6 +105,7 @@ typedef struct {
     int32_t table_n;         /* CMOS noise table length                                    */
     uint64_t seed;           /* Philox key for native draws                                */
     uint64_t counter;        /* Philox counter base (e.g. frame index)                     */
+    const int64_t *d_frame;  /* optional device counter f added to counter (graph replay)   */
 } ScCameraParams;
 
 typedef struct {
@@ -115,11 +116,16 @@ typedef struct {
     int32_t pad;
     int64_t step0;           /* global index of the frame's first sub-step (Philox counter) */
     uint64_t seed;           /* Philox key                                                  */
+    const int64_t *d_frame;  /* optional device counter f: step0 += f * n_sub (graph replay) */
     double lower[3], upper[3];        /* box of the periodic / reflecting boundary          */
     double scale, origin[3], unit_x[3], unit_y[3], unit_z[3];  /* preprocessing transform  */
 } ScDiffuseParams;
 
 int sc_get_version(void);
+
+/* *d_counter += delta on the stream: advances the device frame counter read by
+ * sc_diffuse_steps and sc_camera, so that a captured frame can be replayed. */
+int sc_counter_add(int64_t *d_counter, int64_t delta, void *stream);
 const char *sc_last_error(void);
 
 /* Radial PSF tables for n_keys depths, n_r radii each (r_i = i * res).
@@ -176,6 +182,24 @@ int sc_emitter_steps(const ScStepParams *p, const double *d_particles,
                      const int32_t *d_key_slot,
                      double *d_budget, double *d_optinfo, ScStepRec *d_recs,
                      int32_t *d_status, void *stream);
+
+/* The footprint half of sc_emitter_steps alone: depth key and footprint of
+ * every (sub-step, slot) whose normalisation sits in d_recs[..].x0 (written
+ * by sc_native_substeps).                                                    */
+int sc_emitter_footprints(const ScStepParams *p, const double *d_particles,
+                          const int32_t *d_key_slot, ScStepRec *d_recs, int32_t *d_status,
+                          void *stream);
+
+/* Native frame sub-steps: sc_diffuse_steps fused with the emitter physics of
+ * sc_emitter_steps (excitation, emitted photons, photon budget,
+ * normalisation) for trajectories that live on the device; the normalisation
+ * of each (sub-step, slot) goes to d_recs[..].x0 for sc_emitter_footprints.
+ * Replaces move_points and __overlay_molecule_plane's per-particle physics
+ * (src/scopyon/sampling.py:88-119, src/scopyon/_epifm.py:1267-1315).       */
+int sc_native_substeps(const ScDiffuseParams *p, const ScStepParams *sp, double *d_pos,
+                       const int32_t *d_class, const double *d_sigma, const double *d_normals,
+                       const double *d_unit_time, double *d_budget, double *d_particles,
+                       ScStepRec *d_recs, void *stream);
 
 /* Bytes of scratch sc_bin_steps needs for n_rec records on n_tiles_total tiles. */
 size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total);

@@ -50,14 +50,15 @@ class CameraParams(ctypes.Structure):
                 ("readout_noise", ctypes.c_double), ("emgain", ctypes.c_double),
                 ("fullwell", ctypes.c_double), ("offset0", ctypes.c_double),
                 ("gain0", ctypes.c_double), ("table_n", ctypes.c_int32),
-                ("seed", ctypes.c_uint64), ("counter", ctypes.c_uint64)]
+                ("seed", ctypes.c_uint64), ("counter", ctypes.c_uint64),
+                ("d_frame", ctypes.c_void_p)]
 
 
 class DiffuseParams(ctypes.Structure):
     _fields_ = [("n_particles", ctypes.c_int32), ("n_sub", ctypes.c_int32),
                 ("ndim", ctypes.c_int32), ("boundary", ctypes.c_int32),
                 ("n_class", ctypes.c_int32), ("pad", ctypes.c_int32),
-                ("step0", ctypes.c_int64), ("seed", ctypes.c_uint64),
+                ("step0", ctypes.c_int64), ("seed", ctypes.c_uint64), ("d_frame", ctypes.c_void_p),
                 ("lower", ctypes.c_double * 3), ("upper", ctypes.c_double * 3),
                 ("scale", ctypes.c_double), ("origin", ctypes.c_double * 3),
                 ("unit_x", ctypes.c_double * 3), ("unit_y", ctypes.c_double * 3),
@@ -69,9 +70,13 @@ _I = ctypes.c_int
 _D = ctypes.c_double
 _SIG = {
     "sc_get_version": (_I, []),
+    "sc_counter_add": (_I, [_P, ctypes.c_int64, _P]),
     "sc_last_error": (ctypes.c_char_p, []),
     "sc_psf_radial": (_I, [_I, _D, _D, _D, _P, _I, _I, _D, _P, _P]),
     "sc_diffuse_steps": (_I, [ctypes.POINTER(DiffuseParams), _P, _P, _P, _P, _P, _P]),
+    "sc_native_substeps": (_I, [ctypes.POINTER(DiffuseParams), ctypes.POINTER(StepParams), _P, _P,
+                                _P, _P, _P, _P, _P, _P, _P]),
+    "sc_emitter_footprints": (_I, [ctypes.POINTER(StepParams), _P, _P, _P, _P, _P]),
     "sc_psf_quadrant_sat": (_I, [_P, _I, _I, _D, _P, _I, _P]),
     "sc_psf_box_table": (_I, [_P, _I, _I, _I, _I, _P, _P]),
     "sc_emitter_steps": (_I, [ctypes.POINTER(StepParams), _P, _P, _P, _P, _P, _P, _P, _P, _P]),

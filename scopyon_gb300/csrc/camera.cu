@@ -21,6 +21,7 @@ struct CamConsts {
     double qe, background, readout, emgain, fullwell, adc_max, offset0, gain0;
     float qe_f, background_f, readout_f, emgain_f, fullwell_f, adc_max_f, offset0_f, inv_gain0_f;
     uint64_t seed, counter;
+    const int64_t *frame;
 };
 
 // Poisson variate.  Small means: sequential inversion.  Large means: the
@@ -103,6 +104,7 @@ __global__ void camera_kernel(CamConsts c, const float *__restrict__ photons,
                               float *__restrict__ expect, double *__restrict__ adc64,
                               float *__restrict__ adc32, int32_t *status) {
     const int stride = gridDim.x * blockDim.x;
+    const uint64_t counter = c.counter + (c.frame ? (uint64_t)*c.frame : 0);
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.n; p += stride) {
         const double ph = (double)photons[p] + c.background;
         const double e = __dmul_rn(c.qe, ph);
@@ -125,7 +127,7 @@ __global__ void camera_kernel(CamConsts c, const float *__restrict__ photons,
             if (adc32) adc32[p] = (float)v;
             continue;
         }
-        sc::rng_stream rs(c.seed, (uint32_t)p, (uint32_t)c.counter, (uint32_t)(c.counter >> 32));
+        sc::rng_stream rs(c.seed, (uint32_t)p, (uint32_t)counter, (uint32_t)(counter >> 32));
         const float ef = (float)e;
         float signal, noise;
         switch (c.camera) {
@@ -281,6 +283,7 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
     c.inv_gain0_f = (float)(1.0 / p->gain0);
     c.seed = p->seed;
     c.counter = p->counter;
+    c.frame = p->d_frame;
     const int block = 256;
     int grid = (c.n + block - 1) / block;
     if (grid > 152 * 16) grid = 152 * 16;

@@ -124,8 +124,9 @@ int step_consts(const ScStepParams *p, StepConsts &c) {
     c.half_w = (double)p->nw * p->px * 0.5;
     c.half_h = (double)p->nh * p->px * 0.5;
     c.half_sig = p->res * (double)(p->n_signal - 1) * 0.5;
-    c.inv_px = 1.0 / p->px;
     c.inv_res = 1.0 / p->res;
+    c.inv_px_f = (float)(1.0 / p->px);
+    c.inv_res_f = (float)(1.0 / p->res);
     return SC_OK;
 }
 
@@ -151,4 +152,18 @@ extern "C" int sc_emitter_steps(const ScStepParams *p, const double *d_particles
     emitter_footprint_kernel<<<(unsigned)((n_rec + 255) / 256), 256, 0, st>>>(
         c, d_particles, d_key_slot, d_recs, d_status);
     return sc::launch_status("sc_emitter_steps");
+}
+
+extern "C" int sc_emitter_footprints(const ScStepParams *p, const double *d_particles,
+                                     const int32_t *d_key_slot, ScStepRec *d_recs,
+                                     int32_t *d_status, void *stream) {
+    sc::StepConsts c;
+    int rc = sc::step_consts(p, c);
+    if (rc) return rc;
+    if (c.n_particles == 0 || c.n_sub == 0) return SC_OK;
+    SC_REQUIRE(d_particles && d_key_slot && d_recs, "sc_emitter_footprints: NULL pointer");
+    const int64_t n_rec = (int64_t)c.n_sub * c.n_particles;
+    emitter_footprint_kernel<<<(unsigned)((n_rec + 255) / 256), 256, 0, sc::as_stream(stream)>>>(
+        c, d_particles, d_key_slot, d_recs, d_status);
+    return sc::launch_status("sc_emitter_footprints");
 }

@@ -12,7 +12,8 @@ struct StepConsts {
     int nw, nh, n_signal, n_sub, n_particles, max_key;
     double amplitude0, penetration, x_sec, qy, beer, norm_coeff;
     int bleaching, with_optinfo, box_p, box_nq;
-    double half_w, half_h, half_sig, inv_px, inv_res;
+    double half_w, half_h, half_sig, inv_res;
+    float inv_px_f, inv_res_f;
 };
 
 int step_consts(const ScStepParams *p, StepConsts &c);
@@ -27,48 +28,53 @@ __device__ __forceinline__ double emit_photons(const StepConsts &c, double ampli
 }
 
 // floor(x / d) and ceil(x / d) as the reference computes them (one correctly
-// rounded FP64 division, then floor / ceil).  The quotient is estimated with a
-// multiplication by 1/d (relative error ~2^-51); only when the estimate lies
-// within 1e-9 of an integer, where the rounding of the true division could
-// decide the result, is the division itself evaluated.  FP64 division costs
-// dozens of instructions on this GPU; the estimate costs one.
-__device__ __forceinline__ double floor_div(double x, double d, double inv_d) {
-    const double q = x * inv_d;
-    if (fabs(q - rint(q)) > 1e-9 * fmax(1.0, fabs(q))) return floor(q);
+// rounded FP64 division, then floor / ceil).  The quotient is estimated in
+// FP32 (relative error < 2^-22); only when the estimate lies within 1e-3 of an
+// integer -- where the rounding of the true division could decide the result
+// -- is the FP64 division evaluated.  FP64 instructions run at 1/64 of the
+// FP32 rate on this GPU; the estimate costs one conversion.
+__device__ __forceinline__ double floor_div(double x, double d, float inv_d) {
+    const float q = (float)x * inv_d;
+    if (fabsf(q - rintf(q)) > 1e-3f * fmaxf(1.f, fabsf(q))) return (double)floorf(q);
     return floor(x / d);
 }
 
-__device__ __forceinline__ double ceil_div(double x, double d, double inv_d) {
-    const double q = x * inv_d;
-    if (fabs(q - rint(q)) > 1e-9 * fmax(1.0, fabs(q))) return ceil(q);
+__device__ __forceinline__ double ceil_div(double x, double d, float inv_d) {
+    const float q = (float)x * inv_d;
+    if (fabsf(q - rintf(q)) > 1e-3f * fmaxf(1.f, fabsf(q))) return (double)ceilf(q);
     return ceil(x / d);
 }
 
 // Footprint of one axis (_epifm.py:233-258): first pixel, number of bounds,
-// the exact FP64 origin and the first bound's unrounded value (to ~1e-13),
-// also as a double-float.
+// the exact FP64 origin, and the first bound's unrounded value a as a
+// double-float (a_hi + a_lo, ~1e-12 absolute).
 __device__ __forceinline__ void axis_footprint(double half_len, double coord, double half_sig,
-                                               double px, double inv_px, double inv_res,
+                                               double px, float inv_px, double inv_res,
                                                int n_pix, double &origin, int16_t &start,
-                                               int16_t &count, float &a_hi, float &a_lo,
-                                               double &a) {
-    origin = (half_len + coord) - half_sig;
+                                               int16_t &count, float &a_hi, float &a_lo) {
+    const double centre = half_len + coord;
+    origin = centre - half_sig;
     const double lo = floor_div(origin, px, inv_px);
-    const double hi = ceil_div((half_len + coord) + half_sig, px, inv_px);
+    const double hi = ceil_div(centre + half_sig, px, inv_px);
     const double lo_c = fmax(lo, 0.0);
     const double hi_c = fmin(hi, (double)n_pix);
     start = 0;
     count = 0;
     a_hi = a_lo = 0.f;
-    a = 0.0;
     if (!(hi_c >= lo_c)) return;
     const int i0 = (int)lo_c;
     const int n = (int)hi_c - i0 + 1;
     start = (int16_t)i0;
     count = (int16_t)n;
-    a = (__dmul_rn((double)i0, px) - origin) * inv_res;
+    const double a = (__dmul_rn((double)i0, px) - origin) * inv_res;
     a_hi = (float)a;
     a_lo = (float)(a - (double)a_hi);
+}
+
+// a - rint(a) from its double-float form (exact to ~1e-11 near zero).
+__device__ __forceinline__ float frac_to_int(float a_hi, float a_lo, float &r) {
+    r = rintf(a_hi);
+    return (a_hi - r) + a_lo;
 }
 
 __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, double rel1,
@@ -87,7 +93,7 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     const double depth = fabs(rel0);
     int key;
     if (depth < c.depth_cutoff + c.res) {
-        const double kd = floor_div(depth, c.res, c.inv_res);  // int() of a non-negative
+        const double kd = floor_div(depth, c.res, c.inv_res_f);  // int() of a non-negative
         if (kd > (double)c.max_key) {
             flag_status(status, 0, i, s, 0);
             return;
@@ -104,21 +110,23 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     }
     int16_t si, ni, sj, nj;
     float axh, axl, ayh, ayl;
-    double x0, y0, ax, ay;
-    axis_footprint(c.half_w, rel1, c.half_sig, c.px, c.inv_px, c.inv_res, c.nw, x0, si, ni, axh,
-                   axl, ax);
-    axis_footprint(c.half_h, rel2, c.half_sig, c.px, c.inv_px, c.inv_res, c.nh, y0, sj, nj, ayh,
-                   ayl, ay);
+    double x0, y0;
+    axis_footprint(c.half_w, rel1, c.half_sig, c.px, c.inv_px_f, c.inv_res, c.nw, x0, si, ni, axh,
+                   axl);
+    axis_footprint(c.half_h, rel2, c.half_sig, c.px, c.inv_px_f, c.inv_res, c.nh, y0, sj, nj, ayh,
+                   ayl);
     if (ni < 2 || nj < 2) return;
+    float rx, ry;
+    const float dx = frac_to_int(axh, axl, rx), dy = frac_to_int(ayh, ayl, ry);
     // Box path: with an integer pitch of P grid rows, bound k is ceil(a) + P k
     // for every k unless a lies within 1e-9 of an integer (FP64 evaluation
     // noise and the estimate of a are ~1e-12 here); those emitters keep the
     // summed-area path.
-    if (c.box_p > 0 && fabs(ax - rint(ax)) > 1e-9 && fabs(ay - rint(ay)) > 1e-9) {
+    if (c.box_p > 0 && fabsf(dx) > 1e-9f && fabsf(dy) > 1e-9f) {
         // entry of pixel (i_start, j_start) in the phase-major box table of the
-        // key: first rows m = l0 + P >= 1 split as (m mod P, m div P)
+        // key: first rows m = l0 + P >= 1 split as (m mod P, m div P), l0 = ceil(a)
         const int P = c.box_p, NQ = c.box_nq;
-        const int mx = (int)ceil(ax) + P, my = (int)ceil(ay) + P;
+        const int mx = (int)rx + (dx > 0.f ? 1 : 0) + P, my = (int)ry + (dy > 0.f ? 1 : 0) + P;
         rec.box = 1;
         rec.box_off = (int64_t)slot * ((int64_t)P * P * NQ * NQ) +
                       ((int64_t)((mx % P) * P + (my % P)) * NQ + mx / P) * NQ + my / P;

@@ -468,7 +468,7 @@ class FramePipeline:
             ev.setdefault("splat", []).append((e0, e1))
 
     def camera(self, photons, expect, adc64, adc32=None, seed=0, counter=0, draws=None,
-               stream=None):
+               stream=None, d_frame=None):
         """Camera model + ADC on one frame (photons: float32 W*H on the device)."""
         cfg = self.cfg
         s = stream_ptr(stream)
@@ -485,6 +485,7 @@ class FramePipeline:
         cp.offset0, cp.gain0 = float(cfg.offset.flat[0]), float(cfg.gain.flat[0])
         cp.table_n = 0 if self.table_value is None else self.table_value.numel()
         cp.seed, cp.counter = int(seed) & (2 ** 64 - 1), int(counter) & (2 ** 64 - 1)
+        cp.d_frame = None if d_frame is None else d_frame.data_ptr()
         inj_noise = inj_signal = inj_uniform = None
         if draws is not None:
             dev = self.device
@@ -555,7 +556,7 @@ class FramePipeline:
                                      bleaching, stream)
 
     def run_frame_device(self, part, ut, n_sub, n, with_optinfo=True, draws=None, seed=0,
-                         counter=0, present=None, bleaching=None, stream=None):
+                         counter=0, present=None, bleaching=None, stream=None, d_frame=None):
         """One frame from device tensors: part (n_sub*n*5 f64), ut (n_sub f64)."""
         s = stream_ptr(stream)
         self.ensure_slots(n)
@@ -570,5 +571,78 @@ class FramePipeline:
                  ptr(self.budget), ptr(optinfo), ptr(recs), ptr(self.status), s)
         self.splat_records(recs, n_rec, self.image, stream=stream)
         self.camera(self.image, self.expect, self.adc, seed=seed, counter=counter, draws=draws,
-                    stream=stream)
+                    stream=stream, d_frame=d_frame)
         return self.expect, self.adc, (optinfo[: n * 8].view(n, 8) if with_optinfo else None)
+
+
+class FrameGraph:
+    """Frames of device trajectories replayed from one captured CUDA graph.
+
+    Every frame runs the same kernel sequence -- Brownian sub-steps, emitter
+    physics and footprints, tile binning, splat, camera -- on fixed buffers;
+    the only per-frame quantity, the frame index that offsets the Philox
+    counters, lives in device memory and is advanced by the graph itself.
+    Launch cost per frame is one graph launch.  Outputs (``pipe.expect``,
+    ``pipe.adc``) are overwritten by each frame.
+    """
+
+    def __init__(self, pipe, traj, n_sub, unit_time, first_frame=0, transform=None, seed=0,
+                 use_graph=True):
+        self.pipe, self.traj, self.n_sub = pipe, traj, int(n_sub)
+        self.n = traj.n_particles
+        dev = pipe.device
+        traj.prepare_uniform(self.n_sub)
+        if traj._index != first_frame * self.n_sub:
+            traj.advance_to(first_frame * self.n_sub, transform)
+        self.frame = torch.full((1,), int(first_frame), dtype=torch.int64, device=dev)
+        self.part = torch.empty(self.n_sub * self.n * 5, dtype=torch.float64, device=dev)
+        self.ut = torch.full((self.n_sub,), float(unit_time), dtype=torch.float64, device=dev)
+        self.transform = transform
+        self.seed = int(seed)
+        pipe.ensure_slots(self.n)
+        self.graph = None
+        self.use_graph = use_graph
+        self.frames_done = 0
+
+    def _launch(self):
+        pipe, traj, s = self.pipe, self.traj, stream_ptr()
+        n_rec = self.n_sub * self.n
+        recs = pipe._buf("recs", max(n_rec, 1) * (_lib.STEP_REC_BYTES // 4), torch.int32)
+        dp = traj.params(0, self.n_sub, **(self.transform or {}))
+        dp.d_frame = self.frame.data_ptr()
+        sp = pipe.step_params(self.n_sub, self.n, False)
+        call("sc_native_substeps", dp, sp, ptr(traj._pos), ptr(traj._g_class), ptr(traj._g_sigma),
+             None, ptr(self.ut), ptr(pipe.budget), ptr(self.part), ptr(recs), s)
+        call("sc_emitter_footprints", sp, ptr(self.part), ptr(pipe.psf.key_slot), ptr(recs),
+             ptr(pipe.status), s)
+        pipe.splat_records(recs, n_rec, pipe.image)
+        pipe.camera(pipe.image, pipe.expect, pipe.adc, seed=self.seed, d_frame=self.frame)
+        call("sc_counter_add", ptr(self.frame), 1, s)
+
+    def capture(self):
+        """Run one frame eagerly (allocates every buffer), then capture the next."""
+        self._launch()
+        self.frames_done += 1
+        if not self.use_graph:
+            return
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._launch()
+        self.graph = g
+
+    def step(self):
+        if self.graph is None and self.use_graph:
+            self.capture()
+            return
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._launch()
+        self.frames_done += 1
+
+    @property
+    def launches_per_frame(self):
+        # native sub-steps, footprints, bin count/scan/scatter/sort, splat box/sat/merge,
+        # camera, counter (plus one memset)
+        return 11

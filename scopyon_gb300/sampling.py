@@ -183,6 +183,29 @@ class DeviceTrajectories:
              stream_ptr(stream))
         self._index = g0 + n
 
+    def prepare_uniform(self, n_sub):
+        """Device sigma / class tensors for frames of n_sub steps on a uniform time grid."""
+        dt = numpy.diff(self.times)
+        if len(dt) == 0 or not numpy.allclose(dt, dt[0], rtol=0, atol=1e-15):
+            raise ValueError("graph replay needs uniformly spaced time points")
+        if self.normals is not None:
+            raise ValueError("graph replay draws Philox normals; exact trajectories replay eagerly")
+        sig = numpy.zeros((n_sub, self.D.shape[0], 3))
+        sig[:, :, : self.ndim] = numpy.sqrt(2 * self.D * dt[0])
+        self._g_sigma = torch.from_numpy(sig).to(self.device)
+        self._g_class = torch.from_numpy(self.klass).to(self.device)
+        if self._pos is None:
+            self.reset()
+
+    def launch_frame(self, n_sub, out, d_frame, transform=None, stream=None):
+        """Enqueue one frame's sub-steps, step index taken from the device counter
+        ``d_frame`` (frame f covers steps f * n_sub ... f * n_sub + n_sub - 1).
+        Fixed arguments only, so it can be captured in a CUDA graph."""
+        p = self.params(0, n_sub, **(transform or {}))
+        p.d_frame = d_frame.data_ptr()
+        call("sc_diffuse_steps", p, ptr(self._pos), ptr(self._g_class), ptr(self._g_sigma), None,
+             ptr(out), stream_ptr(stream))
+
     def advance_to(self, k, transform=None, stream=None):
         if self._pos is None or self._index > k:
             self.reset()

@@ -179,3 +179,63 @@ def test_poisson_sampler_distribution(sg):
         chi2 = (((obs - exp) ** 2) / exp)[keep].sum()
         dof = keep.sum() - 1
         assert stats.chi2.sf(chi2, dof) > 1e-4, (photons, chi2, dof)
+
+
+def test_frame_graph_replay_matches_eager(sg):
+    """Frames replayed from one captured CUDA graph equal eagerly launched frames."""
+    from scopyon_gb300.base import _psf_for
+    from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {
+        "magnification": 100, "light_source": {"angle": 0.0},
+        "detector": {"type": "CMOS", "image_size": [48, 40], "exposure_time": 0.004},
+        "effects": {"photo_bleaching": {"switch": True, "half_life": 0.01}},
+        "gpu": {"cmos_noise": "scmos"}}})
+    outs = []
+    for use_graph in (False, True):
+        rng = numpy.random.RandomState(6)
+        eng = EngineConfig(cfg["default"], rng=rng)
+        pipe = FramePipeline(eng, "cuda", psf=_psf_for(eng, torch.device("cuda")))
+        pipe.scmos_sigma_map(rng)
+        t = numpy.arange(6 * 4 + 1) * 1e-3
+        traj = sg.sample_inputs(t, N=300, lower=[-3e-6, -3e-6, -0.3e-6], upper=[3e-6, 3e-6, 0.3e-6],
+                                D=0.5e-12, ndim=3, rng=rng)
+        pipe.psf.ensure(list(range(0, 700)))
+        pipe.ensure_slots(300)
+        pipe.budget[:300].copy_(torch.from_numpy(rng.exponential(0.02, 300) * eng.n_emit0))
+        fg = FrameGraph(pipe, traj, 4, 1e-3, seed=77, use_graph=use_graph)
+        frames = []
+        for _ in range(5):
+            fg.step()
+            frames.append(pipe.adc.cpu().numpy().copy())
+        pipe.check_status()
+        outs.append(numpy.array(frames))
+    numpy.testing.assert_array_equal(outs[0], outs[1])
+    assert outs[0].std(axis=0).max() > 0  # frames differ from one another
+
+
+def test_fused_native_physics_matches_separate_pass(sg):
+    """sc_native_substeps (diffusion + physics fused) equals sc_diffuse_steps followed by
+    sc_emitter_steps on the same Philox trajectory: identical expectation images."""
+    from scopyon_gb300.base import _psf_for
+    from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {
+        "magnification": 100,
+        "detector": {"type": "EMCCD", "image_size": [40, 40], "exposure_time": 0.004},
+        "effects": {"photo_bleaching": {"switch": False}}}})
+    t = numpy.arange(4 * 4 + 1) * 1e-3
+    traj = sg.sample_inputs(t, N=200, lower=[-2.5e-6, -2.5e-6, -0.2e-6], upper=[2.5e-6, 2.5e-6, 0.2e-6],
+                            D=0.4e-12, ndim=3, rng=numpy.random.RandomState(12))
+    eng = EngineConfig(cfg["default"])
+    pipe = FramePipeline(eng, "cuda", psf=_psf_for(eng, torch.device("cuda")))
+    pipe.psf.ensure(list(range(0, 800)))
+    fg = FrameGraph(pipe, traj.copy(), 4, 1e-3, seed=3, use_graph=False)
+    fused = []
+    for _ in range(4):
+        fg.step()
+        fused.append(pipe.expect.cpu().numpy().copy())
+    sim = sg.EPIFMSimulator(cfg, method="default", rng=numpy.random.RandomState(0))
+    sep = [info["expectation"] for _, info in sim.generate_images(traj.copy(), 4, full_output=True)]
+    for a, b in zip(fused, sep):
+        numpy.testing.assert_array_equal(a.reshape(40, 40).astype(float), b)

@@ -214,6 +214,24 @@ int sc_bin_steps(const ScStepRec *d_recs, int n_rec,
                  const ScSplatParams *p, void *d_ws, size_t ws_bytes,
                  int32_t *d_tile_start, int32_t *d_items, int32_t *d_status, void *stream);
 
+/* Largest tile count (tiles per image x images) sc_bin_steps_static takes. */
+#define SC_BIN_STATIC_MAX_TILES 65536
+
+/* sc_bin_steps without a caller workspace: the per-bin counts and cursors
+ * live in a fixed 1 MiB device array inside the library (room for
+ * SC_BIN_STATIC_MAX_TILES tiles; more returns SC_ERR_ARG).  For callers that
+ * cannot allocate device memory -- a C or FFI host handed only the record and
+ * output buffers, or a frame loop that must not allocate -- it calls no
+ * allocator.  The first call on a device looks up the array's address with
+ * that device current; make that first call before any stream capture.  The
+ * array is shared by every call on a device: calls that overlap in time (on
+ * different streams or host threads) race on it and must be serialised.
+ * No counterpart in the reference, which bins nothing
+ * (src/scopyon/_epifm.py:1262-1264).                                        */
+int sc_bin_steps_static(const ScStepRec *d_recs, int n_rec, const ScSplatParams *p,
+                        int32_t *d_tile_start, int32_t *d_items, int32_t *d_status,
+                        void *stream);
+
 /* Bytes of scratch sc_splat needs: one FP32 (tile + halo)^2 buffer per tile. */
 size_t sc_splat_workspace_bytes(const ScSplatParams *p);
 

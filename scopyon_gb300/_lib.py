@@ -83,6 +83,7 @@ _SIG = {
     "sc_bin_workspace_bytes": (ctypes.c_size_t, [_I, _I]),
     "sc_bin_steps": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P, _P, _P,
                           _P]),
+    "sc_bin_steps_static": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, _P, _P, _P]),
     "sc_splat_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(SplatParams)]),
     "sc_splat": (_I, [_P, _P, _P, _P, _P, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P,
                       _P, _P]),

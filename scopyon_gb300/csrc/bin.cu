@@ -10,6 +10,8 @@
 // bin's list is then sorted by record index: the final order is the
 // reference's own accumulation order (sub-step, then particle) and does not
 // depend on scheduling.
+#include <mutex>
+
 #include "sc_common.cuh"
 #include "bin.cuh"
 
@@ -219,4 +221,55 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
     bin_scatter_kernel<<<sgrid, 256, 0, s>>>(d_recs, n_rec, g, cursor, d_items);
     bin_sort_kernel<<<n_bins, 256, 0, s>>>(d_tile_start, d_items);
     return sc::launch_status("sc_bin_steps");
+}
+
+// ---------------------------------------------------------------------------
+// sc_bin_steps_static: the same counting sort with its counts and cursors in
+// a fixed device array instead of a caller workspace, for callers that have
+// no device allocator to hand (a C or FFI host that is given only the record
+// and output buffers) or that must not allocate per frame.
+namespace {
+
+static __device__ __align__(256) int32_t g_bin_scratch[4 * SC_BIN_STATIC_MAX_TILES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void *g_scratch_ptr[kMaxDevices];
+
+// Address of g_bin_scratch on the current device, looked up once per device.
+int bin_scratch(void **out) {
+    int dev = -1;
+    int rc = sc::cuda_status(cudaGetDevice(&dev), "sc_bin_steps_static: cudaGetDevice");
+    if (rc) return rc;
+    SC_REQUIRE(dev >= 0 && dev < kMaxDevices, "sc_bin_steps_static: device %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (g_scratch_ptr[dev] == nullptr) {
+        void *p = nullptr;
+        rc = sc::cuda_status(cudaGetSymbolAddress(&p, g_bin_scratch),
+                             "sc_bin_steps_static: cudaGetSymbolAddress");
+        if (rc) return rc;
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return SC_OK;
+}
+
+}  // namespace
+
+extern "C" int sc_bin_steps_static(const ScStepRec *d_recs, int n_rec, const ScSplatParams *p,
+                                   int32_t *d_tile_start, int32_t *d_items, int32_t *d_status,
+                                   void *stream) {
+    sc::TileGeom g;
+    int rc = sc::tile_geom(p, g);
+    if (rc) return rc;
+    SC_REQUIRE(g.n_tiles <= SC_BIN_STATIC_MAX_TILES,
+               "sc_bin_steps_static: %d tiles exceed the fixed scratch of %d tiles", g.n_tiles,
+               SC_BIN_STATIC_MAX_TILES);
+    void *ws = nullptr;
+    rc = bin_scratch(&ws);
+    if (rc) return rc;
+    // sc_bin_steps clears the counts on the stream before counting; the
+    // cursors are written by the scan.
+    return sc_bin_steps(d_recs, n_rec, p, ws, sizeof(g_bin_scratch), d_tile_start, d_items,
+                        d_status, stream);
 }

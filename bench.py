@@ -34,6 +34,7 @@ sys.path.insert(0, ROOT)
 N_EMIT = 20000
 IMAGE = 512
 SUBSTEPS = 20
+E2E_FRAMES = 20  # frames timed through the public API with host trajectories
 EXPOSURE = 0.010
 PX = 16e-6 / 100
 HALF = IMAGE * PX / 2
@@ -103,7 +104,7 @@ class ClockSampler:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.file,
                 stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -140,13 +141,13 @@ def splat_algorithmic_bytes(n_rec, tile, halo):
 
     Per emitter-step: its item index (4 B), the 32-byte record head, and the
     footprint's box-table block: (n_px)^2 FP32 pixel sums, n_px =
-    ceil(1998 nm / px) + 1 pixels per axis on average.  Per tile: the FP64
+    1998 nm / px + 1 pixels per axis on average.  Per tile: the FP32
     (tile + halo)^2 buffer written and read back by the merge; per pixel one
     FP32 image write.
     """
     n_px = 1998e-9 / PX + 1
     n_tiles = (IMAGE // tile) ** 2
-    return (n_rec * (4 + 32 + 4 * n_px * n_px) + n_tiles * (tile + halo) ** 2 * 8 * 2
+    return (n_rec * (4 + 32 + 4 * n_px * n_px) + n_tiles * (tile + halo) ** 2 * 4 * 2
             + 4 * IMAGE * IMAGE)
 
 
@@ -174,7 +175,7 @@ def gb300_arm(args, rank, world):
     pipe.scmos_sigma_map(rng)
     t0 = time.time()
     if args.small:
-        pipe.psf.ensure(list(range(0, int((Z_HALF + 0.3e-6) / 1e-9))))
+        pipe.psf.ensure(list(range(0, int(Z_HALF / 1e-9) + 2)))
     else:
         pipe.psf.ensure_all()
     torch.cuda.synchronize()
@@ -182,10 +183,14 @@ def gb300_arm(args, rank, world):
 
     # trajectories on the device: two populations (D = 0.01 and 1 um^2/s), Philox normals
     n_timing = 4
-    n_frames = args.warmup + args.steps + n_timing
+    n_frames = args.warmup + args.steps + n_timing + 8000
     dt = EXPOSURE / SUBSTEPS
     t = numpy.arange(n_frames * SUBSTEPS + 1) * dt
-    box = dict(lower=[-HALF, -HALF, -Z_HALF], upper=[HALF, HALF, Z_HALF], ndim=3, device=dev)
+    # reflecting walls at the field's edges and at z = +-Z_HALF keep the
+    # emitter density of the initial state (and, for --small, the depths
+    # inside the keys built above)
+    box = dict(lower=[-HALF, -HALF, -Z_HALF], upper=[HALF, HALF, Z_HALF], ndim=3, device=dev,
+               boundary="reflecting")
     slow = sg.sample_inputs(t, N=N_EMIT // 2, D=0.01e-12, rng=rng, **box)
     fast = sg.sample_inputs(t, N=N_EMIT - N_EMIT // 2, D=D_FAST, rng=rng, start=N_EMIT // 2, **box)
     traj = sg.concatenate(slow, fast)
@@ -200,8 +205,10 @@ def gb300_arm(args, rank, world):
     pipe.check_status()
     if world > 1:
         torch.distributed.barrier()
+    live0 = float((pipe.budget[:N_EMIT] > 0).float().mean())
     clocks = ClockSampler(dev.index)
     clocks.start()
+    time.sleep(0.15)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     start.record()
@@ -211,10 +218,10 @@ def gb300_arm(args, rank, world):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    live1 = float((pipe.budget[:N_EMIT] > 0).float().mean())
     elapsed_ms = start.elapsed_time(end)
-    clk = clocks.stop()
-    pipe.check_status()
-    # the splat's own duration: the same frames, launched eagerly with events around it
+    # the splat's own duration: the frames right after the timed ones, launched
+    # eagerly with events around the splat
     fg.graph, fg.use_graph = None, False
     pipe.kernel_events = {}
     for _ in range(n_timing):
@@ -222,6 +229,17 @@ def gb300_arm(args, rank, world):
     torch.cuda.synchronize()
     splat_ms = [a.elapsed_time(b) for a, b in pipe.kernel_events["splat"]]
     pipe.kernel_events = None
+    # keep the GPU busy with untimed graph frames so that nvidia-smi (100 ms
+    # period) samples the clocks under this load for at least 1 s in all
+    fg.use_graph = True
+    pad_ms = 1000.0 - elapsed_ms
+    t_pad = time.perf_counter()
+    while (time.perf_counter() - t_pad) * 1e3 < pad_ms and fg.frames_done + 50 < n_frames:
+        for _ in range(50):
+            fg.step()
+        torch.cuda.synchronize()
+    clk = clocks.stop()
+    pipe.check_status()
     if world > 1:
         tt = torch.tensor([elapsed_ms], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -254,11 +272,14 @@ def gb300_arm(args, rank, world):
                            "(one CUDA graph replay)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (PSF tables %.1f GB)" % tables_gb,
+                   "boundary": "reflecting",
+                   "timed_frames": [args.warmup, args.warmup + args.steps],
+                   "live_emitters": [round(live0, 4), round(live1, 4)],
                    "psf_build_s": round(psf_build_s, 3)},
         "e2e": e2e,
         "gpu_launches": fg.launches_per_frame * args.steps,
         "clocks": clk,
-        "roofline": {"kernel": "splat_box_kernel + splat_sat_kernel + splat_merge_kernel",
+        "roofline": {"kernel": "splat_box_tma_kernel + splat_sat_kernel + splat_merge_kernel",
                      "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
@@ -275,7 +296,8 @@ def e2e_arm(args, cfg, dev, rank, world):
     """Frames/s through the public API with host trajectories."""
     import torch
     import scopyon_gb300 as sg
-    n_frames = args.warmup + args.steps
+    steps = min(args.steps, E2E_FRAMES)
+    n_frames = args.warmup + steps
     times, pos = trajectories(n_frames, seed=21 + rank)
     ids = numpy.arange(N_EMIT, dtype=float)
     # host inputs exactly as scopyon.sample_inputs returns them: [(t, (N, 5) [x, y, z, id, 1])]
@@ -289,7 +311,7 @@ def e2e_arm(args, cfg, dev, rank, world):
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         img = next(gen)
         img.as_array()
     torch.cuda.synchronize()
@@ -298,7 +320,7 @@ def e2e_arm(args, cfg, dev, rank, world):
         t = torch.tensor([dt], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         dt = float(t.item())
-    return {"value": world * args.steps / dt, "unit": "frames/s",
+    return {"value": world * steps / dt, "unit": "frames/s", "frames": steps,
             "h2d_bytes_per_step": SUBSTEPS * N_EMIT * 5 * 8 + SUBSTEPS * 8,
             "d2h_bytes_per_step": IMAGE * IMAGE * 8 + 16}
 
@@ -406,8 +428,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--small", action="store_true",
-                    help="profiling case: depth range +-0.1 um and D = 0.01 um^2/s for all "
-                         "emitters (about 130 PSF keys, 3.7 GB of tables), no e2e or CPU legs")
+                    help="profiling case: depth range +-0.1 um between reflecting walls and "
+                         "D = 0.01 um^2/s for all emitters (102 PSF keys, 2.9 GB of tables), "
+                         "no e2e or CPU legs")
     args = ap.parse_args()
     if args.small:
         global Z_HALF, D_FAST

@@ -37,7 +37,8 @@ extern "C" {
 
 /* Status word written by kernels into a caller buffer (int[4]):
  * [0] error flags (bit0 bad PSF key, bit1 missing table, bit2 bounds overflow,
- *     bit3 RNG loop bound hit, bit4 capacity), [1..3] first offending index. */
+ *     bit3 RNG loop bound hit, bit4 capacity, bit5 a bounded wait for an
+ *     asynchronous copy ran out), [1..3] first offending index. */
 #define SC_STATUS_WORDS 4
 
 /* One emitter during one exposure sub-step, ready to be splatted (64 bytes).
@@ -48,8 +49,10 @@ typedef struct {
     int16_t j_start, n_j;/* same along y; n_i < 2 or n_j < 2 means nothing to splat   */
     float w;             /* normalisation * res^2: photons per unit table sum          */
     int32_t slot;        /* PSF table slot of the depth key; -1: nothing to splat      */
-    int32_t box;         /* 1: bounds are l0 + P*k exactly, use the box table          */
-    int32_t pad;
+    int32_t box;         /* 0: summed-area path; else bounds are l0 + P*k exactly and  */
+                         /* box - 1 is the phase (m_x mod P) * P + (m_y mod P) of the   */
+                         /* box-table block that holds the footprint                   */
+    int32_t box_local;   /* box path: that entry's (row << 16) | column in its block   */
     double x0, y0;       /* footprint origin along x / y in metres (exact FP64)      */
     float ax_hi, ax_lo;  /* (i_start*px - x0)/res as a double-float                   */
     float ay_hi, ay_lo;  /* (j_start*px - y0)/res as a double-float                   */
@@ -91,6 +94,7 @@ typedef struct {
     int32_t rec_per_image;   /* records per image (record r is in image r / rec_per_image); */
                              /* 0 means every record belongs to image 0                     */
     int32_t box_p, box_nq;   /* box tables: P rows per pixel and NQ pixel offsets, or 0     */
+    int32_t n_slots;         /* depth-key tables held in d_sat / d_box                      */
     double px, res;
 } ScSplatParams;
 
@@ -160,9 +164,15 @@ int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, const int32_t *d_c
  * every pixel start row m_x, m_y in [-P, NQ*P - P), the sum of the cartesian
  * grid over [m_x, m_x+P) x [m_y, m_y+P) clipped to the grid, stored as FP32 in
  * phase-major order [key][m_x mod P][m_y mod P][m_x div P][m_y div P] (with m
- * shifted by +P), NQ = (2 n_r - 1 + P - 1) / P + 1.  Built from the quadrant
- * tables of sc_psf_quadrant_sat.  With it, one emitter's footprint is one
- * contiguous block (the pixel sums of overlay_signal_, src/scopyon/_epifm.py:277-282). */
+ * shifted by +P), NQ = (2 n_r - 1 + P - 1) / P + 1.  Each (m_x mod P,
+ * m_y mod P) phase block of NQ x NQ values starts SC_BOX_BLOCK_FLOATS(NQ)
+ * floats after the previous one (NQ^2 rounded up to 16 bytes, padding zero),
+ * so a key takes P * P * SC_BOX_BLOCK_FLOATS(NQ) floats.  Built from the
+ * quadrant tables of sc_psf_quadrant_sat.  With it, one emitter's footprint
+ * is one contiguous, 16-byte aligned block (the pixel sums of
+ * overlay_signal_, src/scopyon/_epifm.py:277-282).                         */
+#define SC_BOX_BLOCK_FLOATS(nq) ((((nq) * (nq)) + 3) & ~3)
+
 int sc_psf_box_table(const float *d_sat, int n_keys, int n_r, int sat_pitch, int box_p,
                      float *d_box, void *stream);
 

@@ -159,14 +159,18 @@ __global__ void box_table_kernel(const float2 *__restrict__ sat, int n_r, int pi
     const int key = blockIdx.y;
     const int n_signal = 2 * n_r - 1;
     const float2 *G = sat + (size_t)key * (n_r + 1) * pitch;
-    const int per_key = P * P * nq * nq;  // < 2^31 for any grid the API accepts
+    const int nb = SC_BOX_BLOCK_FLOATS(nq);
+    const int per_key = P * P * nb;  // < 2^31 for any grid the API accepts
     float *out = box + (size_t)key * per_key;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < per_key; e += gridDim.x * blockDim.x) {
-        int rest = e;
-        const int qy = rest % nq; rest /= nq;
-        const int qx = rest % nq; rest /= nq;
-        const int ry = rest % P;
-        const int rx = rest / P;
+        const int inner = e % nb, phase = e / nb;
+        if (inner >= nq * nq) {  // block padding
+            out[e] = 0.f;
+            continue;
+        }
+        const int qy = inner % nq, qx = inner / nq;
+        const int ry = phase % P;
+        const int rx = phase / P;
         int a0 = qx * P + rx - P, b0 = qy * P + ry - P;
         int a1 = min(a0 + P, n_signal), b1 = min(b0 + P, n_signal);
         a0 = max(a0, 0);

@@ -34,7 +34,8 @@ struct SplatConsts {
     double px, res;
     float b_hi, b_lo;  // px / res as a double-float
     const float *box;  // box tables (NULL when px / res is not an integer)
-    int box_nq;        // row stride of a box table block
+    int box_nq;        // rows and columns of a box table block
+    int box_p;         // grid rows per pixel of the box tables
 };
 
 // Footprint bound k of one axis: ceil(((start + k) * px - origin) / res) with
@@ -197,6 +198,266 @@ splat_box_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__
     }
 }
 
+// ---------------------------------------------------------------------------
+// Box path, bulk-copy form.
+//
+// A box record's pixel sums are one contiguous phase block of the box table
+// (NQ x NQ floats, 16-byte aligned), and every entry of the block outside the
+// footprint is zero as well (those pixels do not meet the PSF grid).  One
+// cp.async.bulk moves the block into shared memory; the warp then adds it into
+// its tile buffer: block row q goes to buffer row q + dr, block column v to
+// buffer column v + dc (dr = ox - qx0, dc = oy - qy0 for a footprint whose
+// first pixel, entry (qx0, qy0) of the block, sits at (ox, oy) in the buffer).
+// A lane owns block column lane % 16 (lanes >= NQ idle) of the rows of parity
+// lane / 16.
+//
+// The tile buffer has a guard row and column before it, and the stage
+// buffers a zero row when NQ is odd, so a footprint whose block starts at
+// most one row and column before its first pixel -- every footprint not
+// clipped by the image's low edges -- is added as NQ / 2 unconditional row
+// pairs.  The others visit only the rows and columns that land in the buffer.
+// The buffer keeps even and odd rows in two halves 16 banks apart, so the
+// two rows a warp instruction touches never share a bank.
+//
+// Each warp runs a ring of `stages` block buffers with one mbarrier each; the
+// lane that decoded a record issues its copy, `stages` records ahead, so an SM
+// holds about warps x stages blocks of HBM reads in flight.  Record m of the
+// tile's list is taken by warp m mod NW; the NW buffers are summed at the end.
+
+constexpr uint32_t kWaitTries = 4096;      // polls per wait, each suspending up to:
+constexpr uint32_t kSuspendNs = 500000;    // 0.5 ms (a copy lands in microseconds)
+// Tile-buffer half row stride: 32 floats, with the odd half 16 floats (mod 32)
+// after the even one, so the two rows a warp instruction touches -- (even,
+// odd) at equal half-row index or (odd, even) one index apart -- are 16 banks
+// apart either way.
+constexpr int kBulkBsr = 32;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+// Waits until the phase of this parity has completed: at most kWaitTries
+// polls, each suspending the thread until completion or kSuspendNs.  The
+// result is uniform across the warp.
+__device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok = 0;
+    for (uint32_t tries = 0; tries < kWaitTries && !ok; ++tries) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
+            : "memory");
+    }
+    return __all_sync(0xffffffffu, ok != 0);
+}
+
+// One lane: global [src, src + bytes) -> shared dst, completion on bar.
+// src, dst and bytes are multiples of 16 bytes.
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes,
+                                          uint64_t *bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Splat descriptor of one record, decoded by the lane that loaded it:
+// (w, (dr + 128) | (dc + 128) << 8, rows [qlo, qhi) as qlo | qhi << 8,
+// bit 0: splat it, bit 1: the unconditional path applies).
+template <int NQ>
+__device__ __forceinline__ int4 decode_record(const ScStepRec *recs, const int32_t *items, int m,
+                                              bool valid, int x0, int y0, const SplatConsts &c,
+                                              int64_t table_floats, int nb, const float *&src,
+                                              int32_t *status, int tile) {
+    src = c.box;
+    if (!valid) return make_int4(0, 0, 0, 0);
+    const int4 *hp = reinterpret_cast<const int4 *>(recs + __ldg(items + m));
+    const int4 a = __ldg(hp), b = __ldg(hp + 1);
+    const int i_start = (int)(int16_t)(a.z & 0xffff), ni = (a.z >> 16) - 1;
+    const int j_start = (int)(int16_t)(a.w & 0xffff), nj = (a.w >> 16) - 1;
+    const int ox = i_start - x0, oy = j_start - y0;
+    const int qx0 = b.w >> 16, qy0 = b.w & 0xffff;
+    const int64_t off = ((int64_t)a.y << 32) | (uint32_t)a.x;
+    const int64_t blk = off - ((int64_t)qx0 * NQ + qy0);
+    bool ok = in_buffer(ox, oy, ni, nj, c.edge);
+    if (!ok) sc::flag_status(status, 2, i_start, j_start, tile);
+    if (blk < 0 || blk + nb > table_floats || (blk & 3) != 0) {
+        sc::flag_status(status, 2, (int)(blk >> 32), (int)blk, tile);
+        ok = false;
+    } else {
+        src = c.box + blk;
+    }
+    const int dr = ox - qx0, dc = oy - qy0;
+    const int qlo = max(0, -dr), qhi = min(NQ, c.edge - dr);
+    const int flags = (ok ? 1 : 0) | (ok && dr >= -1 && dc >= -1 ? 2 : 0);
+    return make_int4(b.x, (dr + 128) | ((dc + 128) << 8), qlo | (qhi << 8), flags);
+}
+
+template <int NW, int NQ>
+__global__ void __launch_bounds__(NW * 32, 20 / NW)
+splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
+                      const int32_t *__restrict__ items, SplatConsts c, int stages, int half_rows,
+                      int64_t table_floats, float *__restrict__ ws, int32_t *status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int BSR = kBulkBsr;
+    constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;  // stage buffer floats
+    constexpr int NB = SC_BOX_BLOCK_FLOATS(NQ);
+    const int E = c.edge, EE = c.edge * c.edge;
+    const int HB = half_rows * BSR + 16;  // odd half starts 16 banks after the even half
+    const int BS = (2 * HB + 31) & ~31;
+    float *acc = reinterpret_cast<float *>(smem_raw);                   // [NW][BS]
+    int4 *descs = reinterpret_cast<int4 *>(acc + NW * BS);              // [NW][2][32]
+    float *stage = reinterpret_cast<float *>(descs + NW * 64);          // [NW][stages][SB]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(stage + NW * stages * SB);  // [NW][stages]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x;
+    const int t = tile % c.tiles_per_image;
+    const int x0 = (t / c.tiles_y) * c.tile, y0 = (t % c.tiles_y) * c.tile;
+    for (int i = threadIdx.x; i < NW * BS; i += blockDim.x) acc[i] = 0.f;
+    for (int i = threadIdx.x; i < NW * stages * SB; i += blockDim.x) stage[i] = 0.f;
+    if (threadIdx.x < NW * stages) mbar_init(bars + threadIdx.x, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+
+    const int it0 = tile_start[tile], it1 = tile_start[tile + 1];
+    // records of this warp: m_k = it0 + warp + NW k, k < K
+    const int K = it1 - it0 > warp ? (it1 - it0 - warp + NW - 1) / NW : 0;
+    // buffer (r, c) is half (r + 1) & 1, entry ((r + 1) >> 1) * BSR + c + 1
+    float *my_acc = acc + warp * BS;
+    int4 *my_desc = descs + warp * 64;
+    float *my_stage = stage + warp * stages * SB;
+    uint64_t *my_bars = bars + warp * stages;
+    constexpr uint32_t bytes = NB * 4u;
+    const int col = lane & 15, rsel = lane >> 4;
+
+    // lane l decodes records 32 q + l of chunks q (cur) and q + 1 (nxt); the
+    // descriptors go to shared memory, the block addresses stay in registers
+    const float *cur_src, *nxt_src;
+    my_desc[lane] = decode_record<NQ>(recs, items, it0 + warp + NW * lane, lane < K, x0, y0, c,
+                                      table_floats, NB, cur_src, status, tile);
+    my_desc[32 + lane] =
+        decode_record<NQ>(recs, items, it0 + warp + NW * (32 + lane), 32 + lane < K, x0, y0, c,
+                          table_floats, NB, nxt_src, status, tile);
+    __syncwarp();
+    if (lane < min(stages, K)) bulk_copy(my_stage + lane * SB, cur_src, bytes, my_bars + lane);
+    int s = 0;
+    uint32_t parity = 0;
+    int k = 0;
+    for (; k < K; ++k) {
+        if (k > 0 && (k & 31) == 0) {
+            // chunk k / 32 + 1 replaces chunk k / 32 - 1, whose records are all done
+            cur_src = nxt_src;
+            const int kk = k + 32 + lane;
+            my_desc[(((k >> 5) + 1) & 1) * 32 + lane] =
+                decode_record<NQ>(recs, items, it0 + warp + NW * kk, kk < K, x0, y0, c,
+                                  table_floats, NB, nxt_src, status, tile);
+            __syncwarp();
+        }
+        if (!warp_wait(my_bars + s, parity)) {
+            if (lane == 0) sc::flag_status(status, 5, k, warp, tile);
+            break;
+        }
+        const int4 d = my_desc[((k >> 5) & 1) * 32 + (k & 31)];
+        if (d.w & 1) {
+            const float w = __int_as_float(d.x);
+            const int dr = (d.y & 0xff) - 128, dc = ((d.y >> 8) & 0xff) - 128;
+            // this lane's rows q = 2 i + rsel land in buffer rows dr + q
+            const int R = dr + 1 + rsel;
+            const float *B = my_stage + s * SB + rsel * NQ + col;
+            float *D = my_acc + (R & 1) * HB + (R >> 1) * BSR + dc + 1 + col;
+            if (d.w & 2) {
+                if (col < NQ) {
+#pragma unroll
+                    for (int i = 0; i < PAIRS; ++i)
+                        D[i * BSR] = fmaf(w, B[2 * i * NQ], D[i * BSR]);
+                }
+            } else {
+                const int qlo = d.z & 0xff, qhi = (d.z >> 8) & 0xff;
+                if (col < NQ && col + dc >= 0) {
+#pragma unroll
+                    for (int i = 0; i < PAIRS; ++i) {
+                        const int q = 2 * i + rsel;
+                        if (q >= qlo && q < qhi) D[i * BSR] = fmaf(w, B[2 * i * NQ], D[i * BSR]);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        // refill this buffer with record k + stages: its own lane issues
+        const int kn = k + stages;
+        if (kn < K && lane == (kn & 31))
+            bulk_copy(my_stage + s * SB, ((kn >> 5) == (k >> 5)) ? cur_src : nxt_src, bytes,
+                      my_bars + s);
+        if (++s == stages) {
+            s = 0;
+            parity ^= 1u;
+        }
+    }
+    if (k < K) {
+        // a wait ran out: wait (bounded) for every copy still in flight before
+        // the CTA's shared memory is released
+        const int last = min(K, k + stages);
+        for (int j = k; j < last; ++j) warp_wait(my_bars + j % stages, (uint32_t)((j / stages) & 1));
+    }
+    __syncthreads();
+    float *out = ws + (size_t)tile * EE;
+    for (int p = threadIdx.x; p < EE; p += blockDim.x) {
+        const int r = p / E, cc = p - (p / E) * E;
+        const int off = ((r + 1) & 1) * HB + ((r + 1) >> 1) * BSR + cc + 1;
+        float sum = 0.f;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) sum += acc[w * BS + off];
+        out[p] = sum;
+    }
+}
+
+// Bulk-copy box launch for block size NQ; done stays false when the geometry
+// does not fit it (the direct kernel then runs).
+template <int NW, int NQ>
+int launch_bulk(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
+                const SplatConsts &c, int n_tiles, int n_slots, float *ws, int32_t *status,
+                cudaStream_t s, bool &done) {
+    done = false;
+    constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;
+    constexpr int NB = SC_BOX_BLOCK_FLOATS(NQ);
+    // buffer rows -1 .. tile + 2 PAIRS - 2 and columns -1 .. tile + 14 are reachable
+    if (n_slots <= 0 || c.box_nq != NQ || c.tile + 15 > kBulkBsr || c.edge + 1 > kBulkBsr)
+        return SC_OK;
+    const int rows = max(c.edge, c.tile + 2 * PAIRS - 1) + 1;
+    const int half_rows = ((rows + 1) / 2 + 3) & ~3;  // multiple of 4: halves 16 banks apart
+    const int64_t table_floats = (int64_t)n_slots * c.box_p * c.box_p * NB;
+    const size_t fixed = (size_t)NW * ((2 * (half_rows * kBulkBsr + 16) + 31) & ~31) * sizeof(float) +
+                         (size_t)NW * 64 * sizeof(int4);
+    auto bulk_smem = [&](int st) {
+        return fixed + (size_t)NW * st * SB * sizeof(float) + (size_t)NW * st * sizeof(uint64_t);
+    };
+    int stages = 8;
+    while (stages > 1 && bulk_smem(stages) > 160 * 1024) --stages;
+    const size_t smem = bulk_smem(stages);
+    if (smem > 160 * 1024) return SC_OK;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(splat_box_bulk_kernel<NW, NQ>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return sc::cuda_status(e, "sc_splat: smem attribute");
+    }
+    splat_box_bulk_kernel<NW, NQ><<<n_tiles, NW * 32, smem, s>>>(
+        recs, tile_start, items, c, stages, half_rows, table_floats, ws, status);
+    done = true;
+    return sc::launch_status("sc_splat bulk-copy box");
+}
+
 // Summed-area path: the tile's second bin.  Adds into the tile buffer the box
 // kernel wrote (accumulate = 1) or writes it (accumulate = 0, no box tables).
 template <int NW>
@@ -273,10 +534,26 @@ __global__ void splat_merge_kernel(const float *__restrict__ ws, SplatConsts c, 
 
 template <int NW>
 int launch_splat(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
-                 const float2 *sat, const SplatConsts &c, int n_tiles, bool box, float *ws,
-                 int32_t *status, cudaStream_t s) {
+                 const float2 *sat, const SplatConsts &c, int n_tiles, int n_slots, bool box,
+                 float *ws, int32_t *status, cudaStream_t s) {
     const int ee = c.edge * c.edge;
     const int bs = (ee + 31) & ~31;
+    if (box) {
+        // bulk-copy kernel for blocks of 12..16 rows (pixels of 134..181 grid rows)
+        bool done = false;
+        int rc = SC_OK;
+        switch (c.box_nq) {
+            case 12: rc = launch_bulk<NW, 12>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            case 13: rc = launch_bulk<NW, 13>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            case 14: rc = launch_bulk<NW, 14>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            case 15: rc = launch_bulk<NW, 15>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            case 16: rc = launch_bulk<NW, 16>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            default: break;
+        }
+        if (rc) return rc;
+        if (done) box = false;  // the summed-area pass below accumulates
+    }
+    const bool staged = !box && c.box != nullptr;
     if (box) {
         const size_t smem = (size_t)NW * bs * sizeof(float) + (size_t)NW * 64 * sizeof(int4);
         SC_REQUIRE(smem <= 227 * 1024, "sc_splat: tile %d + halo %d needs %zu bytes of shared "
@@ -299,7 +576,7 @@ int launch_splat(const ScStepRec *recs, const int32_t *tile_start, const int32_t
         if (e != cudaSuccess) return sc::cuda_status(e, "sc_splat: smem attribute");
     }
     splat_sat_kernel<NW><<<n_tiles, NW * 32, smem, s>>>(recs, tile_start, items, sat, c, n_tiles,
-                                                        box ? 1 : 0, ws, status);
+                                                        (box || staged) ? 1 : 0, ws, status);
     return sc::launch_status("sc_splat summed-area");
 }
 
@@ -325,6 +602,7 @@ int splat_consts(const ScSplatParams *p, const sc::TileGeom &g, SplatConsts &c) 
     c.b_lo = (float)(b - (double)c.b_hi);
     c.box = nullptr;
     c.box_nq = 0;
+    c.box_p = 0;
     return SC_OK;
 }
 
@@ -354,16 +632,17 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
                    "sc_splat: box_p=%d / box_nq=%d inconsistent", p->box_p, p->box_nq);
         c.box = d_box;
         c.box_nq = p->box_nq;
+        c.box_p = p->box_p;
     }
     const float2 *sat = reinterpret_cast<const float2 *>(d_sat);
     cudaStream_t s = sc::as_stream(stream);
     float *ws = static_cast<float *>(d_ws);
     const bool box = d_box != nullptr;
     switch (g.warps) {
-        case 1: rc = launch_splat<1>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, box, ws, d_status, s); break;
-        case 2: rc = launch_splat<2>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, box, ws, d_status, s); break;
-        case 4: rc = launch_splat<4>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, box, ws, d_status, s); break;
-        default: rc = launch_splat<8>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, box, ws, d_status, s); break;
+        case 1: rc = launch_splat<1>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, box, ws, d_status, s); break;
+        case 2: rc = launch_splat<2>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, box, ws, d_status, s); break;
+        case 4: rc = launch_splat<4>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, box, ws, d_status, s); break;
+        default: rc = launch_splat<8>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, box, ws, d_status, s); break;
     }
     if (rc) return rc;
     const int64_t total = (int64_t)g.nw * g.nh * g.n_images;

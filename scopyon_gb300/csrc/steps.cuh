@@ -86,7 +86,7 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     rec.i_start = rec.j_start = 0;
     rec.n_i = rec.n_j = 0;
     rec.box = 0;
-    rec.pad = 0;
+    rec.box_local = 0;
     rec.slot = -1;
     rec.w = 0.f;
     if (norm <= 0.0) return;  // overlay_signal returns early (_epifm.py:216-217)
@@ -125,11 +125,13 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     if (c.box_p > 0 && fabsf(dx) > 1e-9f && fabsf(dy) > 1e-9f) {
         // entry of pixel (i_start, j_start) in the phase-major box table of the
         // key: first rows m = l0 + P >= 1 split as (m mod P, m div P), l0 = ceil(a)
-        const int P = c.box_p, NQ = c.box_nq;
+        const int P = c.box_p, NQ = c.box_nq, NB = SC_BOX_BLOCK_FLOATS(NQ);
         const int mx = (int)rx + (dx > 0.f ? 1 : 0) + P, my = (int)ry + (dy > 0.f ? 1 : 0) + P;
-        rec.box = 1;
-        rec.box_off = (int64_t)slot * ((int64_t)P * P * NQ * NQ) +
-                      ((int64_t)((mx % P) * P + (my % P)) * NQ + mx / P) * NQ + my / P;
+        const int phase = (mx % P) * P + (my % P);
+        rec.box = 1 + phase;
+        rec.box_local = ((mx / P) << 16) | (my / P);
+        rec.box_off = (int64_t)slot * ((int64_t)P * P * NB) + (int64_t)phase * NB +
+                      (mx / P) * NQ + my / P;
     }
     rec.x0 = x0;
     rec.y0 = y0;

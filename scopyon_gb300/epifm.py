@@ -212,7 +212,8 @@ class PSFTables:
         self.box_p = cfg.box_p
         n_signal = 2 * self.n_r - 1
         self.box_nq = (n_signal + self.box_p - 1) // self.box_p + 1 if self.box_p else 0
-        self.box_floats = self.box_p ** 2 * self.box_nq ** 2
+        self.box_block = (self.box_nq ** 2 + 3) & ~3  # phase blocks start on 16 bytes
+        self.box_floats = self.box_p ** 2 * self.box_block
         self.box = torch.empty(0, dtype=torch.float32, device=device) if self.box_p else None
 
     def _depth_of_key(self, key):
@@ -439,6 +440,7 @@ class FramePipeline:
         p.n_r, p.sat_pitch = self.psf.n_r, self.psf.pitch
         p.n_images, p.rec_per_image = n_images, rec_per_image
         p.box_p, p.box_nq = self.psf.box_p, self.psf.box_nq
+        p.n_slots = self.psf.capacity
         p.px, p.res = self.cfg.px, PSF_RES
         return p
 
@@ -529,7 +531,10 @@ class FramePipeline:
                 msgs.append("random-variate loop bound reached")
             if bits & 16:
                 msgs.append("bin capacity exceeded (%d entries)" % st[1])
-            raise _lib.ScopyonGPUError(_lib.SC_ERR_CAPACITY, "; ".join(msgs))
+            if bits & 32:
+                msgs.append("bounded wait for an asynchronous copy ran out (tile %d)" % st[3])
+            code = _lib.SC_ERR_TIMEOUT if bits == 32 else _lib.SC_ERR_CAPACITY
+            raise _lib.ScopyonGPUError(code, "; ".join(msgs))
 
     def run_frame(self, particles, unit_times, with_optinfo=True, draws=None, seed=0, counter=0,
                   present=None, bleaching=None, stream=None):

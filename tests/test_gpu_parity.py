@@ -77,9 +77,12 @@ def test_box_table(lib, golden):
     lib.call("sc_psf_quadrant_sat", lib.ptr(_dev(radial)), 1, 1000, 1e-9, lib.ptr(sat), pitch,
              lib.stream_ptr())
     nq = (1999 + P - 1) // P + 1
-    box = torch.zeros(P * P * nq * nq, dtype=torch.float32, device="cuda")
+    nb = (nq * nq + 3) & ~3
+    box = torch.full((P * P * nb,), -1.0, dtype=torch.float32, device="cuda")
     lib.call("sc_psf_box_table", lib.ptr(sat), 1, 1000, pitch, P, lib.ptr(box), lib.stream_ptr())
-    got = box.cpu().numpy().reshape(P, P, nq, nq)
+    blocks = box.cpu().numpy().reshape(P, P, nb)
+    assert (blocks[:, :, nq * nq:] == 0).all()  # block padding
+    got = blocks[:, :, :nq * nq].reshape(P, P, nq, nq)
     full = O.radial_to_cartesian(O.radial_grid(), radial[0])
     csum = numpy.zeros((2000, 2000))
     csum[1:, 1:] = full.cumsum(0).cumsum(1)

@@ -15,7 +15,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 REC = numpy.dtype([("box_off", "<i8"), ("i_start", "<i2"), ("n_i", "<i2"), ("j_start", "<i2"),
-                   ("n_j", "<i2"), ("w", "<f4"), ("slot", "<i4"), ("box", "<i4"), ("pad", "<i4"),
+                   ("n_j", "<i2"), ("w", "<f4"), ("slot", "<i4"), ("box", "<i4"), ("box_local", "<i4"),
                    ("x0", "<f8"), ("y0", "<f8"), ("ax_hi", "<f4"), ("ax_lo", "<f4"),
                    ("ay_hi", "<f4"), ("ay_lo", "<f4")])
 

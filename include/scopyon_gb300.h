@@ -193,23 +193,19 @@ int sc_emitter_steps(const ScStepParams *p, const double *d_particles,
                      double *d_budget, double *d_optinfo, ScStepRec *d_recs,
                      int32_t *d_status, void *stream);
 
-/* The footprint half of sc_emitter_steps alone: depth key and footprint of
- * every (sub-step, slot) whose normalisation sits in d_recs[..].x0 (written
- * by sc_native_substeps).                                                    */
-int sc_emitter_footprints(const ScStepParams *p, const double *d_particles,
-                          const int32_t *d_key_slot, ScStepRec *d_recs, int32_t *d_status,
-                          void *stream);
-
-/* Native frame sub-steps: sc_diffuse_steps fused with the emitter physics of
- * sc_emitter_steps (excitation, emitted photons, photon budget,
- * normalisation) for trajectories that live on the device; the normalisation
- * of each (sub-step, slot) goes to d_recs[..].x0 for sc_emitter_footprints.
- * Replaces move_points and __overlay_molecule_plane's per-particle physics
- * (src/scopyon/sampling.py:88-119, src/scopyon/_epifm.py:1267-1315).       */
-int sc_native_substeps(const ScDiffuseParams *p, const ScStepParams *sp, double *d_pos,
-                       const int32_t *d_class, const double *d_sigma, const double *d_normals,
-                       const double *d_unit_time, double *d_budget, double *d_particles,
-                       ScStepRec *d_recs, void *stream);
+/* Native frame records: sc_diffuse_steps and sc_emitter_steps in one pass
+ * for trajectories that live on the device.  For every (sub-step, particle)
+ * the Brownian move, excitation, emitted photons, photon budget, depth key
+ * and footprint are computed in the same order and with the same operations
+ * as those two calls, so d_recs ([n_sub][n_particles]) equals theirs bit for
+ * bit; the formatted positions are not stored.  d_pos and d_budget are
+ * advanced to the end of the frame.  Replaces move_points and
+ * __overlay_molecule_plane (src/scopyon/sampling.py:88-119,
+ * src/scopyon/_epifm.py:1267-1360).                                        */
+int sc_native_records(const ScDiffuseParams *p, const ScStepParams *sp, double *d_pos,
+                      const int32_t *d_class, const double *d_sigma, const double *d_normals,
+                      const double *d_unit_time, double *d_budget, const int32_t *d_key_slot,
+                      ScStepRec *d_recs, int32_t *d_status, void *stream);
 
 /* Bytes of scratch sc_bin_steps needs for n_rec records on n_tiles_total tiles. */
 size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total);

@@ -75,9 +75,8 @@ _SIG = {
     "sc_last_error": (ctypes.c_char_p, []),
     "sc_psf_radial": (_I, [_I, _D, _D, _D, _P, _I, _I, _D, _P, _P]),
     "sc_diffuse_steps": (_I, [ctypes.POINTER(DiffuseParams), _P, _P, _P, _P, _P, _P]),
-    "sc_native_substeps": (_I, [ctypes.POINTER(DiffuseParams), ctypes.POINTER(StepParams), _P, _P,
-                                _P, _P, _P, _P, _P, _P, _P]),
-    "sc_emitter_footprints": (_I, [ctypes.POINTER(StepParams), _P, _P, _P, _P, _P]),
+    "sc_native_records": (_I, [ctypes.POINTER(DiffuseParams), ctypes.POINTER(StepParams), _P, _P,
+                               _P, _P, _P, _P, _P, _P, _P, _P]),
     "sc_psf_quadrant_sat": (_I, [_P, _I, _I, _D, _P, _I, _P]),
     "sc_psf_box_table": (_I, [_P, _I, _I, _I, _I, _P, _P]),
     "sc_emitter_steps": (_I, [ctypes.POINTER(StepParams), _P, _P, _P, _P, _P, _P, _P, _P, _P]),

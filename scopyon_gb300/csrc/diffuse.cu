@@ -31,6 +31,7 @@ __device__ __forceinline__ double wrap_axis(double x, double lo, double hi, int 
         return r + lo;
     }
     if (boundary == 2) {  // reflecting walls at lo and hi
+        if (x >= lo && x <= hi) return x;
         for (int it = 0; it < 64 && (x < lo || x > hi); ++it) x = x < lo ? 2 * lo - x : 2 * hi - x;
         return fmin(fmax(x, lo), hi);
     }
@@ -73,21 +74,14 @@ __device__ __forceinline__ void philox_normals(const DiffConsts &c, int i, uint6
     nrm[2] = rb * cb;
 }
 
-// One thread per particle, sub-steps in order.  With physics (native frames)
-// the thread also runs the emitter physics of each sub-step -- excitation,
-// emitted photons, the photon-budget chain -- and parks the normalisation in
-// the record's x0 field for the footprint pass (0: nothing to splat).
-template <bool PHYSICS>
-__global__ void diffuse_kernel(DiffConsts c, sc::StepConsts sc_, double *pos, const int32_t *klass,
-                               const double *sigma, const double *normals, double *particles,
-                               const double *unit_time, double *budget, ScStepRec *recs) {
+// One thread per particle, sub-steps in order.
+__global__ void diffuse_kernel(DiffConsts c, double *pos, const int32_t *klass,
+                               const double *sigma, const double *normals, double *particles) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
     const int k = klass ? klass[i] : 0;
     const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
-    double b = PHYSICS && sc_.bleaching ? budget[i] : 0.0;
-    const bool epi = PHYSICS && isinf(sc_.penetration);
     for (int s = 0; s < c.n_sub; ++s) {
         const size_t idx = (size_t)s * c.n + i;
         double *q = particles + idx * 5;
@@ -98,23 +92,6 @@ __global__ void diffuse_kernel(DiffConsts c, sc::StepConsts sc_, double *pos, co
         q[2] = f[2];
         q[3] = (double)i;
         q[4] = 1.0;
-        if (PHYSICS) {
-            const double ut = unit_time[s];
-            const double rel0 = f[0] - sc_.focal[0];
-            double p_state = 1.0;
-            const double amp = epi ? sc_.amplitude0
-                                   : __dmul_rn(sc_.amplitude0, exp(-fabs(rel0) / sc_.penetration));
-            const double n_emit = sc::emit_photons(sc_, amp, ut);
-            if (sc_.bleaching) {
-                double nb = b - n_emit;
-                if (nb <= 0) {
-                    nb = 0;
-                    p_state = 0.0;
-                }
-                b = nb;
-            }
-            recs[idx].x0 = __dmul_rn(sc_.norm_coeff, __dmul_rn(p_state, n_emit) / (4.0 * M_PI));
-        }
         // one Brownian step: x_d += sigma_d * n_d (the reference's 0.0 + sigma * gauss)
         const double *sg = sigma + ((size_t)s * c.n_class + k) * 3;
         if (normals) {
@@ -123,7 +100,7 @@ __global__ void diffuse_kernel(DiffConsts c, sc::StepConsts sc_, double *pos, co
         } else {
             float nrm[3];
             philox_normals(c, i, (uint64_t)(step0 + s), nrm);
-            for (int d = 0; d < c.ndim; ++d) p[d] += sg[d] * (double)nrm[d];
+            for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], (double)nrm[d], p[d]);
         }
         if (c.boundary)
             for (int d = 0; d < c.ndim; ++d) p[d] = wrap_axis(p[d], c.lower[d], c.upper[d], c.boundary);
@@ -131,7 +108,150 @@ __global__ void diffuse_kernel(DiffConsts c, sc::StepConsts sc_, double *pos, co
     pos[3 * i] = p[0];
     pos[3 * i + 1] = p[1];
     pos[3 * i + 2] = p[2];
-    if (PHYSICS && sc_.bleaching) budget[i] = b;
+}
+
+// Native frame records for 32 particles per CTA, in three phases per chunk of
+// up to 32 sub-steps:
+//   1. all warps draw the Philox normals of every (sub-step, particle); under
+//      EPI (amplitude independent of depth) the emitted photons and the
+//      normalisation of each sub-step are computed once;
+//   2. warp 0, one lane per particle, runs the position chain and the
+//      photon-budget chain in sub-step order with the operations of
+//      diffuse_kernel and emitter_physics_kernel, storing each sub-step's
+//      position and normalisation in shared memory;
+//   3. all warps build the records, a warp per sub-step and a lane per
+//      particle (32 consecutive records, coalesced stores).
+// The records equal those of sc_diffuse_steps followed by sc_emitter_steps bit
+// for bit.  FP64 work runs with full warps only (GB300's FP64 rate is ~1/64 of
+// FP32, so a warp with a few active lanes wastes it).
+constexpr int kRecWarps = 4;
+
+// Shared memory of one CTA for `chunk` sub-steps: positions [chunk][32][3] and
+// normalisations [chunk][32] (FP64), per-sub-step photons and live-emitter
+// normalisation [chunk] (FP64), normals [chunk][32][3] (FP32).
+inline size_t rec_shared_bytes(int chunk) {
+    return (size_t)chunk * (32 * 3 * sizeof(double) + 32 * sizeof(double) + 2 * sizeof(double) +
+                            32 * 3 * sizeof(float));
+}
+
+__global__ void __launch_bounds__(kRecWarps * 32, 8)
+native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
+                      const int32_t *klass, const double *sigma, const double *normals,
+                      const double *unit_time, double *budget, const int32_t *key_slot,
+                      ScStepRec *recs, int32_t *status) {
+    extern __shared__ double rec_smem[];
+    double *s_pos = rec_smem;
+    double *s_norm = s_pos + chunk * 32 * 3;
+    double *s_emit = s_norm + chunk * 32;
+    double *s_norm1 = s_emit + chunk;
+    float *s_nrm = reinterpret_cast<float *>(s_norm1 + chunk);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * 32 + lane;  // this lane's particle
+    const bool live = i < c.n;
+    const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
+    const bool epi = isinf(k.penetration);
+    double p[3] = {0.0, 0.0, 0.0}, b = 0.0;
+    int cls = 0;
+    if (warp == 0 && live) {
+        p[0] = pos[3 * i];
+        p[1] = pos[3 * i + 1];
+        p[2] = pos[3 * i + 2];
+        b = k.bleaching ? budget[i] : 0.0;
+        cls = klass ? klass[i] : 0;
+    }
+    for (int s0 = 0; s0 < c.n_sub; s0 += chunk) {
+        const int ns = min(chunk, c.n_sub - s0);
+        // 1. normals; per-sub-step photons and normalisation under EPI
+        if (!normals) {
+            for (int j = warp; j < ns; j += kRecWarps) {
+                float nrm[3] = {0.f, 0.f, 0.f};
+                if (live) philox_normals(c, i, (uint64_t)(step0 + s0 + j), nrm);
+                float *d = s_nrm + (j * 32 + lane) * 3;
+                d[0] = nrm[0];
+                d[1] = nrm[1];
+                d[2] = nrm[2];
+            }
+        }
+        if (epi && warp == kRecWarps - 1) {
+            for (int j = lane; j < ns; j += 32) {
+                const double n_emit = sc::emit_photons(k, k.amplitude0, unit_time[s0 + j]);
+                s_emit[j] = n_emit;
+                // p_state = 1: __dmul_rn(1.0, n_emit) is n_emit
+                s_norm1[j] = __dmul_rn(k.norm_coeff, n_emit / (4.0 * M_PI));
+            }
+        }
+        __syncthreads();
+        // 2. the chains, one lane per particle
+        if (warp == 0 && live) {
+            for (int j = 0; j < ns; ++j) {
+                const int s = s0 + j;
+                double *ps = s_pos + (j * 32 + lane) * 3;
+                ps[0] = p[0];
+                ps[1] = p[1];
+                ps[2] = p[2];
+                double n_emit;
+                if (epi) {
+                    n_emit = s_emit[j];
+                } else {
+                    double f[3];
+                    format_point(c, p, f);
+                    const double rel0 = f[0] - k.focal[0];
+                    n_emit = sc::emit_photons(
+                        k, __dmul_rn(k.amplitude0, exp(-fabs(rel0) / k.penetration)), unit_time[s]);
+                }
+                bool alive = true;
+                if (k.bleaching) {
+                    double nb = b - n_emit;
+                    if (nb <= 0) {
+                        nb = 0;
+                        alive = false;
+                    }
+                    b = nb;
+                }
+                // p_state = 0 gives norm_coeff * (0 / 4 pi) = 0: no record
+                s_norm[j * 32 + lane] =
+                    !alive ? 0.0
+                           : (epi ? s_norm1[j] : __dmul_rn(k.norm_coeff, n_emit / (4.0 * M_PI)));
+                const double *sg = sigma + ((size_t)s * c.n_class + cls) * 3;
+                if (normals) {
+                    const double *nv = normals + ((size_t)s * c.n + i) * c.ndim;
+                    for (int d = 0; d < c.ndim; ++d) p[d] += __dmul_rn(sg[d], nv[d]);
+                } else {
+                    const float *nr = s_nrm + (j * 32 + lane) * 3;
+                    for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], (double)nr[d], p[d]);
+                }
+                if (c.boundary)
+                    for (int d = 0; d < c.ndim; ++d)
+                        p[d] = wrap_axis(p[d], c.lower[d], c.upper[d], c.boundary);
+            }
+        }
+        __syncthreads();
+        // 3. records: warp w takes sub-steps w, w + kRecWarps, ...
+        if (live) {
+            for (int j = warp; j < ns; j += kRecWarps) {
+                const int s = s0 + j;
+                const double *ps = s_pos + (j * 32 + lane) * 3;
+                const double q[3] = {ps[0], ps[1], ps[2]};
+                double f[3];
+                format_point(c, q, f);
+                const double norm = s_norm[j * 32 + lane];
+                ScStepRec rec;
+                if (k.focal_zero)
+                    sc::make_record(k, f[0], f[1], f[2], norm, key_slot, status, i, s, rec);
+                else
+                    sc::make_record(k, f[0] - k.focal[0], f[1] - k.focal[1], f[2] - k.focal[2],
+                                    norm, key_slot, status, i, s, rec);
+                recs[(size_t)s * c.n + i] = rec;
+            }
+        }
+        __syncthreads();
+    }
+    if (warp == 0 && live) {
+        pos[3 * i] = p[0];
+        pos[3 * i + 1] = p[1];
+        pos[3 * i + 2] = p[2];
+        if (k.bleaching) budget[i] = b;
+    }
 }
 
 }  // namespace
@@ -182,18 +302,17 @@ extern "C" int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, const i
     if (rc) return rc;
     if (c.n == 0 || c.n_sub == 0) return SC_OK;
     SC_REQUIRE(d_pos && d_sigma && d_particles, "sc_diffuse_steps: NULL pointer");
-    sc::StepConsts none{};
     const int block = 128;
-    diffuse_kernel<false><<<(c.n + block - 1) / block, block, 0, sc::as_stream(stream)>>>(
-        c, none, d_pos, d_class, d_sigma, d_normals, d_particles, nullptr, nullptr, nullptr);
+    diffuse_kernel<<<(c.n + block - 1) / block, block, 0, sc::as_stream(stream)>>>(
+        c, d_pos, d_class, d_sigma, d_normals, d_particles);
     return sc::launch_status("sc_diffuse_steps");
 }
 
-extern "C" int sc_native_substeps(const ScDiffuseParams *p, const ScStepParams *sp,
-                                  double *d_pos, const int32_t *d_class, const double *d_sigma,
-                                  const double *d_normals, const double *d_unit_time,
-                                  double *d_budget, double *d_particles, ScStepRec *d_recs,
-                                  void *stream) {
+extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *sp, double *d_pos,
+                                 const int32_t *d_class, const double *d_sigma,
+                                 const double *d_normals, const double *d_unit_time,
+                                 double *d_budget, const int32_t *d_key_slot, ScStepRec *d_recs,
+                                 int32_t *d_status, void *stream) {
     DiffConsts c;
     int rc = diff_consts(p, c);
     if (rc) return rc;
@@ -201,13 +320,15 @@ extern "C" int sc_native_substeps(const ScDiffuseParams *p, const ScStepParams *
     rc = sc::step_consts(sp, k);
     if (rc) return rc;
     SC_REQUIRE(k.n_particles == c.n && k.n_sub == c.n_sub,
-               "sc_native_substeps: diffusion and step sizes differ");
+               "sc_native_records: diffusion and step sizes differ");
     if (c.n == 0 || c.n_sub == 0) return SC_OK;
-    SC_REQUIRE(d_pos && d_sigma && d_particles && d_unit_time && d_recs,
-               "sc_native_substeps: NULL pointer");
-    SC_REQUIRE(!k.bleaching || d_budget, "sc_native_substeps: bleaching needs a budget array");
-    const int block = 64;
-    diffuse_kernel<true><<<(c.n + block - 1) / block, block, 0, sc::as_stream(stream)>>>(
-        c, k, d_pos, d_class, d_sigma, d_normals, d_particles, d_unit_time, d_budget, d_recs);
-    return sc::launch_status("sc_native_substeps");
+    SC_REQUIRE(d_pos && d_sigma && d_unit_time && d_key_slot && d_recs,
+               "sc_native_records: NULL pointer");
+    SC_REQUIRE(!k.bleaching || d_budget, "sc_native_records: bleaching needs a budget array");
+    const int chunk = c.n_sub < 32 ? c.n_sub : 32;
+    const size_t smem = rec_shared_bytes(chunk);
+    native_records_kernel<<<(c.n + 31) / 32, kRecWarps * 32, smem, sc::as_stream(stream)>>>(
+        c, k, chunk, d_pos, d_class, d_sigma, d_normals, d_unit_time, d_budget, d_key_slot, d_recs,
+        d_status);
+    return sc::launch_status("sc_native_records");
 }

@@ -51,6 +51,51 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
+// hi + lo of a double, on the device (three FP64-pipe conversions and one add).
+__device__ __forceinline__ df df_from(double x) {
+    const float h = __double2float_rn(x);
+    return df{h, __double2float_rn(x - (double)h)};
+}
+
+// (s, e) with |e| small against s -> normalised pair (Fast2Sum).
+__device__ __forceinline__ df df_norm(float s, float e) {
+    const float h = s + e;
+    return df{h, e - (h - s)};
+}
+
+__device__ __forceinline__ df df_add(df a, df b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e += a.lo + b.lo;
+    return df_norm(s, e);
+}
+
+__device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
+
+// Product with an error-free FMA for hi * hi; relative error ~2^-46.
+__device__ __forceinline__ df df_mul(df a, df b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return df_norm(p, e);
+}
+
+// a * k for an integer |k| < 2^24 (exact as a float).
+__device__ __forceinline__ df df_mul_i(df a, int k) {
+    const float kf = (float)k;
+    const float p = a.hi * kf;
+    float e = fmaf(a.hi, kf, -p);
+    e = fmaf(a.lo, kf, e);
+    return df_norm(p, e);
+}
+
+// Nearest integer r of a = hi + lo and the remainder a - r (exact to ~2^-46 |a|).
+__device__ __forceinline__ float df_round(df a, float &r) {
+    r = rintf(a.hi);
+    return (a.hi - r) + a.lo;
+}
+
 // acc += sign * (hi + lo), keeping acc as an unnormalised (s, e) pair.
 __device__ __forceinline__ void df_acc(float &s, float &e, float hi, float lo, float sign) {
     float t, err;

@@ -81,8 +81,12 @@ __global__ void emitter_footprint_kernel(sc::StepConsts c, const double *particl
     const double norm = recs[idx].x0;
     const double *q = particles + idx * 5;
     ScStepRec rec;
-    sc::make_record(c, q[0] - c.focal[0], q[1] - c.focal[1], q[2] - c.focal[2], norm, key_slot,
-                    status, (int)(idx % c.n_particles), (int)(idx / c.n_particles), rec);
+    const int i = (int)(idx % c.n_particles), s = (int)(idx / c.n_particles);
+    if (c.focal_zero)
+        sc::make_record(c, q[0], q[1], q[2], norm, key_slot, status, i, s, rec);
+    else
+        sc::make_record(c, q[0] - c.focal[0], q[1] - c.focal[1], q[2] - c.focal[2], norm,
+                        key_slot, status, i, s, rec);
     recs[idx] = rec;
 }
 
@@ -127,6 +131,19 @@ int step_consts(const ScStepParams *p, StepConsts &c) {
     c.inv_res = 1.0 / p->res;
     c.inv_px_f = (float)(1.0 / p->px);
     c.inv_res_f = (float)(1.0 / p->res);
+    auto split = [](double v) {
+        const float h = (float)v;
+        return df{h, (float)(v - (double)h)};
+    };
+    c.half_w_df = split(c.half_w);
+    c.half_h_df = split(c.half_h);
+    c.half_sig_df = split(c.half_sig);
+    c.nhalf_sig_df = split(-c.half_sig);
+    c.inv_px_df = split(1.0 / p->px);
+    c.px_df = split(p->px);
+    c.inv_res_df = split(c.inv_res);
+    c.cut_f = (float)(p->depth_cutoff + p->res);
+    c.focal_zero = p->focal[0] == 0.0 && p->focal[1] == 0.0 && p->focal[2] == 0.0;
     return SC_OK;
 }
 
@@ -152,18 +169,4 @@ extern "C" int sc_emitter_steps(const ScStepParams *p, const double *d_particles
     emitter_footprint_kernel<<<(unsigned)((n_rec + 255) / 256), 256, 0, st>>>(
         c, d_particles, d_key_slot, d_recs, d_status);
     return sc::launch_status("sc_emitter_steps");
-}
-
-extern "C" int sc_emitter_footprints(const ScStepParams *p, const double *d_particles,
-                                     const int32_t *d_key_slot, ScStepRec *d_recs,
-                                     int32_t *d_status, void *stream) {
-    sc::StepConsts c;
-    int rc = sc::step_consts(p, c);
-    if (rc) return rc;
-    if (c.n_particles == 0 || c.n_sub == 0) return SC_OK;
-    SC_REQUIRE(d_particles && d_key_slot && d_recs, "sc_emitter_footprints: NULL pointer");
-    const int64_t n_rec = (int64_t)c.n_sub * c.n_particles;
-    emitter_footprint_kernel<<<(unsigned)((n_rec + 255) / 256), 256, 0, sc::as_stream(stream)>>>(
-        c, d_particles, d_key_slot, d_recs, d_status);
-    return sc::launch_status("sc_emitter_footprints");
 }

@@ -14,6 +14,10 @@ struct StepConsts {
     int bleaching, with_optinfo, box_p, box_nq;
     double half_w, half_h, half_sig, inv_res;
     float inv_px_f, inv_res_f;
+    // double-float copies for the footprint arithmetic
+    df half_w_df, half_h_df, half_sig_df, nhalf_sig_df, inv_px_df, px_df, inv_res_df;
+    float cut_f;      // fl32(depth_cutoff + res)
+    int focal_zero;   // focal point at the origin: depths and offsets need no subtraction
 };
 
 int step_consts(const ScStepParams *p, StepConsts &c);
@@ -27,56 +31,63 @@ __device__ __forceinline__ double emit_photons(const StepConsts &c, double ampli
     return __dmul_rn(__dmul_rn(c.qy, n_abs), c.beer);
 }
 
-// floor(x / d) and ceil(x / d) as the reference computes them (one correctly
-// rounded FP64 division, then floor / ceil).  The quotient is estimated in
-// FP32 (relative error < 2^-22); only when the estimate lies within 1e-3 of an
-// integer -- where the rounding of the true division could decide the result
-// -- is the FP64 division evaluated.  FP64 instructions run at 1/64 of the
-// FP32 rate on this GPU; the estimate costs one conversion.
-__device__ __forceinline__ double floor_div(double x, double d, float inv_d) {
-    const float q = (float)x * inv_d;
-    if (fabsf(q - rintf(q)) > 1e-3f * fmaxf(1.f, fabsf(q))) return (double)floorf(q);
-    return floor(x / d);
+// Footprint arithmetic.  The reference evaluates, in FP64,
+//   origin = (half_len + coord) - half_sig,  top = (half_len + coord) + half_sig,
+//   first pixel floor(origin / px), last ceil(top / px), bounds ceil((i px - origin) / res)
+// (_epifm.py:233-258).  Here the same quantities are carried as double-floats
+// (hi + lo, ~2^-46 relative, FP32 pipe; GB300 runs FP64 at ~1/64 of the FP32
+// rate).  Every floor / ceil whose double-float argument lies within kDfMargin
+// of an integer is re-evaluated with the reference's FP64 expression, so the
+// pixel ranges, depth keys and box decisions are the reference's.
+constexpr float kDfMargin = 1e-7f;  // absolute, on quotients below 2^22
+
+// floor / ceil of a double-float with the exact fallback decided by the caller.
+__device__ __forceinline__ bool df_floor(df q, int &v) {
+    float r;
+    const float d = df_round(q, r);
+    v = (int)r - (d < 0.f ? 1 : 0);
+    return fabsf(d) > kDfMargin;
 }
 
-__device__ __forceinline__ double ceil_div(double x, double d, float inv_d) {
-    const float q = (float)x * inv_d;
-    if (fabsf(q - rintf(q)) > 1e-3f * fmaxf(1.f, fabsf(q))) return (double)ceilf(q);
-    return ceil(x / d);
+__device__ __forceinline__ bool df_ceil(df q, int &v) {
+    float r;
+    const float d = df_round(q, r);
+    v = (int)r + (d > 0.f ? 1 : 0);
+    return fabsf(d) > kDfMargin;
 }
 
-// Footprint of one axis (_epifm.py:233-258): first pixel, number of bounds,
-// the exact FP64 origin, and the first bound's unrounded value a as a
-// double-float (a_hi + a_lo, ~1e-12 absolute).
-__device__ __forceinline__ void axis_footprint(double half_len, double coord, double half_sig,
-                                               double px, float inv_px, double inv_res,
-                                               int n_pix, double &origin, int16_t &start,
+// Footprint of one axis: first pixel, number of bounds, and the first bound's
+// unrounded value a = (start px - origin) / res as a double-float.  Returns
+// false when the footprint misses the image.
+__device__ __forceinline__ bool axis_footprint(const StepConsts &c, double half_len, df hl,
+                                               double coord, int n_pix, int16_t &start,
                                                int16_t &count, float &a_hi, float &a_lo) {
-    const double centre = half_len + coord;
-    origin = centre - half_sig;
-    const double lo = floor_div(origin, px, inv_px);
-    const double hi = ceil_div(centre + half_sig, px, inv_px);
-    const double lo_c = fmax(lo, 0.0);
-    const double hi_c = fmin(hi, (double)n_pix);
-    start = 0;
-    count = 0;
-    a_hi = a_lo = 0.f;
-    if (!(hi_c >= lo_c)) return;
-    const int i0 = (int)lo_c;
-    const int n = (int)hi_c - i0 + 1;
+    const df x = df_from(coord);
+    const df centre = df_add(hl, x);
+    const df org = df_add(centre, c.nhalf_sig_df);
+    const df top = df_add(centre, c.half_sig_df);
+    df qlo = df_mul(org, c.inv_px_df), qhi = df_mul(top, c.inv_px_df);
+    // far outside the image (and beyond int range): nothing to splat
+    if (!(qhi.hi > -4.f) || !(qlo.hi < (float)n_pix + 4.f)) return false;
+    qlo.hi = fmaxf(qlo.hi, -8.f);  // only the clamped first pixel 0 matters below this
+    qhi.hi = fminf(qhi.hi, (float)n_pix + 8.f);
+    int lo, hi;
+    if (!df_floor(qlo, lo)) lo = (int)floor(((half_len + coord) - c.half_sig) / c.px);
+    if (!df_ceil(qhi, hi)) hi = (int)ceil(((half_len + coord) + c.half_sig) / c.px);
+    const int i0 = max(lo, 0), i1 = min(hi, n_pix);
+    if (i1 < i0) return false;
     start = (int16_t)i0;
-    count = (int16_t)n;
-    const double a = (__dmul_rn((double)i0, px) - origin) * inv_res;
-    a_hi = (float)a;
-    a_lo = (float)(a - (double)a_hi);
+    count = (int16_t)(i1 - i0 + 1);
+    const df a = df_mul(df_add(df_mul_i(c.px_df, i0), df_neg(org)), c.inv_res_df);
+    a_hi = a.hi;
+    a_lo = a.lo;
+    return true;
 }
 
-// a - rint(a) from its double-float form (exact to ~1e-11 near zero).
-__device__ __forceinline__ float frac_to_int(float a_hi, float a_lo, float &r) {
-    r = rintf(a_hi);
-    return (a_hi - r) + a_lo;
-}
-
+// The splat record of one emitter at one sub-step: depth key and table slot,
+// footprint along x and y, box-table entry when the pixel bounds are a fixed
+// stride apart, and the weight w = norm * res^2.  rel0..2 are the emitter's
+// depth, x and y relative to the focal point.
 __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, double rel1,
                                             double rel2, double norm, const int32_t *key_slot,
                                             int32_t *status, int i, int s, ScStepRec &rec) {
@@ -90,17 +101,20 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     rec.slot = -1;
     rec.w = 0.f;
     if (norm <= 0.0) return;  // overlay_signal returns early (_epifm.py:216-217)
+    // depth key: int(|depth| / res) inside depth_cutoff + res, else -1 (_epifm.py:76-88)
     const double depth = fabs(rel0);
-    int key;
-    if (depth < c.depth_cutoff + c.res) {
-        const double kd = floor_div(depth, c.res, c.inv_res_f);  // int() of a non-negative
-        if (kd > (double)c.max_key) {
+    const float df32 = __double2float_rn(depth);
+    bool inside = df32 < c.cut_f * (1.f - 1e-6f);
+    if (!(inside || df32 > c.cut_f * (1.f + 1e-6f))) inside = depth < c.depth_cutoff + c.res;
+    int key = -1;
+    if (inside) {
+        const float q = df32 * c.inv_res_f;  // three roundings: |error| < 2e-7 q
+        const float r = rintf(q);
+        key = fabsf(q - r) > 5e-7f * fmaxf(1.f, q) ? (int)floorf(q) : (int)floor(depth / c.res);
+        if (key > c.max_key) {
             flag_status(status, 0, i, s, 0);
             return;
         }
-        key = (int)kd;
-    } else {
-        key = -1;
     }
     const int idx = key >= 0 ? key : c.max_key + 1;
     const int slot = key_slot[idx];
@@ -108,20 +122,17 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
         flag_status(status, 1, i, s, key);
         return;
     }
-    int16_t si, ni, sj, nj;
+    int16_t si = 0, ni = 0, sj = 0, nj = 0;
     float axh, axl, ayh, ayl;
-    double x0, y0;
-    axis_footprint(c.half_w, rel1, c.half_sig, c.px, c.inv_px_f, c.inv_res, c.nw, x0, si, ni, axh,
-                   axl);
-    axis_footprint(c.half_h, rel2, c.half_sig, c.px, c.inv_px_f, c.inv_res, c.nh, y0, sj, nj, ayh,
-                   ayl);
+    if (!axis_footprint(c, c.half_w, c.half_w_df, rel1, c.nw, si, ni, axh, axl)) return;
+    if (!axis_footprint(c, c.half_h, c.half_h_df, rel2, c.nh, sj, nj, ayh, ayl)) return;
     if (ni < 2 || nj < 2) return;
     float rx, ry;
-    const float dx = frac_to_int(axh, axl, rx), dy = frac_to_int(ayh, ayl, ry);
+    const float dx = df_round(df{axh, axl}, rx), dy = df_round(df{ayh, ayl}, ry);
     // Box path: with an integer pitch of P grid rows, bound k is ceil(a) + P k
     // for every k unless a lies within 1e-9 of an integer (FP64 evaluation
-    // noise and the estimate of a are ~1e-12 here); those emitters keep the
-    // summed-area path.
+    // noise is ~1e-12 here, the double-float a within 1e-9 of it); those
+    // emitters keep the summed-area path, which needs the FP64 origins.
     if (c.box_p > 0 && fabsf(dx) > 1e-9f && fabsf(dy) > 1e-9f) {
         // entry of pixel (i_start, j_start) in the phase-major box table of the
         // key: first rows m = l0 + P >= 1 split as (m mod P, m div P), l0 = ceil(a)
@@ -132,9 +143,10 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
         rec.box_local = ((mx / P) << 16) | (my / P);
         rec.box_off = (int64_t)slot * ((int64_t)P * P * NB) + (int64_t)phase * NB +
                       (mx / P) * NQ + my / P;
+    } else {
+        rec.x0 = (c.half_w + rel1) - c.half_sig;
+        rec.y0 = (c.half_h + rel2) - c.half_sig;
     }
-    rec.x0 = x0;
-    rec.y0 = y0;
     rec.ax_hi = axh;
     rec.ax_lo = axl;
     rec.ay_hi = ayh;

@@ -600,7 +600,6 @@ class FrameGraph:
         if traj._index != first_frame * self.n_sub:
             traj.advance_to(first_frame * self.n_sub, transform)
         self.frame = torch.full((1,), int(first_frame), dtype=torch.int64, device=dev)
-        self.part = torch.empty(self.n_sub * self.n * 5, dtype=torch.float64, device=dev)
         self.ut = torch.full((self.n_sub,), float(unit_time), dtype=torch.float64, device=dev)
         self.transform = transform
         self.seed = int(seed)
@@ -616,9 +615,8 @@ class FrameGraph:
         dp = traj.params(0, self.n_sub, **(self.transform or {}))
         dp.d_frame = self.frame.data_ptr()
         sp = pipe.step_params(self.n_sub, self.n, False)
-        call("sc_native_substeps", dp, sp, ptr(traj._pos), ptr(traj._g_class), ptr(traj._g_sigma),
-             None, ptr(self.ut), ptr(pipe.budget), ptr(self.part), ptr(recs), s)
-        call("sc_emitter_footprints", sp, ptr(self.part), ptr(pipe.psf.key_slot), ptr(recs),
+        call("sc_native_records", dp, sp, ptr(traj._pos), ptr(traj._g_class), ptr(traj._g_sigma),
+             None, ptr(self.ut), ptr(pipe.budget), ptr(pipe.psf.key_slot), ptr(recs),
              ptr(pipe.status), s)
         pipe.splat_records(recs, n_rec, pipe.image)
         pipe.camera(pipe.image, pipe.expect, pipe.adc, seed=self.seed, d_frame=self.frame)
@@ -648,6 +646,6 @@ class FrameGraph:
 
     @property
     def launches_per_frame(self):
-        # native sub-steps, footprints, bin count/scan/scatter/sort, splat box/sat/merge,
-        # camera, counter (plus one memset)
-        return 11
+        # native records, bin count/scan/scatter/sort, splat box/sat/merge, camera,
+        # counter (plus one memset)
+        return 10

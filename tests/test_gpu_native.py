@@ -215,8 +215,9 @@ def test_frame_graph_replay_matches_eager(sg):
 
 
 def test_fused_native_physics_matches_separate_pass(sg):
-    """sc_native_substeps (diffusion + physics fused) equals sc_diffuse_steps followed by
-    sc_emitter_steps on the same Philox trajectory: identical expectation images."""
+    """sc_native_records (diffusion, physics and footprints in one pass) equals
+    sc_diffuse_steps followed by sc_emitter_steps on the same Philox trajectory:
+    identical expectation images."""
     from scopyon_gb300.base import _psf_for
     from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
     cfg = sg.DefaultConfiguration()

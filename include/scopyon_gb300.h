@@ -199,16 +199,31 @@ int sc_emitter_steps(const ScStepParams *p, const double *d_particles,
  * and footprint are computed in the same order and with the same operations
  * as those two calls, so d_recs ([n_sub][n_particles]) equals theirs bit for
  * bit; the formatted positions are not stored.  d_pos and d_budget are
- * advanced to the end of the frame.  Replaces move_points and
+ * advanced to the end of the frame.  With bin_p (else NULL), each record is
+ * also counted into its tile bin in d_bin_ws (a full sc_bin_workspace_bytes
+ * workspace whose counts sc_bin_reset cleared), ready for sc_bin_finish.  Replaces move_points and
  * __overlay_molecule_plane (src/scopyon/sampling.py:88-119,
  * src/scopyon/_epifm.py:1267-1360).                                        */
 int sc_native_records(const ScDiffuseParams *p, const ScStepParams *sp, double *d_pos,
                       const int32_t *d_class, const double *d_sigma, const double *d_normals,
                       const double *d_unit_time, double *d_budget, const int32_t *d_key_slot,
-                      ScStepRec *d_recs, int32_t *d_status, void *stream);
+                      ScStepRec *d_recs, const ScSplatParams *bin_p, void *d_bin_ws,
+                      size_t bin_ws_bytes, int32_t *d_status, void *stream);
 
-/* Bytes of scratch sc_bin_steps needs for n_rec records on n_tiles_total tiles. */
+/* Bytes of scratch sc_bin_steps uses for n_rec records on n_tiles_total
+ * tiles: the counts and cursors of every bin (16 bytes per tile), then the
+ * bin of every record (4 bytes each).  A workspace of only the first part is
+ * also accepted; the scatter then recomputes each record's bin.            */
 size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total);
+
+/* Clears the bin counts of a binning workspace (a memset on the stream). */
+int sc_bin_reset(const ScSplatParams *p, void *d_ws, size_t ws_bytes, void *stream);
+
+/* Scan, placement and per-bin sort of records a producer has counted into a
+ * full binning workspace (sc_native_records with bin_p): the second half of
+ * sc_bin_steps, with the same outputs.                                      */
+int sc_bin_finish(int n_rec, const ScSplatParams *p, void *d_ws, size_t ws_bytes,
+                  int32_t *d_tile_start, int32_t *d_items, void *stream);
 
 /* Deterministic counting sort of records by the tile that holds their first
  * footprint pixel, box-path records in bins [0, n_tiles) and summed-area-path

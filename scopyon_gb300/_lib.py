@@ -76,11 +76,14 @@ _SIG = {
     "sc_psf_radial": (_I, [_I, _D, _D, _D, _P, _I, _I, _D, _P, _P]),
     "sc_diffuse_steps": (_I, [ctypes.POINTER(DiffuseParams), _P, _P, _P, _P, _P, _P]),
     "sc_native_records": (_I, [ctypes.POINTER(DiffuseParams), ctypes.POINTER(StepParams), _P, _P,
-                               _P, _P, _P, _P, _P, _P, _P, _P]),
+                               _P, _P, _P, _P, _P, _P, ctypes.POINTER(SplatParams), _P,
+                               ctypes.c_size_t, _P, _P]),
     "sc_psf_quadrant_sat": (_I, [_P, _I, _I, _D, _P, _I, _P]),
     "sc_psf_box_table": (_I, [_P, _I, _I, _I, _I, _P, _P]),
     "sc_emitter_steps": (_I, [ctypes.POINTER(StepParams), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sc_bin_workspace_bytes": (ctypes.c_size_t, [_I, _I]),
+    "sc_bin_reset": (_I, [ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P]),
+    "sc_bin_finish": (_I, [_I, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P, _P, _P]),
     "sc_bin_steps": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P, _P, _P,
                           _P]),
     "sc_bin_steps_static": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, _P, _P, _P]),

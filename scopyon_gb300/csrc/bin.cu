@@ -5,11 +5,14 @@
 // under the tile that holds its first footprint pixel, so one CTA can sum all
 // of a tile's footprints (which reach into a halo past the tile) in shared
 // memory with no global atomics on pixels.  Box-path and summed-area-path
-// records go to separate bins (bin t and n_tiles + t for tile t).  Records
-// are counted per bin, scattered with one atomic cursor per bin, and each
-// bin's list is then sorted by record index: the final order is the
-// reference's own accumulation order (sub-step, then particle) and does not
-// depend on scheduling.
+// records go to separate bins (bin t and n_tiles + t for tile t).  Counting a
+// record into its bin (one atomic add) also gives its rank in the bin; after
+// an exclusive scan of the counts each record is stored at its bin's offset
+// plus its rank, and each bin's list is then sorted by record index: the
+// final order is the reference's own accumulation order (sub-step, then
+// particle) and does not depend on scheduling.  A record producer can do the
+// counting itself (sc_bin_record), leaving scan, placement and sort to
+// sc_bin_finish.
 #include <mutex>
 
 #include "sc_common.cuh"
@@ -17,41 +20,65 @@
 
 namespace {
 
-constexpr int kSortSmem = 4096;  // tile lists up to this length are sorted in shared memory
-
-// Per-bin counts: a shared-memory histogram per CTA when the bins fit, else
-// global atomics directly.
-__global__ void bin_count_kernel(const ScStepRec *recs, int n_rec, sc::TileGeom g, int n_bins,
-                                 int use_smem, int32_t *tile_count) {
-    extern __shared__ int32_t hist[];
-    if (use_smem) {
-        for (int t = threadIdx.x; t < n_bins; t += blockDim.x) hist[t] = 0;
-        __syncthreads();
-    }
+// Per-bin counts with global atomics (about 50 records per bin, spread over
+// thousands of bins, so contention is low).  With rank, each record's bin and
+// rank within the bin are kept for the placement pass.
+__global__ void bin_count_kernel(const ScStepRec *recs, int n_rec, sc::TileGeom g,
+                                 int32_t *tile_count, int32_t *rec_bin, int32_t *rec_rank) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rec; r += gridDim.x * blockDim.x) {
-        const int t = sc::record_tile(recs[r], r, g);
-        if (t >= 0) atomicAdd(use_smem ? &hist[t] : &tile_count[t], 1);
-    }
-    if (use_smem) {
-        __syncthreads();
-        for (int t = threadIdx.x; t < n_bins; t += blockDim.x)
-            if (hist[t]) atomicAdd(&tile_count[t], hist[t]);
+        if (rec_bin)
+            sc::bin_record(g, recs[r], r, tile_count, rec_bin, rec_rank);
+        else {
+            const int t = sc::record_tile(recs[r], r, g);
+            if (t >= 0) atomicAdd(&tile_count[t], 1);
+        }
     }
 }
 
-// Single-CTA exclusive scan of per-tile counts -> tile_start[0..n_tiles]; the
-// scatter cursors start at the same offsets.
-__global__ void bin_tile_scan_kernel(const int32_t *tile_count, int n_tiles, int32_t *tile_start,
-                                     int32_t *cursor) {
+constexpr int kScanThreads = 1024, kScanItems = 8;
+
+__device__ __forceinline__ void load8(const int32_t *p, bool vec, int n_left, int32_t v[8]) {
+    if (vec && n_left >= 8) {
+        const int4 a = *reinterpret_cast<const int4 *>(p), b = *reinterpret_cast<const int4 *>(p + 4);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = u < n_left ? p[u] : 0;
+    }
+}
+
+__device__ __forceinline__ void store8(int32_t *p, bool vec, int n_left, const int32_t v[8]) {
+    if (vec && n_left >= 8) {
+        *reinterpret_cast<int4 *>(p) = make_int4(v[0], v[1], v[2], v[3]);
+        *reinterpret_cast<int4 *>(p + 4) = make_int4(v[4], v[5], v[6], v[7]);
+    } else {
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if (u < n_left) p[u] = v[u];
+    }
+}
+
+// Single-CTA exclusive scan of the bin counts -> tile_start[0..n_bins] (and
+// the scatter cursors when given).  Each thread scans 8 consecutive bins, with
+// 16-byte loads and stores where the arrays allow.
+__global__ void __launch_bounds__(kScanThreads)
+bin_tile_scan_kernel(const int32_t *tile_count, int n_bins, int32_t *tile_start, int32_t *cursor) {
     __shared__ int32_t warp_tot[32];
     __shared__ int32_t carry_s;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool vin = ((uintptr_t)tile_count & 15) == 0;
+    const bool vout = ((uintptr_t)tile_start & 15) == 0 && (!cursor || ((uintptr_t)cursor & 15) == 0);
     if (threadIdx.x == 0) carry_s = 0;
     __syncthreads();
-    for (int base = 0; base < n_tiles; base += blockDim.x) {
-        const int t = base + threadIdx.x;
-        const int32_t v = t < n_tiles ? tile_count[t] : 0;
-        int32_t x = v;
+    for (int base = 0; base < n_bins; base += kScanThreads * kScanItems) {
+        const int t0 = base + threadIdx.x * kScanItems;
+        const int n_left = n_bins - t0;
+        int32_t v[kScanItems], sum = 0;
+        load8(tile_count + t0, vin, n_left, v);
+#pragma unroll
+        for (int u = 0; u < kScanItems; ++u) sum += v[u];
+        int32_t x = sum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int32_t n = __shfl_up_sync(0xffffffffu, x, o);
@@ -60,7 +87,7 @@ __global__ void bin_tile_scan_kernel(const int32_t *tile_count, int n_tiles, int
         if (lane == 31) warp_tot[warp] = x;
         __syncthreads();
         if (warp == 0) {
-            int32_t w = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+            int32_t w = warp_tot[lane];
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int32_t n = __shfl_up_sync(0xffffffffu, w, o);
@@ -69,23 +96,90 @@ __global__ void bin_tile_scan_kernel(const int32_t *tile_count, int n_tiles, int
             warp_tot[lane] = w;
         }
         __syncthreads();
-        const int32_t incl = x + (warp > 0 ? warp_tot[warp - 1] : 0) + carry_s;
-        if (t < n_tiles) {
-            tile_start[t] = incl - v;
-            cursor[t] = incl - v;
+        int32_t run = x - sum + (warp > 0 ? warp_tot[warp - 1] : 0) + carry_s;
+        int32_t out[kScanItems];
+#pragma unroll
+        for (int u = 0; u < kScanItems; ++u) {
+            out[u] = run;
+            run += v[u];
+        }
+        if (n_left > 0) {
+            store8(tile_start + t0, vout, n_left, out);
+            if (cursor) store8(cursor + t0, vout, n_left, out);
         }
         __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry_s = incl;
+        if (threadIdx.x == kScanThreads - 1) carry_s = run;
         __syncthreads();
     }
-    if (threadIdx.x == 0) tile_start[n_tiles] = carry_s;
+    if (threadIdx.x == 0) tile_start[n_bins] = carry_s;
 }
 
+// Each record to its bin's offset plus its rank.
+__global__ void bin_place_kernel(const int32_t *rec_bin, const int32_t *rec_rank, int n_rec,
+                                 const int32_t *tile_start, int32_t *items) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rec; r += gridDim.x * blockDim.x) {
+        const int t = rec_bin[r];
+        if (t >= 0) items[__ldg(tile_start + t) + rec_rank[r]] = r;
+    }
+}
+
+// Without rank storage: one atomic cursor per bin, each record's bin
+// recomputed from its head.
 __global__ void bin_scatter_kernel(const ScStepRec *recs, int n_rec, sc::TileGeom g,
                                    int32_t *cursor, int32_t *items) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rec; r += gridDim.x * blockDim.x) {
         const int t = sc::record_tile(recs[r], r, g);
         if (t >= 0) items[atomicAdd(&cursor[t], 1)] = r;
+    }
+}
+
+// Bitonic sort of 32 PL values held PL per lane (element e = PL lane + r),
+// ascending; padding values sort to the end.
+template <int PL>
+__device__ __forceinline__ void warp_sort(int32_t v[PL], int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32 * PL; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= PL) {
+#pragma unroll
+                for (int r = 0; r < PL; ++r) {
+                    const int32_t other = __shfl_xor_sync(0xffffffffu, v[r], j / PL);
+                    const int e = lane * PL + r;
+                    const bool keep_min = ((e & k) == 0) == ((e & j) == 0);
+                    v[r] = keep_min ? min(v[r], other) : max(v[r], other);
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < PL; ++r) {
+                    const int q = r ^ j;
+                    if (r < q) {
+                        const bool up = ((lane * PL + r) & k) == 0;
+                        const int32_t a = v[r], b = v[q];
+                        if ((a > b) == up) {
+                            v[r] = b;
+                            v[q] = a;
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int PL>
+__device__ __forceinline__ void warp_sort_list(int32_t *list, int n, int lane) {
+    int32_t v[PL];
+#pragma unroll
+    for (int r = 0; r < PL; ++r) {
+        const int e = lane * PL + r;
+        v[r] = e < n ? list[e] : INT32_MAX;
+    }
+    warp_sort<PL>(v, lane);
+#pragma unroll
+    for (int r = 0; r < PL; ++r) {
+        const int e = lane * PL + r;
+        if (e < n) list[e] = v[r];
     }
 }
 
@@ -102,43 +196,58 @@ __device__ __forceinline__ void cmp_swap(int32_t *a, int i, int l, int n) {
 
 // Bitonic sorting network in its "flip" form (every comparator ascending), so
 // that a list of any length n sorts in place with virtual +inf padding up to
-// the next power of two.  Called by a whole CTA; a is shared or global memory
-// owned by this CTA.
-__device__ void bitonic_flip_sort(int32_t *a, int n) {
+// the next power of two; run by one warp on a list in global memory (bins of
+// more than 512 records, which only dense clusters of emitters produce).
+__device__ void warp_flip_sort(int32_t *a, int n, int lane) {
     int n2 = 1;
     while (n2 < n) n2 <<= 1;
     for (int k = 2; k <= n2; k <<= 1) {
-        for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        for (int i = lane; i < n2; i += 32) {
             const int l = i ^ (k - 1);
             if (l > i) cmp_swap(a, i, l, n);
         }
-        __syncthreads();
+        __syncwarp();
         for (int j = k >> 2; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+            for (int i = lane; i < n2; i += 32) {
                 const int l = i ^ j;
                 if (l > i) cmp_swap(a, i, l, n);
             }
-            __syncthreads();
+            __syncwarp();
         }
     }
 }
 
-// One CTA per tile: sort the tile's record indices ascending, in shared
-// memory when the list fits, in place in global memory otherwise.
-__global__ void bin_sort_kernel(const int32_t *tile_start, int32_t *items) {
-    __shared__ int32_t buf[kSortSmem];
-    const int t = blockIdx.x;
+constexpr int kSortWarps = 8;
+
+// One warp per bin: the bin's record indices sorted ascending, in registers
+// up to 512 of them (4 or 16 per lane), in global memory beyond.
+__global__ void __launch_bounds__(kSortWarps * 32)
+bin_sort_kernel(const int32_t *tile_start, int n_bins, int32_t *items) {
+    const int lane = threadIdx.x & 31;
+    const int t = blockIdx.x * kSortWarps + (threadIdx.x >> 5);
+    if (t >= n_bins) return;
     const int b0 = tile_start[t], n = tile_start[t + 1] - b0;
     if (n <= 1) return;
     int32_t *list = items + b0;
-    if (n <= kSortSmem) {
-        for (int i = threadIdx.x; i < n; i += blockDim.x) buf[i] = list[i];
-        __syncthreads();
-        bitonic_flip_sort(buf, n);
-        for (int i = threadIdx.x; i < n; i += blockDim.x) list[i] = buf[i];
-        return;
-    }
-    bitonic_flip_sort(list, n);
+    if (n <= 128)
+        warp_sort_list<4>(list, n, lane);
+    else if (n <= 512)
+        warp_sort_list<16>(list, n, lane);
+    else
+        warp_flip_sort(list, n, lane);
+}
+
+// Scan, placement and sort of counted records.
+int bin_finish(int n_rec, const sc::TileGeom &g, int32_t *tile_count, const int32_t *rec_bin,
+               const int32_t *rec_rank, int32_t *tile_start, int32_t *items, cudaStream_t s) {
+    const int n_bins = 2 * g.n_tiles;
+    bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(tile_count, n_bins, tile_start, nullptr);
+    int grid = (n_rec + 255) / 256;
+    if (grid > 152 * 8) grid = 152 * 8;
+    bin_place_kernel<<<grid, 256, 0, s>>>(rec_bin, rec_rank, n_rec, tile_start, items);
+    bin_sort_kernel<<<(n_bins + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(
+        tile_start, n_bins, items);
+    return sc::launch_status("sc_bin_finish");
 }
 
 }  // namespace
@@ -173,11 +282,61 @@ int tile_geom(const ScSplatParams *p, TileGeom &g) {
     return SC_OK;
 }
 
+int bin_layout(const TileGeom &g, int n_rec, void *d_ws, size_t ws_bytes, BinLayout &b) {
+    const int n_bins = 2 * g.n_tiles;
+    b.count = static_cast<int32_t *>(d_ws);
+    b.cursor = b.count + n_bins;
+    const bool full = ws_bytes >= sc_bin_workspace_bytes(n_rec, g.n_tiles);
+    b.rec_bin = full ? b.cursor + n_bins : nullptr;
+    b.rec_rank = full ? b.rec_bin + n_rec : nullptr;
+    return SC_OK;
+}
+
 }  // namespace sc
+
+// Workspace: counts and cursors of the 2 bins of every tile, then the bin and
+// the rank of every record.  A workspace holding only the counts and cursors
+// also works (the scatter then uses atomic cursors and recomputes each
+// record's bin from its head).
+static size_t bin_counts_bytes(int n_tiles_total) {
+    return (size_t)4 * n_tiles_total * sizeof(int32_t);
+}
 
 extern "C" size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total) {
     if (n_rec <= 0 || n_tiles_total <= 0) return 0;
-    return (size_t)4 * n_tiles_total * sizeof(int32_t);  // counts and cursors of 2 bins per tile
+    return bin_counts_bytes(n_tiles_total) + (size_t)2 * n_rec * sizeof(int32_t);
+}
+
+extern "C" int sc_bin_reset(const ScSplatParams *p, void *d_ws, size_t ws_bytes, void *stream) {
+    sc::TileGeom g;
+    int rc = sc::tile_geom(p, g);
+    if (rc) return rc;
+    SC_REQUIRE(d_ws && ws_bytes >= bin_counts_bytes(g.n_tiles), "sc_bin_reset: workspace %zu < %zu",
+               ws_bytes, bin_counts_bytes(g.n_tiles));
+    return sc::cuda_status(cudaMemsetAsync(d_ws, 0, sizeof(int32_t) * 2 * g.n_tiles,
+                                           sc::as_stream(stream)),
+                           "sc_bin_reset");
+}
+
+extern "C" int sc_bin_finish(int n_rec, const ScSplatParams *p, void *d_ws, size_t ws_bytes,
+                             int32_t *d_tile_start, int32_t *d_items, void *stream) {
+    sc::TileGeom g;
+    int rc = sc::tile_geom(p, g);
+    if (rc) return rc;
+    SC_REQUIRE(n_rec >= 0, "n_rec=%d", n_rec);
+    SC_REQUIRE(d_tile_start != nullptr, "sc_bin_finish: tile_start is NULL");
+    cudaStream_t s = sc::as_stream(stream);
+    if (n_rec == 0)
+        return sc::cuda_status(
+            cudaMemsetAsync(d_tile_start, 0, sizeof(int32_t) * (2 * g.n_tiles + 1), s),
+            "sc_bin_finish");
+    SC_REQUIRE(d_ws && d_items, "sc_bin_finish: NULL pointer");
+    SC_REQUIRE(ws_bytes >= sc_bin_workspace_bytes(n_rec, g.n_tiles),
+               "sc_bin_finish: workspace %zu < %zu bytes (counts, bins and ranks)", ws_bytes,
+               sc_bin_workspace_bytes(n_rec, g.n_tiles));
+    sc::BinLayout b;
+    sc::bin_layout(g, n_rec, d_ws, ws_bytes, b);
+    return bin_finish(n_rec, g, b.count, b.rec_bin, b.rec_rank, d_tile_start, d_items, s);
 }
 
 extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatParams *p,
@@ -196,30 +355,25 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
             "sc_bin_steps");
     }
     SC_REQUIRE(d_recs && d_items && d_ws, "sc_bin_steps: NULL pointer");
-    SC_REQUIRE(ws_bytes >= sc_bin_workspace_bytes(n_rec, g.n_tiles),
-               "sc_bin_steps: workspace %zu < %zu bytes", ws_bytes,
-               sc_bin_workspace_bytes(n_rec, g.n_tiles));
+    SC_REQUIRE(ws_bytes >= bin_counts_bytes(g.n_tiles), "sc_bin_steps: workspace %zu < %zu bytes",
+               ws_bytes, bin_counts_bytes(g.n_tiles));
     SC_REQUIRE(g.rec_per_image == 0 || (int64_t)g.rec_per_image * g.n_images >= n_rec,
                "sc_bin_steps: rec_per_image too small for n_rec");
     const int n_bins = 2 * g.n_tiles;
-    int32_t *tile_count = static_cast<int32_t *>(d_ws);
-    int32_t *cursor = tile_count + n_bins;
-    rc = sc::cuda_status(cudaMemsetAsync(tile_count, 0, sizeof(int32_t) * n_bins, s),
+    sc::BinLayout b;
+    sc::bin_layout(g, n_rec, d_ws, ws_bytes, b);
+    rc = sc::cuda_status(cudaMemsetAsync(b.count, 0, sizeof(int32_t) * n_bins, s),
                          "sc_bin_steps memset");
     if (rc) return rc;
-    const size_t smem = (size_t)n_bins * sizeof(int32_t);
-    const int use_smem = smem <= 96 * 1024;
-    if (use_smem && smem > 48 * 1024)
-        cudaFuncSetAttribute(bin_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int grid = (n_rec + 1023) / 1024;
-    if (grid > 152 * 4) grid = 152 * 4;
-    bin_count_kernel<<<grid, 256, use_smem ? smem : 0, s>>>(d_recs, n_rec, g, n_bins, use_smem,
-                                                           tile_count);
-    bin_tile_scan_kernel<<<1, 1024, 0, s>>>(tile_count, n_bins, d_tile_start, cursor);
-    int sgrid = (n_rec + 255) / 256;
-    if (sgrid > 152 * 16) sgrid = 152 * 16;
-    bin_scatter_kernel<<<sgrid, 256, 0, s>>>(d_recs, n_rec, g, cursor, d_items);
-    bin_sort_kernel<<<n_bins, 256, 0, s>>>(d_tile_start, d_items);
+    int grid = (n_rec + 255) / 256;
+    if (grid > 152 * 8) grid = 152 * 8;
+    bin_count_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.count, b.rec_bin, b.rec_rank);
+    if (b.rec_bin) return bin_finish(n_rec, g, b.count, b.rec_bin, b.rec_rank, d_tile_start,
+                                     d_items, s);
+    bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(b.count, n_bins, d_tile_start, b.cursor);
+    bin_scatter_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.cursor, d_items);
+    bin_sort_kernel<<<(n_bins + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(
+        d_tile_start, n_bins, d_items);
     return sc::launch_status("sc_bin_steps");
 }
 

@@ -11,7 +11,13 @@ struct TileGeom {
 };
 
 int tile_geom(const ScSplatParams *p, TileGeom &g);
-int bin_chunk(int n_rec, int n_tiles);
+
+// Pointers into a binning workspace: per-bin counts and cursors, then (when
+// the workspace is large enough) each record's bin and rank in its bin.
+struct BinLayout {
+    int32_t *count, *cursor, *rec_bin, *rec_rank;
+};
+int bin_layout(const TileGeom &g, int n_rec, void *d_ws, size_t ws_bytes, BinLayout &b);
 
 // Bin of a record: the tile holding its first footprint pixel, plus n_tiles
 // for records that take the summed-area path; -1 when it has no pixels.
@@ -21,6 +27,14 @@ __device__ __forceinline__ int record_tile(const ScStepRec &rec, int r, const Ti
     if (img >= g.n_images || rec.i_start >= g.nw || rec.j_start >= g.nh) return -1;
     const int t = img * g.tiles_per_image + (rec.i_start / g.tile) * g.tiles_y + rec.j_start / g.tile;
     return rec.box ? t : t + g.n_tiles;
+}
+
+// Counts record r into its bin and keeps its bin and rank (-1: no bin).
+__device__ __forceinline__ void bin_record(const TileGeom &g, const ScStepRec &rec, int r,
+                                           int32_t *count, int32_t *rec_bin, int32_t *rec_rank) {
+    const int t = record_tile(rec, r, g);
+    rec_bin[r] = t;
+    rec_rank[r] = t >= 0 ? atomicAdd(&count[t], 1) : -1;
 }
 
 }  // namespace sc

@@ -10,6 +10,7 @@
 // global step) or, for parity with the reference, from a caller array.
 // Boundaries: none (reference), periodic (sampling2), reflecting (this engine).
 #include "sc_common.cuh"
+#include "bin.cuh"
 #include "steps.cuh"
 
 namespace {
@@ -138,7 +139,7 @@ __global__ void __launch_bounds__(kRecWarps * 32, 8)
 native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                       const int32_t *klass, const double *sigma, const double *normals,
                       const double *unit_time, double *budget, const int32_t *key_slot,
-                      ScStepRec *recs, int32_t *status) {
+                      ScStepRec *recs, sc::TileGeom g, sc::BinLayout bl, int32_t *status) {
     extern __shared__ double rec_smem[];
     double *s_pos = rec_smem;
     double *s_norm = s_pos + chunk * 32 * 3;
@@ -242,6 +243,7 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                     sc::make_record(k, f[0] - k.focal[0], f[1] - k.focal[1], f[2] - k.focal[2],
                                     norm, key_slot, status, i, s, rec);
                 recs[(size_t)s * c.n + i] = rec;
+                if (bl.count) sc::bin_record(g, rec, s * c.n + i, bl.count, bl.rec_bin, bl.rec_rank);
             }
         }
         __syncthreads();
@@ -312,6 +314,7 @@ extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *s
                                  const int32_t *d_class, const double *d_sigma,
                                  const double *d_normals, const double *d_unit_time,
                                  double *d_budget, const int32_t *d_key_slot, ScStepRec *d_recs,
+                                 const ScSplatParams *bin_p, void *d_bin_ws, size_t bin_ws_bytes,
                                  int32_t *d_status, void *stream) {
     DiffConsts c;
     int rc = diff_consts(p, c);
@@ -325,10 +328,24 @@ extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *s
     SC_REQUIRE(d_pos && d_sigma && d_unit_time && d_key_slot && d_recs,
                "sc_native_records: NULL pointer");
     SC_REQUIRE(!k.bleaching || d_budget, "sc_native_records: bleaching needs a budget array");
+    sc::TileGeom g{};
+    sc::BinLayout bl{nullptr, nullptr, nullptr, nullptr};
+    if (bin_p) {
+        rc = sc::tile_geom(bin_p, g);
+        if (rc) return rc;
+        const int64_t n_rec = (int64_t)c.n * c.n_sub;
+        SC_REQUIRE(n_rec < (1ll << 31), "sc_native_records: %lld records", (long long)n_rec);
+        SC_REQUIRE(g.n_images == 1 && g.nw == k.nw && g.nh == k.nh,
+                   "sc_native_records: bin geometry is not the frame's");
+        SC_REQUIRE(d_bin_ws && bin_ws_bytes >= sc_bin_workspace_bytes((int)n_rec, g.n_tiles),
+                   "sc_native_records: bin workspace %zu < %zu bytes", bin_ws_bytes,
+                   sc_bin_workspace_bytes((int)n_rec, g.n_tiles));
+        sc::bin_layout(g, (int)n_rec, d_bin_ws, bin_ws_bytes, bl);
+    }
     const int chunk = c.n_sub < 32 ? c.n_sub : 32;
     const size_t smem = rec_shared_bytes(chunk);
     native_records_kernel<<<(c.n + 31) / 32, kRecWarps * 32, smem, sc::as_stream(stream)>>>(
         c, k, chunk, d_pos, d_class, d_sigma, d_normals, d_unit_time, d_budget, d_key_slot, d_recs,
-        d_status);
+        g, bl, d_status);
     return sc::launch_status("sc_native_records");
 }

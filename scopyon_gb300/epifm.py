@@ -444,18 +444,30 @@ class FramePipeline:
         p.px, p.res = self.cfg.px, PSF_RES
         return p
 
-    def splat_records(self, recs, n_rec, image, n_images=1, rec_per_image=0, stream=None):
-        """Bin records by tile and splat them into ``image`` (n_images x W x H, float32)."""
-        s = stream_ptr(stream)
+    def bin_buffers(self, n_rec, n_images=1, rec_per_image=0):
+        """Splat parameters and the binning workspace, items and bin offsets."""
         sp = self.splat_params(n_images, rec_per_image)
         n_tiles = self.tiles_x * self.tiles_y * n_images
-        L = _lib.load()
-        ws_bytes = L.sc_bin_workspace_bytes(n_rec, n_tiles)
+        ws_bytes = _lib.load().sc_bin_workspace_bytes(n_rec, n_tiles)
         ws = self._buf("ws", (ws_bytes + 3) // 4, torch.int32)
         items = self._buf("items", n_rec, torch.int32)
         tile_start = self._buf("tile_start", 2 * n_tiles + 1, torch.int32)
-        call("sc_bin_steps", ptr(recs), n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items),
-             ptr(self.status), s)
+        return sp, ws, ws_bytes, items, tile_start
+
+    def splat_records(self, recs, n_rec, image, n_images=1, rec_per_image=0, stream=None,
+                      counted=False):
+        """Bin records by tile and splat them into ``image`` (n_images x W x H, float32).
+
+        counted: the records' producer already counted them into the binning
+        workspace (sc_native_records), so only sc_bin_finish runs here."""
+        s = stream_ptr(stream)
+        sp, ws, ws_bytes, items, tile_start = self.bin_buffers(n_rec, n_images, rec_per_image)
+        if counted:
+            call("sc_bin_finish", n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items), s)
+        else:
+            call("sc_bin_steps", ptr(recs), n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start),
+                 ptr(items), ptr(self.status), s)
+        L = _lib.load()
         sws_bytes = L.sc_splat_workspace_bytes(sp)
         sws = self._buf("splat_ws", (sws_bytes + 3) // 4, torch.float32)
         ev = self.kernel_events
@@ -615,10 +627,12 @@ class FrameGraph:
         dp = traj.params(0, self.n_sub, **(self.transform or {}))
         dp.d_frame = self.frame.data_ptr()
         sp = pipe.step_params(self.n_sub, self.n, False)
+        bsp, ws, ws_bytes, _, _ = pipe.bin_buffers(n_rec)
+        call("sc_bin_reset", bsp, ptr(ws), ws_bytes, s)
         call("sc_native_records", dp, sp, ptr(traj._pos), ptr(traj._g_class), ptr(traj._g_sigma),
-             None, ptr(self.ut), ptr(pipe.budget), ptr(pipe.psf.key_slot), ptr(recs),
-             ptr(pipe.status), s)
-        pipe.splat_records(recs, n_rec, pipe.image)
+             None, ptr(self.ut), ptr(pipe.budget), ptr(pipe.psf.key_slot), ptr(recs), bsp,
+             ptr(ws), ws_bytes, ptr(pipe.status), s)
+        pipe.splat_records(recs, n_rec, pipe.image, counted=True)
         pipe.camera(pipe.image, pipe.expect, pipe.adc, seed=self.seed, d_frame=self.frame)
         call("sc_counter_add", ptr(self.frame), 1, s)
 
@@ -646,6 +660,6 @@ class FrameGraph:
 
     @property
     def launches_per_frame(self):
-        # native records, bin count/scan/scatter/sort, splat box/sat/merge, camera,
-        # counter (plus one memset)
-        return 10
+        # native records (counting into bins), bin scan/place/sort, splat
+        # box/sat/merge, camera, counter (plus one memset)
+        return 9

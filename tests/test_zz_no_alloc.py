@@ -64,7 +64,7 @@ def numpy_bins(r, p):
     return start, order
 
 
-def run(lib, fn, recs_h, p, ws=None):
+def run(lib, fn, recs_h, p, counts_only=False):
     L = lib.load()
     n = len(recs_h)
     n_tiles = p.tiles_x * p.tiles_y * p.n_images
@@ -78,7 +78,7 @@ def run(lib, fn, recs_h, p, ws=None):
         rc = L.sc_bin_steps_static(P(recs.data_ptr()), n, ctypes.byref(p), P(start.data_ptr()),
                                    P(items.data_ptr()), P(status.data_ptr()), s)
     else:
-        ws_bytes = L.sc_bin_workspace_bytes(n, n_tiles)
+        ws_bytes = 16 * n_tiles if counts_only else L.sc_bin_workspace_bytes(n, n_tiles)
         ws = torch.empty((ws_bytes + 3) // 4, dtype=torch.int32, device="cuda")
         rc = L.sc_bin_steps(P(recs.data_ptr()), n, ctypes.byref(p), P(ws.data_ptr()), ws_bytes,
                             P(start.data_ptr()), P(items.data_ptr()), P(status.data_ptr()), s)
@@ -88,7 +88,7 @@ def run(lib, fn, recs_h, p, ws=None):
     return start, items.cpu().numpy()[:start[-1]]
 
 
-@pytest.mark.parametrize("shape", [(512, 512, 1), (96, 64, 2)])
+@pytest.mark.parametrize("shape", [(512, 512, 1), (96, 64, 2), (16, 16, 1)])
 def test_static_matches_workspace_entry_point(lib, shape):
     nw, nh, n_images = shape
     rng = numpy.random.RandomState(11)
@@ -101,6 +101,9 @@ def test_static_matches_workspace_entry_point(lib, shape):
         w_start, w_items = run(lib, "workspace", r, p)
         numpy.testing.assert_array_equal(s_start, w_start)
         numpy.testing.assert_array_equal(s_items, w_items)
+        c_start, c_items = run(lib, "workspace", r, p, counts_only=True)
+        numpy.testing.assert_array_equal(c_start, w_start)
+        numpy.testing.assert_array_equal(c_items, w_items)
         e_start, e_items = numpy_bins(r, p)
         numpy.testing.assert_array_equal(s_start, e_start)
         numpy.testing.assert_array_equal(s_items, e_items)

@@ -235,6 +235,51 @@ int sc_bin_steps(const ScStepRec *d_recs, int n_rec,
                  const ScSplatParams *p, void *d_ws, size_t ws_bytes,
                  int32_t *d_tile_start, int32_t *d_items, int32_t *d_status, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Differentiable expected image (Gaussian PSF).  The reference's Gaussian
+ * point-spread function (src/scopyon/_epifm.py:133-134), integrated over each
+ * pixel analytically instead of on its 1-nm grid (:224-282), with the TIRF
+ * excitation exp(-|z - z_focal| / d) of :1281-1289 as depth dependence:
+ *   mu[f][i][j] = bg[f] + sum_e I_e A(z_e) Gx_e(i) Gy_e(j).
+ * Emitters are float4 (x, y, z, I): metres from the image centre and photons;
+ * sigma (metres) is a device scalar.  New in this engine: the reference has
+ * no gradients.                                                              */
+typedef struct {
+    int32_t nw, nh;          /* image size                                        */
+    int32_t n_frames;        /* frames, each with n_emit emitters                 */
+    int32_t n_emit;
+    int32_t half_win;        /* R: a (2R+1)^2 pixel window per emitter (1..15)    */
+    int32_t tile;            /* forward tile edge (8 or 16)                       */
+    double px;               /* pixel length on the sample (metres)               */
+    double inv_pen;          /* 1 / penetration depth (0: EPI, A = 1)             */
+    double z_focal;
+} ScGaussParams;
+
+/* Bytes of device workspace sc_gauss_forward needs. */
+size_t sc_gauss_workspace_bytes(const ScGaussParams *p);
+
+/* d_mu[n_frames][nw][nh] = expected photons (d_bg[n_frames] may be NULL). */
+int sc_gauss_forward(const ScGaussParams *p, const float *d_emit, const float *d_sigma,
+                     const float *d_bg, void *d_ws, size_t ws_bytes, float *d_mu,
+                     int32_t *d_status, void *stream);
+
+/* Adjoint of sc_gauss_forward: from d_grad_mu = dL/dmu, d_grad_emit (float4
+ * per emitter: dL/dx, dL/dy, dL/dz, dL/dI) and, if not NULL, each emitter's
+ * share of dL/dsigma (sum them for the total; dL/dbg[f] is the sum of
+ * d_grad_mu over frame f).                                                  */
+int sc_gauss_backward(const ScGaussParams *p, const float *d_emit, const float *d_sigma,
+                      const float *d_grad_mu, float *d_grad_emit, float *d_grad_sigma_e,
+                      void *stream);
+
+/* d_out[s] = sum of d_x[s * seg_len .. (s + 1) * seg_len) in FP64, in a fixed
+ * order. */
+int sc_segment_sum(const float *d_x, int64_t seg_len, int n_seg, double *d_out, void *stream);
+
+/* Poisson negative log-likelihood per segment, sum(mu - k log mu) in FP64,
+ * and (if d_grad_mu is not NULL) its gradient 1 - k / mu.                    */
+int sc_poisson_nll(const float *d_mu, const float *d_counts, int64_t seg_len, int n_seg,
+                   double *d_loss, float *d_grad_mu, void *stream);
+
 /* Largest tile count (tiles per image x images) sc_bin_steps_static takes. */
 #define SC_BIN_STATIC_MAX_TILES 65536
 

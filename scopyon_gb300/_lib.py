@@ -66,6 +66,12 @@ class DiffuseParams(ctypes.Structure):
                 ("unit_z", ctypes.c_double * 3)]
 
 
+class GaussParams(ctypes.Structure):
+    _fields_ = [("nw", ctypes.c_int32), ("nh", ctypes.c_int32), ("n_frames", ctypes.c_int32),
+                ("n_emit", ctypes.c_int32), ("half_win", ctypes.c_int32), ("tile", ctypes.c_int32),
+                ("px", ctypes.c_double), ("inv_pen", ctypes.c_double), ("z_focal", ctypes.c_double)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
@@ -93,6 +99,12 @@ _SIG = {
     "sc_camera": (_I, [ctypes.POINTER(CameraParams), _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                        _P, _P, _P, _P, _P]),
     "sc_emccd_exact": (_I, [_P, _D, _D, _P, _I, _D, _P, _P, _P]),
+    "sc_gauss_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(GaussParams)]),
+    "sc_gauss_forward": (_I, [ctypes.POINTER(GaussParams), _P, _P, _P, _P, ctypes.c_size_t, _P,
+                              _P, _P]),
+    "sc_gauss_backward": (_I, [ctypes.POINTER(GaussParams), _P, _P, _P, _P, _P, _P]),
+    "sc_segment_sum": (_I, [_P, ctypes.c_int64, _I, _P, _P]),
+    "sc_poisson_nll": (_I, [_P, _P, ctypes.c_int64, _I, _P, _P, _P]),
 }
 
 

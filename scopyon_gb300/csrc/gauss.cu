@@ -1,0 +1,445 @@
+// Differentiable expected image with the Gaussian PSF, and its adjoint.
+//
+// Model (the reference's Gaussian PSF path, _epifm.py:133-134 and :224-282,
+// with the TIRF excitation of _epifm.py:1281-1289 as the depth dependence):
+//   mu[f, i, j] = bg[f] + sum_e I_e A(z_e) Gx_e(i) Gy_e(j)
+//   Gx_e(i) = Phi((u_i + px - x_e) / sigma) - Phi((u_i - x_e) / sigma),
+//   u_i = i px - W px / 2 (pixel i's low edge), Phi the normal CDF,
+//   A(z) = exp(-|z - z_focal| / d) (1 under EPI, d = inf).
+// The reference samples the same Gaussian on a 1-nm grid and sums the
+// samples over each pixel; here the pixel integral is analytic, so that it
+// can be differentiated.  Each emitter covers a (2R+1)^2 pixel window around
+// its centre pixel (R = half_win, about 5.5 sigma: the truncated tails are
+// below 1e-7 of the emitter's photons).
+//
+// Forward: one splat record per emitter, binned by tile (sc_bin_steps), a CTA
+// per tile adds its emitters' separable windows into per-warp buffers in list
+// order, and a merge pass sums the buffers covering each pixel in a fixed
+// order: deterministic.  Adjoint: one warp per emitter gathers dL/dmu over
+// its window: sum g Gx Gy, sum g dGx Gy, sum g Gx dGy and the sigma terms,
+// per-lane sums then fixed warp reductions: deterministic.
+#include <math.h>
+
+#include "sc_common.cuh"
+#include "bin.cuh"
+
+namespace {
+
+constexpr float kInvSqrt2 = 0.70710678118654752f;
+constexpr float kInvSqrt2Pi = 0.39894228040143268f;
+
+// Phi(b) - Phi(a) for a <= b, without cancellation in either tail.
+__device__ __forceinline__ float cdf_diff(float a, float b) {
+    if (a >= 0.f) return 0.5f * (erfcf(a * kInvSqrt2) - erfcf(b * kInvSqrt2));
+    if (b <= 0.f) return 0.5f * (erfcf(-b * kInvSqrt2) - erfcf(-a * kInvSqrt2));
+    return 1.f - 0.5f * (erfcf(b * kInvSqrt2) + erfcf(-a * kInvSqrt2));
+}
+
+__device__ __forceinline__ float pdf(float t) { return kInvSqrt2Pi * __expf(-0.5f * t * t); }
+
+struct GaussConsts {
+    int nw, nh, n_frames, n_emit, R;
+    double px, half_w, half_h, inv_pen, z_focal;
+};
+
+// Window of one emitter along one axis: centre pixel ic and the fraction fx
+// of the way across it (x_rel = (x + half) / px = ic + fx), both exact to FP32.
+__device__ __forceinline__ void axis_centre(double x, double half, double px, int &ic, float &fx) {
+    const double xr = (x + half) / px;
+    const double fl = floor(xr);
+    ic = (int)fmax(fmin(fl, 1e9), -1e9);
+    fx = (float)(xr - fl);
+}
+
+__device__ __forceinline__ float amplitude(const GaussConsts &c, float z) {
+    return c.inv_pen > 0.0 ? __expf(-fabsf(z - (float)c.z_focal) * (float)c.inv_pen) : 1.f;
+}
+
+// One splat record per emitter (binned by the tile of its first pixel):
+// i_start, n_i (bounds = pixels + 1), ax_hi = fx, ax_lo = i_start - ic, and
+// the same along y; w = I A(z).  Emitters whose window misses the image get
+// slot -1.
+__global__ void gauss_records_kernel(GaussConsts c, const float4 *emit, ScStepRec *recs) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= c.n_frames * c.n_emit) return;
+    const float4 e = emit[r];
+    ScStepRec rec;
+    rec.box_off = 0;
+    rec.x0 = rec.y0 = 0.0;
+    rec.box = 1;
+    rec.box_local = 0;
+    rec.slot = -1;
+    rec.i_start = rec.j_start = 0;
+    rec.n_i = rec.n_j = 0;
+    rec.ax_hi = rec.ax_lo = rec.ay_hi = rec.ay_lo = 0.f;
+    rec.w = e.w * amplitude(c, e.z);
+    int icx, icy;
+    float fx, fy;
+    axis_centre(e.x, c.half_w, c.px, icx, fx);
+    axis_centre(e.y, c.half_h, c.px, icy, fy);
+    const int i0 = max(icx - c.R, 0), i1 = min(icx + c.R, c.nw - 1);
+    const int j0 = max(icy - c.R, 0), j1 = min(icy + c.R, c.nh - 1);
+    if (i1 >= i0 && j1 >= j0 && isfinite(fx) && isfinite(fy)) {
+        rec.slot = 0;
+        rec.i_start = (int16_t)i0;
+        rec.n_i = (int16_t)(i1 - i0 + 2);
+        rec.j_start = (int16_t)j0;
+        rec.n_j = (int16_t)(j1 - j0 + 2);
+        rec.ax_hi = fx;
+        rec.ax_lo = (float)(i0 - icx);
+        rec.ay_hi = fy;
+        rec.ay_lo = (float)(j0 - icy);
+    }
+    recs[r] = rec;
+}
+
+// Pixel integral of the unit Gaussian over pixel offset d (from the centre
+// pixel) for an emitter at fraction f of its centre pixel; s = px / sigma.
+__device__ __forceinline__ float gauss_pixel(int d, float f, float s) {
+    return cdf_diff(((float)d - f) * s, ((float)d + 1.f - f) * s);
+}
+
+// Tile splat: warp m mod NW takes the m-th record of the tile's list.
+template <int NW>
+__global__ void __launch_bounds__(NW * 32)
+gauss_splat_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
+                   const int32_t *__restrict__ items, sc::TileGeom g, const float *sigma_p,
+                   double px, float *__restrict__ ws) {
+    extern __shared__ float sm[];
+    const int E = g.edge, EE = E * E;
+    const int BS = (EE + 31) & ~31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x;
+    const int t = tile % g.tiles_per_image;
+    const int x0 = (t / g.tiles_y) * g.tile, y0 = (t % g.tiles_y) * g.tile;
+    for (int i = threadIdx.x; i < NW * BS; i += blockDim.x) sm[i] = 0.f;
+    __syncthreads();
+    float *buf = sm + warp * BS;
+    const float s = (float)(px / (double)*sigma_p);
+    const int it0 = tile_start[tile], it1 = tile_start[tile + 1];
+    for (int m = it0 + warp; m < it1; m += NW) {
+        const ScStepRec &rec = recs[__ldg(items + m)];
+        const int ni = rec.n_i - 1, nj = rec.n_j - 1;
+        const int ox = rec.i_start - x0, oy = rec.j_start - y0;
+        const float gx = lane < ni ? gauss_pixel((int)rec.ax_lo + lane, rec.ax_hi, s) : 0.f;
+        const float gy = lane < nj ? rec.w * gauss_pixel((int)rec.ay_lo + lane, rec.ay_hi, s) : 0.f;
+        if (ox < 0 || oy < 0 || ox + ni > E || oy + nj > E) continue;  // not produced by records
+        for (int a = 0; a < ni; ++a) {
+            const float gxa = __shfl_sync(0xffffffffu, gx, a);
+            if (lane < nj) {
+                float *d = buf + (ox + a) * E + oy + lane;
+                *d = fmaf(gxa, gy, *d);
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    float *out = ws + (size_t)tile * EE;
+    for (int p = threadIdx.x; p < EE; p += blockDim.x) {
+        float sum = 0.f;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) sum += sm[w * BS + p];
+        out[p] = sum;
+    }
+}
+
+// Per pixel: background plus the tile buffers that cover it, in a fixed order.
+__global__ void gauss_merge_kernel(const float *__restrict__ ws, sc::TileGeom g,
+                                   const float *__restrict__ bg, float *__restrict__ mu) {
+    const int n = g.nw * g.nh, E = g.edge, EE = E * E;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (int64_t)n * g.n_images;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int img = (int)(q / n);
+        const int p = (int)(q - (int64_t)img * n);
+        const int i = p / g.nh, j = p - (p / g.nh) * g.nh;
+        const int tx = i / g.tile, ty = j / g.tile;
+        const float *tiles = ws + (size_t)img * g.tiles_per_image * EE;
+        float sum = 0.f;
+        for (int a = 0; a <= tx; ++a) {
+            const int li = i - (tx - a) * g.tile;
+            if (li >= E) break;
+            for (int b = 0; b <= ty; ++b) {
+                const int lj = j - (ty - b) * g.tile;
+                if (lj >= E) break;
+                sum += tiles[(size_t)((tx - a) * g.tiles_y + (ty - b)) * EE + li * E + lj];
+            }
+        }
+        mu[q] = (bg ? bg[img] : 0.f) + sum;
+    }
+}
+
+// Pixel value, x derivative (per pixel offset, times -1/sigma later) and
+// sigma derivative factors of one window pixel.
+struct PixTerms {
+    float g, dg, sg;  // G, (phi(b) - phi(a)), (b phi(b) - a phi(a))
+};
+
+__device__ __forceinline__ PixTerms pix_terms(int d, float f, float s) {
+    const float a = ((float)d - f) * s, b = ((float)d + 1.f - f) * s;
+    const float pa = pdf(a), pb = pdf(b);
+    return PixTerms{cdf_diff(a, b), pb - pa, b * pb - a * pa};
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Adjoint: one warp per emitter.  With g = dL/dmu over the window,
+//   S1 = sum g Gx Gy,  Sx = sum g (dGx/dx) Gy,  Sy = sum g Gx (dGy/dy),
+//   Ss = sum g (dGx/dsigma Gy + Gx dGy/dsigma),
+// dL/dx = c Sx, dL/dy = c Sy, dL/dI = A S1, dL/dz = I A'(z) S1 and the
+// emitter's share of dL/dsigma is c Ss (c = I A(z)).
+__global__ void gauss_backward_kernel(GaussConsts c, const float4 *__restrict__ emit,
+                                      const float *sigma_p, const float *__restrict__ grad_mu,
+                                      float4 *__restrict__ grad_emit, float *grad_sigma_e) {
+    const int warps = blockDim.x >> 5;
+    const int r = blockIdx.x * warps + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (r >= c.n_frames * c.n_emit) return;
+    const int f = r / c.n_emit;
+    const float4 e = emit[r];
+    const float sigma = *sigma_p;
+    const float s = (float)(c.px / (double)sigma);
+    int icx, icy;
+    float fx, fy;
+    axis_centre(e.x, c.half_w, c.px, icx, fx);
+    axis_centre(e.y, c.half_h, c.px, icy, fy);
+    const int K = 2 * c.R + 1;
+    const int i0 = icx - c.R, j0 = icy - c.R;
+    // lane b: column j0 + b (window column terms); row terms go by shuffle
+    const bool col_ok = lane < K && j0 + lane >= 0 && j0 + lane < c.nh && isfinite(fy);
+    const PixTerms ty = lane < K ? pix_terms(lane - c.R, fy, s) : PixTerms{0.f, 0.f, 0.f};
+    const PixTerms tx = lane < K ? pix_terms(lane - c.R, fx, s) : PixTerms{0.f, 0.f, 0.f};
+    float acc_g = 0.f, acc_d = 0.f, acc_s = 0.f;
+    const float *G = grad_mu + (size_t)f * c.nw * c.nh;
+    for (int a = 0; a < K; ++a) {
+        const float gx = __shfl_sync(0xffffffffu, tx.g, a);
+        const float dgx = __shfl_sync(0xffffffffu, tx.dg, a);
+        const float sgx = __shfl_sync(0xffffffffu, tx.sg, a);
+        const int i = i0 + a;
+        if (i < 0 || i >= c.nw || !col_ok) continue;
+        const float gv = __ldg(G + (size_t)i * c.nh + j0 + lane);
+        acc_g = fmaf(gv, gx, acc_g);
+        acc_d = fmaf(gv, dgx, acc_d);
+        acc_s = fmaf(gv, sgx, acc_s);
+    }
+    // fold the column terms
+    const float S1 = warp_sum(acc_g * ty.g);
+    const float Sdx = warp_sum(acc_d * ty.g);
+    const float Sdy = warp_sum(acc_g * ty.dg);
+    const float Ss = warp_sum(acc_s * ty.g + acc_g * ty.sg);
+    if (lane == 0) {
+        const float A = amplitude(c, e.z);
+        const float cc = e.w * A;
+        const float inv_sigma = 1.f / sigma;
+        // d/dx Phi((u - x) / sigma) = -phi / sigma; d/dsigma = -t phi / sigma
+        float4 gr;
+        gr.x = -cc * inv_sigma * Sdx;
+        gr.y = -cc * inv_sigma * Sdy;
+        const float dz = e.z - (float)c.z_focal;
+        gr.z = c.inv_pen > 0.0 ? -e.w * A * (float)c.inv_pen * (dz > 0.f ? 1.f : (dz < 0.f ? -1.f : 0.f)) * S1
+                               : 0.f;
+        gr.w = A * S1;
+        grad_emit[r] = gr;
+        if (grad_sigma_e) grad_sigma_e[r] = -cc * inv_sigma * Ss;
+    }
+}
+
+constexpr int kSumThreads = 256;
+
+// Per segment: sum of n values in FP64, in a fixed order (a CTA per segment).
+__global__ void __launch_bounds__(kSumThreads)
+segment_sum_kernel(const float *__restrict__ x, int64_t seg_len, double *out) {
+    __shared__ double part[kSumThreads / 32];
+    const float *xs = x + (size_t)blockIdx.x * seg_len;
+    double acc = 0.0;
+    for (int64_t k = threadIdx.x; k < seg_len; k += kSumThreads) acc += (double)xs[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kSumThreads / 32; ++w) t += part[w];
+        out[blockIdx.x] = t;
+    }
+}
+
+// Poisson negative log-likelihood per segment, sum(mu - k log mu) in FP64,
+// and its gradient 1 - k / mu.
+__global__ void __launch_bounds__(kSumThreads)
+poisson_nll_kernel(const float *__restrict__ mu, const float *__restrict__ k, int64_t seg_len,
+                   double *loss, float *grad) {
+    __shared__ double part[kSumThreads / 32];
+    const size_t base = (size_t)blockIdx.x * seg_len;
+    double acc = 0.0;
+    for (int64_t q = threadIdx.x; q < seg_len; q += kSumThreads) {
+        const float m = mu[base + q], kk = k[base + q];
+        acc += (double)m - (double)kk * log((double)m);
+        if (grad) grad[base + q] = 1.f - kk / m;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kSumThreads / 32; ++w) t += part[w];
+        loss[blockIdx.x] = t;
+    }
+}
+
+int gauss_consts(const ScGaussParams *p, GaussConsts &c) {
+    SC_REQUIRE(p != nullptr, "gauss params are NULL");
+    SC_REQUIRE(p->nw > 0 && p->nh > 0 && p->nw < 32767 && p->nh < 32767, "image %dx%d", p->nw, p->nh);
+    SC_REQUIRE(p->n_frames >= 1 && p->n_emit >= 0, "n_frames=%d n_emit=%d", p->n_frames, p->n_emit);
+    SC_REQUIRE((int64_t)p->n_frames * p->n_emit < (1ll << 31), "too many emitters");
+    SC_REQUIRE(p->half_win >= 1 && p->half_win <= 15, "half_win=%d must be in [1, 15]", p->half_win);
+    SC_REQUIRE(p->tile == 8 || p->tile == 16, "tile=%d must be 8 or 16", p->tile);
+    SC_REQUIRE(p->px > 0, "px must be positive");
+    SC_REQUIRE(p->inv_pen >= 0, "inv_pen must be >= 0");
+    c.nw = p->nw;
+    c.nh = p->nh;
+    c.n_frames = p->n_frames;
+    c.n_emit = p->n_emit;
+    c.R = p->half_win;
+    c.px = p->px;
+    c.half_w = p->nw * p->px * 0.5;
+    c.half_h = p->nh * p->px * 0.5;
+    c.inv_pen = p->inv_pen;
+    c.z_focal = p->z_focal;
+    return SC_OK;
+}
+
+// Splat parameters of the forward: tiles of p->tile, halo 2R (a window spans
+// 2R + 1 pixels from its first one), one image per frame.
+ScSplatParams gauss_splat_params(const ScGaussParams *p) {
+    ScSplatParams sp{};
+    sp.nw = p->nw;
+    sp.nh = p->nh;
+    sp.tile = p->tile;
+    sp.halo = 2 * p->half_win;
+    sp.warps = 4;
+    sp.tiles_x = (p->nw + p->tile - 1) / p->tile;
+    sp.tiles_y = (p->nh + p->tile - 1) / p->tile;
+    sp.n_images = p->n_frames;
+    sp.rec_per_image = p->n_emit;
+    return sp;
+}
+
+struct GaussWorkspace {
+    ScStepRec *recs;
+    int32_t *tile_start, *items;
+    void *bin_ws;
+    size_t bin_bytes;
+    float *tiles;
+    size_t total;
+};
+
+GaussWorkspace gauss_workspace(const ScGaussParams *p, void *base) {
+    const ScSplatParams sp = gauss_splat_params(p);
+    const int n_rec = p->n_frames * p->n_emit;
+    const int n_tiles = sp.tiles_x * sp.tiles_y * sp.n_images;
+    const int E = sp.tile + sp.halo;
+    auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    GaussWorkspace w{};
+    char *b = static_cast<char *>(base);
+    size_t off = 0;
+    w.recs = reinterpret_cast<ScStepRec *>(b + off);
+    off += up((size_t)(n_rec > 0 ? n_rec : 1) * sizeof(ScStepRec));
+    w.tile_start = reinterpret_cast<int32_t *>(b + off);
+    off += up((size_t)(2 * n_tiles + 1) * sizeof(int32_t));
+    w.items = reinterpret_cast<int32_t *>(b + off);
+    off += up((size_t)(n_rec > 0 ? n_rec : 1) * sizeof(int32_t));
+    w.bin_ws = b + off;
+    w.bin_bytes = sc_bin_workspace_bytes(n_rec > 0 ? n_rec : 1, n_tiles);
+    off += up(w.bin_bytes);
+    w.tiles = reinterpret_cast<float *>(b + off);
+    off += up((size_t)n_tiles * E * E * sizeof(float));
+    w.total = off;
+    return w;
+}
+
+}  // namespace
+
+extern "C" size_t sc_gauss_workspace_bytes(const ScGaussParams *p) {
+    GaussConsts c;
+    if (gauss_consts(p, c) != SC_OK) return 0;
+    return gauss_workspace(p, nullptr).total;
+}
+
+extern "C" int sc_gauss_forward(const ScGaussParams *p, const float *d_emit, const float *d_sigma,
+                                const float *d_bg, void *d_ws, size_t ws_bytes, float *d_mu,
+                                int32_t *d_status, void *stream) {
+    GaussConsts c;
+    int rc = gauss_consts(p, c);
+    if (rc) return rc;
+    SC_REQUIRE(d_sigma && d_mu && d_ws, "sc_gauss_forward: NULL pointer");
+    SC_REQUIRE(c.n_emit == 0 || d_emit, "sc_gauss_forward: emitters are NULL");
+    const GaussWorkspace w = gauss_workspace(p, d_ws);
+    SC_REQUIRE(ws_bytes >= w.total, "sc_gauss_forward: workspace %zu < %zu bytes", ws_bytes, w.total);
+    cudaStream_t s = sc::as_stream(stream);
+    const ScSplatParams sp = gauss_splat_params(p);
+    sc::TileGeom g;
+    rc = sc::tile_geom(&sp, g);
+    if (rc) return rc;
+    const int n_rec = c.n_frames * c.n_emit;
+    if (n_rec > 0) {
+        gauss_records_kernel<<<(n_rec + 255) / 256, 256, 0, s>>>(
+            c, reinterpret_cast<const float4 *>(d_emit), w.recs);
+        rc = sc_bin_steps(w.recs, n_rec, &sp, w.bin_ws, w.bin_bytes, w.tile_start, w.items,
+                          d_status, stream);
+        if (rc) return rc;
+        const int E = g.edge, BS = (E * E + 31) & ~31;
+        const size_t smem = (size_t)4 * BS * sizeof(float);
+        SC_REQUIRE(smem <= 48 * 1024, "sc_gauss_forward: tile buffers need %zu bytes", smem);
+        gauss_splat_kernel<4><<<g.n_tiles, 128, smem, s>>>(w.recs, w.tile_start, w.items, g,
+                                                           d_sigma, c.px, w.tiles);
+    } else {
+        rc = sc::cuda_status(
+            cudaMemsetAsync(w.tiles, 0, (size_t)g.n_tiles * g.edge * g.edge * sizeof(float), s),
+            "sc_gauss_forward");
+        if (rc) return rc;
+    }
+    const int64_t n_px = (int64_t)c.nw * c.nh * c.n_frames;
+    int grid = (int)((n_px + 255) / 256);
+    if (grid > 152 * 16) grid = 152 * 16;
+    gauss_merge_kernel<<<grid, 256, 0, s>>>(w.tiles, g, d_bg, d_mu);
+    return sc::launch_status("sc_gauss_forward");
+}
+
+extern "C" int sc_gauss_backward(const ScGaussParams *p, const float *d_emit, const float *d_sigma,
+                                 const float *d_grad_mu, float *d_grad_emit,
+                                 float *d_grad_sigma_e, void *stream) {
+    GaussConsts c;
+    int rc = gauss_consts(p, c);
+    if (rc) return rc;
+    const int n_rec = c.n_frames * c.n_emit;
+    if (n_rec == 0) return SC_OK;
+    SC_REQUIRE(d_emit && d_sigma && d_grad_mu && d_grad_emit, "sc_gauss_backward: NULL pointer");
+    gauss_backward_kernel<<<(n_rec + 7) / 8, 256, 0, sc::as_stream(stream)>>>(
+        c, reinterpret_cast<const float4 *>(d_emit), d_sigma, d_grad_mu,
+        reinterpret_cast<float4 *>(d_grad_emit), d_grad_sigma_e);
+    return sc::launch_status("sc_gauss_backward");
+}
+
+extern "C" int sc_segment_sum(const float *d_x, int64_t seg_len, int n_seg, double *d_out,
+                              void *stream) {
+    SC_REQUIRE(seg_len >= 0 && n_seg >= 0, "sc_segment_sum: negative size");
+    if (n_seg == 0) return SC_OK;
+    SC_REQUIRE(d_out && (seg_len == 0 || d_x), "sc_segment_sum: NULL pointer");
+    segment_sum_kernel<<<n_seg, kSumThreads, 0, sc::as_stream(stream)>>>(d_x, seg_len, d_out);
+    return sc::launch_status("sc_segment_sum");
+}
+
+extern "C" int sc_poisson_nll(const float *d_mu, const float *d_counts, int64_t seg_len, int n_seg,
+                              double *d_loss, float *d_grad_mu, void *stream) {
+    SC_REQUIRE(seg_len >= 0 && n_seg >= 0, "sc_poisson_nll: negative size");
+    if (n_seg == 0) return SC_OK;
+    SC_REQUIRE(d_mu && d_counts && d_loss, "sc_poisson_nll: NULL pointer");
+    poisson_nll_kernel<<<n_seg, kSumThreads, 0, sc::as_stream(stream)>>>(d_mu, d_counts, seg_len,
+                                                                          d_loss, d_grad_mu);
+    return sc::launch_status("sc_poisson_nll");
+}

@@ -257,6 +257,7 @@ def gb300_arm(args, rank, world):
     value = world * args.steps / (elapsed_ms / 1e3)
 
     e2e = None if args.small else e2e_arm(args, cfg, dev, rank, world)
+    fwd_bwd = None if args.small else fwd_bwd_arm(args, dev)
 
     splat_avg_ms = sum(splat_ms) / len(splat_ms)
     n_rec = sum(splat_recs) / len(splat_recs)
@@ -285,9 +286,10 @@ def gb300_arm(args, rank, world):
                    "live_emitters": [round(live0, 4), round(live1, 4)],
                    "psf_build_s": round(psf_build_s, 3)},
         "e2e": e2e,
+        "fwd_bwd": fwd_bwd,
         "gpu_launches": fg.launches_per_frame * args.steps,
         "clocks": clk,
-        "roofline": {"kernel": "splat_box_tma_kernel + splat_sat_kernel + splat_merge_kernel",
+        "roofline": {"kernel": "splat_box_bulk_kernel + splat_sat_kernel + splat_merge_kernel",
                      "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
@@ -334,6 +336,84 @@ def e2e_arm(args, cfg, dev, rank, world):
     return {"value": world * steps / dt, "unit": "frames/s", "frames": steps,
             "h2d_bytes_per_step": SUBSTEPS * N_EMIT * 5 * 8 + SUBSTEPS * 8,
             "d2h_bytes_per_step": IMAGE * IMAGE * 8 + 16}
+
+
+# ------------------------------------------------------- differentiable form
+def _graph_time(fn, steps, warmup):
+    """ms per call of fn replayed from a CUDA graph (warm-up calls run eagerly first)."""
+    import torch
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(warmup):
+            fn()
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fn()
+    for _ in range(warmup):
+        g.replay()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(steps):
+        g.replay()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def fwd_bwd_case(dev, frames, n_emit, image, sigma, penetration, z_half, steps, warmup, seed):
+    """Forward and forward + Poisson NLL + adjoint of the differentiable image."""
+    import torch
+    from scopyon_gb300 import differentiable as dm
+    rng = numpy.random.RandomState(seed)
+    half = image * PX * 0.5
+    e = numpy.zeros((frames, n_emit, 4), dtype=numpy.float32)
+    e[..., 0] = rng.uniform(-half, half, (frames, n_emit))
+    e[..., 1] = rng.uniform(-half, half, (frames, n_emit))
+    e[..., 2] = rng.uniform(-z_half, z_half, (frames, n_emit))
+    e[..., 3] = rng.lognormal(math.log(2000.0), 0.3, (frames, n_emit))
+    model = dm.GaussianImageModel(image, image, PX, 1.5 * sigma, penetration=penetration,
+                                  device=dev)
+    emit = torch.tensor(e, device=dev).requires_grad_(True)
+    bg = torch.full((frames,), 10.0, device=dev).requires_grad_(True)
+    sig = torch.tensor(sigma, dtype=torch.float32, device=dev).requires_grad_(True)
+    with torch.no_grad():
+        counts = torch.poisson(dm.expected_image(emit, bg, sig, model).double(),
+                               generator=torch.Generator(dev).manual_seed(seed)).float()
+
+    def forward():
+        with torch.no_grad():
+            return dm.expected_image(emit, bg, sig, model)
+
+    def step():
+        loss = dm.poisson_nll(dm.expected_image(emit, bg, sig, model), counts)
+        return torch.autograd.grad(loss, [emit, bg, sig])
+
+    fwd_ms = _graph_time(forward, steps, warmup)
+    fb_ms = _graph_time(step, steps, warmup)
+    return {"frames": frames, "emitters_per_frame": n_emit, "image": [image, image],
+            "sigma_nm": sigma * 1e9, "window_px": 2 * model.half_win + 1,
+            "illumination": "EPI" if math.isinf(penetration) else
+            "TIRF, %.0f nm penetration" % (penetration * 1e9),
+            "forward_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "fwd_bwd_over_forward": fb_ms / fwd_ms,
+            "fwd_bwd_frames_per_s": frames / (fb_ms / 1e3)}
+
+
+def fwd_bwd_arm(args, dev):
+    """fwd+bwd frames/s of the differentiable image at 512^2 px, 20k emitters, and
+    on a batch of 64 frames of 128^2 px with 200 emitters each."""
+    steps = max(20, args.steps)
+    headline = fwd_bwd_case(dev, 1, N_EMIT, IMAGE, 90e-9, math.inf, 1e-6, steps, args.warmup, 5)
+    batch = fwd_bwd_case(dev, 64, 200, 128, 120e-9, 300e-9, 0.5e-6, steps, args.warmup, 6)
+    return {"value": headline["fwd_bwd_frames_per_s"], "unit": "frames/s",
+            "workload": "differentiable Gaussian-PSF image, 512^2 px, 20k emitters: forward, "
+                        "FP64 Poisson NLL, adjoint (dL/dx, dy, dz, dI, dbg, dsigma); one CUDA "
+                        "graph replay per step",
+            "dtype": "f32 (FP64 loss reduction)", "headline": headline,
+            "batch_64x128px_200": batch}
 
 
 # ---------------------------------------------------------------- CPU baseline

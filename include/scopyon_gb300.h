@@ -271,14 +271,20 @@ int sc_gauss_backward(const ScGaussParams *p, const float *d_emit, const float *
                       const float *d_grad_mu, float *d_grad_emit, float *d_grad_sigma_e,
                       void *stream);
 
-/* d_out[s] = sum of d_x[s * seg_len .. (s + 1) * seg_len) in FP64, in a fixed
- * order. */
-int sc_segment_sum(const float *d_x, int64_t seg_len, int n_seg, double *d_out, void *stream);
+/* Bytes of scratch the two reductions below need for n_seg segments of
+ * seg_len values (partial sums of up to 64 CTAs per segment).               */
+size_t sc_reduce_scratch_bytes(int64_t seg_len, int n_seg);
 
-/* Poisson negative log-likelihood per segment, sum(mu - k log mu) in FP64,
- * and (if d_grad_mu is not NULL) its gradient 1 - k / mu.                    */
+/* d_out[s] = sum of d_x[s * seg_len .. (s + 1) * seg_len) in FP64, in a fixed
+ * order (deterministic). */
+int sc_segment_sum(const float *d_x, int64_t seg_len, int n_seg, void *d_scratch,
+                   size_t scratch_bytes, double *d_out, void *stream);
+
+/* Poisson negative log-likelihood per segment, sum(mu - k log mu) accumulated
+ * in FP64, and (if d_grad_mu is not NULL) its gradient 1 - k / mu.           */
 int sc_poisson_nll(const float *d_mu, const float *d_counts, int64_t seg_len, int n_seg,
-                   double *d_loss, float *d_grad_mu, void *stream);
+                   void *d_scratch, size_t scratch_bytes, double *d_loss, float *d_grad_mu,
+                   void *stream);
 
 /* Largest tile count (tiles per image x images) sc_bin_steps_static takes. */
 #define SC_BIN_STATIC_MAX_TILES 65536

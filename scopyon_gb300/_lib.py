@@ -103,8 +103,9 @@ _SIG = {
     "sc_gauss_forward": (_I, [ctypes.POINTER(GaussParams), _P, _P, _P, _P, ctypes.c_size_t, _P,
                               _P, _P]),
     "sc_gauss_backward": (_I, [ctypes.POINTER(GaussParams), _P, _P, _P, _P, _P, _P]),
-    "sc_segment_sum": (_I, [_P, ctypes.c_int64, _I, _P, _P]),
-    "sc_poisson_nll": (_I, [_P, _P, ctypes.c_int64, _I, _P, _P, _P]),
+    "sc_reduce_scratch_bytes": (ctypes.c_size_t, [ctypes.c_int64, _I]),
+    "sc_segment_sum": (_I, [_P, ctypes.c_int64, _I, _P, ctypes.c_size_t, _P, _P]),
+    "sc_poisson_nll": (_I, [_P, _P, ctypes.c_int64, _I, _P, ctypes.c_size_t, _P, _P, _P]),
 }
 
 

@@ -248,47 +248,81 @@ __global__ void gauss_backward_kernel(GaussConsts c, const float4 *__restrict__ 
 }
 
 constexpr int kSumThreads = 256;
+constexpr int kSumChunk = 8192;    // values per CTA and pass
+constexpr int kSumMaxParts = 64;   // CTAs per segment
 
-// Per segment: sum of n values in FP64, in a fixed order (a CTA per segment).
-__global__ void __launch_bounds__(kSumThreads)
-segment_sum_kernel(const float *__restrict__ x, int64_t seg_len, double *out) {
-    __shared__ double part[kSumThreads / 32];
-    const float *xs = x + (size_t)blockIdx.x * seg_len;
-    double acc = 0.0;
-    for (int64_t k = threadIdx.x; k < seg_len; k += kSumThreads) acc += (double)xs[k];
+__device__ __forceinline__ double block_sum(double acc, double *part) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
+    double t = 0.0;
+    if (threadIdx.x == 0)
         for (int w = 0; w < kSumThreads / 32; ++w) t += part[w];
-        out[blockIdx.x] = t;
-    }
+    return t;
 }
 
-// Poisson negative log-likelihood per segment, sum(mu - k log mu) in FP64,
-// and its gradient 1 - k / mu.
+// Part x of segment y: the chunks x, x + parts, ... of kSumChunk values,
+// summed in FP64 in a fixed order into partial[y][x].
+// With counts, the terms are the Poisson NLL mu - k log mu and grad gets
+// 1 - k / mu.
 __global__ void __launch_bounds__(kSumThreads)
-poisson_nll_kernel(const float *__restrict__ mu, const float *__restrict__ k, int64_t seg_len,
-                   double *loss, float *grad) {
+partial_sum_kernel(const float *__restrict__ x, const float *__restrict__ counts, int64_t seg_len,
+                   float *grad, double *partial) {
     __shared__ double part[kSumThreads / 32];
-    const size_t base = (size_t)blockIdx.x * seg_len;
+    const int parts = gridDim.x;
+    const size_t base = (size_t)blockIdx.y * seg_len;
     double acc = 0.0;
-    for (int64_t q = threadIdx.x; q < seg_len; q += kSumThreads) {
-        const float m = mu[base + q], kk = k[base + q];
-        acc += (double)m - (double)kk * log((double)m);
-        if (grad) grad[base + q] = 1.f - kk / m;
+    for (int64_t c0 = (int64_t)blockIdx.x * kSumChunk; c0 < seg_len; c0 += (int64_t)parts * kSumChunk) {
+        const int64_t c1 = c0 + kSumChunk < seg_len ? c0 + kSumChunk : seg_len;
+        for (int64_t q = c0 + threadIdx.x; q < c1; q += kSumThreads) {
+            const float m = x[base + q];
+            if (counts) {
+                const float kk = counts[base + q];
+                // logf is within an ulp; the FP64 accumulation is what a
+                // sum over millions of pixels needs
+                acc += (double)m - (double)kk * (double)logf(m);
+                if (grad) grad[base + q] = 1.f - kk / m;
+            } else {
+                acc += (double)m;
+            }
+        }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < kSumThreads / 32; ++w) t += part[w];
-        loss[blockIdx.x] = t;
-    }
+    const double t = block_sum(acc, part);
+    if (threadIdx.x == 0) partial[(size_t)blockIdx.y * parts + blockIdx.x] = t;
+}
+
+// out[y] = sum of partial[y][0 .. parts) in order.
+__global__ void finish_sum_kernel(const double *partial, int parts, int n_seg, double *out) {
+    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= n_seg) return;
+    double t = 0.0;
+    for (int k = 0; k < parts; ++k) t += partial[(size_t)y * parts + k];
+    out[y] = t;
+}
+
+int sum_parts(int64_t seg_len) {
+    int64_t parts = (seg_len + kSumChunk - 1) / kSumChunk;
+    if (parts < 1) parts = 1;
+    if (parts > kSumMaxParts) parts = kSumMaxParts;
+    return (int)parts;
+}
+
+int launch_reduce(const float *x, const float *counts, int64_t seg_len, int n_seg, void *scratch,
+                  size_t scratch_bytes, float *grad, double *out, cudaStream_t s) {
+    SC_REQUIRE(seg_len >= 0 && n_seg >= 0, "negative size");
+    if (n_seg == 0) return SC_OK;
+    SC_REQUIRE(n_seg <= 65535, "n_seg=%d exceeds 65535", n_seg);
+    SC_REQUIRE(out && (seg_len == 0 || x), "NULL pointer");
+    const int parts = sum_parts(seg_len);
+    SC_REQUIRE(scratch && scratch_bytes >= (size_t)parts * n_seg * sizeof(double),
+               "reduction scratch %zu < %zu bytes", scratch_bytes,
+               (size_t)parts * n_seg * sizeof(double));
+    double *partial = static_cast<double *>(scratch);
+    partial_sum_kernel<<<dim3((unsigned)parts, (unsigned)n_seg), kSumThreads, 0, s>>>(
+        x, counts, seg_len, grad, partial);
+    finish_sum_kernel<<<(n_seg + 127) / 128, 128, 0, s>>>(partial, parts, n_seg, out);
+    return sc::launch_status("reduction");
 }
 
 int gauss_consts(const ScGaussParams *p, GaussConsts &c) {
@@ -425,21 +459,21 @@ extern "C" int sc_gauss_backward(const ScGaussParams *p, const float *d_emit, co
     return sc::launch_status("sc_gauss_backward");
 }
 
-extern "C" int sc_segment_sum(const float *d_x, int64_t seg_len, int n_seg, double *d_out,
-                              void *stream) {
-    SC_REQUIRE(seg_len >= 0 && n_seg >= 0, "sc_segment_sum: negative size");
-    if (n_seg == 0) return SC_OK;
-    SC_REQUIRE(d_out && (seg_len == 0 || d_x), "sc_segment_sum: NULL pointer");
-    segment_sum_kernel<<<n_seg, kSumThreads, 0, sc::as_stream(stream)>>>(d_x, seg_len, d_out);
-    return sc::launch_status("sc_segment_sum");
+extern "C" size_t sc_reduce_scratch_bytes(int64_t seg_len, int n_seg) {
+    if (seg_len < 0 || n_seg <= 0) return 0;
+    return (size_t)sum_parts(seg_len) * n_seg * sizeof(double);
+}
+
+extern "C" int sc_segment_sum(const float *d_x, int64_t seg_len, int n_seg, void *d_scratch,
+                              size_t scratch_bytes, double *d_out, void *stream) {
+    return launch_reduce(d_x, nullptr, seg_len, n_seg, d_scratch, scratch_bytes, nullptr, d_out,
+                         sc::as_stream(stream));
 }
 
 extern "C" int sc_poisson_nll(const float *d_mu, const float *d_counts, int64_t seg_len, int n_seg,
-                              double *d_loss, float *d_grad_mu, void *stream) {
-    SC_REQUIRE(seg_len >= 0 && n_seg >= 0, "sc_poisson_nll: negative size");
-    if (n_seg == 0) return SC_OK;
-    SC_REQUIRE(d_mu && d_counts && d_loss, "sc_poisson_nll: NULL pointer");
-    poisson_nll_kernel<<<n_seg, kSumThreads, 0, sc::as_stream(stream)>>>(d_mu, d_counts, seg_len,
-                                                                          d_loss, d_grad_mu);
-    return sc::launch_status("sc_poisson_nll");
+                              void *d_scratch, size_t scratch_bytes, double *d_loss,
+                              float *d_grad_mu, void *stream) {
+    SC_REQUIRE(n_seg == 0 || d_counts, "sc_poisson_nll: counts are NULL");
+    return launch_reduce(d_mu, d_counts, seg_len, n_seg, d_scratch, scratch_bytes, d_grad_mu,
+                         d_loss, sc::as_stream(stream));
 }

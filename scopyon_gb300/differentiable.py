@@ -26,6 +26,19 @@ from . import _lib
 from ._lib import call, ptr, stream_ptr
 
 
+_scratch = {}
+
+
+def _reduce_scratch(seg_len, n_seg, device):
+    """A cached device scratch large enough for one reduction of this shape."""
+    n = _lib.load().sc_reduce_scratch_bytes(int(seg_len), int(n_seg))
+    t = _scratch.get(device)
+    if t is None or t.numel() < n:
+        t = torch.empty(max(n, 8), dtype=torch.uint8, device=device)
+        _scratch[device] = t
+    return t, n
+
+
 class GaussianImageModel:
     """Geometry of the differentiable image: W x H pixels of ``px`` metres.
 
@@ -109,10 +122,13 @@ class _ExpectedImage(torch.autograd.Function):
         g_sig_e = torch.empty(F, N, dtype=torch.float32, device=emitters.device)
         s = stream_ptr()
         call("sc_gauss_backward", p, ptr(emitters), ptr(sig), ptr(g), ptr(g_emit), ptr(g_sig_e), s)
-        g_bg = torch.empty(F, dtype=torch.float64, device=emitters.device)
-        call("sc_segment_sum", ptr(g), model.nw * model.nh, F, ptr(g_bg), s)
-        g_sigma = torch.empty(1, dtype=torch.float64, device=emitters.device)
-        call("sc_segment_sum", ptr(g_sig_e), F * N, 1, ptr(g_sigma), s)
+        dev = emitters.device
+        g_bg = torch.empty(F, dtype=torch.float64, device=dev)
+        scr, n = _reduce_scratch(model.nw * model.nh, F, dev)
+        call("sc_segment_sum", ptr(g), model.nw * model.nh, F, ptr(scr), n, ptr(g_bg), s)
+        g_sigma = torch.empty(1, dtype=torch.float64, device=dev)
+        scr, n = _reduce_scratch(F * N, 1, dev)
+        call("sc_segment_sum", ptr(g_sig_e), F * N, 1, ptr(scr), n, ptr(g_sigma), s)
         return g_emit, g_bg.float(), g_sigma.float().reshape(()), None
 
 
@@ -138,7 +154,9 @@ class _PoissonNLL(torch.autograd.Function):
         seg = mu.numel() // F
         loss = torch.empty(F, dtype=torch.float64, device=mu.device)
         grad = torch.empty_like(mu)
-        call("sc_poisson_nll", ptr(mu), ptr(counts), seg, F, ptr(loss), ptr(grad), stream_ptr())
+        scr, n = _reduce_scratch(seg, F, mu.device)
+        call("sc_poisson_nll", ptr(mu), ptr(counts), seg, F, ptr(scr), n, ptr(loss), ptr(grad),
+             stream_ptr())
         ctx.save_for_backward(grad)
         return loss.sum()
 

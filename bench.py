@@ -402,18 +402,67 @@ def fwd_bwd_case(dev, frames, n_emit, image, sigma, penetration, z_half, steps, 
             "fwd_bwd_frames_per_s": frames / (fb_ms / 1e3)}
 
 
+def diffusion_grad_case(dev, n_emit, image, T, steps, warmup, seed):
+    """dL/dD through T Brownian sub-steps: forward (positions, summed frame,
+    Gaussian-approximated sCMOS likelihood) and forward + backward (positions
+    regenerated from their Philox counters, adjoint, reparameterised dL/dD)."""
+    import torch
+    from scopyon_gb300 import differentiable as dm
+    rng = numpy.random.RandomState(seed)
+    half = image * PX * 0.5
+    e = numpy.zeros((n_emit, 4), dtype=numpy.float32)
+    e[:, 0] = rng.uniform(-half, half, n_emit)
+    e[:, 1] = rng.uniform(-half, half, n_emit)
+    e[:, 3] = rng.lognormal(math.log(2000.0), 0.3, n_emit)
+    sigma, dt, D_true = 120e-9, EXPOSURE / T, 0.05e-12
+    model = dm.GaussianImageModel(image, image, PX, 1.5 * sigma, device=dev)
+    emit = torch.tensor(e, device=dev)
+    sig = torch.tensor(sigma, dtype=torch.float32, device=dev)
+    # sCMOS read-noise variance per pixel: sigma ~ lognormal(ln 1.5, 0.4)
+    var_map = torch.tensor(rng.lognormal(math.log(1.5), 0.4, (image, image)) ** 2,
+                           dtype=torch.float32, device=dev)
+    with torch.no_grad():
+        pos = dm.diffusion_positions(torch.tensor(D_true, device=dev), emit, T, dt, seed=seed)
+        mu = dm.expected_image(pos.reshape(1, -1, 4), torch.full((1,), 10.0, device=dev), sig,
+                               model)[0]
+        counts = mu + torch.sqrt(mu + var_map) * torch.randn(
+            mu.shape, device=dev, generator=torch.Generator(dev).manual_seed(seed))
+        del pos, mu
+    D = torch.tensor(0.03e-12, dtype=torch.float32, device=dev).requires_grad_(True)
+
+    def loss_fn(d):
+        return dm.diffusion_loss(d, emit, counts, sig, model, T, dt, seed=seed + 1,
+                                 background=10.0, readout_var=var_map)
+
+    def forward():
+        with torch.no_grad():
+            return loss_fn(D)
+
+    def step():
+        return torch.autograd.grad(loss_fn(D), [D])
+
+    fwd_ms = _graph_time(forward, steps, warmup)
+    fb_ms = _graph_time(step, steps, warmup)
+    return {"emitters": n_emit, "image": [image, image], "substeps": T,
+            "D_um2_per_s": 0.05, "sigma_nm": sigma * 1e9,
+            "loss": "Gaussian-approximated sCMOS NLL of the summed frame, FP64 reduction",
+            "forward_ms": fwd_ms, "fwd_bwd_ms": fb_ms, "fwd_bwd_over_forward": fb_ms / fwd_ms,
+            "emitter_steps_per_s_fwd_bwd": n_emit * T / (fb_ms / 1e3)}
+
+
 def fwd_bwd_arm(args, dev):
     """fwd+bwd frames/s of the differentiable image at 512^2 px, 20k emitters, and
     on a batch of 64 frames of 128^2 px with 200 emitters each."""
     steps = max(20, args.steps)
     headline = fwd_bwd_case(dev, 1, N_EMIT, IMAGE, 90e-9, math.inf, 1e-6, steps, args.warmup, 5)
     batch = fwd_bwd_case(dev, 64, 200, 128, 120e-9, 300e-9, 0.5e-6, steps, args.warmup, 6)
+    dgrad = diffusion_grad_case(dev, 100000, 2048, 100, max(5, args.steps // 4), args.warmup, 9)
     return {"value": headline["fwd_bwd_frames_per_s"], "unit": "frames/s",
             "workload": "differentiable Gaussian-PSF image, 512^2 px, 20k emitters: forward, "
                         "FP64 Poisson NLL, adjoint (dL/dx, dy, dz, dI, dbg, dsigma); one CUDA "
                         "graph replay per step",
             "dtype": "f32 (FP64 loss reduction)", "headline": headline,
-            "batch_64x128px_200": batch}
+            "batch_64x128px_200": batch, "diffusion_dD_100k_2048px_T100": dgrad}
 
 
 # ---------------------------------------------------------------- CPU baseline

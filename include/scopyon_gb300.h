@@ -286,6 +286,35 @@ int sc_poisson_nll(const float *d_mu, const float *d_counts, int64_t seg_len, in
                    void *d_scratch, size_t scratch_bytes, double *d_loss, float *d_grad_mu,
                    void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Gradient through diffusion (new: the reference has no gradients).  Emitter
+ * e (float4 x, y, z, I) moves in 2-D as p_t = p0 + sqrt(2 D dt) Z_t, Z_t the
+ * sum of its first t Philox normal pairs (src/scopyon/sampling.py:88-119),
+ * and contributes I / T photons at each of T sub-steps (the unit_time
+ * weights of src/scopyon/_epifm.py:1183-1199).  D is a device scalar (m^2/s).
+ * Positions are regenerated from the counters, never stored across passes.  */
+
+/* Bytes of scratch sc_gauss_nll / sc_diffusion_dD need for n values. */
+size_t sc_dgrad_scratch_bytes(int64_t n_values);
+
+/* d_out[t][e] = (x_t, y_t, z, I / T), t < T.  d_normals ([T][n][2], else
+ * NULL) replace the Philox draws.                                          */
+int sc_diffusion_positions(const float *d_emit, int n, int T, const float *d_D, double dt,
+                           uint64_t seed, const float *d_normals, float *d_out, void *stream);
+
+/* Gaussian approximation of the camera likelihood of counts k given mu, with
+ * variance mu + r2 (r2: d_var_map per pixel, else var):
+ * *d_loss = sum (k - mu)^2 / (2 v) + log(v) / 2 (FP64), d_grad_mu = dL/dmu.  */
+int sc_gauss_nll(const float *d_mu, const float *d_counts, int64_t n, const float *d_var_map,
+                 double var, void *d_scratch, size_t scratch_bytes, double *d_loss,
+                 float *d_grad_mu, void *stream);
+
+/* *d_dD = sum_{t,e} dL/dp_t . (p_t - p0) / (2 D) (FP64) from the positions of
+ * sc_diffusion_positions and their gradients (float4: dL/dx, dL/dy, ...).   */
+int sc_diffusion_dD(const float *d_pos, const float *d_emit, int n, int T,
+                    const float *d_grad_pos, const float *d_D, void *d_scratch,
+                    size_t scratch_bytes, double *d_dD, void *stream);
+
 /* Largest tile count (tiles per image x images) sc_bin_steps_static takes. */
 #define SC_BIN_STATIC_MAX_TILES 65536
 

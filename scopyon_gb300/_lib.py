@@ -104,6 +104,10 @@ _SIG = {
                               _P, _P]),
     "sc_gauss_backward": (_I, [ctypes.POINTER(GaussParams), _P, _P, _P, _P, _P, _P]),
     "sc_reduce_scratch_bytes": (ctypes.c_size_t, [ctypes.c_int64, _I]),
+    "sc_dgrad_scratch_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
+    "sc_diffusion_positions": (_I, [_P, _I, _I, _P, _D, ctypes.c_uint64, _P, _P, _P]),
+    "sc_gauss_nll": (_I, [_P, _P, ctypes.c_int64, _P, _D, _P, ctypes.c_size_t, _P, _P, _P]),
+    "sc_diffusion_dD": (_I, [_P, _P, _I, _I, _P, _P, _P, ctypes.c_size_t, _P, _P]),
     "sc_segment_sum": (_I, [_P, ctypes.c_int64, _I, _P, ctypes.c_size_t, _P, _P]),
     "sc_poisson_nll": (_I, [_P, _P, ctypes.c_int64, _I, _P, ctypes.c_size_t, _P, _P, _P]),
 }

@@ -14,6 +14,12 @@ gradients with respect to emitter x, y, z, intensity, background and the PSF
 width sigma. ``poisson_nll`` reduces the Poisson negative log-likelihood in
 FP64 on the GPU.
 
+``diffusion_loss`` differentiates a summed frame through Brownian
+trajectories with respect to the diffusion coefficient D, using the
+reparameterisation ``dp_t/dD = (p_t - p0) / (2 D)``. The backward pass
+regenerates the trajectories from their Philox counters instead of storing
+them.
+
 The reference has no gradients; this module extends it on the same geometry
 and configuration.
 """
@@ -169,3 +175,93 @@ class _PoissonNLL(torch.autograd.Function):
 def poisson_nll(mu, counts):
     """sum(mu - k log mu) over all pixels (FP64 on the GPU), differentiable in mu."""
     return _PoissonNLL.apply(mu, counts)
+
+
+def _dgrad_scratch(n, device):
+    nbytes = _lib.load().sc_dgrad_scratch_bytes(int(n))
+    key = ("dgrad", device)
+    t = _scratch.get(key)
+    if t is None or t.numel() < nbytes:
+        t = torch.empty(max(nbytes, 8), dtype=torch.uint8, device=device)
+        _scratch[key] = t
+    return t, nbytes
+
+
+def diffusion_positions(D, emitters, T, dt, seed=0, normals=None):
+    """(T, N, 4) float32 sub-step positions (x_t, y_t, z, I / T) of emitters
+    (N, 4) diffusing with coefficient D (device scalar, m^2/s) for T steps of
+    dt; normals (T, N, 2), if given, replace the Philox draws."""
+    N = emitters.shape[0]
+    out = torch.empty(T, N, 4, dtype=torch.float32, device=emitters.device)
+    call("sc_diffusion_positions", ptr(emitters), N, int(T), ptr(D), float(dt),
+         int(seed) & (2 ** 64 - 1), ptr(normals), ptr(out), stream_ptr())
+    return out
+
+
+class _DiffusionLoss(torch.autograd.Function):
+
+    @staticmethod
+    def forward(ctx, D, emitters, counts, sigma, model, T, dt, seed, background, var, var_map,
+                normals):
+        D = D.reshape(1).contiguous().float()
+        emitters = emitters.contiguous().float()
+        dev = emitters.device
+        N = emitters.shape[0]
+        pos = diffusion_positions(D, emitters, T, dt, seed, normals)
+        sig = sigma.reshape(1).contiguous().float()
+        p = model.params(1, N * T)
+        ws, nbytes = model.workspace(p)
+        mu = torch.empty(1, model.nw, model.nh, dtype=torch.float32, device=dev)
+        bg = torch.full((1,), float(background), dtype=torch.float32, device=dev)
+        status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
+        s = stream_ptr()
+        call("sc_gauss_forward", p, ptr(pos), ptr(sig), ptr(bg), ptr(ws), nbytes, ptr(mu),
+             ptr(status), s)
+        del pos  # trajectories are not kept for the backward pass
+        grad_mu = torch.empty_like(mu)
+        loss = torch.empty(1, dtype=torch.float64, device=dev)
+        scr, n = _dgrad_scratch(mu.numel(), dev)
+        call("sc_gauss_nll", ptr(mu), ptr(counts.contiguous().float()), mu.numel(), ptr(var_map),
+             float(var), ptr(scr), n, ptr(loss), ptr(grad_mu), s)
+        ctx.save_for_backward(D, emitters, grad_mu, sig, normals if normals is not None else D)
+        ctx.has_normals = normals is not None
+        ctx.model, ctx.T, ctx.dt, ctx.seed = model, T, dt, seed
+        return loss.reshape(())
+
+    @staticmethod
+    def backward(ctx, g):
+        D, emitters, grad_mu, sig, normals = ctx.saved_tensors
+        normals = normals if ctx.has_normals else None
+        model, T = ctx.model, ctx.T
+        N = emitters.shape[0]
+        dev = emitters.device
+        # regenerate the trajectories from their counters
+        pos = diffusion_positions(D, emitters, T, ctx.dt, ctx.seed, normals)
+        p = model.params(1, N * T)
+        grad_pos = torch.empty_like(pos)
+        s = stream_ptr()
+        call("sc_gauss_backward", p, ptr(pos), ptr(sig), ptr(grad_mu), ptr(grad_pos), None, s)
+        dD = torch.empty(1, dtype=torch.float64, device=dev)
+        scr, n = _dgrad_scratch(N * T, dev)
+        call("sc_diffusion_dD", ptr(pos), ptr(emitters), N, int(T), ptr(grad_pos), ptr(D),
+             ptr(scr), n, ptr(dD), s)
+        return (dD * g).float().reshape(()), None, None, None, None, None, None, None, None, \
+            None, None, None
+
+
+def diffusion_loss(D, emitters, counts, sigma, model, T, dt, seed=0, background=0.0,
+                   readout_var=0.0, normals=None):
+    """Gaussian-approximated negative log-likelihood of the frame summed over T
+    sub-steps of Brownian motion, differentiable in D (a scalar tensor, m^2/s).
+
+    emitters: (N, 4) float32 CUDA tensor of start x, y (metres from the image
+    centre), z and photons per frame; counts: (W, H) observed frame; sigma:
+    PSF width (scalar tensor, metres); model: a ``GaussianImageModel``;
+    readout_var: scalar or (W, H) tensor, the variance added to the shot
+    noise; normals: (T, N, 2) float32 in place of the Philox draws."""
+    var_map = readout_var if torch.is_tensor(readout_var) else None
+    var = 0.0 if var_map is not None else float(readout_var)
+    if var_map is not None:
+        var_map = var_map.contiguous().float()
+    return _DiffusionLoss.apply(D, emitters, counts, sigma, model, int(T), float(dt), int(seed),
+                                float(background), var, var_map, normals)

@@ -228,7 +228,8 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
                 particles[s_i, sl] = a
                 present[s_i, sl] = 1
         if s_count:
-            pipe.psf.ensure(cfg.depth_keys(particles[:, :, 0].ravel() - focal0))
+            depth = particles[:, :, 0]
+            pipe.psf.ensure_depth_range(float(depth.min()) - focal0, float(depth.max()) - focal0)
         frame_draws = draws.next_frame() if draws is not None and draws.frames else None
         seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | int(rng.randint(0, 2 ** 31 - 1)) \
             if frame_draws is None else 0

@@ -266,6 +266,27 @@ class PSFTables:
                 self.key_slot_host[k if k >= 0 else self.max_key + 1] = first + j
         self.key_slot.copy_(torch.from_numpy(self.key_slot_host))
 
+    def ensure_depth_range(self, dmin, dmax, stream=None):
+        """Build every key a depth in [dmin, dmax] (relative to the focal
+        plane) can map to.  Keys grow with |depth| up to the cutoff, so the
+        keys of the two extreme |depths| bound them all: a contiguous range,
+        checked against the built set without sorting the per-emitter keys."""
+        if not (math.isfinite(dmin) and math.isfinite(dmax)):
+            raise ValueError("non-finite emitter depth")
+        lo = 0.0 if dmin <= 0.0 <= dmax else min(abs(dmin), abs(dmax))
+        hi = max(abs(dmin), abs(dmax))
+        k_lo, k_hi = (int(k) for k in self.cfg.depth_keys([lo, hi]))
+        if k_lo < 0:  # every depth is past the cutoff
+            wanted = [-1]
+        else:
+            top = self.max_key if k_hi < 0 else k_hi
+            wanted = list(range(k_lo, top + 1)) + ([-1] if k_hi < 0 else [])
+        have = self.key_slot_host
+        if all(have[k if k >= 0 else self.max_key + 1] >= 0 for k in (wanted[0], wanted[-1])) and \
+                (have[k_lo: (self.max_key if k_hi < 0 else k_hi) + 1] >= 0).all():
+            return
+        self.ensure(wanted, stream)
+
     def ensure_all(self, stream=None):
         self.ensure(list(range(0, self.max_key + 1)) + [-1], stream)
 

@@ -123,6 +123,8 @@ typedef struct {
     const int64_t *d_frame;  /* optional device counter f: step0 += f * n_sub (graph replay) */
     double lower[3], upper[3];        /* box of the periodic / reflecting boundary          */
     double scale, origin[3], unit_x[3], unit_y[3], unit_z[3];  /* preprocessing transform  */
+    const double *d_class_box;        /* optional [n_class][6] (lower xyz, upper xyz): a box */
+                                      /* per diffusion class in place of lower / upper       */
 } ScDiffuseParams;
 
 int sc_get_version(void);

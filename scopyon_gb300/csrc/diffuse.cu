@@ -22,7 +22,20 @@ struct DiffConsts {
     uint64_t seed;
     double lower[3], upper[3];
     double scale, origin[3], ux[3], uy[3], uz[3];
+    const double *class_box;  // [n_class][6] lower xyz, upper xyz (optional)
 };
+
+// Wall box of a particle's class: the class table's entry, else the common box.
+__device__ __forceinline__ void class_walls(const DiffConsts &c, int cls, int d, double &lo,
+                                            double &hi) {
+    if (c.class_box) {
+        lo = c.class_box[cls * 6 + d];
+        hi = c.class_box[cls * 6 + 3 + d];
+    } else {
+        lo = c.lower[d];
+        hi = c.upper[d];
+    }
+}
 
 __device__ __forceinline__ double wrap_axis(double x, double lo, double hi, int boundary) {
     if (boundary == 1) {  // periodic: (x - lo) mod (hi - lo) + lo, result in [lo, hi)
@@ -104,7 +117,11 @@ __global__ void diffuse_kernel(DiffConsts c, double *pos, const int32_t *klass,
             for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], (double)nrm[d], p[d]);
         }
         if (c.boundary)
-            for (int d = 0; d < c.ndim; ++d) p[d] = wrap_axis(p[d], c.lower[d], c.upper[d], c.boundary);
+            for (int d = 0; d < c.ndim; ++d) {
+                double lo, hi;
+                class_walls(c, k, d, lo, hi);
+                p[d] = wrap_axis(p[d], lo, hi, c.boundary);
+            }
     }
     pos[3 * i] = p[0];
     pos[3 * i + 1] = p[1];
@@ -222,8 +239,11 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                     for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], (double)nr[d], p[d]);
                 }
                 if (c.boundary)
-                    for (int d = 0; d < c.ndim; ++d)
-                        p[d] = wrap_axis(p[d], c.lower[d], c.upper[d], c.boundary);
+                    for (int d = 0; d < c.ndim; ++d) {
+                        double lo, hi;
+                        class_walls(c, cls, d, lo, hi);
+                        p[d] = wrap_axis(p[d], lo, hi, c.boundary);
+                    }
             }
         }
         __syncthreads();
@@ -266,7 +286,7 @@ int diff_consts(const ScDiffuseParams *p, DiffConsts &c) {
     SC_REQUIRE(p->ndim == 2 || p->ndim == 3, "sc_diffuse_steps: ndim=%d must be 2 or 3", p->ndim);
     SC_REQUIRE(p->boundary >= 0 && p->boundary <= 2, "sc_diffuse_steps: boundary=%d", p->boundary);
     SC_REQUIRE(p->n_class >= 1, "sc_diffuse_steps: n_class=%d", p->n_class);
-    if (p->boundary)
+    if (p->boundary && !p->d_class_box)
         for (int d = 0; d < p->ndim; ++d)
             SC_REQUIRE(p->upper[d] > p->lower[d], "sc_diffuse_steps: empty box along axis %d", d);
     c.n = p->n_particles;
@@ -276,6 +296,7 @@ int diff_consts(const ScDiffuseParams *p, DiffConsts &c) {
     c.n_class = p->n_class;
     c.step0 = p->step0;
     c.frame = p->d_frame;
+    c.class_box = p->d_class_box;
     c.seed = p->seed;
     c.scale = p->scale;
     bool ident = p->scale == 1.0;

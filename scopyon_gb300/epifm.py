@@ -373,6 +373,15 @@ class FramePipeline:
         # name -> [(start, end) CUDA events]; set to a dict to time kernels in place
         self.kernel_events = None
 
+    def set_tiles(self, tile, warps):
+        """Use tiles of tile x tile pixels and `warps` warps per splat CTA."""
+        if tile not in (8, 16, 32) or warps not in (1, 2, 4, 8):
+            raise ValueError("tile must be 8, 16 or 32 and warps 1, 2, 4 or 8")
+        nw, nh = self.nw, self.nh
+        self.tile, self.warps = int(tile), int(warps)
+        self.tiles_x = (nw + self.tile - 1) // self.tile
+        self.tiles_y = (nh + self.tile - 1) // self.tile
+
     def _pick_tile(self):
         """(tile edge, warps per tile CTA) that fit shared memory; see tune_tiles."""
         for tile, warps in ((8, 4), (8, 2), (8, 1)):

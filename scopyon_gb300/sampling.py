@@ -77,7 +77,7 @@ class DeviceTrajectories:
     """
 
     def __init__(self, times, points, D, ndim, seed, normals=None, boundary="none",
-                 lower=None, upper=None, klass=None, device=None):
+                 lower=None, upper=None, klass=None, device=None, class_box=None):
         self.times = numpy.asarray(times, dtype=float)
         self.points0 = numpy.asarray(points, dtype=float)   # (N, ndim + 2) host
         self.ndim = int(ndim)
@@ -90,6 +90,9 @@ class DeviceTrajectories:
         self.klass = (numpy.zeros(len(self.points0), dtype=numpy.int32) if klass is None
                       else numpy.asarray(klass, dtype=numpy.int32))
         self.device = torch.device(device or "cuda")
+        # optional walls per class: (n_class, 6) lower xyz, upper xyz
+        self.class_box = None if class_box is None else torch.as_tensor(
+            numpy.asarray(class_box, dtype=float).reshape(-1, 6), device=self.device)
         self._pos = None
         self._index = 0
 
@@ -117,9 +120,10 @@ class DeviceTrajectories:
         return float(self.times[k]), self.copy().materialize(k)
 
     def copy(self):
+        box = None if self.class_box is None else self.class_box.cpu().numpy()
         return DeviceTrajectories(self.times, self.points0, self.D, self.ndim, self.seed,
                                   self.normals, self.boundary, self.lower, self.upper, self.klass,
-                                  self.device)
+                                  self.device, class_box=box)
 
     def materialize(self, k):
         """Host (N, ndim + 2) points at time index k (advances this object)."""
@@ -159,6 +163,7 @@ class DeviceTrajectories:
             p.origin[d] = float(origin[d])
             p.unit_x[d], p.unit_y[d], p.unit_z[d] = float(unit_x[d]), float(unit_y[d]), float(unit_z[d])
         p.scale = float(scale)
+        p.d_class_box = None if self.class_box is None else self.class_box.data_ptr()
         return p
 
     def run(self, g0, n, out, transform=None, stream=None):

@@ -258,6 +258,7 @@ def gb300_arm(args, rank, world):
 
     e2e = None if args.small else e2e_arm(args, cfg, dev, rank, world)
     fwd_bwd = None if args.small else fwd_bwd_arm(args, dev)
+    batched = None if args.small else batched_arm(args, dev)
 
     splat_avg_ms = sum(splat_ms) / len(splat_ms)
     n_rec = sum(splat_recs) / len(splat_recs)
@@ -287,6 +288,7 @@ def gb300_arm(args, rank, world):
                    "psf_build_s": round(psf_build_s, 3)},
         "e2e": e2e,
         "fwd_bwd": fwd_bwd,
+        "batched": batched,
         "gpu_launches": fg.launches_per_frame * args.steps,
         "clocks": clk,
         "roofline": {"kernel": "splat_box_bulk_kernel + splat_sat_kernel + splat_merge_kernel",
@@ -463,6 +465,107 @@ def fwd_bwd_arm(args, dev):
                         "graph replay per step",
             "dtype": "f32 (FP64 loss reduction)", "headline": headline,
             "batch_64x128px_200": batch, "diffusion_dD_100k_2048px_T100": dgrad}
+
+
+# ------------------------------------------------------------- batched form
+def config1(exposure=0.030):
+    """Single-channel TIRF, EGFP, 160 nm pixels, EMCCD (QE 0.92, gain 300,
+    readout 100 e-, offset 2000, 16-bit), 100 photons per emitter per ms."""
+    import scopyon_gb300 as sg
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {
+        "magnification": 100,
+        "fluorophore": {"type": "EGFP"},
+        "detector": {"type": "EMCCD", "exposure_time": exposure, "QE": 0.92, "emgain": 300,
+                     "readout_noise": 100},
+        "analog_to_digital_converter": {"bit": 16, "offset": 2000, "fullwell": 800000},
+        "light_source": {"flux_density": 1.1745e7},
+        "effects": {"photo_bleaching": {"switch": False}}}})
+    return cfg
+
+
+def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123):
+    """field-frames/s of 256 fields (edges 128/256/512 px, emitters log-uniform
+    in [10, 50000], D log-uniform in [0.001, 1] um^2/s) batched in one canvas,
+    next to the plain method's per-field frame loop."""
+    import torch
+    from scopyon_gb300.base import _psf_for
+    from scopyon_gb300.batch import BatchedFields
+    from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
+    from scopyon_gb300.sampling import DeviceTrajectories
+    rng = numpy.random.RandomState(seed)
+    sizes = rng.choice([128, 256, 512], n_fields)
+    counts = numpy.exp(rng.uniform(math.log(10), math.log(50000), n_fields)).astype(int)
+    D = numpy.exp(rng.uniform(math.log(1e-3), math.log(1.0), n_fields)) * 1e-12
+    cfg = config1()
+    t0 = time.time()
+    bf = BatchedFields(cfg, sizes, counts, D, frames, substeps, seed=seed, device=dev)
+    tune = bf.autotune(frames=1)
+    bf.step()  # capture
+    for _ in range(args.warmup):
+        bf.step()
+    steps = min(args.steps, frames - len(tune) - 2 - args.warmup)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(steps):
+        bf.step()
+    b.record()
+    torch.cuda.synchronize()
+    bf.pipe.check_status()
+    batch_ms = a.elapsed_time(b) / steps
+    setup_s = time.time() - t0
+    del bf
+    torch.cuda.empty_cache()
+
+    # the plain method, one field at a time: a pipeline, trajectories and frame per field
+    fields = []
+    for k in range(n_fields):
+        fc = config1()
+        fc.update({"default": {"detector": {"image_size": [int(sizes[k])] * 2}}})
+        eng = EngineConfig(fc["default"], rng=numpy.random.RandomState(k))
+        pipe = FramePipeline(eng, dev, psf=_psf_for(eng, dev))
+        pipe.psf.ensure([0])
+        half = sizes[k] * eng.px / 2
+        pts = numpy.zeros((counts[k], 4))
+        pts[:, :2] = rng.uniform(-half, half, (counts[k], 2))
+        pts[:, 2] = numpy.arange(counts[k])
+        pts[:, 3] = 1.0
+        times = numpy.arange(8 * substeps + 1) * (eng.exposure_time / substeps)
+        traj = DeviceTrajectories(times, pts, [[D[k], D[k]]], 2, k, boundary="reflecting",
+                                  lower=[-half, -half, 0], upper=[half, half, 0], device=dev)
+        pipe.ensure_slots(counts[k])
+        fields.append(FrameGraph(pipe, traj, substeps, eng.exposure_time / substeps, seed=k,
+                                 use_graph=False))
+
+    def loop_ms(n):
+        for fg in fields:
+            fg.step()
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(n):
+            for fg in fields:
+                fg.step()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / n
+
+    plain_eager_ms = loop_ms(2)
+    for fg in fields:
+        fg.use_graph = True
+    plain_graph_ms = loop_ms(2)
+    return {"value": n_fields / (batch_ms / 1e3), "unit": "field-frames/s",
+            "workload": "%d fields of view, edges 128/256/512 px, %d emitters in all "
+                        "(log-uniform 10..50000 per field), D log-uniform 0.001..1 um^2/s, "
+                        "%d sub-steps per 30 ms frame, TIRF EGFP, EMCCD camera"
+                        % (n_fields, int(counts.sum()), substeps),
+            "batched_ms_per_frame_of_all_fields": batch_ms,
+            "plain_per_field_loop_ms": plain_eager_ms,
+            "plain_per_field_graphs_ms": plain_graph_ms,
+            "batched_over_plain_loop": plain_eager_ms / batch_ms,
+            "batched_over_plain_graphs": plain_graph_ms / batch_ms,
+            "autotune_splat_ms": {"%dx%d/%dw" % (t, t, w): ms for (t, w), ms in tune.items()},
+            "setup_s": setup_s}
 
 
 # ---------------------------------------------------------------- CPU baseline

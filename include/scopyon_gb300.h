@@ -213,9 +213,11 @@ int sc_native_records(const ScDiffuseParams *p, const ScStepParams *sp, double *
                       size_t bin_ws_bytes, int32_t *d_status, void *stream);
 
 /* Bytes of scratch sc_bin_steps uses for n_rec records on n_tiles_total
- * tiles: the counts and cursors of every bin (16 bytes per tile), then the
- * bin of every record (4 bytes each).  A workspace of only the first part is
- * also accepted; the scatter then recomputes each record's bin.            */
+ * tiles: the counts and cursors of every bin (16 bytes per tile), the bin and
+ * rank of every record (8 bytes each), and a list of the bins too long to
+ * sort in one warp (8 bytes per tile + 4).  A workspace of only the first
+ * part is also accepted; the scatter then recomputes each record's bin and
+ * long bins are sorted by one warp each.                                    */
 size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total);
 
 /* Clears the bin counts of a binning workspace (a memset on the stream). */

@@ -114,7 +114,7 @@ class BatchedFields:
         self.tuning = None
 
     # ------------------------------------------------------------------
-    def autotune(self, candidates=((8, 4), (8, 2), (16, 4), (16, 8)), frames=2):
+    def autotune(self, candidates=((8, 4), (8, 2), (16, 2), (16, 4), (16, 8)), frames=2):
         """Time the splat of the batch for each (tile, warps) choice on a few
         eager frames; keep the fastest.  Returns {(tile, warps): ms}."""
         pipe, fg = self.pipe, self.graph

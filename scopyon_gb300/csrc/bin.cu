@@ -220,9 +220,11 @@ __device__ void warp_flip_sort(int32_t *a, int n, int lane) {
 constexpr int kSortWarps = 8;
 
 // One warp per bin: the bin's record indices sorted ascending, in registers
-// up to 512 of them (4 or 16 per lane), in global memory beyond.
+// up to 512 of them (4 or 16 per lane).  Longer lists go to `big` (a count
+// and the bin indices) for bin_sort_big_kernel, or, without that list, are
+// sorted here in global memory.
 __global__ void __launch_bounds__(kSortWarps * 32)
-bin_sort_kernel(const int32_t *tile_start, int n_bins, int32_t *items) {
+bin_sort_kernel(const int32_t *tile_start, int n_bins, int32_t *items, int32_t *big) {
     const int lane = threadIdx.x & 31;
     const int t = blockIdx.x * kSortWarps + (threadIdx.x >> 5);
     if (t >= n_bins) return;
@@ -233,21 +235,83 @@ bin_sort_kernel(const int32_t *tile_start, int n_bins, int32_t *items) {
         warp_sort_list<4>(list, n, lane);
     else if (n <= 512)
         warp_sort_list<16>(list, n, lane);
-    else
+    else if (big) {
+        if (lane == 0) big[1 + atomicAdd(big, 1)] = t;
+    } else {
         warp_flip_sort(list, n, lane);
+    }
+}
+
+constexpr int kBigThreads = 512;
+constexpr int kBigSmem = 12288;  // list entries sorted in shared memory (48 KB)
+
+// Flip-form bitonic network run by a whole CTA on `a` (shared or global).
+__device__ void cta_flip_sort(int32_t *a, int n) {
+    int n2 = 1;
+    while (n2 < n) n2 <<= 1;
+    for (int k = 2; k <= n2; k <<= 1) {
+        for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+            const int l = i ^ (k - 1);
+            if (l > i) cmp_swap(a, i, l, n);
+        }
+        __syncthreads();
+        for (int j = k >> 2; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) cmp_swap(a, i, l, n);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// The long lists: CTAs take bins from the list in turn and sort each with the
+// whole CTA, in shared memory up to kBigSmem entries.
+__global__ void __launch_bounds__(kBigThreads)
+bin_sort_big_kernel(const int32_t *tile_start, const int32_t *big, int32_t *items) {
+    __shared__ int32_t buf[kBigSmem];
+    const int count = big[0];
+    for (int q = blockIdx.x; q < count; q += gridDim.x) {
+        const int t = big[1 + q];
+        const int b0 = tile_start[t], n = tile_start[t + 1] - b0;
+        int32_t *list = items + b0;
+        if (n <= kBigSmem) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) buf[i] = list[i];
+            __syncthreads();
+            cta_flip_sort(buf, n);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) list[i] = buf[i];
+        } else {
+            cta_flip_sort(list, n);
+        }
+        __syncthreads();
+    }
+}
+
+// Per-bin sort of the placed lists; `big` (count + list, cleared here) takes
+// the long ones to a CTA each when the workspace holds it.
+int bin_sort(int n_bins, int32_t *tile_start, int32_t *items, int32_t *big, cudaStream_t s) {
+    if (big) {
+        int rc = sc::cuda_status(cudaMemsetAsync(big, 0, sizeof(int32_t), s), "bin sort");
+        if (rc) return rc;
+    }
+    bin_sort_kernel<<<(n_bins + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(
+        tile_start, n_bins, items, big);
+    if (big) bin_sort_big_kernel<<<152 * 2, kBigThreads, 0, s>>>(tile_start, big, items);
+    return sc::launch_status("bin sort");
 }
 
 // Scan, placement and sort of counted records.
 int bin_finish(int n_rec, const sc::TileGeom &g, int32_t *tile_count, const int32_t *rec_bin,
-               const int32_t *rec_rank, int32_t *tile_start, int32_t *items, cudaStream_t s) {
+               const int32_t *rec_rank, int32_t *big, int32_t *tile_start, int32_t *items,
+               cudaStream_t s) {
     const int n_bins = 2 * g.n_tiles;
     bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(tile_count, n_bins, tile_start, nullptr);
     int grid = (n_rec + 255) / 256;
     if (grid > 152 * 8) grid = 152 * 8;
     bin_place_kernel<<<grid, 256, 0, s>>>(rec_bin, rec_rank, n_rec, tile_start, items);
-    bin_sort_kernel<<<(n_bins + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(
-        tile_start, n_bins, items);
-    return sc::launch_status("sc_bin_finish");
+    int rc = sc::launch_status("sc_bin_finish");
+    if (rc) return rc;
+    return bin_sort(n_bins, tile_start, items, big, s);
 }
 
 }  // namespace
@@ -289,6 +353,7 @@ int bin_layout(const TileGeom &g, int n_rec, void *d_ws, size_t ws_bytes, BinLay
     const bool full = ws_bytes >= sc_bin_workspace_bytes(n_rec, g.n_tiles);
     b.rec_bin = full ? b.cursor + n_bins : nullptr;
     b.rec_rank = full ? b.rec_bin + n_rec : nullptr;
+    b.big = full ? b.rec_rank + n_rec : nullptr;
     return SC_OK;
 }
 
@@ -304,7 +369,9 @@ static size_t bin_counts_bytes(int n_tiles_total) {
 
 extern "C" size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total) {
     if (n_rec <= 0 || n_tiles_total <= 0) return 0;
-    return bin_counts_bytes(n_tiles_total) + (size_t)2 * n_rec * sizeof(int32_t);
+    // + the bin and rank of every record, + the list of long bins (count + bins)
+    return bin_counts_bytes(n_tiles_total) + (size_t)2 * n_rec * sizeof(int32_t) +
+           (size_t)(2 * n_tiles_total + 1) * sizeof(int32_t);
 }
 
 extern "C" int sc_bin_reset(const ScSplatParams *p, void *d_ws, size_t ws_bytes, void *stream) {
@@ -336,7 +403,7 @@ extern "C" int sc_bin_finish(int n_rec, const ScSplatParams *p, void *d_ws, size
                sc_bin_workspace_bytes(n_rec, g.n_tiles));
     sc::BinLayout b;
     sc::bin_layout(g, n_rec, d_ws, ws_bytes, b);
-    return bin_finish(n_rec, g, b.count, b.rec_bin, b.rec_rank, d_tile_start, d_items, s);
+    return bin_finish(n_rec, g, b.count, b.rec_bin, b.rec_rank, b.big, d_tile_start, d_items, s);
 }
 
 extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatParams *p,
@@ -368,13 +435,13 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
     int grid = (n_rec + 255) / 256;
     if (grid > 152 * 8) grid = 152 * 8;
     bin_count_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.count, b.rec_bin, b.rec_rank);
-    if (b.rec_bin) return bin_finish(n_rec, g, b.count, b.rec_bin, b.rec_rank, d_tile_start,
-                                     d_items, s);
+    if (b.rec_bin) return bin_finish(n_rec, g, b.count, b.rec_bin, b.rec_rank, b.big,
+                                     d_tile_start, d_items, s);
     bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(b.count, n_bins, d_tile_start, b.cursor);
     bin_scatter_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.cursor, d_items);
-    bin_sort_kernel<<<(n_bins + kSortWarps - 1) / kSortWarps, kSortWarps * 32, 0, s>>>(
-        d_tile_start, n_bins, d_items);
-    return sc::launch_status("sc_bin_steps");
+    rc = sc::launch_status("sc_bin_steps");
+    if (rc) return rc;
+    return bin_sort(n_bins, d_tile_start, d_items, nullptr, s);
 }
 
 // ---------------------------------------------------------------------------

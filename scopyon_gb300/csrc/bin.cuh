@@ -16,6 +16,7 @@ int tile_geom(const ScSplatParams *p, TileGeom &g);
 // the workspace is large enough) each record's bin and rank in its bin.
 struct BinLayout {
     int32_t *count, *cursor, *rec_bin, *rec_rank;
+    int32_t *big;  // count of long bins, then their indices
 };
 int bin_layout(const TileGeom &g, int n_rec, void *d_ws, size_t ws_bytes, BinLayout &b);
 

@@ -106,10 +106,11 @@ __global__ void camera_kernel(CamConsts c, const float *__restrict__ photons,
     const int stride = gridDim.x * blockDim.x;
     const uint64_t counter = c.counter + (c.frame ? (uint64_t)*c.frame : 0);
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.n; p += stride) {
-        const double ph = (double)photons[p] + c.background;
-        const double e = __dmul_rn(c.qe, ph);
-        if (expect) expect[p] = (float)e;
         if (c.exact) {
+            // E = QE (photons + background) with the reference's FP64 rounding
+            const double ph = (double)photons[p] + c.background;
+            const double e = __dmul_rn(c.qe, ph);
+            if (expect) expect[p] = (float)e;
             double noise, signal;
             if (c.camera == SC_CAM_CMOS_TABLE && inj_uniform)
                 noise = table_value[table_index(table_cdf, c.table_n, inj_uniform[p])];
@@ -127,8 +128,10 @@ __global__ void camera_kernel(CamConsts c, const float *__restrict__ photons,
             if (adc32) adc32[p] = (float)v;
             continue;
         }
+        // native draws: FP32 throughout (GB300's FP64 rate is ~1/64 of FP32)
+        const float ef = c.qe_f * (photons[p] + c.background_f);
+        if (expect) expect[p] = ef;
         sc::rng_stream rs(c.seed, (uint32_t)p, (uint32_t)counter, (uint32_t)(counter >> 32));
-        const float ef = (float)e;
         float signal, noise;
         switch (c.camera) {
             case SC_CAM_EMCCD: {

@@ -56,8 +56,8 @@ __device__ __forceinline__ double wrap_axis(double x, double lo, double hi, int 
 __device__ __forceinline__ void format_point(const DiffConsts &c, const double *p, double *q) {
     if (c.ndim == 2) {
         q[0] = 0.0;
-        q[1] = __dmul_rn(p[0], c.scale);
-        q[2] = __dmul_rn(p[1], c.scale);
+        q[1] = c.scale == 1.0 ? p[0] : __dmul_rn(p[0], c.scale);
+        q[2] = c.scale == 1.0 ? p[1] : __dmul_rn(p[1], c.scale);
     } else if (c.identity) {
         q[0] = p[2];
         q[1] = p[0];
@@ -350,7 +350,7 @@ extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *s
                "sc_native_records: NULL pointer");
     SC_REQUIRE(!k.bleaching || d_budget, "sc_native_records: bleaching needs a budget array");
     sc::TileGeom g{};
-    sc::BinLayout bl{nullptr, nullptr, nullptr, nullptr};
+    sc::BinLayout bl{nullptr, nullptr, nullptr, nullptr, nullptr};
     if (bin_p) {
         rc = sc::tile_geom(bin_p, g);
         if (rc) return rc;

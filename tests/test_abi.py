@@ -59,7 +59,8 @@ def test_host_side_validation_needs_no_gpu():
                       None) == _lib.SC_ERR_ARG
     assert b"tile=12" in L.sc_last_error()
     assert L.sc_bin_workspace_bytes(0, 16) == 0
-    assert L.sc_bin_workspace_bytes(100, 16) == 16 * 16 + 8 * 100  # counts, cursors; bins, ranks
+    # counts, cursors; bins, ranks; long-bin list
+    assert L.sc_bin_workspace_bytes(100, 16) == 16 * 16 + 8 * 100 + 4 * (2 * 16 + 1)
     p.tile, p.tiles_x, p.tiles_y = 16, 4, 4
     assert L.sc_splat_workspace_bytes(ctypes.byref(p)) == 16 * 30 * 30 * 4
 

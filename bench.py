@@ -170,7 +170,8 @@ def gb300_arm(args, rank, world):
     import torch
     import scopyon_gb300 as sg
     from scopyon_gb300.base import _psf_for
-    from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
+    from scopyon_gb300.epifm import (TILE_CANDIDATES, EngineConfig, FrameGraph, FramePipeline,
+                                     tune_tiles)
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
@@ -189,7 +190,7 @@ def gb300_arm(args, rank, world):
 
     # trajectories on the device: two populations (D = 0.01 and 1 um^2/s), Philox normals
     n_timing = 4
-    n_frames = args.warmup + args.steps + n_timing + 8000
+    n_frames = args.warmup + args.steps + n_timing + 8000 + 5 * len(TILE_CANDIDATES)
     dt = EXPOSURE / SUBSTEPS
     t = numpy.arange(n_frames * SUBSTEPS + 1) * dt
     # reflecting walls at the field's edges and at z = +-Z_HALF keep the
@@ -204,6 +205,7 @@ def gb300_arm(args, rank, world):
     beta = eng.half_life / math.log(2.0)
     pipe.budget[:N_EMIT].copy_(torch.from_numpy(rng.exponential(beta, N_EMIT) * eng.n_emit0))
     fg = FrameGraph(pipe, traj, SUBSTEPS, dt, seed=1234 + rank)
+    tune = tune_tiles(fg, frames=3)  # tile / warps autotuner: 5 frames per choice
     fg.capture()
     for _ in range(args.warmup - 1):
         fg.step()
@@ -278,6 +280,8 @@ def gb300_arm(args, rank, world):
                    "camera": "sCMOS per-pixel sigma, 12-bit",
                    "psf": "Born-Wolf TRITC, %d depth keys" % len(pipe.psf.slot_of),
                    "tile": pipe.tile, "warps_per_tile": pipe.warps,
+                   "tile_autotune_ms_per_frame": {"%dx%d/%dw" % (t, t, w): round(ms, 4)
+                                                  for (t, w), ms in tune.items()},
                    "step": "one frame: Brownian sub-steps, physics, binning, splat, camera "
                            "(one CUDA graph replay)",
                    "parallelism": "replicas" if world > 1 else "single",
@@ -504,7 +508,7 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123):
     bf.step()  # capture
     for _ in range(args.warmup):
         bf.step()
-    steps = min(args.steps, frames - len(tune) - 2 - args.warmup)
+    steps = min(args.steps, frames - 4 * len(tune) - 2 - args.warmup)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     a.record()
@@ -564,7 +568,7 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123):
             "plain_per_field_graphs_ms": plain_graph_ms,
             "batched_over_plain_loop": plain_eager_ms / batch_ms,
             "batched_over_plain_graphs": plain_graph_ms / batch_ms,
-            "autotune_splat_ms": {"%dx%d/%dw" % (t, t, w): ms for (t, w), ms in tune.items()},
+            "autotune_ms_per_frame": {"%dx%d/%dw" % (t, t, w): ms for (t, w), ms in tune.items()},
             "setup_s": setup_s}
 
 

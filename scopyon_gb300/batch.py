@@ -27,7 +27,7 @@ import torch
 
 from . import _lib
 from .base import _psf_for
-from .epifm import EngineConfig, FrameGraph, FramePipeline
+from .epifm import TILE_CANDIDATES, EngineConfig, FrameGraph, FramePipeline, tune_tiles
 from .sampling import DeviceTrajectories
 
 GAP = 16
@@ -114,28 +114,11 @@ class BatchedFields:
         self.tuning = None
 
     # ------------------------------------------------------------------
-    def autotune(self, candidates=((8, 4), (8, 2), (16, 2), (16, 4), (16, 8)), frames=2):
-        """Time the splat of the batch for each (tile, warps) choice on a few
-        eager frames; keep the fastest.  Returns {(tile, warps): ms}."""
-        pipe, fg = self.pipe, self.graph
-        fg.graph, fg.use_graph = None, False
-        times = {}
-        for tile, warps in candidates:
-            try:
-                pipe.set_tiles(tile, warps)
-                pipe.kernel_events = {}
-                for _ in range(frames):
-                    fg.step()
-                torch.cuda.synchronize()
-                ev = pipe.kernel_events["splat"]
-                times[(tile, warps)] = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
-            except (ValueError, _lib.ScopyonGPUError):
-                continue
-            finally:
-                pipe.kernel_events = None
-        best = min(times, key=times.get)
-        pipe.set_tiles(*best)
-        fg.use_graph = True
+    def autotune(self, candidates=TILE_CANDIDATES, frames=2):
+        """Time whole batch frames (graph replays) for each (tile, warps)
+        choice; keep the fastest.  Returns {(tile, warps): ms per frame}."""
+        times = tune_tiles(self.graph, candidates, frames)
+        best = (self.pipe.tile, self.pipe.warps)
         self.tuning = {"%dx%d tiles, %d warps" % (t, t, w): ms for (t, w), ms in times.items()}
         self.tuning["chosen"] = "%dx%d tiles, %d warps" % (best[0], best[0], best[1])
         return times

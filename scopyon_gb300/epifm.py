@@ -622,6 +622,41 @@ class FramePipeline:
         return self.expect, self.adc, (optinfo[: n * 8].view(n, 8) if with_optinfo else None)
 
 
+TILE_CANDIDATES = ((8, 4), (8, 2), (16, 2), (16, 4), (16, 8))
+
+
+def tune_tiles(graph, candidates=TILE_CANDIDATES, frames=3):
+    """Autotuner of the tile shape: for each (tile edge, warps per splat CTA)
+    choice, capture the frame graph of ``graph`` (a FrameGraph) and time
+    ``frames`` replays of the whole frame (binning, splat and merge all depend
+    on the tile); keep the fastest on its pipeline and return
+    {(tile, warps): ms per frame}.  The frames run are frames of the
+    simulation (the trajectories advance)."""
+    pipe = graph.pipe
+    times = {}
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for tile, warps in candidates:
+        try:
+            pipe.set_tiles(tile, warps)
+            graph.graph, graph.use_graph = None, True
+            graph.step()  # one eager frame, then capture
+            graph.step()
+            torch.cuda.synchronize()
+            a.record()
+            for _ in range(frames):
+                graph.step()
+            b.record()
+            torch.cuda.synchronize()
+            times[(tile, warps)] = a.elapsed_time(b) / frames
+        except (ValueError, _lib.ScopyonGPUError):
+            continue
+    graph.graph = None
+    if not times:
+        raise RuntimeError("no tile configuration ran")
+    pipe.set_tiles(*min(times, key=times.get))
+    return times
+
+
 class FrameGraph:
     """Frames of device trajectories replayed from one captured CUDA graph.
 

@@ -114,7 +114,7 @@ def test_autotune_and_graph_replay(sg):
     sizes = list(rng.choice([32, 64, 128], 12))
     counts = list(numpy.exp(rng.uniform(math.log(10), math.log(2000), 12)).astype(int))
     D = list(numpy.exp(rng.uniform(math.log(1e-15), math.log(1e-12), 12)))
-    bf = BatchedFields(config1(sg), sizes, counts, D, frames=8, substeps=4, seed=5)
+    bf = BatchedFields(config1(sg), sizes, counts, D, frames=24, substeps=4, seed=5)
     times = bf.autotune(frames=1)
     assert times and bf.tuning["chosen"]
     for _ in range(3):

@@ -152,9 +152,10 @@ def splat_algorithmic_bytes(n_rec, tile, halo):
 
 
 # DRAM bytes (read + write) of the three splat kernels per splatted record:
-# 398.5 MB over 395,829 box records in one frame of `bench.py --small`
-# (ncu --set full, dram__bytes_read.sum + dram__bytes_write.sum).
-SPLAT_TRAFFIC_PER_RECORD = 398.5e6 / 395829
+# 387.0 MB over 383,289 box records in one frame of
+# `bench.py --small --tile 8 --warps 4` (ncu --set full,
+# dram__bytes_read.sum + dram__bytes_write.sum).
+SPLAT_TRAFFIC_PER_RECORD = 387.0e6 / 383289
 
 
 def load_peaks():
@@ -205,7 +206,11 @@ def gb300_arm(args, rank, world):
     beta = eng.half_life / math.log(2.0)
     pipe.budget[:N_EMIT].copy_(torch.from_numpy(rng.exponential(beta, N_EMIT) * eng.n_emit0))
     fg = FrameGraph(pipe, traj, SUBSTEPS, dt, seed=1234 + rank)
-    tune = tune_tiles(fg, frames=3)  # tile / warps autotuner: 5 frames per choice
+    if args.tile:  # a fixed tile shape (reproducible profiling), else the autotuner
+        pipe.set_tiles(args.tile, args.warps)
+        tune = {}
+    else:
+        tune = tune_tiles(fg, frames=3)  # 5 frames per choice
     fg.capture()
     for _ in range(args.warmup - 1):
         fg.step()
@@ -674,6 +679,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tile", type=int, default=0,
+                    help="splat tile edge (8 or 16); default: autotuned")
+    ap.add_argument("--warps", type=int, default=4, help="warps per splat tile with --tile")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: depth range +-0.1 um between reflecting walls and "
                          "D = 0.01 um^2/s for all emitters (102 PSF keys, 2.9 GB of tables), "

@@ -207,7 +207,7 @@ def gb300_arm(args, rank, world):
     pipe.budget[:N_EMIT].copy_(torch.from_numpy(rng.exponential(beta, N_EMIT) * eng.n_emit0))
     fg = FrameGraph(pipe, traj, SUBSTEPS, dt, seed=1234 + rank)
     if args.tile:  # a fixed tile shape (reproducible profiling), else the autotuner
-        pipe.set_tiles(args.tile, args.warps)
+        pipe.set_tiles(args.tile, args.warps, args.stages)
         tune = {}
     else:
         tune = tune_tiles(fg, frames=3)  # 5 frames per choice
@@ -285,8 +285,9 @@ def gb300_arm(args, rank, world):
                    "camera": "sCMOS per-pixel sigma, 12-bit",
                    "psf": "Born-Wolf TRITC, %d depth keys" % len(pipe.psf.slot_of),
                    "tile": pipe.tile, "warps_per_tile": pipe.warps,
-                   "tile_autotune_ms_per_frame": {"%dx%d/%dw" % (t, t, w): round(ms, 4)
-                                                  for (t, w), ms in tune.items()},
+                   "stages": pipe.stages,
+                   "tile_autotune_ms_per_frame": {"%dx%d/%dw/%ds" % (t, t, w, st): round(ms, 4)
+                                                  for (t, w, st), ms in tune.items()},
                    "step": "one frame: Brownian sub-steps, physics, binning, splat, camera "
                            "(one CUDA graph replay)",
                    "parallelism": "replicas" if world > 1 else "single",
@@ -573,7 +574,8 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123):
             "plain_per_field_graphs_ms": plain_graph_ms,
             "batched_over_plain_loop": plain_eager_ms / batch_ms,
             "batched_over_plain_graphs": plain_graph_ms / batch_ms,
-            "autotune_ms_per_frame": {"%dx%d/%dw" % (t, t, w): ms for (t, w), ms in tune.items()},
+            "autotune_ms_per_frame": {"%dx%d/%dw/%ds" % (t, t, w, st): ms
+                                      for (t, w, st), ms in tune.items()},
             "setup_s": setup_s}
 
 
@@ -682,6 +684,8 @@ def main():
     ap.add_argument("--tile", type=int, default=0,
                     help="splat tile edge (8 or 16); default: autotuned")
     ap.add_argument("--warps", type=int, default=4, help="warps per splat tile with --tile")
+    ap.add_argument("--stages", type=int, default=4,
+                    help="box-table block copies in flight per splat warp with --tile")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: depth range +-0.1 um between reflecting walls and "
                          "D = 0.01 um^2/s for all emitters (102 PSF keys, 2.9 GB of tables), "

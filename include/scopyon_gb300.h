@@ -95,6 +95,7 @@ typedef struct {
                              /* 0 means every record belongs to image 0                     */
     int32_t box_p, box_nq;   /* box tables: P rows per pixel and NQ pixel offsets, or 0     */
     int32_t n_slots;         /* depth-key tables held in d_sat / d_box                      */
+    int32_t box_stages;      /* block copies in flight per splat warp (1..8; 0: 4)          */
     double px, res;
 } ScSplatParams;
 

@@ -40,7 +40,7 @@ class SplatParams(ctypes.Structure):
                 ("n_r", ctypes.c_int32), ("sat_pitch", ctypes.c_int32),
                 ("n_images", ctypes.c_int32), ("rec_per_image", ctypes.c_int32),
                 ("box_p", ctypes.c_int32), ("box_nq", ctypes.c_int32),
-                ("n_slots", ctypes.c_int32),
+                ("n_slots", ctypes.c_int32), ("box_stages", ctypes.c_int32),
                 ("px", ctypes.c_double), ("res", ctypes.c_double)]
 
 

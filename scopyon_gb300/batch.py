@@ -118,9 +118,10 @@ class BatchedFields:
         """Time whole batch frames (graph replays) for each (tile, warps)
         choice; keep the fastest.  Returns {(tile, warps): ms per frame}."""
         times = tune_tiles(self.graph, candidates, frames)
-        best = (self.pipe.tile, self.pipe.warps)
-        self.tuning = {"%dx%d tiles, %d warps" % (t, t, w): ms for (t, w), ms in times.items()}
-        self.tuning["chosen"] = "%dx%d tiles, %d warps" % (best[0], best[0], best[1])
+        name = "%dx%d tiles, %d warps, %d stages"
+        self.tuning = {name % (t, t, w, st): ms for (t, w, st), ms in times.items()}
+        self.tuning["chosen"] = name % (self.pipe.tile, self.pipe.tile, self.pipe.warps,
+                                        self.pipe.stages)
         return times
 
     def step(self):

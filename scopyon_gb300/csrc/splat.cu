@@ -427,8 +427,8 @@ splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restr
 // does not fit it (the direct kernel then runs).
 template <int NW, int NQ>
 int launch_bulk(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
-                const SplatConsts &c, int n_tiles, int n_slots, float *ws, int32_t *status,
-                cudaStream_t s, bool &done) {
+                const SplatConsts &c, int n_tiles, int n_slots, int want_stages, float *ws,
+                int32_t *status, cudaStream_t s, bool &done) {
     done = false;
     constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;
     constexpr int NB = SC_BOX_BLOCK_FLOATS(NQ);
@@ -443,7 +443,7 @@ int launch_bulk(const ScStepRec *recs, const int32_t *tile_start, const int32_t 
     auto bulk_smem = [&](int st) {
         return fixed + (size_t)NW * st * SB * sizeof(float) + (size_t)NW * st * sizeof(uint64_t);
     };
-    int stages = 8;
+    int stages = want_stages > 0 ? want_stages : 4;
     while (stages > 1 && bulk_smem(stages) > 160 * 1024) --stages;
     const size_t smem = bulk_smem(stages);
     if (smem > 160 * 1024) return SC_OK;
@@ -534,8 +534,8 @@ __global__ void splat_merge_kernel(const float *__restrict__ ws, SplatConsts c, 
 
 template <int NW>
 int launch_splat(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
-                 const float2 *sat, const SplatConsts &c, int n_tiles, int n_slots, bool box,
-                 float *ws, int32_t *status, cudaStream_t s) {
+                 const float2 *sat, const SplatConsts &c, int n_tiles, int n_slots, int stages,
+                 bool box, float *ws, int32_t *status, cudaStream_t s) {
     const int ee = c.edge * c.edge;
     const int bs = (ee + 31) & ~31;
     if (box) {
@@ -543,11 +543,11 @@ int launch_splat(const ScStepRec *recs, const int32_t *tile_start, const int32_t
         bool done = false;
         int rc = SC_OK;
         switch (c.box_nq) {
-            case 12: rc = launch_bulk<NW, 12>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
-            case 13: rc = launch_bulk<NW, 13>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
-            case 14: rc = launch_bulk<NW, 14>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
-            case 15: rc = launch_bulk<NW, 15>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
-            case 16: rc = launch_bulk<NW, 16>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            case 12: rc = launch_bulk<NW, 12>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
+            case 13: rc = launch_bulk<NW, 13>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
+            case 14: rc = launch_bulk<NW, 14>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
+            case 15: rc = launch_bulk<NW, 15>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
+            case 16: rc = launch_bulk<NW, 16>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
             default: break;
         }
         if (rc) return rc;
@@ -625,6 +625,8 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
     rc = splat_consts(p, g, c);
     if (rc) return rc;
     SC_REQUIRE(d_tile_start && d_image && d_ws, "sc_splat: NULL pointer");
+    SC_REQUIRE(p->box_stages >= 0 && p->box_stages <= 8, "sc_splat: box_stages=%d not in 0..8",
+               p->box_stages);
     SC_REQUIRE(ws_bytes >= sc_splat_workspace_bytes(p), "sc_splat: workspace %zu < %zu bytes",
                ws_bytes, sc_splat_workspace_bytes(p));
     if (d_box) {
@@ -639,10 +641,10 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
     float *ws = static_cast<float *>(d_ws);
     const bool box = d_box != nullptr;
     switch (g.warps) {
-        case 1: rc = launch_splat<1>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, box, ws, d_status, s); break;
-        case 2: rc = launch_splat<2>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, box, ws, d_status, s); break;
-        case 4: rc = launch_splat<4>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, box, ws, d_status, s); break;
-        default: rc = launch_splat<8>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, box, ws, d_status, s); break;
+        case 1: rc = launch_splat<1>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, box, ws, d_status, s); break;
+        case 2: rc = launch_splat<2>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, box, ws, d_status, s); break;
+        case 4: rc = launch_splat<4>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, box, ws, d_status, s); break;
+        default: rc = launch_splat<8>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, box, ws, d_status, s); break;
     }
     if (rc) return rc;
     const int64_t total = (int64_t)g.nw * g.nh * g.n_images;

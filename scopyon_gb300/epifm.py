@@ -363,6 +363,7 @@ class FramePipeline:
         # pixels a footprint reaches past its first one
         self.halo = int(math.ceil(PSF_RES * (n_signal - 1) / cfg.px)) + 1
         self.tile, self.warps = self._pick_tile()
+        self.stages = 4
         if cfg.tile:
             self.tile = cfg.tile
         self.tiles_x = (nw + self.tile - 1) // self.tile
@@ -373,12 +374,13 @@ class FramePipeline:
         # name -> [(start, end) CUDA events]; set to a dict to time kernels in place
         self.kernel_events = None
 
-    def set_tiles(self, tile, warps):
-        """Use tiles of tile x tile pixels and `warps` warps per splat CTA."""
-        if tile not in (8, 16, 32) or warps not in (1, 2, 4, 8):
-            raise ValueError("tile must be 8, 16 or 32 and warps 1, 2, 4 or 8")
+    def set_tiles(self, tile, warps, stages=4):
+        """Use tiles of tile x tile pixels, `warps` warps per splat CTA and
+        `stages` box-table block copies in flight per warp."""
+        if tile not in (8, 16, 32) or warps not in (1, 2, 4, 8) or not 1 <= stages <= 8:
+            raise ValueError("tile must be 8, 16 or 32, warps 1, 2, 4 or 8, stages 1..8")
         nw, nh = self.nw, self.nh
-        self.tile, self.warps = int(tile), int(warps)
+        self.tile, self.warps, self.stages = int(tile), int(warps), int(stages)
         self.tiles_x = (nw + self.tile - 1) // self.tile
         self.tiles_y = (nh + self.tile - 1) // self.tile
 
@@ -471,6 +473,7 @@ class FramePipeline:
         p.n_images, p.rec_per_image = n_images, rec_per_image
         p.box_p, p.box_nq = self.psf.box_p, self.psf.box_nq
         p.n_slots = self.psf.capacity
+        p.box_stages = self.stages
         p.px, p.res = self.cfg.px, PSF_RES
         return p
 
@@ -622,22 +625,23 @@ class FramePipeline:
         return self.expect, self.adc, (optinfo[: n * 8].view(n, 8) if with_optinfo else None)
 
 
-TILE_CANDIDATES = ((8, 4), (8, 2), (16, 2), (16, 4), (16, 8))
+TILE_CANDIDATES = ((8, 4, 4), (8, 4, 8), (8, 2, 6), (16, 4, 4), (16, 8, 4), (16, 4, 8))
 
 
 def tune_tiles(graph, candidates=TILE_CANDIDATES, frames=3):
-    """Autotuner of the tile shape: for each (tile edge, warps per splat CTA)
-    choice, capture the frame graph of ``graph`` (a FrameGraph) and time
+    """Autotuner of the splat launch: for each (tile edge, warps per splat CTA,
+    block copies in flight per warp) choice, capture the frame graph of
+    ``graph`` (a FrameGraph) and time
     ``frames`` replays of the whole frame (binning, splat and merge all depend
     on the tile); keep the fastest on its pipeline and return
-    {(tile, warps): ms per frame}.  The frames run are frames of the
+    {(tile, warps, stages): ms per frame}.  The frames run are frames of the
     simulation (the trajectories advance)."""
     pipe = graph.pipe
     times = {}
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for tile, warps in candidates:
+    for cand in candidates:
         try:
-            pipe.set_tiles(tile, warps)
+            pipe.set_tiles(*cand)
             graph.graph, graph.use_graph = None, True
             graph.step()  # one eager frame, then capture
             graph.step()
@@ -647,7 +651,7 @@ def tune_tiles(graph, candidates=TILE_CANDIDATES, frames=3):
                 graph.step()
             b.record()
             torch.cuda.synchronize()
-            times[(tile, warps)] = a.elapsed_time(b) / frames
+            times[tuple(cand)] = a.elapsed_time(b) / frames
         except (ValueError, _lib.ScopyonGPUError):
             continue
     graph.graph = None

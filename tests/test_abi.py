@@ -68,6 +68,6 @@ def test_host_side_validation_needs_no_gpu():
 def test_struct_sizes_match_c_layout():
     from scopyon_gb300 import _lib
     assert ctypes.sizeof(_lib.StepParams) == 136
-    assert ctypes.sizeof(_lib.SplatParams) == 72
+    assert ctypes.sizeof(_lib.SplatParams) == 80
     assert ctypes.sizeof(_lib.CameraParams) == 112
     assert ctypes.sizeof(_lib.DiffuseParams) == 208

@@ -271,10 +271,12 @@ int sc_gauss_forward(const ScGaussParams *p, const float *d_emit, const float *d
 /* Adjoint of sc_gauss_forward: from d_grad_mu = dL/dmu, d_grad_emit (float4
  * per emitter: dL/dx, dL/dy, dL/dz, dL/dI) and, if not NULL, each emitter's
  * share of dL/dsigma (sum them for the total; dL/dbg[f] is the sum of
- * d_grad_mu over frame f).                                                  */
+ * d_grad_mu over frame f).  d_ws is the workspace sc_gauss_forward filled for
+ * the same p, emitters and sigma (its records and tile bins are reused); it
+ * must not have been reused in between.                                     */
 int sc_gauss_backward(const ScGaussParams *p, const float *d_emit, const float *d_sigma,
-                      const float *d_grad_mu, float *d_grad_emit, float *d_grad_sigma_e,
-                      void *stream);
+                      const void *d_ws, size_t ws_bytes, const float *d_grad_mu,
+                      float *d_grad_emit, float *d_grad_sigma_e, void *stream);
 
 /* Bytes of scratch the two reductions below need for n_seg segments of
  * seg_len values (partial sums of up to 64 CTAs per segment).               */

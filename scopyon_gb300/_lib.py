@@ -102,7 +102,8 @@ _SIG = {
     "sc_gauss_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(GaussParams)]),
     "sc_gauss_forward": (_I, [ctypes.POINTER(GaussParams), _P, _P, _P, _P, ctypes.c_size_t, _P,
                               _P, _P]),
-    "sc_gauss_backward": (_I, [ctypes.POINTER(GaussParams), _P, _P, _P, _P, _P, _P]),
+    "sc_gauss_backward": (_I, [ctypes.POINTER(GaussParams), _P, _P, _P, ctypes.c_size_t, _P, _P,
+                                 _P, _P]),
     "sc_reduce_scratch_bytes": (ctypes.c_size_t, [ctypes.c_int64, _I]),
     "sc_dgrad_scratch_bytes": (ctypes.c_size_t, [ctypes.c_int64]),
     "sc_diffusion_positions": (_I, [_P, _I, _I, _P, _D, ctypes.c_uint64, _P, _P, _P]),

@@ -55,7 +55,7 @@ __global__ void diffusion_positions_kernel(const float4 *__restrict__ emit, int 
 
 constexpr int kThreads = 256;
 constexpr int kChunk = 8192;
-constexpr int kMaxParts = 64;
+constexpr int kMaxParts = 1216;  // 8 CTAs on each of 152 SMs
 
 __device__ __forceinline__ double block_sum(double acc, double *part) {
 #pragma unroll
@@ -88,8 +88,10 @@ gauss_nll_kernel(const float *__restrict__ mu, const float *__restrict__ k, int6
         for (int64_t q = c0 + threadIdx.x; q < c1; q += kThreads) {
             const float m = mu[q], r = k[q] - m;
             const float v = m + (r2_map ? r2_map[q] : r2);
-            acc += (double)r * (double)r / (2.0 * (double)v) + 0.5 * (double)logf(v);
-            if (grad) grad[q] = -r / v - r * r / (2.f * v * v) + 0.5f / v;
+            const float iv = 1.f / v, hr = 0.5f * r * r * iv;
+            // each pixel's term in FP32 (within a few ulp), summed in FP64
+            acc += (double)hr + 0.5 * (double)logf(v);
+            if (grad) grad[q] = -r * iv - hr * iv + 0.5f * iv;
         }
     }
     const double t = block_sum(acc, part);
@@ -105,21 +107,27 @@ dD_partial_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ emi
     double acc = 0.0;
     for (int64_t c0 = (int64_t)blockIdx.x * kChunk; c0 < total; c0 += (int64_t)parts * kChunk) {
         const int64_t c1 = c0 + kChunk < total ? c0 + kChunk : total;
+        int e = (int)((c0 + threadIdx.x) % n);  // emitter of value q (q = t n + e)
         for (int64_t q = c0 + threadIdx.x; q < c1; q += kThreads) {
-            const float4 p = pos[q], g = grad[q], p0 = emit[q % n];
+            const float4 p = pos[q], g = grad[q], p0 = emit[e];
             acc += (double)g.x * (double)(p.x - p0.x) + (double)g.y * (double)(p.y - p0.y);
+            e += kThreads;
+            while (e >= n) e -= n;
         }
     }
     const double t = block_sum(acc, part);
     if (threadIdx.x == 0) partial[blockIdx.x] = t;
 }
 
-// out = scale * sum of partial[0 .. parts) in order (scale: 1, or 1 / (2 D)).
+// out = scale * sum of partial[0 .. parts) (scale: 1, or 1 / (2 D)), one
+// warp: lane l sums partials l, l + 32, ... in order, then a butterfly.
 __global__ void finish_kernel(const double *partial, int parts, const float *D, double *out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int lane = threadIdx.x;
     double t = 0.0;
-    for (int k = 0; k < parts; ++k) t += partial[k];
-    out[0] = D ? t / (2.0 * (double)*D) : t;
+    for (int k = lane; k < parts; k += 32) t += partial[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) out[0] = D ? t / (2.0 * (double)*D) : t;
 }
 
 }  // namespace

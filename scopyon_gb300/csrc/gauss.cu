@@ -12,12 +12,15 @@
 // its centre pixel (R = half_win, about 5.5 sigma: the truncated tails are
 // below 1e-7 of the emitter's photons).
 //
-// Forward: one splat record per emitter, binned by tile (sc_bin_steps), a CTA
-// per tile adds its emitters' separable windows into per-warp buffers in list
-// order, and a merge pass sums the buffers covering each pixel in a fixed
-// order: deterministic.  Adjoint: one warp per emitter gathers dL/dmu over
-// its window: sum g Gx Gy, sum g dGx Gy, sum g Gx dGy and the sigma terms,
-// per-lane sums then fixed warp reductions: deterministic.
+// Forward: one splat record per emitter, binned by tile (sc_bin_steps); the
+// tile kernel adds its emitters' separable windows into a tile buffer in
+// list order, and a merge pass sums the buffers covering each pixel in a
+// fixed order: deterministic.  Adjoint: each binned record gathers dL/dmu
+// over its window from a copy of the tile's area in shared memory: sum g Gx
+// Gy, sum g dGx Gy, sum g Gx dGy and the sigma terms, in a fixed order.
+// Windows of up to 15 pixels (R <= 7) take the tile kernels below (a warp per
+// tile, registers for the buffer); wider ones the per-pixel kernels (a warp
+// per record, one lane per window column).
 #include <math.h>
 
 #include "sc_common.cuh"
@@ -39,16 +42,35 @@ __device__ __forceinline__ float pdf(float t) { return kInvSqrt2Pi * __expf(-0.5
 
 struct GaussConsts {
     int nw, nh, n_frames, n_emit, R;
-    double px, half_w, half_h, inv_pen, z_focal;
+    double px, inv_pen, z_focal;
+    float inv_hi, inv_lo;  // 1 / px as a double-float
+    float mid_w, mid_h;    // nw / 2 and nh / 2 (exact)
 };
 
 // Window of one emitter along one axis: centre pixel ic and the fraction fx
-// of the way across it (x_rel = (x + half) / px = ic + fx), both exact to FP32.
-__device__ __forceinline__ void axis_centre(double x, double half, double px, int &ic, float &fx) {
-    const double xr = (x + half) / px;
-    const double fl = floor(xr);
-    ic = (int)fmax(fmin(fl, 1e9), -1e9);
-    fx = (float)(xr - fl);
+// of the way across it, x_rel = (x + n px / 2) / px = x / px + n / 2 = ic + fx.
+// x / px is formed as a double-float (about 44 bits), so fx is the FP32
+// rounding of the exact fraction except in rare double-rounding cases; no
+// FP64 instruction is needed.
+__device__ __forceinline__ void axis_centre(float x, float inv_hi, float inv_lo, float mid, int &ic,
+                                            float &fx) {
+    const float p = x * inv_hi;
+    const float pe = fmaf(x, inv_lo, fmaf(x, inv_hi, -p));  // x inv - p, to FP32
+    const float s = p + mid;                                 // two-sum of p and mid
+    const float bb = s - p;
+    const float se = ((p - (s - bb)) + (mid - bb)) + pe;
+    const float hi = s + se, lo = se - (hi - s);
+    float fl = floorf(hi);
+    float fr = (hi - fl) + lo;  // hi - fl is exact
+    if (fr < 0.f) {
+        fl -= 1.f;
+        fr += 1.f;
+    } else if (fr >= 1.f) {
+        fl += 1.f;
+        fr -= 1.f;
+    }
+    ic = (int)fminf(fmaxf(fl, -1e9f), 1e9f);
+    fx = fr;
 }
 
 __device__ __forceinline__ float amplitude(const GaussConsts &c, float z) {
@@ -75,8 +97,8 @@ __global__ void gauss_records_kernel(GaussConsts c, const float4 *emit, ScStepRe
     rec.w = e.w * amplitude(c, e.z);
     int icx, icy;
     float fx, fy;
-    axis_centre(e.x, c.half_w, c.px, icx, fx);
-    axis_centre(e.y, c.half_h, c.px, icy, fy);
+    axis_centre(e.x, c.inv_hi, c.inv_lo, c.mid_w, icx, fx);
+    axis_centre(e.y, c.inv_hi, c.inv_lo, c.mid_h, icy, fy);
     const int i0 = max(icx - c.R, 0), i1 = min(icx + c.R, c.nw - 1);
     const int j0 = max(icy - c.R, 0), j1 = min(icy + c.R, c.nh - 1);
     if (i1 >= i0 && j1 >= j0 && isfinite(fx) && isfinite(fy)) {
@@ -204,8 +226,8 @@ __global__ void gauss_backward_kernel(GaussConsts c, const float4 *__restrict__ 
     const float s = (float)(c.px / (double)sigma);
     int icx, icy;
     float fx, fy;
-    axis_centre(e.x, c.half_w, c.px, icx, fx);
-    axis_centre(e.y, c.half_h, c.px, icy, fy);
+    axis_centre(e.x, c.inv_hi, c.inv_lo, c.mid_w, icx, fx);
+    axis_centre(e.y, c.inv_hi, c.inv_lo, c.mid_h, icy, fy);
     const int K = 2 * c.R + 1;
     const int i0 = icx - c.R, j0 = icy - c.R;
     // lane b: column j0 + b (window column terms); row terms go by shuffle
@@ -247,9 +269,267 @@ __global__ void gauss_backward_kernel(GaussConsts c, const float4 *__restrict__ 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tile kernels for windows of up to 15 pixels (R <= 7), one warp per tile.
+//
+// A window along one axis has K + 1 edges t_k = ((float)(lo + k) - f) s
+// (lo: its first pixel's offset from the centre pixel); pixel k integrates
+// to Phi(t_{k+1}) - Phi(t_k).  Each edge's erfc is evaluated once and shared
+// by the two pixels on either side, and the difference is formed exactly as
+// cdf_diff forms it, so pixel values equal the per-pixel kernels' bit for bit.
+
+constexpr int kTileWarps = 4;
+
+__device__ __forceinline__ float edge_t(int lo, int k, float f, float s) {
+    return ((float)(lo + k) - f) * s;
+}
+
+__device__ __forceinline__ float edge_erfc(float t) { return erfcf(fabsf(t) * kInvSqrt2); }
+
+__device__ __forceinline__ float pixel_from_edges(float ta, float tb, float va, float vb) {
+    if (ta >= 0.f) return 0.5f * (va - vb);
+    if (tb <= 0.f) return 0.5f * (vb - va);
+    return 1.f - 0.5f * (vb + va);
+}
+
+// A record's x integrals into row[0 .. P) and its w * y integrals into
+// row[P .. 2P): window pixel k at position o + k (the first n of the window;
+// the rest of the window and everything outside it are 0).  The two axes
+// run in one loop, two independent chains per step.
+template <int K, int P>
+__device__ __forceinline__ void stage_record(const ScStepRec &rec, int ox, int oy, int ni, int nj,
+                                             float s, float *row) {
+#pragma unroll
+    for (int z = 0; z < P - K; ++z) {
+        row[z < ox ? z : z + K] = 0.f;
+        row[P + (z < oy ? z : z + K)] = 0.f;
+    }
+    const int lx = (int)rec.ax_lo, ly = (int)rec.ay_lo;
+    const float fx = rec.ax_hi, fy = rec.ay_hi, w = rec.w;
+    float tax = edge_t(lx, 0, fx, s), vax = edge_erfc(tax);
+    float tay = edge_t(ly, 0, fy, s), vay = edge_erfc(tay);
+    float *px_out = row + ox, *py_out = row + P + oy;
+#pragma unroll 1
+    for (int k = 0; k < K; ++k) {
+        const float tbx = edge_t(lx, k + 1, fx, s), vbx = edge_erfc(tbx);
+        const float tby = edge_t(ly, k + 1, fy, s), vby = edge_erfc(tby);
+        px_out[k] = k < ni ? pixel_from_edges(tax, tbx, vax, vbx) : 0.f;
+        py_out[k] = k < nj ? w * pixel_from_edges(tay, tby, vay, vby) : 0.f;
+        tax = tbx;
+        vax = vbx;
+        tay = tby;
+        vay = vby;
+    }
+}
+
+// First pixel of a binned record relative to its tile, and its window sizes;
+// a record that does not fit the tile buffer (not one the records kernel
+// writes) contributes nothing.
+template <int K>
+__device__ __forceinline__ void tile_window(const ScStepRec &rec, int x0, int y0, int tile,
+                                            int &ox, int &oy, int &ni, int &nj) {
+    ox = rec.i_start - x0;
+    oy = rec.j_start - y0;
+    ni = rec.n_i - 1;
+    nj = rec.n_j - 1;
+    if (ox < 0 || oy < 0 || ox >= tile || oy >= tile || ni > K || nj > K) ox = oy = ni = nj = 0;
+}
+
+// Forward, output-stationary: the warp of a tile keeps the tile's (E x E,
+// E <= P) buffer in registers, lane (lr, lc) owning rows lr*P/4 .. +P/4 and
+// columns lc*P/8 .. +P/8.  Lanes stage 32 records at a time (lane l: record
+// l's x integrals and w * y integrals, zero-padded to P), then every lane
+// adds the records' outer products to its block in list order:
+// deterministic, and one fused multiply-add per pixel per record.
+template <int R, int P>
+__global__ void __launch_bounds__(kTileWarps * 32)
+gauss_tile_splat_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
+                        const int32_t *__restrict__ items, sc::TileGeom g, const float *sigma_p,
+                        double px, float *__restrict__ ws) {
+    constexpr int K = 2 * R + 1;
+    constexpr int BR = P / 4, BC = P / 8;
+    constexpr int STR = 2 * P + 2;  // staged record: x[P], w y[P]; 2-way store conflicts at most
+    static_assert(BR % 2 == 0, "row blocks are read as float2");
+    __shared__ __align__(16) float stage[kTileWarps][32 * STR];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x * kTileWarps + warp;
+    if (tile >= g.n_tiles) return;
+    const int t = tile % g.tiles_per_image;
+    const int x0 = (t / g.tiles_y) * g.tile, y0 = (t % g.tiles_y) * g.tile;
+    const int E = g.edge;
+    float *st = stage[warp];
+    const float s = (float)(px / (double)*sigma_p);
+    const int lr = lane >> 3, lc = lane & 7;
+    float acc[BR][BC];
+#pragma unroll
+    for (int i = 0; i < BR; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) acc[i][j] = 0.f;
+    const int it0 = tile_start[tile], it1 = tile_start[tile + 1];
+    for (int m0 = it0; m0 < it1; m0 += 32) {
+        const int cnt = min(32, it1 - m0);
+        if (lane < cnt) {
+            const ScStepRec &rec = recs[__ldg(items + m0 + lane)];
+            int ox, oy, ni, nj;
+            tile_window<K>(rec, x0, y0, g.tile, ox, oy, ni, nj);
+            stage_record<K, P>(rec, ox, oy, ni, nj, s, st + lane * STR);
+        }
+        __syncwarp();
+        for (int r = 0; r < cnt; ++r) {
+            const float *row = st + r * STR;
+            float gx[BR], gy[BC];
+#pragma unroll
+            for (int i = 0; i < BR; i += 2) {
+                const float2 v = *reinterpret_cast<const float2 *>(row + lr * BR + i);
+                gx[i] = v.x;
+                gx[i + 1] = v.y;
+            }
+#pragma unroll
+            for (int j = 0; j < BC; ++j) gy[j] = row[P + lc * BC + j];
+#pragma unroll
+            for (int i = 0; i < BR; ++i)
+#pragma unroll
+                for (int j = 0; j < BC; ++j) acc[i][j] = fmaf(gx[i], gy[j], acc[i][j]);
+        }
+        __syncwarp();
+    }
+    float *out = ws + (size_t)tile * E * E;
+#pragma unroll
+    for (int i = 0; i < BR; ++i)
+#pragma unroll
+        for (int j = 0; j < BC; ++j) {
+            const int pi = lr * BR + i, pj = lc * BC + j;
+            if (pi < E && pj < E) out[pi * E + pj] = acc[i][j];
+        }
+}
+
+// Adjoint, one thread per binned record: the warp of a tile copies dL/dmu
+// over the tile's E x E buffer area into shared memory (0 outside the
+// image), then each lane takes records l, l + 32, ... of the tile's list and
+// forms, over its window,
+//   h(a) = sum_b G[a][b] gy(b) (and with dgy, sgy),
+//   S1 = sum_a gx(a) h(a), Sdx = sum_a dgx(a) h(a), Sdy = sum_a gx(a) hd(a),
+//   Ss = sum_a sgx(a) h(a) + gx(a) hs(a),
+// in a fixed order.  The y terms live in registers; the x terms are formed
+// row by row from the running edge.
+constexpr int kPatchStride = 40;  // 8 (mod 32): first pixels (ox, oy) spread over the banks
+constexpr int kPatchRows = 16 + 2 * 7;
+
+template <int R>
+__global__ void __launch_bounds__(kTileWarps * 32)
+gauss_tile_backward_kernel(GaussConsts c, const ScStepRec *__restrict__ recs,
+                           const int32_t *__restrict__ tile_start,
+                           const int32_t *__restrict__ items, sc::TileGeom g,
+                           const float4 *__restrict__ emit, const float *sigma_p,
+                           const float *__restrict__ grad_mu, float4 *__restrict__ grad_emit,
+                           float *grad_sigma_e) {
+    constexpr int K = 2 * R + 1;
+    constexpr int S = kPatchStride;
+    __shared__ float patch[kTileWarps][kPatchRows * S];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x * kTileWarps + warp;
+    if (tile >= g.n_tiles) return;
+    const int img = tile / g.tiles_per_image;
+    const int t = tile - img * g.tiles_per_image;
+    const int x0 = (t / g.tiles_y) * g.tile, y0 = (t % g.tiles_y) * g.tile;
+    const int E = g.edge;
+    const int it0 = tile_start[tile], it1 = tile_start[tile + 1];
+    if (it0 == it1) return;
+    float *pt = patch[warp];
+    const float *G = grad_mu + (size_t)img * c.nw * c.nh;
+    const int j = y0 + lane;
+    for (int a = 0; a < E; ++a) {
+        const int i = x0 + a;
+        if (lane < E) pt[a * S + lane] = (i < c.nw && j < c.nh) ? __ldg(G + (size_t)i * c.nh + j) : 0.f;
+    }
+    __syncwarp();
+    const float sigma = *sigma_p;
+    const float s = (float)(c.px / (double)sigma);
+    for (int m = it0 + lane; m < it1; m += 32) {
+        const int r = __ldg(items + m);
+        const ScStepRec &rec = recs[r];
+        int ox, oy, ni, nj;
+        tile_window<K>(rec, x0, y0, g.tile, ox, oy, ni, nj);
+        float gy[K], dgy[K], sgy[K];
+        {
+            const int lo = (int)rec.ay_lo;
+            const float f = rec.ay_hi;
+            float ta = edge_t(lo, 0, f, s), va = edge_erfc(ta), pa = pdf(ta);
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const float tb = edge_t(lo, k + 1, f, s), vb = edge_erfc(tb), pb = pdf(tb);
+                const bool ok = k < nj;
+                gy[k] = ok ? pixel_from_edges(ta, tb, va, vb) : 0.f;
+                dgy[k] = ok ? pb - pa : 0.f;
+                sgy[k] = ok ? tb * pb - ta * pa : 0.f;
+                ta = tb;
+                va = vb;
+                pa = pb;
+            }
+        }
+        float S1 = 0.f, Sdx = 0.f, Sdy = 0.f, Ss = 0.f;
+        {
+            const int lo = (int)rec.ax_lo;
+            const float f = rec.ax_hi;
+            const float *p0 = pt + ox * S + oy;
+            float ta = edge_t(lo, 0, f, s), va = edge_erfc(ta), pa = pdf(ta);
+#pragma unroll 1
+            for (int a = 0; a < ni; ++a) {
+                const float tb = edge_t(lo, a + 1, f, s), vb = edge_erfc(tb), pb = pdf(tb);
+                const float gx = pixel_from_edges(ta, tb, va, vb);
+                const float dgx = pb - pa, sgx = tb * pb - ta * pa;
+                float hg = 0.f, hd = 0.f, hs = 0.f;
+#pragma unroll
+                for (int b = 0; b < K; ++b) {
+                    const float gv = p0[a * S + b];
+                    hg = fmaf(gv, gy[b], hg);
+                    hd = fmaf(gv, dgy[b], hd);
+                    hs = fmaf(gv, sgy[b], hs);
+                }
+                S1 = fmaf(gx, hg, S1);
+                Sdx = fmaf(dgx, hg, Sdx);
+                Sdy = fmaf(gx, hd, Sdy);
+                Ss = fmaf(sgx, hg, fmaf(gx, hs, Ss));
+                ta = tb;
+                va = vb;
+                pa = pb;
+            }
+        }
+        const float4 e = emit[r];
+        const float A = amplitude(c, e.z);
+        const float cc = e.w * A;
+        const float inv_sigma = 1.f / sigma;
+        float4 gr;
+        gr.x = -cc * inv_sigma * Sdx;
+        gr.y = -cc * inv_sigma * Sdy;
+        const float dz = e.z - (float)c.z_focal;
+        gr.z = c.inv_pen > 0.0
+                   ? -e.w * A * (float)c.inv_pen * (dz > 0.f ? 1.f : (dz < 0.f ? -1.f : 0.f)) * S1
+                   : 0.f;
+        gr.w = A * S1;
+        grad_emit[r] = gr;
+        if (grad_sigma_e) grad_sigma_e[r] = -cc * inv_sigma * Ss;
+    }
+}
+
+template <int R>
+void launch_tile_splat(int P, int grid, cudaStream_t st, const ScStepRec *recs,
+                       const int32_t *tile_start, const int32_t *items, const sc::TileGeom &g,
+                       const float *sigma, double px, float *ws) {
+    if (P == 24)
+        gauss_tile_splat_kernel<R, 24><<<grid, kTileWarps * 32, 0, st>>>(recs, tile_start, items,
+                                                                         g, sigma, px, ws);
+    else
+        gauss_tile_splat_kernel<R, 32><<<grid, kTileWarps * 32, 0, st>>>(recs, tile_start, items,
+                                                                         g, sigma, px, ws);
+}
+
+// Tile kernels take windows of R <= 7 on tiles of 8 or 16 pixels.
+bool tile_path(const GaussConsts &c) { return c.R <= 7; }
+
 constexpr int kSumThreads = 256;
 constexpr int kSumChunk = 8192;    // values per CTA and pass
-constexpr int kSumMaxParts = 64;   // CTAs per segment
+constexpr int kSumMaxParts = 1216; // CTAs per segment (8 on each of 152 SMs)
 
 __device__ __forceinline__ double block_sum(double acc, double *part) {
 #pragma unroll
@@ -292,13 +572,18 @@ partial_sum_kernel(const float *__restrict__ x, const float *__restrict__ counts
     if (threadIdx.x == 0) partial[(size_t)blockIdx.y * parts + blockIdx.x] = t;
 }
 
-// out[y] = sum of partial[y][0 .. parts) in order.
+// out[y] = sum of partial[y][0 .. parts), a warp per segment: lane l sums
+// partials l, l + 32, ... in order, then a butterfly (the same bits on every
+// lane and every run).
 __global__ void finish_sum_kernel(const double *partial, int parts, int n_seg, double *out) {
-    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
     if (y >= n_seg) return;
     double t = 0.0;
-    for (int k = 0; k < parts; ++k) t += partial[(size_t)y * parts + k];
-    out[y] = t;
+    for (int k = lane; k < parts; k += 32) t += partial[(size_t)y * parts + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) out[y] = t;
 }
 
 int sum_parts(int64_t seg_len) {
@@ -321,7 +606,7 @@ int launch_reduce(const float *x, const float *counts, int64_t seg_len, int n_se
     double *partial = static_cast<double *>(scratch);
     partial_sum_kernel<<<dim3((unsigned)parts, (unsigned)n_seg), kSumThreads, 0, s>>>(
         x, counts, seg_len, grad, partial);
-    finish_sum_kernel<<<(n_seg + 127) / 128, 128, 0, s>>>(partial, parts, n_seg, out);
+    finish_sum_kernel<<<(n_seg + 3) / 4, 128, 0, s>>>(partial, parts, n_seg, out);
     return sc::launch_status("reduction");
 }
 
@@ -340,8 +625,11 @@ int gauss_consts(const ScGaussParams *p, GaussConsts &c) {
     c.n_emit = p->n_emit;
     c.R = p->half_win;
     c.px = p->px;
-    c.half_w = p->nw * p->px * 0.5;
-    c.half_h = p->nh * p->px * 0.5;
+    const double inv = 1.0 / p->px;
+    c.inv_hi = (float)inv;
+    c.inv_lo = (float)(inv - (double)c.inv_hi);
+    c.mid_w = 0.5f * (float)p->nw;
+    c.mid_h = 0.5f * (float)p->nh;
     c.inv_pen = p->inv_pen;
     c.z_focal = p->z_focal;
     return SC_OK;
@@ -426,11 +714,26 @@ extern "C" int sc_gauss_forward(const ScGaussParams *p, const float *d_emit, con
         rc = sc_bin_steps(w.recs, n_rec, &sp, w.bin_ws, w.bin_bytes, w.tile_start, w.items,
                           d_status, stream);
         if (rc) return rc;
-        const int E = g.edge, BS = (E * E + 31) & ~31;
-        const size_t smem = (size_t)4 * BS * sizeof(float);
-        SC_REQUIRE(smem <= 48 * 1024, "sc_gauss_forward: tile buffers need %zu bytes", smem);
-        gauss_splat_kernel<4><<<g.n_tiles, 128, smem, s>>>(w.recs, w.tile_start, w.items, g,
-                                                           d_sigma, c.px, w.tiles);
+        if (tile_path(c)) {
+            const int P = g.edge <= 24 ? 24 : 32;
+            const int grid = (g.n_tiles + kTileWarps - 1) / kTileWarps;
+            switch (c.R) {
+#define SC_TILE_SPLAT(RR)                                                                   \
+    case RR:                                                                                \
+        launch_tile_splat<RR>(P, grid, s, w.recs, w.tile_start, w.items, g, d_sigma, c.px, \
+                              w.tiles);                                                     \
+        break;
+                SC_TILE_SPLAT(1) SC_TILE_SPLAT(2) SC_TILE_SPLAT(3) SC_TILE_SPLAT(4)
+                SC_TILE_SPLAT(5) SC_TILE_SPLAT(6) SC_TILE_SPLAT(7)
+#undef SC_TILE_SPLAT
+            }
+        } else {
+            const int E = g.edge, BS = (E * E + 31) & ~31;
+            const size_t smem = (size_t)4 * BS * sizeof(float);
+            SC_REQUIRE(smem <= 48 * 1024, "sc_gauss_forward: tile buffers need %zu bytes", smem);
+            gauss_splat_kernel<4><<<g.n_tiles, 128, smem, s>>>(w.recs, w.tile_start, w.items, g,
+                                                               d_sigma, c.px, w.tiles);
+        }
     } else {
         rc = sc::cuda_status(
             cudaMemsetAsync(w.tiles, 0, (size_t)g.n_tiles * g.edge * g.edge * sizeof(float), s),
@@ -445,17 +748,52 @@ extern "C" int sc_gauss_forward(const ScGaussParams *p, const float *d_emit, con
 }
 
 extern "C" int sc_gauss_backward(const ScGaussParams *p, const float *d_emit, const float *d_sigma,
-                                 const float *d_grad_mu, float *d_grad_emit,
-                                 float *d_grad_sigma_e, void *stream) {
+                                 const void *d_ws, size_t ws_bytes, const float *d_grad_mu,
+                                 float *d_grad_emit, float *d_grad_sigma_e, void *stream) {
     GaussConsts c;
     int rc = gauss_consts(p, c);
     if (rc) return rc;
     const int n_rec = c.n_frames * c.n_emit;
     if (n_rec == 0) return SC_OK;
     SC_REQUIRE(d_emit && d_sigma && d_grad_mu && d_grad_emit, "sc_gauss_backward: NULL pointer");
-    gauss_backward_kernel<<<(n_rec + 7) / 8, 256, 0, sc::as_stream(stream)>>>(
-        c, reinterpret_cast<const float4 *>(d_emit), d_sigma, d_grad_mu,
-        reinterpret_cast<float4 *>(d_grad_emit), d_grad_sigma_e);
+    cudaStream_t s = sc::as_stream(stream);
+    if (!tile_path(c)) {
+        gauss_backward_kernel<<<(n_rec + 7) / 8, 256, 0, s>>>(
+            c, reinterpret_cast<const float4 *>(d_emit), d_sigma, d_grad_mu,
+            reinterpret_cast<float4 *>(d_grad_emit), d_grad_sigma_e);
+        return sc::launch_status("sc_gauss_backward");
+    }
+    // the records and bins sc_gauss_forward left in the workspace
+    SC_REQUIRE(d_ws, "sc_gauss_backward: the forward's workspace is NULL");
+    const GaussWorkspace w = gauss_workspace(p, const_cast<void *>(d_ws));
+    SC_REQUIRE(ws_bytes >= w.total, "sc_gauss_backward: workspace %zu < %zu bytes", ws_bytes,
+               w.total);
+    const ScSplatParams sp = gauss_splat_params(p);
+    sc::TileGeom g;
+    rc = sc::tile_geom(&sp, g);
+    if (rc) return rc;
+    // records outside every tile (windows that miss the image) get zeros
+    rc = sc::cuda_status(cudaMemsetAsync(d_grad_emit, 0, (size_t)n_rec * sizeof(float4), s),
+                         "sc_gauss_backward");
+    if (rc) return rc;
+    if (d_grad_sigma_e) {
+        rc = sc::cuda_status(cudaMemsetAsync(d_grad_sigma_e, 0, (size_t)n_rec * sizeof(float), s),
+                             "sc_gauss_backward");
+        if (rc) return rc;
+    }
+    const int grid = (g.n_tiles + kTileWarps - 1) / kTileWarps;
+    const float4 *e4 = reinterpret_cast<const float4 *>(d_emit);
+    float4 *g4 = reinterpret_cast<float4 *>(d_grad_emit);
+    switch (c.R) {
+#define SC_TILE_BWD(RR)                                                                        \
+    case RR:                                                                                   \
+        gauss_tile_backward_kernel<RR><<<grid, kTileWarps * 32, 0, s>>>(                       \
+            c, w.recs, w.tile_start, w.items, g, e4, d_sigma, d_grad_mu, g4, d_grad_sigma_e); \
+        break;
+        SC_TILE_BWD(1) SC_TILE_BWD(2) SC_TILE_BWD(3) SC_TILE_BWD(4)
+        SC_TILE_BWD(5) SC_TILE_BWD(6) SC_TILE_BWD(7)
+#undef SC_TILE_BWD
+    }
     return sc::launch_status("sc_gauss_backward");
 }
 

@@ -61,7 +61,6 @@ class GaussianImageModel:
         self.z_focal = float(z_focal)
         self.tile = int(tile)
         self.device = torch.device(device or "cuda")
-        self._ws = None
 
     @classmethod
     def from_config(cls, config, sigma_max=None, device=None):
@@ -81,10 +80,10 @@ class GaussianImageModel:
         return p
 
     def workspace(self, p):
+        """A fresh forward workspace (records and tile bins); the backward pass
+        of the same call reads it, so calls do not share one."""
         n = _lib.load().sc_gauss_workspace_bytes(p)
-        if self._ws is None or self._ws.numel() < n:
-            self._ws = torch.empty(max(n, 1), dtype=torch.uint8, device=self.device)
-        return self._ws, n
+        return torch.empty(max(n, 1), dtype=torch.uint8, device=self.device), n
 
 
 def _check_inputs(emitters, background, sigma, model):
@@ -113,13 +112,13 @@ class _ExpectedImage(torch.autograd.Function):
         status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=emitters.device)
         call("sc_gauss_forward", p, ptr(emitters), ptr(sig), ptr(background), ptr(ws), nbytes,
              ptr(mu), ptr(status), stream_ptr())
-        ctx.save_for_backward(emitters, sig)
+        ctx.save_for_backward(emitters, sig, ws)
         ctx.model = model
         return mu
 
     @staticmethod
     def backward(ctx, grad_mu):
-        emitters, sig = ctx.saved_tensors
+        emitters, sig, ws = ctx.saved_tensors
         model = ctx.model
         F, N = emitters.shape[:2]
         g = grad_mu.contiguous().float()
@@ -127,7 +126,8 @@ class _ExpectedImage(torch.autograd.Function):
         g_emit = torch.empty_like(emitters)
         g_sig_e = torch.empty(F, N, dtype=torch.float32, device=emitters.device)
         s = stream_ptr()
-        call("sc_gauss_backward", p, ptr(emitters), ptr(sig), ptr(g), ptr(g_emit), ptr(g_sig_e), s)
+        call("sc_gauss_backward", p, ptr(emitters), ptr(sig), ptr(ws), ws.numel(), ptr(g),
+             ptr(g_emit), ptr(g_sig_e), s)
         dev = emitters.device
         g_bg = torch.empty(F, dtype=torch.float64, device=dev)
         scr, n = _reduce_scratch(model.nw * model.nh, F, dev)
@@ -223,14 +223,15 @@ class _DiffusionLoss(torch.autograd.Function):
         scr, n = _dgrad_scratch(mu.numel(), dev)
         call("sc_gauss_nll", ptr(mu), ptr(counts.contiguous().float()), mu.numel(), ptr(var_map),
              float(var), ptr(scr), n, ptr(loss), ptr(grad_mu), s)
-        ctx.save_for_backward(D, emitters, grad_mu, sig, normals if normals is not None else D)
+        ctx.save_for_backward(D, emitters, grad_mu, sig, ws,
+                              normals if normals is not None else D)
         ctx.has_normals = normals is not None
         ctx.model, ctx.T, ctx.dt, ctx.seed = model, T, dt, seed
         return loss.reshape(())
 
     @staticmethod
     def backward(ctx, g):
-        D, emitters, grad_mu, sig, normals = ctx.saved_tensors
+        D, emitters, grad_mu, sig, ws, normals = ctx.saved_tensors
         normals = normals if ctx.has_normals else None
         model, T = ctx.model, ctx.T
         N = emitters.shape[0]
@@ -240,7 +241,8 @@ class _DiffusionLoss(torch.autograd.Function):
         p = model.params(1, N * T)
         grad_pos = torch.empty_like(pos)
         s = stream_ptr()
-        call("sc_gauss_backward", p, ptr(pos), ptr(sig), ptr(grad_mu), ptr(grad_pos), None, s)
+        call("sc_gauss_backward", p, ptr(pos), ptr(sig), ptr(ws), ws.numel(), ptr(grad_mu),
+             ptr(grad_pos), None, s)
         dD = torch.empty(1, dtype=torch.float64, device=dev)
         scr, n = _dgrad_scratch(N * T, dev)
         call("sc_diffusion_dD", ptr(pos), ptr(emitters), N, int(T), ptr(grad_pos), ptr(D),

@@ -55,9 +55,9 @@ def reference_image(emit, bg, sigma, model):
     return bg[:, None, None] + torch.einsum("fn,fni,fnj->fij", c, gx, gy)
 
 
-def make_case(dm, seed, F=3, N=60, nw=48, nh=40, pen=math.inf, sigma=1.3 * PX):
+def make_case(dm, seed, F=3, N=60, nw=48, nh=40, pen=math.inf, sigma=1.3 * PX, tile=8):
     rng = numpy.random.RandomState(seed)
-    model = dm.GaussianImageModel(nw, nh, PX, 1.5 * sigma, penetration=pen)
+    model = dm.GaussianImageModel(nw, nh, PX, 1.5 * sigma, penetration=pen, tile=tile)
     e = numpy.zeros((F, N, 4))
     e[..., 0] = rng.uniform(-0.55, 0.55, (F, N)) * nw * PX  # some windows leave the image
     e[..., 1] = rng.uniform(-0.55, 0.55, (F, N)) * nh * PX
@@ -67,9 +67,16 @@ def make_case(dm, seed, F=3, N=60, nw=48, nh=40, pen=math.inf, sigma=1.3 * PX):
     return model, e, bg, sigma
 
 
-@pytest.mark.parametrize("pen", [math.inf, 300e-9])
-def test_forward_matches_fp64(dm, pen):
-    model, e, bg, sigma = make_case(dm, 1, pen=pen)
+# (illumination, sigma in pixels, tile): sigma 1.3 px gives R = 11 (the per-pixel
+# kernels), 0.8 px R = 7 and 0.45 px R = 4 (the tile kernels, buffers of 24 and
+# 32 pixels a side)
+CASES = [(math.inf, 1.3, 8), (300e-9, 1.3, 8), (math.inf, 0.8, 8), (300e-9, 0.8, 16),
+         (math.inf, 0.45, 16), (300e-9, 0.45, 8)]
+
+
+@pytest.mark.parametrize("pen,sigma_px,tile", CASES)
+def test_forward_matches_fp64(dm, pen, sigma_px, tile):
+    model, e, bg, sigma = make_case(dm, 1, pen=pen, sigma=sigma_px * PX, tile=tile)
     emit = torch.tensor(e, dtype=torch.float32, device="cuda")
     mu = dm.expected_image(emit, torch.tensor(bg, dtype=torch.float32, device="cuda"),
                            torch.tensor(sigma, dtype=torch.float32, device="cuda"), model)
@@ -89,9 +96,9 @@ def _loss64(emit, bg, sigma, model, counts):
     return (mu - counts * torch.log(mu)).sum()
 
 
-@pytest.mark.parametrize("pen", [math.inf, 300e-9])
-def test_gradients_match_fp64_autograd_and_finite_differences(dm, pen):
-    model, e, bg, sigma = make_case(dm, 2, pen=pen)
+@pytest.mark.parametrize("pen,sigma_px,tile", CASES)
+def test_gradients_match_fp64_autograd_and_finite_differences(dm, pen, sigma_px, tile):
+    model, e, bg, sigma = make_case(dm, 2, pen=pen, sigma=sigma_px * PX, tile=tile)
     dev = "cuda"
     emit = torch.tensor(e, dtype=torch.float32, device=dev)
     emit[..., 2] += 1e-9 * (emit[..., 2] == 0)  # keep |z - z_focal| differentiable
@@ -150,6 +157,30 @@ def test_gradients_match_fp64_autograd_and_finite_differences(dm, pen):
         fd = (_loss64(emit.double(), b64, s64 + hs, model, counts.double()) -
               _loss64(emit.double(), b64, s64 - hs, model, counts.double())).item() / (2 * hs)
     assert abs(sig_g.grad.item() - fd) <= 2e-3 * abs(fd)
+
+
+def test_interleaved_forwards_keep_their_own_workspace(dm):
+    """Two forward calls before one backward: each backward pass reads the
+    records and bins of its own forward call."""
+    model, e, bg, sigma = make_case(dm, 4, sigma=0.8 * PX)
+    dev = "cuda"
+    bg_t = torch.tensor(bg, dtype=torch.float32, device=dev)
+    sig_t = torch.tensor(sigma, dtype=torch.float32, device=dev)
+    e1 = torch.tensor(e, dtype=torch.float32, device=dev)
+    e2 = e1.flip(1).contiguous()
+    e2[..., 0] += 0.4 * PX
+    with torch.no_grad():
+        counts = torch.poisson(dm.expected_image(e1, bg_t, sig_t, model).double(),
+                               generator=torch.Generator(dev).manual_seed(2)).float()
+    grads = []
+    for pair in ((e1, e2), (e1, None), (None, e2)):
+        leaves = [x.clone().requires_grad_(True) if x is not None else None for x in pair]
+        loss = sum(dm.poisson_nll(dm.expected_image(x, bg_t, sig_t, model), counts)
+                   for x in leaves if x is not None)
+        loss.backward()
+        grads.append([x.grad if x is not None else None for x in leaves])
+    assert torch.equal(grads[0][0], grads[1][0])
+    assert torch.equal(grads[0][1], grads[2][1])
 
 
 def test_adam_localisation(dm):

@@ -300,12 +300,188 @@ int bin_sort(int n_bins, int32_t *tile_start, int32_t *items, int32_t *big, cuda
     return sc::launch_status("bin sort");
 }
 
+// ---------------------------------------------------------------------------
+// Large record sets: a stable LSD radix sort of the record indices by bin
+// instead of placement by atomic rank plus a sort of every list.  Input is
+// rec_bin in record order (bin -1: key n_bins, after every bin); each pass
+// partitions by one digit of at most 9 bits and keeps the order of equal
+// digits, so the result is ordered by bin and then by record index: the
+// same lists as placement plus sort.  A pass is three kernels: per-block
+// digit counts (blocks of 4096 records), a scan over blocks per digit, and
+// the scatter, where each warp ranks its records among equal digits with
+// __match_any_sync in record order.
+
+constexpr int kRxThreads = 512, kRxWarps = kRxThreads / 32, kRxPerWarp = 256;
+constexpr int kRxBlock = kRxWarps * kRxPerWarp;  // 4096 records
+constexpr int kRxMaxBits = 9, kRxMaxBuckets = 1 << kRxMaxBits;
+constexpr int kRxScanThreads = 1024;
+
+__device__ __forceinline__ int rx_key(const int32_t *keys, int q, int sentinel) {
+    const int k = keys[q];
+    return k < 0 ? sentinel : k;
+}
+
+// counts[d * nb + b] = records of block b whose digit is d.
+__global__ void __launch_bounds__(kRxThreads)
+radix_upsweep_kernel(const int32_t *__restrict__ keys, int n, int sentinel, int shift, int bits,
+                     int nb, int32_t *__restrict__ counts) {
+    __shared__ int32_t hist[kRxMaxBuckets];
+    const int buckets = 1 << bits;
+    for (int d = threadIdx.x; d < buckets; d += kRxThreads) hist[d] = 0;
+    __syncthreads();
+    const int q0 = blockIdx.x * kRxBlock, q1 = min(n, q0 + kRxBlock);
+    for (int q = q0 + threadIdx.x; q < q1; q += kRxThreads)
+        atomicAdd(&hist[(rx_key(keys, q, sentinel) >> shift) & (buckets - 1)], 1);
+    __syncthreads();
+    for (int d = threadIdx.x; d < buckets; d += kRxThreads)
+        counts[(size_t)d * nb + blockIdx.x] = hist[d];
+}
+
+// Inclusive scan over a CTA of kRxScanThreads / kRxThreads threads; returns
+// this thread's inclusive value and leaves the CTA total in *total_out.
+template <int NT>
+__device__ __forceinline__ int cta_inclusive_scan(int v, int32_t *warp_tot, int *total_out) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int t = lane < NT / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        warp_tot[lane] = t;
+    }
+    __syncthreads();
+    const int r = x + (warp ? warp_tot[warp - 1] : 0);
+    *total_out = warp_tot[NT / 32 - 1];
+    __syncthreads();
+    return r;
+}
+
+// One CTA per digit d: counts[d][0 .. nb) becomes its exclusive scan over
+// blocks, total[d] the digit's record count.
+__global__ void __launch_bounds__(kRxScanThreads)
+radix_scan_kernel(int32_t *__restrict__ counts, int nb, int32_t *__restrict__ total) {
+    __shared__ int32_t warp_tot[32];
+    int32_t *c = counts + (size_t)blockIdx.x * nb;
+    int carry = 0;
+    for (int base = 0; base < nb; base += kRxScanThreads) {
+        const int i = base + threadIdx.x;
+        const int v = i < nb ? c[i] : 0;
+        int tot;
+        const int incl = cta_inclusive_scan<kRxScanThreads>(v, warp_tot, &tot);
+        if (i < nb) c[i] = carry + incl - v;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) total[blockIdx.x] = carry;
+}
+
+// Stable scatter of block b: position = start of the digit (scan of the
+// totals) + records of the digit in earlier blocks + earlier warps of this
+// block + rank within the warp (32 records at a time, in record order).
+__global__ void __launch_bounds__(kRxThreads)
+radix_downsweep_kernel(const int32_t *__restrict__ keys_in, const int32_t *__restrict__ vals_in,
+                       int n, int sentinel, int shift, int bits, int nb,
+                       const int32_t *__restrict__ counts, const int32_t *__restrict__ total,
+                       int32_t *__restrict__ keys_out, int32_t *__restrict__ vals_out) {
+    __shared__ int32_t whist[kRxWarps][kRxMaxBuckets];
+    __shared__ int32_t base_s[kRxMaxBuckets];
+    __shared__ int32_t warp_tot[32];
+    const int buckets = 1 << bits;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    {
+        const int d = threadIdx.x;  // buckets <= kRxThreads
+        const int v = d < buckets ? total[d] : 0;
+        int tot;
+        const int incl = cta_inclusive_scan<kRxThreads>(v, warp_tot, &tot);
+        if (d < buckets) base_s[d] = incl - v + counts[(size_t)d * nb + blockIdx.x];
+    }
+    for (int d = lane; d < buckets; d += 32) whist[warp][d] = 0;
+    __syncwarp();
+    const int q_warp = blockIdx.x * kRxBlock + warp * kRxPerWarp;
+    constexpr int R = kRxPerWarp / 32;
+    int key[R], loc[R], val[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int q = q_warp + r * 32 + lane;
+        const bool ok = q < n;
+        const int k = ok ? rx_key(keys_in, q, sentinel) : 0;
+        const int d = ok ? (k >> shift) & (buckets - 1) : -1;
+        val[r] = ok ? (vals_in ? vals_in[q] : q) : 0;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        const int pre = ok ? whist[warp][d] : 0;
+        __syncwarp();
+        if (ok && rank == 0) whist[warp][d] = pre + __popc(peers);
+        __syncwarp();
+        key[r] = k;
+        loc[r] = pre + rank;
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < buckets; d += kRxThreads) {
+        int acc = base_s[d];
+#pragma unroll
+        for (int w = 0; w < kRxWarps; ++w) {
+            const int t = whist[w][d];
+            whist[w][d] = acc;
+            acc += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int q = q_warp + r * 32 + lane;
+        if (q < n) {
+            const int pos = whist[warp][(key[r] >> shift) & (buckets - 1)] + loc[r];
+            if (keys_out) keys_out[pos] = key[r];
+            vals_out[pos] = val[r];
+        }
+    }
+}
+
+// items = record indices ordered by bin, then index (bins of -1 at the end).
+// rec_bin and keys_tmp are overwritten; vals_tmp, counts and total are
+// scratch of n, kRxMaxBuckets * ceil(n / kRxBlock) and kRxMaxBuckets ints.
+int radix_bins(int n, int n_bins, int32_t *rec_bin, int32_t *keys_tmp, int32_t *vals_tmp,
+               int32_t *counts, int32_t *total, int32_t *items, cudaStream_t s) {
+    int bits = 1;
+    while ((1 << bits) <= n_bins) ++bits;  // keys 0 .. n_bins
+    const int passes = (bits + kRxMaxBits - 1) / kRxMaxBits;
+    const int dbits = (bits + passes - 1) / passes;
+    const int nb = (n + kRxBlock - 1) / kRxBlock;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = p * dbits;
+        const int pb = min(dbits, bits - shift);
+        const int32_t *in_keys = p == 0 ? rec_bin : (p % 2 ? keys_tmp : rec_bin);
+        int32_t *out_keys = p == passes - 1 ? nullptr : (p % 2 ? rec_bin : keys_tmp);
+        const int32_t *in_vals = p == 0 ? nullptr : ((passes - p) % 2 ? vals_tmp : items);
+        int32_t *out_vals = (passes - 1 - p) % 2 ? vals_tmp : items;
+        radix_upsweep_kernel<<<nb, kRxThreads, 0, s>>>(in_keys, n, n_bins, shift, pb, nb, counts);
+        radix_scan_kernel<<<1 << pb, kRxScanThreads, 0, s>>>(counts, nb, total);
+        radix_downsweep_kernel<<<nb, kRxThreads, 0, s>>>(in_keys, in_vals, n, n_bins, shift, pb,
+                                                         nb, counts, total, out_keys, out_vals);
+    }
+    return sc::launch_status("radix bins");
+}
+
 // Scan, placement and sort of counted records.
-int bin_finish(int n_rec, const sc::TileGeom &g, int32_t *tile_count, const int32_t *rec_bin,
-               const int32_t *rec_rank, int32_t *big, int32_t *tile_start, int32_t *items,
-               cudaStream_t s) {
+int bin_finish(int n_rec, const sc::TileGeom &g, int32_t *tile_count, int32_t *rec_bin,
+               const sc::BinLayout &b, int32_t *tile_start, int32_t *items, cudaStream_t s) {
     const int n_bins = 2 * g.n_tiles;
     bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(tile_count, n_bins, tile_start, nullptr);
+    if (b.rx_vals)
+        return radix_bins(n_rec, n_bins, rec_bin, b.rec_rank, b.rx_vals, b.rx_counts, b.rx_total,
+                          items, s);
+    const int32_t *rec_rank = b.rec_rank;
+    int32_t *big = b.big;
     int grid = (n_rec + 255) / 256;
     if (grid > 152 * 8) grid = 152 * 8;
     bin_place_kernel<<<grid, 256, 0, s>>>(rec_bin, rec_rank, n_rec, tile_start, items);
@@ -354,6 +530,14 @@ int bin_layout(const TileGeom &g, int n_rec, void *d_ws, size_t ws_bytes, BinLay
     b.rec_bin = full ? b.cursor + n_bins : nullptr;
     b.rec_rank = full ? b.rec_bin + n_rec : nullptr;
     b.big = full ? b.rec_rank + n_rec : nullptr;
+    b.rx_vals = b.rx_counts = b.rx_total = nullptr;
+    if (full && n_rec >= kRadixMinRecords) {
+        uintptr_t p = reinterpret_cast<uintptr_t>(b.big + 2 * g.n_tiles + 1);
+        p = (p + 15) & ~(uintptr_t)15;
+        b.rx_vals = reinterpret_cast<int32_t *>(p);
+        b.rx_counts = b.rx_vals + n_rec;
+        b.rx_total = b.rx_counts + (size_t)kRxMaxBuckets * ((n_rec + kRxBlock - 1) / kRxBlock);
+    }
     return SC_OK;
 }
 
@@ -370,8 +554,14 @@ static size_t bin_counts_bytes(int n_tiles_total) {
 extern "C" size_t sc_bin_workspace_bytes(int n_rec, int n_tiles_total) {
     if (n_rec <= 0 || n_tiles_total <= 0) return 0;
     // + the bin and rank of every record, + the list of long bins (count + bins)
-    return bin_counts_bytes(n_tiles_total) + (size_t)2 * n_rec * sizeof(int32_t) +
-           (size_t)(2 * n_tiles_total + 1) * sizeof(int32_t);
+    size_t bytes = bin_counts_bytes(n_tiles_total) + (size_t)2 * n_rec * sizeof(int32_t) +
+                   (size_t)(2 * n_tiles_total + 1) * sizeof(int32_t);
+    // + the radix sort's values, per-block digit counts and digit totals
+    if (n_rec >= sc::kRadixMinRecords)
+        bytes += 16 + sizeof(int32_t) * ((size_t)n_rec +
+                                         (size_t)kRxMaxBuckets * ((n_rec + kRxBlock - 1) / kRxBlock) +
+                                         kRxMaxBuckets);
+    return bytes;
 }
 
 extern "C" int sc_bin_reset(const ScSplatParams *p, void *d_ws, size_t ws_bytes, void *stream) {
@@ -403,7 +593,7 @@ extern "C" int sc_bin_finish(int n_rec, const ScSplatParams *p, void *d_ws, size
                sc_bin_workspace_bytes(n_rec, g.n_tiles));
     sc::BinLayout b;
     sc::bin_layout(g, n_rec, d_ws, ws_bytes, b);
-    return bin_finish(n_rec, g, b.count, b.rec_bin, b.rec_rank, b.big, d_tile_start, d_items, s);
+    return bin_finish(n_rec, g, b.count, b.rec_bin, b, d_tile_start, d_items, s);
 }
 
 extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatParams *p,
@@ -435,8 +625,7 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
     int grid = (n_rec + 255) / 256;
     if (grid > 152 * 8) grid = 152 * 8;
     bin_count_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.count, b.rec_bin, b.rec_rank);
-    if (b.rec_bin) return bin_finish(n_rec, g, b.count, b.rec_bin, b.rec_rank, b.big,
-                                     d_tile_start, d_items, s);
+    if (b.rec_bin) return bin_finish(n_rec, g, b.count, b.rec_bin, b, d_tile_start, d_items, s);
     bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(b.count, n_bins, d_tile_start, b.cursor);
     bin_scatter_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.cursor, d_items);
     rc = sc::launch_status("sc_bin_steps");

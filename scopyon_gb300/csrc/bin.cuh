@@ -17,7 +17,12 @@ int tile_geom(const ScSplatParams *p, TileGeom &g);
 struct BinLayout {
     int32_t *count, *cursor, *rec_bin, *rec_rank;
     int32_t *big;  // count of long bins, then their indices
+    // radix sort scratch (record sets of kRadixMinRecords or more), else NULL
+    int32_t *rx_vals, *rx_counts, *rx_total;
 };
+
+// From this many records on, bin lists are ordered by a radix sort.
+constexpr int kRadixMinRecords = 1 << 20;
 int bin_layout(const TileGeom &g, int n_rec, void *d_ws, size_t ws_bytes, BinLayout &b);
 
 // Bin of a record: the tile holding its first footprint pixel, plus n_tiles

@@ -169,6 +169,11 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
     const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
     const bool epi = isinf(k.penetration);
     double p[3] = {0.0, 0.0, 0.0}, b = 0.0;
+    // last depth offset and unit time seen by this lane's chain, with their
+    // photons and normalisation: a particle whose depth does not change
+    // (two-dimensional inputs) evaluates the TIRF exponential once
+    double rel_prev = nan(""), ut_prev = nan(""), amp_prev = 0.0, emit_prev = 0.0;
+    double norm_prev = 0.0;
     int cls = 0;
     if (warp == 0 && live) {
         p[0] = pos[3 * i];
@@ -214,8 +219,18 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                     double f[3];
                     format_point(c, p, f);
                     const double rel0 = f[0] - k.focal[0];
-                    n_emit = sc::emit_photons(
-                        k, __dmul_rn(k.amplitude0, exp(-fabs(rel0) / k.penetration)), unit_time[s]);
+                    const double ut = unit_time[s];
+                    if (rel0 != rel_prev) {  // NaN never compares equal: first step
+                        amp_prev = __dmul_rn(k.amplitude0, exp(-fabs(rel0) / k.penetration));
+                        rel_prev = rel0;
+                        ut_prev = nan("");
+                    }
+                    if (ut != ut_prev) {
+                        emit_prev = sc::emit_photons(k, amp_prev, ut);
+                        norm_prev = __dmul_rn(k.norm_coeff, emit_prev / (4.0 * M_PI));
+                        ut_prev = ut;
+                    }
+                    n_emit = emit_prev;
                 }
                 bool alive = true;
                 if (k.bleaching) {
@@ -227,9 +242,7 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                     b = nb;
                 }
                 // p_state = 0 gives norm_coeff * (0 / 4 pi) = 0: no record
-                s_norm[j * 32 + lane] =
-                    !alive ? 0.0
-                           : (epi ? s_norm1[j] : __dmul_rn(k.norm_coeff, n_emit / (4.0 * M_PI)));
+                s_norm[j * 32 + lane] = !alive ? 0.0 : (epi ? s_norm1[j] : norm_prev);
                 const double *sg = sigma + ((size_t)s * c.n_class + cls) * 3;
                 if (normals) {
                     const double *nv = normals + ((size_t)s * c.n + i) * c.ndim;

@@ -80,8 +80,13 @@ __device__ __forceinline__ float amplitude(const GaussConsts &c, float z) {
 // One splat record per emitter (binned by the tile of its first pixel):
 // i_start, n_i (bounds = pixels + 1), ax_hi = fx, ax_lo = i_start - ic, and
 // the same along y; w = I A(z).  Emitters whose window misses the image get
-// slot -1.
-__global__ void gauss_records_kernel(GaussConsts c, const float4 *emit, ScStepRec *recs) {
+// slot -1.  Each record is counted into its bin as it is written (count,
+// rec_bin, rec_rank: the binning workspace's counts, bins and ranks).  The
+// FP64 origin (x0, y0) of the footprint path is not written: nothing on this
+// path reads it.
+__global__ void gauss_records_kernel(GaussConsts c, const float4 *emit, ScStepRec *recs,
+                                     sc::TileGeom g, int32_t *count, int32_t *rec_bin,
+                                     int32_t *rec_rank) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= c.n_frames * c.n_emit) return;
     const float4 e = emit[r];
@@ -112,7 +117,12 @@ __global__ void gauss_records_kernel(GaussConsts c, const float4 *emit, ScStepRe
         rec.ay_hi = fy;
         rec.ay_lo = (float)(j0 - icy);
     }
-    recs[r] = rec;
+    int4 *dst = reinterpret_cast<int4 *>(recs + r);
+    const int4 *src = reinterpret_cast<const int4 *>(&rec);
+    dst[0] = src[0];
+    dst[1] = src[1];
+    dst[3] = src[3];
+    sc::bin_record(g, rec, r, count, rec_bin, rec_rank);
 }
 
 // Pixel integral of the unit Gaussian over pixel offset d (from the centre
@@ -695,6 +705,7 @@ extern "C" size_t sc_gauss_workspace_bytes(const ScGaussParams *p) {
 extern "C" int sc_gauss_forward(const ScGaussParams *p, const float *d_emit, const float *d_sigma,
                                 const float *d_bg, void *d_ws, size_t ws_bytes, float *d_mu,
                                 int32_t *d_status, void *stream) {
+    (void)d_status;  // no data check on this path writes a status word
     GaussConsts c;
     int rc = gauss_consts(p, c);
     if (rc) return rc;
@@ -709,10 +720,14 @@ extern "C" int sc_gauss_forward(const ScGaussParams *p, const float *d_emit, con
     if (rc) return rc;
     const int n_rec = c.n_frames * c.n_emit;
     if (n_rec > 0) {
+        sc::BinLayout b;
+        sc::bin_layout(g, n_rec, w.bin_ws, w.bin_bytes, b);
+        rc = sc_bin_reset(&sp, w.bin_ws, w.bin_bytes, stream);
+        if (rc) return rc;
         gauss_records_kernel<<<(n_rec + 255) / 256, 256, 0, s>>>(
-            c, reinterpret_cast<const float4 *>(d_emit), w.recs);
-        rc = sc_bin_steps(w.recs, n_rec, &sp, w.bin_ws, w.bin_bytes, w.tile_start, w.items,
-                          d_status, stream);
+            c, reinterpret_cast<const float4 *>(d_emit), w.recs, g, b.count, b.rec_bin,
+            b.rec_rank);
+        rc = sc_bin_finish(n_rec, &sp, w.bin_ws, w.bin_bytes, w.tile_start, w.items, stream);
         if (rc) return rc;
         if (tile_path(c)) {
             const int P = g.edge <= 24 ? 24 : 32;

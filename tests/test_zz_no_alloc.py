@@ -54,8 +54,8 @@ def numpy_bins(r, p):
     n_tiles = p.tiles_x * p.tiles_y * p.n_images
     ok = ((r["n_i"] >= 2) & (r["n_j"] >= 2) & (r["slot"] >= 0) & (img < p.n_images)
           & (r["i_start"] < p.nw) & (r["j_start"] < p.nh))
-    t = (img * p.tiles_x * p.tiles_y + (r["i_start"] // p.tile) * p.tiles_y
-         + r["j_start"] // p.tile)
+    i0, j0 = r["i_start"].astype(numpy.int64), r["j_start"].astype(numpy.int64)
+    t = img * p.tiles_x * p.tiles_y + (i0 // p.tile) * p.tiles_y + j0 // p.tile
     b = numpy.where(r["box"] != 0, t, t + n_tiles)
     b = numpy.where(ok, b, -1)
     counts = numpy.bincount(b[ok], minlength=2 * n_tiles)
@@ -107,6 +107,25 @@ def test_static_matches_workspace_entry_point(lib, shape):
         e_start, e_items = numpy_bins(r, p)
         numpy.testing.assert_array_equal(s_start, e_start)
         numpy.testing.assert_array_equal(s_items, e_items)
+
+
+@pytest.mark.parametrize("shape", [(4096, 2048, 1), (256, 256, 1), (1024, 512, 3)])
+def test_radix_path_matches_sort_path(lib, shape):
+    """From 2^20 records on, sc_bin_steps orders the lists with a radix sort:
+    the same start offsets and lists as the sort path and numpy, with 2 and 3
+    digit passes, dense bins (over 700 records each) and records in no bin."""
+    nw, nh, n_images = shape
+    rng = numpy.random.RandomState(5)
+    n = 1500000 + 77
+    rpi = -(-n // n_images) if n_images > 1 else 0
+    p = params(lib, nw, nh, n_images=n_images, rec_per_image=rpi)
+    r = random_records(rng, n, nw, nh)
+    w_start, w_items = run(lib, "workspace", r, p)
+    e_start, e_items = numpy_bins(r, p)
+    numpy.testing.assert_array_equal(w_start, e_start)
+    numpy.testing.assert_array_equal(w_items, e_items)
+    c_start, c_items = run(lib, "workspace", r, p, counts_only=True)
+    numpy.testing.assert_array_equal(c_items, w_items)
 
 
 def test_static_rejects_too_many_tiles(lib):

@@ -244,6 +244,8 @@ def gb300_arm(args, rank, world):
         splat_recs.append(int(pipe._cap["tile_start"][2 * pipe.tiles_x * pipe.tiles_y]))
     torch.cuda.synchronize()
     splat_ms = [a.elapsed_time(b) for a, b in pipe.kernel_events["splat"]]
+    stage_ms = {k: sum(a.elapsed_time(b) for a, b in pipe.kernel_events[k]) /
+                len(pipe.kernel_events[k]) for k in ("records", "camera")}
     pipe.kernel_events = None
     # keep the GPU busy with untimed graph frames so that nvidia-smi (100 ms
     # period) samples the clocks under this load for at least 1 s in all
@@ -310,7 +312,8 @@ def gb300_arm(args, rank, world):
                                        "capture of the profiling case, times records",
                      "algorithmic_bytes": alg, "records": n_rec,
                      "avg_launch_ms": splat_avg_ms,
-                     "timed_on": "%d eager frames after the timed graph replays" % n_timing},
+                     "timed_on": "%d eager frames after the timed graph replays" % n_timing,
+                     "stages": stage_rooflines(stage_ms, pipe, SUBSTEPS * N_EMIT, peak)},
     }
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline()
@@ -494,10 +497,34 @@ def config1(exposure=0.030):
     return cfg
 
 
-def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123):
+def stage_rooflines(stage_ms, pipe, n_rec, peak):
+    # n_rec: records written per frame (every emitter at every sub-step)
+    """HBM roofline of the two stages around the splat, from their CUDA-event
+    durations on the same eager frames.  Algorithmic bytes: the records stage
+    reads and writes each emitter's FP64 position (48 B), photon budget
+    (16 B) and class (4 B) and writes each record (64 B) with its bin and rank
+    (8 B); the camera reads each pixel's photons and read-noise sigma (8 B)
+    and writes the expectation (4 B) and the FP64 ADC count (8 B)."""
+    n_px = pipe.nw * pipe.nh
+    out = {}
+    for name, alg, bound in (
+            ("records", N_EMIT * 68 + n_rec * 72,
+             "FP64 position chains and footprint arithmetic (FP64 pipe), not HBM"),
+            ("camera", n_px * (8 + (4 if pipe.sigma is not None else 0) + 8),
+             "per-pixel Poisson and normal draws (FP32 and SFU pipes), not HBM")):
+        ms = stage_ms[name]
+        gbs = alg / (ms / 1e3) / 1e9
+        out[name] = {"avg_launch_ms": ms, "algorithmic_bytes": alg, "achieved": gbs,
+                     "unit": "GB/s", "frac": gbs / peak, "limited_by": bound}
+    return out
+
+
+def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=True):
     """field-frames/s of 256 fields (edges 128/256/512 px, emitters log-uniform
     in [10, 50000], D log-uniform in [0.001, 1] um^2/s) batched in one canvas,
-    next to the plain method's per-field frame loop."""
+    next to the plain method's per-field frame loop (loop=False: the batch
+    alone, for profiling; with --tile, a fixed tile shape instead of the
+    autotuner)."""
     import torch
     from scopyon_gb300.base import _psf_for
     from scopyon_gb300.batch import BatchedFields
@@ -510,7 +537,11 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123):
     cfg = config1()
     t0 = time.time()
     bf = BatchedFields(cfg, sizes, counts, D, frames, substeps, seed=seed, device=dev)
-    tune = bf.autotune(frames=1)
+    if args.tile:
+        bf.pipe.set_tiles(args.tile, args.warps, args.stages)
+        tune = {}
+    else:
+        tune = bf.autotune(frames=1)
     bf.step()  # capture
     for _ in range(args.warmup):
         bf.step()
@@ -527,6 +558,9 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123):
     setup_s = time.time() - t0
     del bf
     torch.cuda.empty_cache()
+    if not loop:
+        return {"value": n_fields / (batch_ms / 1e3), "unit": "field-frames/s",
+                "batched_ms_per_frame_of_all_fields": batch_ms, "setup_s": setup_s}
 
     # the plain method, one field at a time: a pipeline, trajectories and frame per field
     fields = []
@@ -686,6 +720,10 @@ def main():
     ap.add_argument("--warps", type=int, default=4, help="warps per splat tile with --tile")
     ap.add_argument("--stages", type=int, default=4,
                     help="box-table block copies in flight per splat warp with --tile")
+    ap.add_argument("--case", choices=["dgrad", "batched"], default=None,
+                    help="profiling: run one workload alone and print its result object "
+                         "(dgrad: dL/dD at 100k emitters x 100 sub-steps on 2048^2 px; "
+                         "batched: the 256-field canvas without the per-field loop)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: depth range +-0.1 um between reflecting walls and "
                          "D = 0.01 um^2/s for all emitters (102 PSF keys, 2.9 GB of tables), "
@@ -699,6 +737,16 @@ def main():
         ap.error("--warmup must be >= 3")
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.case:
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        if args.case == "dgrad":
+            res = diffusion_grad_case(dev, 100000, 2048, 100, args.steps, args.warmup, 9)
+        else:
+            res = batched_arm(args, dev, loop=False)
+        print(json.dumps(res), flush=True)
+        return
     if args.impl == "reference":
         res = reference_arm(args, rank, world)
         if res is not None:

@@ -307,12 +307,12 @@ int bin_sort(int n_bins, int32_t *tile_start, int32_t *items, int32_t *big, cuda
 // partitions by one digit of at most 9 bits and keeps the order of equal
 // digits, so the result is ordered by bin and then by record index: the
 // same lists as placement plus sort.  A pass is three kernels: per-block
-// digit counts (blocks of 4096 records), a scan over blocks per digit, and
+// digit counts (blocks of 2048 records), a scan over blocks per digit, and
 // the scatter, where each warp ranks its records among equal digits with
 // __match_any_sync in record order.
 
-constexpr int kRxThreads = 512, kRxWarps = kRxThreads / 32, kRxPerWarp = 256;
-constexpr int kRxBlock = kRxWarps * kRxPerWarp;  // 4096 records
+constexpr int kRxThreads = 512, kRxWarps = kRxThreads / 32, kRxPerWarp = 128;
+constexpr int kRxBlock = kRxWarps * kRxPerWarp;  // 2048 records
 constexpr int kRxMaxBits = 9, kRxMaxBuckets = 1 << kRxMaxBits;
 constexpr int kRxScanThreads = 1024;
 
@@ -387,7 +387,7 @@ radix_scan_kernel(int32_t *__restrict__ counts, int nb, int32_t *__restrict__ to
 // Stable scatter of block b: position = start of the digit (scan of the
 // totals) + records of the digit in earlier blocks + earlier warps of this
 // block + rank within the warp (32 records at a time, in record order).
-__global__ void __launch_bounds__(kRxThreads)
+__global__ void __launch_bounds__(kRxThreads, 3)
 radix_downsweep_kernel(const int32_t *__restrict__ keys_in, const int32_t *__restrict__ vals_in,
                        int n, int sentinel, int shift, int bits, int nb,
                        const int32_t *__restrict__ counts, const int32_t *__restrict__ total,
@@ -409,20 +409,30 @@ radix_downsweep_kernel(const int32_t *__restrict__ keys_in, const int32_t *__res
     const int q_warp = blockIdx.x * kRxBlock + warp * kRxPerWarp;
     constexpr int R = kRxPerWarp / 32;
     int key[R], loc[R], val[R];
+    unsigned peers[R];
+    // loads and digit matches of all rounds first (independent), then the
+    // per-warp digit counts round by round
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const int q = q_warp + r * 32 + lane;
         const bool ok = q < n;
-        const int k = ok ? rx_key(keys_in, q, sentinel) : 0;
-        const int d = ok ? (k >> shift) & (buckets - 1) : -1;
+        key[r] = ok ? rx_key(keys_in, q, sentinel) : 0;
         val[r] = ok ? (vals_in ? vals_in[q] : q) : 0;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const int rank = __popc(peers & ((1u << lane) - 1u));
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const bool ok = q_warp + r * 32 + lane < n;
+        peers[r] = __match_any_sync(0xffffffffu, ok ? (key[r] >> shift) & (buckets - 1) : -1);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const bool ok = q_warp + r * 32 + lane < n;
+        const int d = (key[r] >> shift) & (buckets - 1);
+        const int rank = __popc(peers[r] & ((1u << lane) - 1u));
         const int pre = ok ? whist[warp][d] : 0;
         __syncwarp();
-        if (ok && rank == 0) whist[warp][d] = pre + __popc(peers);
+        if (ok && rank == 0) whist[warp][d] = pre + __popc(peers[r]);
         __syncwarp();
-        key[r] = k;
         loc[r] = pre + rank;
     }
     __syncthreads();
@@ -464,6 +474,11 @@ int radix_bins(int n, int n_bins, int32_t *rec_bin, int32_t *keys_tmp, int32_t *
         int32_t *out_keys = p == passes - 1 ? nullptr : (p % 2 ? rec_bin : keys_tmp);
         const int32_t *in_vals = p == 0 ? nullptr : ((passes - p) % 2 ? vals_tmp : items);
         int32_t *out_vals = (passes - 1 - p) % 2 ? vals_tmp : items;
+        if (p == 0) {
+            // shared memory over L1, so that more CTAs of the scatter fit on an SM
+            cudaFuncSetAttribute(radix_downsweep_kernel,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        }
         radix_upsweep_kernel<<<nb, kRxThreads, 0, s>>>(in_keys, n, n_bins, shift, pb, nb, counts);
         radix_scan_kernel<<<1 << pb, kRxScanThreads, 0, s>>>(counts, nb, total);
         radix_downsweep_kernel<<<nb, kRxThreads, 0, s>>>(in_keys, in_vals, n, n_bins, shift, pb,
@@ -624,7 +639,8 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
     if (rc) return rc;
     int grid = (n_rec + 255) / 256;
     if (grid > 152 * 8) grid = 152 * 8;
-    bin_count_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.count, b.rec_bin, b.rec_rank);
+    bin_count_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.count, b.rec_bin,
+                                          sc::rank_array(b));
     if (b.rec_bin) return bin_finish(n_rec, g, b.count, b.rec_bin, b, d_tile_start, d_items, s);
     bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(b.count, n_bins, d_tile_start, b.cursor);
     bin_scatter_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.cursor, d_items);

@@ -35,12 +35,22 @@ __device__ __forceinline__ int record_tile(const ScStepRec &rec, int r, const Ti
     return rec.box ? t : t + g.n_tiles;
 }
 
-// Counts record r into its bin and keeps its bin and rank (-1: no bin).
+// Counts record r into its bin and keeps its bin and, when rec_rank is given,
+// its rank (-1: no bin).  The radix path needs no ranks: its count is a
+// reduction with no value returned.
 __device__ __forceinline__ void bin_record(const TileGeom &g, const ScStepRec &rec, int r,
                                            int32_t *count, int32_t *rec_bin, int32_t *rec_rank) {
     const int t = record_tile(rec, r, g);
     rec_bin[r] = t;
-    rec_rank[r] = t >= 0 ? atomicAdd(&count[t], 1) : -1;
+    if (rec_rank)
+        rec_rank[r] = t >= 0 ? atomicAdd(&count[t], 1) : -1;
+    else if (t >= 0)
+        atomicAdd(&count[t], 1);
+}
+
+// The rank array bin_record should fill: none on the radix path.
+__host__ __device__ __forceinline__ int32_t *rank_array(const BinLayout &b) {
+    return b.rx_vals ? nullptr : b.rec_rank;
 }
 
 }  // namespace sc

@@ -276,7 +276,7 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                     sc::make_record(k, f[0] - k.focal[0], f[1] - k.focal[1], f[2] - k.focal[2],
                                     norm, key_slot, status, i, s, rec);
                 recs[(size_t)s * c.n + i] = rec;
-                if (bl.count) sc::bin_record(g, rec, s * c.n + i, bl.count, bl.rec_bin, bl.rec_rank);
+                if (bl.count) sc::bin_record(g, rec, s * c.n + i, bl.count, bl.rec_bin, sc::rank_array(bl));
             }
         }
         __syncthreads();

@@ -726,7 +726,7 @@ extern "C" int sc_gauss_forward(const ScGaussParams *p, const float *d_emit, con
         if (rc) return rc;
         gauss_records_kernel<<<(n_rec + 255) / 256, 256, 0, s>>>(
             c, reinterpret_cast<const float4 *>(d_emit), w.recs, g, b.count, b.rec_bin,
-            b.rec_rank);
+            sc::rank_array(b));
         rc = sc_bin_finish(n_rec, &sp, w.bin_ws, w.bin_bytes, w.tile_start, w.items, stream);
         if (rc) return rc;
         if (tile_path(c)) {

@@ -7,6 +7,7 @@ bookkeeping (frame windows, molecule ids, random draws taken from the caller's
 Device buffers are torch CUDA tensors, reused across frames.
 """
 
+import contextlib
 import math
 import warnings
 
@@ -503,16 +504,24 @@ class FramePipeline:
         L = _lib.load()
         sws_bytes = L.sc_splat_workspace_bytes(sp)
         sws = self._buf("splat_ws", (sws_bytes + 3) // 4, torch.float32)
+        with self.timed("splat", stream):
+            call("sc_splat", ptr(recs), ptr(tile_start), ptr(items), ptr(self.psf.tables),
+                 ptr(self.psf.box), sp, ptr(sws), sws_bytes, ptr(image), ptr(self.status), s)
+
+    @contextlib.contextmanager
+    def timed(self, name, stream=None):
+        """CUDA events around the enclosed launches when kernel_events is a
+        dict (appended under `name`); nothing otherwise."""
         ev = self.kernel_events
-        if ev is not None:
-            e0 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-        call("sc_splat", ptr(recs), ptr(tile_start), ptr(items), ptr(self.psf.tables),
-             ptr(self.psf.box), sp, ptr(sws), sws_bytes, ptr(image), ptr(self.status), s)
-        if ev is not None:
-            e1 = torch.cuda.Event(enable_timing=True)
-            e1.record(stream)
-            ev.setdefault("splat", []).append((e0, e1))
+        if ev is None:
+            yield
+            return
+        st = stream if stream is not None else torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        yield
+        e1.record(st)
+        ev.setdefault(name, []).append((e0, e1))
 
     def camera(self, photons, expect, adc64, adc32=None, seed=0, counter=0, draws=None,
                stream=None, d_frame=None):
@@ -554,10 +563,11 @@ class FramePipeline:
         if self.camera_kind == _lib.CAM_CMOS_TABLE and self.table_value is None:
             self.load_cmos_table(self.cfg.cmos_table)
             cp.table_n = self.table_value.numel()
-        call("sc_camera", cp, ptr(photons), ptr(self.offset), ptr(self.gain), ptr(self.offset_f),
-             ptr(self.inv_gain_f), ptr(self.sigma), ptr(self.table_value), ptr(self.table_cdf),
-             ptr(inj_noise), ptr(inj_signal), ptr(inj_uniform), ptr(expect), ptr(adc64),
-             ptr(adc32), ptr(self.status), s)
+        with self.timed("camera", stream):
+            call("sc_camera", cp, ptr(photons), ptr(self.offset), ptr(self.gain),
+                 ptr(self.offset_f), ptr(self.inv_gain_f), ptr(self.sigma), ptr(self.table_value),
+                 ptr(self.table_cdf), ptr(inj_noise), ptr(inj_signal), ptr(inj_uniform),
+                 ptr(expect), ptr(adc64), ptr(adc32), ptr(self.status), s)
 
     def check_status(self):
         st = self.status.cpu().numpy()
@@ -698,9 +708,10 @@ class FrameGraph:
         sp = pipe.step_params(self.n_sub, self.n, False)
         bsp, ws, ws_bytes, _, _ = pipe.bin_buffers(n_rec)
         call("sc_bin_reset", bsp, ptr(ws), ws_bytes, s)
-        call("sc_native_records", dp, sp, ptr(traj._pos), ptr(traj._g_class), ptr(traj._g_sigma),
-             None, ptr(self.ut), ptr(pipe.budget), ptr(pipe.psf.key_slot), ptr(recs), bsp,
-             ptr(ws), ws_bytes, ptr(pipe.status), s)
+        with pipe.timed("records"):
+            call("sc_native_records", dp, sp, ptr(traj._pos), ptr(traj._g_class),
+                 ptr(traj._g_sigma), None, ptr(self.ut), ptr(pipe.budget), ptr(pipe.psf.key_slot),
+                 ptr(recs), bsp, ptr(ws), ws_bytes, ptr(pipe.status), s)
         pipe.splat_records(recs, n_rec, pipe.image, counted=True)
         pipe.camera(pipe.image, pipe.expect, pipe.adc, seed=self.seed, d_frame=self.frame)
         call("sc_counter_add", ptr(self.frame), 1, s)
@@ -729,6 +740,12 @@ class FrameGraph:
 
     @property
     def launches_per_frame(self):
-        # native records (counting into bins), bin scan/place/sort, splat
+        # native records (counting into bins), bin scan, then place + sort or,
+        # from 2^20 records on, three kernels per radix digit pass; splat
         # box/sat/merge, camera, counter (plus one memset)
-        return 9
+        n_rec = self.n_sub * self.n
+        if n_rec < (1 << 20):
+            return 9
+        n_bins = 2 * self.pipe.tiles_x * self.pipe.tiles_y
+        bits = max(1, n_bins.bit_length())  # keys 0 .. n_bins
+        return 7 + 3 * (-(-bits // 9))

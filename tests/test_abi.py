@@ -64,7 +64,7 @@ def test_host_side_validation_needs_no_gpu():
     # from 2^20 records on: + the radix sort's values, block digit counts and totals
     n = 1 << 20
     assert L.sc_bin_workspace_bytes(n, 16) == (16 * 16 + 8 * n + 4 * (2 * 16 + 1) + 16 +
-                                               4 * (n + 512 * (n // 4096) + 512))
+                                               4 * (n + 512 * (n // 2048) + 512))
     p.tile, p.tiles_x, p.tiles_y = 16, 4, 4
     assert L.sc_splat_workspace_bytes(ctypes.byref(p)) == 16 * 30 * 30 * 4
 

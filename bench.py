@@ -191,7 +191,10 @@ def gb300_arm(args, rank, world):
 
     # trajectories on the device: two populations (D = 0.01 and 1 um^2/s), Philox normals
     n_timing = 4
-    n_frames = args.warmup + args.steps + n_timing + 8000 + 5 * len(TILE_CANDIDATES)
+    # several frames per graph replay, the records of the next frame running
+    # beside the splat of this one: 4 when the timed frames divide by 4
+    fps = next(k for k in (4, 2, 1) if args.steps % k == 0)
+    n_frames = 4 * (args.warmup + args.steps + n_timing) + 8000 + 20 * len(TILE_CANDIDATES)
     dt = EXPOSURE / SUBSTEPS
     t = numpy.arange(n_frames * SUBSTEPS + 1) * dt
     # reflecting walls at the field's edges and at z = +-Z_HALF keep the
@@ -205,14 +208,15 @@ def gb300_arm(args, rank, world):
     pipe.ensure_slots(N_EMIT)
     beta = eng.half_life / math.log(2.0)
     pipe.budget[:N_EMIT].copy_(torch.from_numpy(rng.exponential(beta, N_EMIT) * eng.n_emit0))
-    fg = FrameGraph(pipe, traj, SUBSTEPS, dt, seed=1234 + rank)
+    fg = FrameGraph(pipe, traj, SUBSTEPS, dt, seed=1234 + rank, frames_per_step=fps)
     if args.tile:  # a fixed tile shape (reproducible profiling), else the autotuner
         pipe.set_tiles(args.tile, args.warps, args.stages)
         tune = {}
     else:
-        tune = tune_tiles(fg, frames=3)  # 5 frames per choice
-    fg.capture()
-    for _ in range(args.warmup - 1):
+        # every choice runs the same frames; the tuner restores the state after
+        tune = tune_tiles(fg, frames=3)  # 5 steps per choice
+    fg.capture()  # one eager step of fps frames, then the capture
+    for _ in range(-(-args.warmup // fps) - 1):  # at least W warm-up frames in all
         fg.step()
     torch.cuda.synchronize()
     pipe.check_status()
@@ -225,7 +229,7 @@ def gb300_arm(args, rank, world):
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     start.record()
-    for _ in range(args.steps):
+    for _ in range(args.steps // fps):
         fg.step()
     end.record()
     torch.cuda.synchronize()
@@ -252,7 +256,7 @@ def gb300_arm(args, rank, world):
     fg.use_graph = True
     pad_ms = 1000.0 - elapsed_ms
     t_pad = time.perf_counter()
-    while (time.perf_counter() - t_pad) * 1e3 < pad_ms and fg.frames_done + 50 < n_frames:
+    while (time.perf_counter() - t_pad) * 1e3 < pad_ms and fg.frames_done + 50 * fps < n_frames:
         for _ in range(50):
             fg.step()
         torch.cuda.synchronize()
@@ -290,8 +294,11 @@ def gb300_arm(args, rank, world):
                    "stages": pipe.stages,
                    "tile_autotune_ms_per_frame": {"%dx%d/%dw/%ds" % (t, t, w, st): round(ms, 4)
                                                   for (t, w, st), ms in tune.items()},
-                   "step": "one frame: Brownian sub-steps, physics, binning, splat, camera "
-                           "(one CUDA graph replay)",
+                   "step": "one frame: Brownian sub-steps, physics, binning, splat, camera; "
+                           "%d frame(s) per CUDA graph replay%s" % (
+                               fps, ", each frame's records kernel (side stream) overlapping "
+                                    "the previous frame's binning, splat and camera"
+                               if fps > 1 else ""),
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (PSF tables %.1f GB)" % tables_gb,
                    "boundary": "reflecting",
@@ -536,7 +543,9 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=
     D = numpy.exp(rng.uniform(math.log(1e-3), math.log(1.0), n_fields)) * 1e-12
     cfg = config1()
     t0 = time.time()
-    bf = BatchedFields(cfg, sizes, counts, D, frames, substeps, seed=seed, device=dev)
+    per_step = 2  # two canvas frames per replay, the second frame's records beside the first splat
+    bf = BatchedFields(cfg, sizes, counts, D, frames, substeps, seed=seed, device=dev,
+                       frames_per_step=per_step)
     if args.tile:
         bf.pipe.set_tiles(args.tile, args.warps, args.stages)
         tune = {}
@@ -545,7 +554,7 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=
     bf.step()  # capture
     for _ in range(args.warmup):
         bf.step()
-    steps = min(args.steps, frames - 4 * len(tune) - 2 - args.warmup)
+    steps = max(1, min(args.steps, frames - 2 - args.warmup) // per_step)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     a.record()
@@ -554,7 +563,7 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=
     b.record()
     torch.cuda.synchronize()
     bf.pipe.check_status()
-    batch_ms = a.elapsed_time(b) / steps
+    batch_ms = a.elapsed_time(b) / (steps * per_step)
     setup_s = time.time() - t0
     del bf
     torch.cuda.empty_cache()

@@ -63,10 +63,13 @@ class BatchedFields:
     config: a ``Configuration`` for every field (image_size is replaced per
     field); sizes: field edges in pixels; counts: emitters per field; D:
     diffusion coefficient per field (m^2/s); frames: frames to simulate;
-    substeps: sub-steps per exposure.
+    substeps: sub-steps per exposure; frames_per_step: frames per ``step``
+    (more than one pipelines them: each frame's records beside the previous
+    frame's splat, see ``FrameGraph``).
     """
 
-    def __init__(self, config, sizes, counts, D, frames, substeps, seed=0, device=None):
+    def __init__(self, config, sizes, counts, D, frames, substeps, seed=0, device=None,
+                 frames_per_step=1):
         self.device = torch.device(device or "cuda")
         self.sizes = [int(s) for s in sizes]
         self.counts = [int(c) for c in counts]
@@ -110,7 +113,7 @@ class BatchedFields:
             self.pipe.budget[:self.n_emit].copy_(torch.from_numpy(
                 rng.exponential(beta, self.n_emit) * self.eng.n_emit0))
         self.graph = FrameGraph(self.pipe, self.traj, self.substeps, self.dt,
-                                seed=int(rng.randint(0, 2 ** 31)))
+                                seed=int(rng.randint(0, 2 ** 31)), frames_per_step=frames_per_step)
         self.tuning = None
 
     # ------------------------------------------------------------------
@@ -125,7 +128,8 @@ class BatchedFields:
         return times
 
     def step(self):
-        """One frame of every field (one graph replay once captured)."""
+        """frames_per_step frames of every field (one graph replay once captured);
+        field_image then shows the last of them."""
         self.graph.step()
 
     def field_image(self, k, what="adc"):

@@ -478,24 +478,26 @@ class FramePipeline:
         p.px, p.res = self.cfg.px, PSF_RES
         return p
 
-    def bin_buffers(self, n_rec, n_images=1, rec_per_image=0):
-        """Splat parameters and the binning workspace, items and bin offsets."""
+    def bin_buffers(self, n_rec, n_images=1, rec_per_image=0, tag=""):
+        """Splat parameters and the binning workspace, items and bin offsets
+        (``tag`` names a second set, for a frame binned while another splats)."""
         sp = self.splat_params(n_images, rec_per_image)
         n_tiles = self.tiles_x * self.tiles_y * n_images
         ws_bytes = _lib.load().sc_bin_workspace_bytes(n_rec, n_tiles)
-        ws = self._buf("ws", (ws_bytes + 3) // 4, torch.int32)
-        items = self._buf("items", n_rec, torch.int32)
-        tile_start = self._buf("tile_start", 2 * n_tiles + 1, torch.int32)
+        ws = self._buf("ws" + tag, (ws_bytes + 3) // 4, torch.int32)
+        items = self._buf("items" + tag, n_rec, torch.int32)
+        tile_start = self._buf("tile_start" + tag, 2 * n_tiles + 1, torch.int32)
         return sp, ws, ws_bytes, items, tile_start
 
     def splat_records(self, recs, n_rec, image, n_images=1, rec_per_image=0, stream=None,
-                      counted=False):
+                      counted=False, tag=""):
         """Bin records by tile and splat them into ``image`` (n_images x W x H, float32).
 
         counted: the records' producer already counted them into the binning
         workspace (sc_native_records), so only sc_bin_finish runs here."""
         s = stream_ptr(stream)
-        sp, ws, ws_bytes, items, tile_start = self.bin_buffers(n_rec, n_images, rec_per_image)
+        sp, ws, ws_bytes, items, tile_start = self.bin_buffers(n_rec, n_images, rec_per_image,
+                                                               tag)
         if counted:
             call("sc_bin_finish", n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items), s)
         else:
@@ -644,12 +646,23 @@ def tune_tiles(graph, candidates=TILE_CANDIDATES, frames=3):
     ``graph`` (a FrameGraph) and time
     ``frames`` replays of the whole frame (binning, splat and merge all depend
     on the tile); keep the fastest on its pipeline and return
-    {(tile, warps, stages): ms per frame}.  The frames run are frames of the
-    simulation (the trajectories advance)."""
+    {(tile, warps, stages): ms per frame}.  Every choice runs the same frames
+    from the same state (positions, photon budgets, frame counter), and that
+    state is restored at the end: the simulation does not advance."""
     pipe = graph.pipe
+    traj = graph.traj
+    state = (traj._pos.clone(), pipe.budget.clone(), graph.frame.clone(), graph.frames_done)
+
+    def restore():
+        traj._pos.copy_(state[0])
+        pipe.budget.copy_(state[1])
+        graph.frame.copy_(state[2])
+        graph.frames_done = state[3]
+
     times = {}
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for cand in candidates:
+        restore()
         try:
             pipe.set_tiles(*cand)
             graph.graph, graph.use_graph = None, True
@@ -661,10 +674,12 @@ def tune_tiles(graph, candidates=TILE_CANDIDATES, frames=3):
                 graph.step()
             b.record()
             torch.cuda.synchronize()
-            times[tuple(cand)] = a.elapsed_time(b) / frames
+            times[tuple(cand)] = a.elapsed_time(b) / (frames * graph.frames_per_step)
         except (ValueError, _lib.ScopyonGPUError):
             continue
     graph.graph = None
+    torch.cuda.synchronize()
+    restore()
     if not times:
         raise RuntimeError("no tile configuration ran")
     pipe.set_tiles(*min(times, key=times.get))
@@ -680,10 +695,22 @@ class FrameGraph:
     counters, lives in device memory and is advanced by the graph itself.
     Launch cost per frame is one graph launch.  Outputs (``pipe.expect``,
     ``pipe.adc``) are overwritten by each frame.
+
+    frames_per_step=k > 1 runs k consecutive frames per step (per graph
+    replay) as a pipeline: the records kernels (which need only the positions
+    and budgets the previous frame left) run in frame order on a high-priority
+    side stream, each into one of two record and bin buffer sets, while the
+    main stream bins, splats and images the frame before.  Frame i + 2's
+    records wait for frame i's image to free its buffer set.  The frames and
+    their results are those of k single steps; only the last frame's outputs
+    remain after the step.
     """
 
     def __init__(self, pipe, traj, n_sub, unit_time, first_frame=0, transform=None, seed=0,
-                 use_graph=True):
+                 use_graph=True, frames_per_step=1):
+        if int(frames_per_step) < 1:
+            raise ValueError("frames_per_step must be at least 1")
+        self.frames_per_step = int(frames_per_step)
         self.pipe, self.traj, self.n_sub = pipe, traj, int(n_sub)
         self.n = traj.n_particles
         dev = pipe.device
@@ -698,28 +725,70 @@ class FrameGraph:
         self.graph = None
         self.use_graph = use_graph
         self.frames_done = 0
+        # the second frame's records: a side stream that the scheduler serves first
+        self._side = torch.cuda.Stream(device=dev, priority=-1) if frames_per_step > 1 else None
 
-    def _launch(self):
+    def _records(self, tag, first_step):
+        """Records of one frame (sub-steps first_step .. + n_sub of the frame
+        counter's frame), counted into the bin buffers named by ``tag``."""
         pipe, traj, s = self.pipe, self.traj, stream_ptr()
         n_rec = self.n_sub * self.n
-        recs = pipe._buf("recs", max(n_rec, 1) * (_lib.STEP_REC_BYTES // 4), torch.int32)
-        dp = traj.params(0, self.n_sub, **(self.transform or {}))
+        recs = pipe._buf("recs" + tag, max(n_rec, 1) * (_lib.STEP_REC_BYTES // 4), torch.int32)
+        dp = traj.params(first_step, self.n_sub, **(self.transform or {}))
         dp.d_frame = self.frame.data_ptr()
         sp = pipe.step_params(self.n_sub, self.n, False)
-        bsp, ws, ws_bytes, _, _ = pipe.bin_buffers(n_rec)
+        bsp, ws, ws_bytes, _, _ = pipe.bin_buffers(n_rec, tag=tag)
         call("sc_bin_reset", bsp, ptr(ws), ws_bytes, s)
         with pipe.timed("records"):
             call("sc_native_records", dp, sp, ptr(traj._pos), ptr(traj._g_class),
                  ptr(traj._g_sigma), None, ptr(self.ut), ptr(pipe.budget), ptr(pipe.psf.key_slot),
                  ptr(recs), bsp, ptr(ws), ws_bytes, ptr(pipe.status), s)
-        pipe.splat_records(recs, n_rec, pipe.image, counted=True)
-        pipe.camera(pipe.image, pipe.expect, pipe.adc, seed=self.seed, d_frame=self.frame)
-        call("sc_counter_add", ptr(self.frame), 1, s)
+        return recs
+
+    def _image(self, recs, tag, frame_offset):
+        """Binning, splat and camera of one frame's records."""
+        pipe = self.pipe
+        pipe.splat_records(recs, self.n_sub * self.n, pipe.image, counted=True, tag=tag)
+        pipe.camera(pipe.image, pipe.expect, pipe.adc, seed=self.seed, counter=frame_offset,
+                    d_frame=self.frame)
+
+    def _launch(self):
+        s = stream_ptr()
+        if self.frames_per_step == 1:
+            self._image(self._records("", 0), "", 0)
+            call("sc_counter_add", ptr(self.frame), 1, s)
+            return
+        main, side, k = torch.cuda.current_stream(), self._side, self.frames_per_step
+        tags = ("", "_b")
+        recs, ready, imaged = [None] * k, [None] * k, [None] * k
+
+        def records(i):
+            if i >= 2:
+                side.wait_event(imaged[i - 2])  # frame i - 2 is done with this buffer set
+            with torch.cuda.stream(side):
+                recs[i] = self._records(tags[i % 2], i * self.n_sub)
+            ready[i] = torch.cuda.Event()
+            ready[i].record(side)
+
+        fork = torch.cuda.Event()
+        fork.record(main)
+        side.wait_event(fork)
+        records(0)
+        if k > 1:
+            records(1)
+        for i in range(k):
+            main.wait_event(ready[i])
+            self._image(recs[i], tags[i % 2], i)
+            imaged[i] = torch.cuda.Event()
+            imaged[i].record(main)
+            if i + 2 < k:
+                records(i + 2)
+        call("sc_counter_add", ptr(self.frame), k, s)
 
     def capture(self):
         """Run one frame eagerly (allocates every buffer), then capture the next."""
         self._launch()
-        self.frames_done += 1
+        self.frames_done += self.frames_per_step
         if not self.use_graph:
             return
         torch.cuda.synchronize()
@@ -736,7 +805,7 @@ class FrameGraph:
             self.graph.replay()
         else:
             self._launch()
-        self.frames_done += 1
+        self.frames_done += self.frames_per_step
 
     @property
     def launches_per_frame(self):

@@ -123,3 +123,22 @@ def test_autotune_and_graph_replay(sg):
     bf.pipe.check_status()
     img = bf.field_image(3)
     assert img.shape == (sizes[3], sizes[3]) and torch.isfinite(img).all()
+
+
+def test_pipelined_steps_match_single_frames(sg):
+    """Two canvas frames per step (the second frame's records beside the first
+    frame's splat) leave the same frame and trajectories as single steps."""
+    from scopyon_gb300.batch import BatchedFields
+    sizes, counts, D = [64, 48, 96], [50, 300, 20], [1e-13, 1e-12, 5e-14]
+    out = []
+    for per_step in (1, 2):
+        bf = BatchedFields(config1(sg), sizes, counts, D, frames=8, substeps=4, seed=9,
+                           frames_per_step=per_step)
+        for _ in range(4 // per_step):
+            bf.step()
+        torch.cuda.synchronize()
+        bf.pipe.check_status()
+        out.append(([bf.field_image(k).clone() for k in range(3)], bf.traj._pos.clone()))
+    for a, b in zip(out[0][0], out[1][0]):
+        assert torch.equal(a, b)
+    assert torch.equal(out[0][1], out[1][1])

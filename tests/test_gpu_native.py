@@ -192,7 +192,7 @@ def test_frame_graph_replay_matches_eager(sg):
         "effects": {"photo_bleaching": {"switch": True, "half_life": 0.01}},
         "gpu": {"cmos_noise": "scmos"}}})
     outs = []
-    for use_graph in (False, True):
+    for use_graph, per_step in ((False, 1), (True, 1), (False, 2), (True, 2), (True, 3)):
         rng = numpy.random.RandomState(6)
         eng = EngineConfig(cfg["default"], rng=rng)
         pipe = FramePipeline(eng, "cuda", psf=_psf_for(eng, torch.device("cuda")))
@@ -203,15 +203,23 @@ def test_frame_graph_replay_matches_eager(sg):
         pipe.psf.ensure(list(range(0, 700)))
         pipe.ensure_slots(300)
         pipe.budget[:300].copy_(torch.from_numpy(rng.exponential(0.02, 300) * eng.n_emit0))
-        fg = FrameGraph(pipe, traj, 4, 1e-3, seed=77, use_graph=use_graph)
+        fg = FrameGraph(pipe, traj, 4, 1e-3, seed=77, use_graph=use_graph,
+                        frames_per_step=per_step)
         frames = []
-        for _ in range(5):
+        for _ in range(6 // per_step):
             fg.step()
+            # a two-frame step leaves the second frame's outputs
             frames.append(pipe.adc.cpu().numpy().copy())
         pipe.check_status()
-        outs.append(numpy.array(frames))
-    numpy.testing.assert_array_equal(outs[0], outs[1])
-    assert outs[0].std(axis=0).max() > 0  # frames differ from one another
+        pos = traj._pos.cpu().numpy().copy()
+        outs.append((numpy.array(frames), pos))
+    numpy.testing.assert_array_equal(outs[0][0], outs[1][0])
+    assert outs[0][0].std(axis=0).max() > 0  # frames differ from one another
+    # several frames per step (each frame's records overlapping the previous
+    # frame's splat) give the same frames and trajectories
+    for k, per_step in ((2, 2), (3, 2), (4, 3)):
+        numpy.testing.assert_array_equal(outs[k][0], outs[0][0][per_step - 1::per_step])
+        numpy.testing.assert_array_equal(outs[k][1], outs[0][1])
 
 
 def test_fused_native_physics_matches_separate_pass(sg):

@@ -490,15 +490,19 @@ class FramePipeline:
         return sp, ws, ws_bytes, items, tile_start
 
     def splat_records(self, recs, n_rec, image, n_images=1, rec_per_image=0, stream=None,
-                      counted=False, tag=""):
+                      counted=False, tag="", binned=False, bufs=None):
         """Bin records by tile and splat them into ``image`` (n_images x W x H, float32).
 
         counted: the records' producer already counted them into the binning
-        workspace (sc_native_records), so only sc_bin_finish runs here."""
+        workspace (sc_native_records), so only sc_bin_finish runs here;
+        binned: the bins are complete too (``finish_bins``), only the splat runs.
+        bufs: the ``bin_buffers`` tuple when the caller has it."""
         s = stream_ptr(stream)
-        sp, ws, ws_bytes, items, tile_start = self.bin_buffers(n_rec, n_images, rec_per_image,
-                                                               tag)
-        if counted:
+        sp, ws, ws_bytes, items, tile_start = bufs or self.bin_buffers(n_rec, n_images,
+                                                                       rec_per_image, tag)
+        if binned:
+            pass
+        elif counted:
             call("sc_bin_finish", n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items), s)
         else:
             call("sc_bin_steps", ptr(recs), n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start),
@@ -509,6 +513,13 @@ class FramePipeline:
         with self.timed("splat", stream):
             call("sc_splat", ptr(recs), ptr(tile_start), ptr(items), ptr(self.psf.tables),
                  ptr(self.psf.box), sp, ptr(sws), sws_bytes, ptr(image), ptr(self.status), s)
+
+    def finish_bins(self, n_rec, tag="", stream=None, bufs=None):
+        """Scan, placement and order of records already counted into the bin
+        buffers named by ``tag`` (sc_bin_finish)."""
+        sp, ws, ws_bytes, items, tile_start = bufs or self.bin_buffers(n_rec, tag=tag)
+        call("sc_bin_finish", n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items),
+             stream_ptr(stream))
 
     @contextlib.contextmanager
     def timed(self, name, stream=None):
@@ -698,9 +709,9 @@ class FrameGraph:
 
     frames_per_step=k > 1 runs k consecutive frames per step (per graph
     replay) as a pipeline: the records kernels (which need only the positions
-    and budgets the previous frame left) run in frame order on a high-priority
-    side stream, each into one of two record and bin buffer sets, while the
-    main stream bins, splats and images the frame before.  Frame i + 2's
+    and budgets the previous frame left) and the binning run in frame order on
+    a high-priority side stream, each into one of two record and bin buffer
+    sets, while the main stream splats and images the frame before.  Frame i + 2's
     records wait for frame i's image to free its buffer set.  The frames and
     their results are those of k single steps; only the last frame's outputs
     remain after the step.
@@ -737,18 +748,22 @@ class FrameGraph:
         dp = traj.params(first_step, self.n_sub, **(self.transform or {}))
         dp.d_frame = self.frame.data_ptr()
         sp = pipe.step_params(self.n_sub, self.n, False)
-        bsp, ws, ws_bytes, _, _ = pipe.bin_buffers(n_rec, tag=tag)
+        bufs = pipe.bin_buffers(n_rec, tag=tag)
+        bsp, ws, ws_bytes, _, _ = bufs
         call("sc_bin_reset", bsp, ptr(ws), ws_bytes, s)
         with pipe.timed("records"):
             call("sc_native_records", dp, sp, ptr(traj._pos), ptr(traj._g_class),
                  ptr(traj._g_sigma), None, ptr(self.ut), ptr(pipe.budget), ptr(pipe.psf.key_slot),
                  ptr(recs), bsp, ptr(ws), ws_bytes, ptr(pipe.status), s)
-        return recs
+        pipe.finish_bins(n_rec, tag, bufs=bufs)
+        return recs, bufs
 
     def _image(self, recs, tag, frame_offset):
-        """Binning, splat and camera of one frame's records."""
+        """Splat and camera of one frame's binned records."""
         pipe = self.pipe
-        pipe.splat_records(recs, self.n_sub * self.n, pipe.image, counted=True, tag=tag)
+        recs, bufs = recs
+        pipe.splat_records(recs, self.n_sub * self.n, pipe.image, tag=tag, binned=True,
+                           bufs=bufs)
         pipe.camera(pipe.image, pipe.expect, pipe.adc, seed=self.seed, counter=frame_offset,
                     d_frame=self.frame)
 

@@ -126,6 +126,13 @@ typedef struct {
     double scale, origin[3], unit_x[3], unit_y[3], unit_z[3];  /* preprocessing transform  */
     const double *d_class_box;        /* optional [n_class][6] (lower xyz, upper xyz): a box */
                                       /* per diffusion class in place of lower / upper       */
+    const double *d_trans;            /* optional [n_sub][n_class][n_class] cumulative       */
+                                      /* transition probabilities per sub-step: after its    */
+                                      /* move, a particle in class a goes to the first b with*/
+                                      /* d_trans[s][a][b] >= u (sampling2.py:52-68); the     */
+                                      /* class array is then updated in place                */
+    const double *d_uniforms;         /* optional [n_sub][n_particles] u for d_trans in place*/
+                                      /* of Philox (the reference's draws)                   */
 } ScDiffuseParams;
 
 int sc_get_version(void);
@@ -156,10 +163,12 @@ int sc_psf_quadrant_sat(const double *d_radial, int n_keys, int n_r, double res,
  * particle then moves by sigma * N(0, 1) per axis, with d_sigma
  * [n_sub][n_class][3] (sqrt(2 D dt) per step, class and axis) and d_class
  * (n, NULL = class 0).  Normals from Philox, or from d_normals
- * ([n_sub][n][ndim]) when given.  Replaces move_points / sample_inputs
- * (src/scopyon/sampling.py:88-162) and the periodic wrap of
- * sampling2.__move_points (src/scopyon/sampling2.py:33-50).               */
-int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, const int32_t *d_class,
+ * ([n_sub][n][ndim]) when given.  With p->d_trans, each particle's class
+ * changes after every move as the transition table says and d_class (then
+ * required) is updated in place.  Replaces move_points / sample_inputs
+ * (src/scopyon/sampling.py:88-162) and sampling2.__move_points /
+ * __transition_states (src/scopyon/sampling2.py:33-68).                    */
+int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, int32_t *d_class,
                      const double *d_sigma, const double *d_normals, double *d_particles,
                      void *stream);
 
@@ -208,7 +217,7 @@ int sc_emitter_steps(const ScStepParams *p, const double *d_particles,
  * __overlay_molecule_plane (src/scopyon/sampling.py:88-119,
  * src/scopyon/_epifm.py:1267-1360).                                        */
 int sc_native_records(const ScDiffuseParams *p, const ScStepParams *sp, double *d_pos,
-                      const int32_t *d_class, const double *d_sigma, const double *d_normals,
+                      int32_t *d_class, const double *d_sigma, const double *d_normals,
                       const double *d_unit_time, double *d_budget, const int32_t *d_key_slot,
                       ScStepRec *d_recs, const ScSplatParams *bin_p, void *d_bin_ws,
                       size_t bin_ws_bytes, int32_t *d_status, void *stream);

@@ -17,7 +17,7 @@ __all__ = [
     "overlay_signal_sat", "quadrant_sat", "snells_law", "emit_photons", "photon_budget",
     "emccd_distribution", "emccd_draw", "adc_counts", "adc_maps", "Params", "NumpyDraws",
     "InjectedDraws", "output_frame", "generate_frames", "format_data", "sample_points",
-    "move_points", "sample_inputs", "cmos_table_draw",
+    "move_points", "sample_inputs", "cmos_table_draw", "sampling2_sample",
 ]
 
 # CODATA exact values; the reference derives the same numbers from pint
@@ -626,4 +626,59 @@ def sample_inputs(t, n, lower, upper, D, ndim, rng, start=0):
         else:
             points = points.copy()
         out.append((current, points))
+    return out
+
+
+# ------------------------------------------------------- multi-state sampler
+def sampling2_sample(t, N, lower, upper, D, transmat, ndim, periodic, rng):
+    """Multi-state Brownian points (``src/scopyon/sampling2.py:15-68``, ``:70-148``).
+
+    Returns one (n, ndim + 2) array [coords, state, id] per time point.  Draw
+    order: initial points per state block and axis (``:15-31``); per time step
+    with dt > 0, one normal per particle and axis, particle-major (``:33-50``),
+    then, with a rate matrix, one uniform per particle (``:52-68``).  The
+    transition uses searchsorted side 'left' (the reference writes 'leff').
+    """
+    N = list(N) if hasattr(N, "__iter__") else [N]
+    lower = numpy.ones(ndim) * lower if numpy.isscalar(lower) else numpy.array(lower, float)
+    upper = numpy.ones(ndim) * upper if numpy.isscalar(upper) else numpy.array(upper, float)
+    for d in range(ndim):
+        if lower[d] > upper[d]:
+            lower[d], upper[d] = upper[d], lower[d]
+    D = numpy.ones(len(N)) * D if numpy.isscalar(D) else numpy.asarray(D, float)
+    pts = numpy.zeros((sum(N), ndim + 2))
+    tot = 0
+    for i, cnt in enumerate(N):
+        for d in range(ndim):
+            pts[tot:tot + cnt, d] = (rng.uniform(lower[d], upper[d], cnt) if lower[d] < upper[d]
+                                     else lower[d])
+        pts[tot:tot + cnt, ndim] = i
+        tot += cnt
+    pts[:, ndim + 1] = numpy.arange(pts.shape[0])
+    out = [pts.copy()]
+    current = t[0]
+    for nxt in t[1:]:
+        if nxt > current:
+            dt = nxt - current
+            state = pts[:, ndim].astype(int)
+            scale = numpy.sqrt(2 * D[state] * dt)
+            pts = pts.copy()
+            pts[:, :ndim] += scale[:, None] * rng.standard_normal((pts.shape[0], ndim))
+            if periodic:
+                for d in range(ndim):
+                    if upper[d] > lower[d]:
+                        pts[:, d] = (pts[:, d] - lower[d]) % (upper[d] - lower[d]) + lower[d]
+                    else:
+                        pts[:, d] = lower[d]
+            if transmat is not None:
+                rates = numpy.asarray(transmat, float)
+                n = rates.shape[0]
+                P = 1 - numpy.exp(-rates * dt)
+                P.ravel()[::n + 1] = 1.0 - P.sum(axis=1)
+                Pacc = P.cumsum(axis=1)
+                u = rng.uniform(0, 1, pts.shape[0])
+                pts[:, ndim] = [numpy.searchsorted(Pacc[s], r, side="left")
+                                for s, r in zip(state, u)]
+            current = nxt
+        out.append(pts)
     return out

@@ -63,7 +63,8 @@ class DiffuseParams(ctypes.Structure):
                 ("lower", ctypes.c_double * 3), ("upper", ctypes.c_double * 3),
                 ("scale", ctypes.c_double), ("origin", ctypes.c_double * 3),
                 ("unit_x", ctypes.c_double * 3), ("unit_y", ctypes.c_double * 3),
-                ("unit_z", ctypes.c_double * 3), ("d_class_box", ctypes.c_void_p)]
+                ("unit_z", ctypes.c_double * 3), ("d_class_box", ctypes.c_void_p),
+                ("d_trans", ctypes.c_void_p), ("d_uniforms", ctypes.c_void_p)]
 
 
 class GaussParams(ctypes.Structure):

@@ -23,6 +23,8 @@ struct DiffConsts {
     double lower[3], upper[3];
     double scale, origin[3], ux[3], uy[3], uz[3];
     const double *class_box;  // [n_class][6] lower xyz, upper xyz (optional)
+    const double *trans;      // [n_sub][n_class][n_class] cumulative transitions (optional)
+    const double *uniforms;   // [n_sub][n] injected transition uniforms (optional)
 };
 
 // Wall box of a particle's class: the class table's entry, else the common box.
@@ -40,6 +42,7 @@ __device__ __forceinline__ void class_walls(const DiffConsts &c, int cls, int d,
 __device__ __forceinline__ double wrap_axis(double x, double lo, double hi, int boundary) {
     if (boundary == 1) {  // periodic: (x - lo) mod (hi - lo) + lo, result in [lo, hi)
         const double len = hi - lo;
+        if (!(len > 0.0)) return lo;  // a flat axis stays on its wall (sampling2.py:44-48)
         double r = fmod(x - lo, len);
         if (r < 0) r += len;
         return r + lo;
@@ -88,13 +91,36 @@ __device__ __forceinline__ void philox_normals(const DiffConsts &c, int i, uint6
     nrm[2] = rb * cb;
 }
 
+// Uniform in [0, 1) with 53 random bits for the class transition of
+// particle i at global step g: Philox4x32-10, counter (i, g, 0x7a5e1f0b).
+__device__ __forceinline__ double philox_uniform(const DiffConsts &c, int i, uint64_t g) {
+    const sc::u4 r = sc::philox4x32_10({(uint32_t)i, (uint32_t)g, (uint32_t)(g >> 32), 0x7a5e1f0bu},
+                                       (uint32_t)c.seed, (uint32_t)(c.seed >> 32));
+    return ((double)(r.x >> 5) * 67108864.0 + (double)(r.y >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+// Class after a move: the first b with cumulative probability row[b] >= u
+// (numpy.searchsorted side 'left', sampling2.py:63-66); the last class when
+// rounding leaves u above every entry.
+__device__ __forceinline__ int next_class(const double *row, int n_class, double u) {
+    int b = 0;
+    while (b < n_class - 1 && row[b] < u) ++b;
+    return b;
+}
+
+// The class transition of particle i after sub-step s (global step g).
+__device__ __forceinline__ int transition(const DiffConsts &c, int cls, int i, int s, uint64_t g) {
+    const double u = c.uniforms ? c.uniforms[(size_t)s * c.n + i] : philox_uniform(c, i, g);
+    return next_class(c.trans + ((size_t)s * c.n_class + cls) * c.n_class, c.n_class, u);
+}
+
 // One thread per particle, sub-steps in order.
-__global__ void diffuse_kernel(DiffConsts c, double *pos, const int32_t *klass,
+__global__ void diffuse_kernel(DiffConsts c, double *pos, int32_t *klass,
                                const double *sigma, const double *normals, double *particles) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.n) return;
     double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
-    const int k = klass ? klass[i] : 0;
+    int k = klass ? klass[i] : 0;
     const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
     for (int s = 0; s < c.n_sub; ++s) {
         const size_t idx = (size_t)s * c.n + i;
@@ -122,10 +148,12 @@ __global__ void diffuse_kernel(DiffConsts c, double *pos, const int32_t *klass,
                 class_walls(c, k, d, lo, hi);
                 p[d] = wrap_axis(p[d], lo, hi, c.boundary);
             }
+        if (c.trans) k = transition(c, k, i, s, (uint64_t)(step0 + s));
     }
     pos[3 * i] = p[0];
     pos[3 * i + 1] = p[1];
     pos[3 * i + 2] = p[2];
+    if (c.trans) klass[i] = k;
 }
 
 // Native frame records for 32 particles per CTA, in three phases per chunk of
@@ -154,7 +182,7 @@ inline size_t rec_shared_bytes(int chunk) {
 
 __global__ void __launch_bounds__(kRecWarps * 32, 8)
 native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
-                      const int32_t *klass, const double *sigma, const double *normals,
+                      int32_t *klass, const double *sigma, const double *normals,
                       const double *unit_time, double *budget, const int32_t *key_slot,
                       ScStepRec *recs, sc::TileGeom g, sc::BinLayout bl, int32_t *status) {
     extern __shared__ double rec_smem[];
@@ -257,6 +285,7 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                         class_walls(c, cls, d, lo, hi);
                         p[d] = wrap_axis(p[d], lo, hi, c.boundary);
                     }
+                if (c.trans) cls = transition(c, cls, i, s, (uint64_t)(step0 + s));
             }
         }
         __syncthreads();
@@ -286,6 +315,7 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
         pos[3 * i + 1] = p[1];
         pos[3 * i + 2] = p[2];
         if (k.bleaching) budget[i] = b;
+        if (c.trans) klass[i] = cls;
     }
 }
 
@@ -301,7 +331,8 @@ int diff_consts(const ScDiffuseParams *p, DiffConsts &c) {
     SC_REQUIRE(p->n_class >= 1, "sc_diffuse_steps: n_class=%d", p->n_class);
     if (p->boundary && !p->d_class_box)
         for (int d = 0; d < p->ndim; ++d)
-            SC_REQUIRE(p->upper[d] > p->lower[d], "sc_diffuse_steps: empty box along axis %d", d);
+            SC_REQUIRE(p->upper[d] > p->lower[d] || (p->boundary == 1 && p->upper[d] == p->lower[d]),
+                       "sc_diffuse_steps: empty box along axis %d", d);
     c.n = p->n_particles;
     c.n_sub = p->n_sub;
     c.ndim = p->ndim;
@@ -310,6 +341,8 @@ int diff_consts(const ScDiffuseParams *p, DiffConsts &c) {
     c.step0 = p->step0;
     c.frame = p->d_frame;
     c.class_box = p->d_class_box;
+    c.trans = p->d_trans;
+    c.uniforms = p->d_uniforms;
     c.seed = p->seed;
     c.scale = p->scale;
     bool ident = p->scale == 1.0;
@@ -330,7 +363,7 @@ int diff_consts(const ScDiffuseParams *p, DiffConsts &c) {
 
 }  // namespace
 
-extern "C" int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, const int32_t *d_class,
+extern "C" int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, int32_t *d_class,
                                 const double *d_sigma, const double *d_normals,
                                 double *d_particles, void *stream) {
     DiffConsts c;
@@ -338,6 +371,7 @@ extern "C" int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, const i
     if (rc) return rc;
     if (c.n == 0 || c.n_sub == 0) return SC_OK;
     SC_REQUIRE(d_pos && d_sigma && d_particles, "sc_diffuse_steps: NULL pointer");
+    SC_REQUIRE(!p->d_trans || d_class, "sc_diffuse_steps: transitions need the class array");
     const int block = 128;
     diffuse_kernel<<<(c.n + block - 1) / block, block, 0, sc::as_stream(stream)>>>(
         c, d_pos, d_class, d_sigma, d_normals, d_particles);
@@ -345,7 +379,7 @@ extern "C" int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, const i
 }
 
 extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *sp, double *d_pos,
-                                 const int32_t *d_class, const double *d_sigma,
+                                 int32_t *d_class, const double *d_sigma,
                                  const double *d_normals, const double *d_unit_time,
                                  double *d_budget, const int32_t *d_key_slot, ScStepRec *d_recs,
                                  const ScSplatParams *bin_p, void *d_bin_ws, size_t bin_ws_bytes,
@@ -362,6 +396,7 @@ extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *s
     SC_REQUIRE(d_pos && d_sigma && d_unit_time && d_key_slot && d_recs,
                "sc_native_records: NULL pointer");
     SC_REQUIRE(!k.bleaching || d_budget, "sc_native_records: bleaching needs a budget array");
+    SC_REQUIRE(!p->d_trans || d_class, "sc_native_records: transitions need the class array");
     sc::TileGeom g{};
     sc::BinLayout bl{nullptr, nullptr, nullptr, nullptr, nullptr};
     if (bin_p) {

@@ -662,13 +662,15 @@ def tune_tiles(graph, candidates=TILE_CANDIDATES, frames=3):
     state is restored at the end: the simulation does not advance."""
     pipe = graph.pipe
     traj = graph.traj
-    state = (traj._pos.clone(), pipe.budget.clone(), graph.frame.clone(), graph.frames_done)
+    state = (traj._pos.clone(), pipe.budget.clone(), graph.frame.clone(), graph.frames_done,
+             traj._cls.clone())
 
     def restore():
         traj._pos.copy_(state[0])
         pipe.budget.copy_(state[1])
         graph.frame.copy_(state[2])
         graph.frames_done = state[3]
+        traj._cls.copy_(state[4])
 
     times = {}
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -745,14 +747,14 @@ class FrameGraph:
         pipe, traj, s = self.pipe, self.traj, stream_ptr()
         n_rec = self.n_sub * self.n
         recs = pipe._buf("recs" + tag, max(n_rec, 1) * (_lib.STEP_REC_BYTES // 4), torch.int32)
-        dp = traj.params(first_step, self.n_sub, **(self.transform or {}))
+        dp = traj.graph_params(first_step, self.n_sub, self.transform)
         dp.d_frame = self.frame.data_ptr()
         sp = pipe.step_params(self.n_sub, self.n, False)
         bufs = pipe.bin_buffers(n_rec, tag=tag)
         bsp, ws, ws_bytes, _, _ = bufs
         call("sc_bin_reset", bsp, ptr(ws), ws_bytes, s)
         with pipe.timed("records"):
-            call("sc_native_records", dp, sp, ptr(traj._pos), ptr(traj._g_class),
+            call("sc_native_records", dp, sp, ptr(traj._pos), ptr(traj._cls),
                  ptr(traj._g_sigma), None, ptr(self.ut), ptr(pipe.budget), ptr(pipe.psf.key_slot),
                  ptr(recs), bsp, ptr(ws), ws_bytes, ptr(pipe.status), s)
         pipe.finish_bins(n_rec, tag, bufs=bufs)

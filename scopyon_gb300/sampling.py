@@ -77,7 +77,8 @@ class DeviceTrajectories:
     """
 
     def __init__(self, times, points, D, ndim, seed, normals=None, boundary="none",
-                 lower=None, upper=None, klass=None, device=None, class_box=None):
+                 lower=None, upper=None, klass=None, device=None, class_box=None,
+                 transmat=None, uniforms=None):
         self.times = numpy.asarray(times, dtype=float)
         self.points0 = numpy.asarray(points, dtype=float)   # (N, ndim + 2) host
         self.ndim = int(ndim)
@@ -93,7 +94,12 @@ class DeviceTrajectories:
         # optional walls per class: (n_class, 6) lower xyz, upper xyz
         self.class_box = None if class_box is None else torch.as_tensor(
             numpy.asarray(class_box, dtype=float).reshape(-1, 6), device=self.device)
+        # optional class transitions (sampling2): rates (n_class, n_class) in 1/s,
+        # and in exact mode the uniforms (T-1, N) drawn in the reference's order
+        self.transmat = None if transmat is None else numpy.asarray(transmat, dtype=float)
+        self.uniforms = uniforms
         self._pos = None
+        self._cls = None  # device classes, changed in place by transitions
         self._index = 0
 
     # -- reference-compatible access -----------------------------------
@@ -121,9 +127,10 @@ class DeviceTrajectories:
 
     def copy(self):
         box = None if self.class_box is None else self.class_box.cpu().numpy()
-        return DeviceTrajectories(self.times, self.points0, self.D, self.ndim, self.seed,
-                                  self.normals, self.boundary, self.lower, self.upper, self.klass,
-                                  self.device, class_box=box)
+        return type(self)(self.times, self.points0, self.D, self.ndim, self.seed,
+                          self.normals, self.boundary, self.lower, self.upper, self.klass,
+                          self.device, class_box=box, transmat=self.transmat,
+                          uniforms=self.uniforms)
 
     def materialize(self, k):
         """Host (N, ndim + 2) points at time index k (advances this object)."""
@@ -137,8 +144,38 @@ class DeviceTrajectories:
     def reset(self):
         pos = numpy.zeros((self.n_particles, 3))
         pos[:, : self.ndim] = self.points0[:, : self.ndim]
-        self._pos = torch.from_numpy(pos).to(self.device)
+        if self._pos is None:
+            self._pos = torch.from_numpy(pos).to(self.device)
+            self._cls = torch.from_numpy(self.klass).to(self.device)
+        else:  # in place: captured frame graphs keep these addresses
+            self._pos.copy_(torch.from_numpy(pos))
+            self._cls.copy_(torch.from_numpy(self.klass))
         self._index = 0
+
+    def classes(self):
+        """Current class of every particle (host int32)."""
+        if self._cls is None:
+            return self.klass.copy()
+        return self._cls.cpu().numpy()
+
+    def _transitions(self, g0, n):
+        """Cumulative transition probabilities of steps g0 .. g0 + n - 1,
+        [n][n_class][n_class], as sampling2.__transition_states forms them
+        (src/scopyon/sampling2.py:52-68); a step of zero length keeps the class
+        (its rows are -1 below the class and 1 from it on)."""
+        nc = self.D.shape[0]
+        out = numpy.zeros((n, nc, nc))
+        for s in range(n):
+            g = g0 + s
+            if g + 1 < len(self.times) and self.times[g + 1] > self.times[g]:
+                dt = self.times[g + 1] - self.times[g]
+                P = 1 - numpy.exp(-self.transmat * dt)
+                P.ravel()[:: nc + 1] = 1.0 - P.sum(axis=1)
+                out[s] = P.cumsum(axis=1)
+            else:
+                out[s] = numpy.where(numpy.arange(nc)[None, :] >= numpy.arange(nc)[:, None],
+                                     1.0, -1.0)
+        return out
 
     def _sigma(self, g0, n):
         """sqrt(2 D dt) per step (of n from time index g0), class and axis, as the reference."""
@@ -183,9 +220,19 @@ class DeviceTrajectories:
                 if g < len(self.normals):
                     nrm[s] = self.normals[g]
             normals = torch.from_numpy(nrm).to(self.device)
-        klass = torch.from_numpy(self.klass).to(self.device)
-        call("sc_diffuse_steps", p, ptr(self._pos), ptr(klass), ptr(sig), ptr(normals), ptr(out),
-             stream_ptr(stream))
+        trans = unif = None
+        if self.transmat is not None:
+            trans = torch.from_numpy(self._transitions(g0, n)).to(self.device)
+            p.d_trans = trans.data_ptr()
+            if self.uniforms is not None:
+                u = numpy.zeros((n, self.n_particles))
+                for s in range(n):
+                    if g0 + s < len(self.uniforms):
+                        u[s] = self.uniforms[g0 + s]
+                unif = torch.from_numpy(u).to(self.device)
+                p.d_uniforms = unif.data_ptr()
+        call("sc_diffuse_steps", p, ptr(self._pos), ptr(self._cls), ptr(sig), ptr(normals),
+             ptr(out), stream_ptr(stream))
         self._index = g0 + n
 
     def prepare_uniform(self, n_sub):
@@ -199,17 +246,31 @@ class DeviceTrajectories:
         sig = numpy.zeros((n_sub, self.D.shape[0], 3))
         sig[:, :, : self.ndim] = numpy.sqrt(2 * self.D * dt[0])
         self._g_sigma = torch.from_numpy(sig).to(self.device)
-        self._g_class = torch.from_numpy(self.klass).to(self.device)
+        self._g_trans = None
+        if self.transmat is not None:
+            nc = self.D.shape[0]
+            P = 1 - numpy.exp(-self.transmat * dt[0])
+            P.ravel()[:: nc + 1] = 1.0 - P.sum(axis=1)
+            self._g_trans = torch.from_numpy(
+                numpy.repeat(P.cumsum(axis=1)[None], n_sub, axis=0)).to(self.device)
         if self._pos is None:
             self.reset()
+
+    def graph_params(self, g0, n_sub, transform=None):
+        """Launch parameters of a captured frame: the uniform sigma and, with
+        transitions, their table for n_sub steps from step g0 of the frame."""
+        p = self.params(g0, n_sub, **(transform or {}))
+        if self._g_trans is not None:
+            p.d_trans = self._g_trans.data_ptr()
+        return p
 
     def launch_frame(self, n_sub, out, d_frame, transform=None, stream=None):
         """Enqueue one frame's sub-steps, step index taken from the device counter
         ``d_frame`` (frame f covers steps f * n_sub ... f * n_sub + n_sub - 1).
         Fixed arguments only, so it can be captured in a CUDA graph."""
-        p = self.params(0, n_sub, **(transform or {}))
+        p = self.graph_params(0, n_sub, transform)
         p.d_frame = d_frame.data_ptr()
-        call("sc_diffuse_steps", p, ptr(self._pos), ptr(self._g_class), ptr(self._g_sigma), None,
+        call("sc_diffuse_steps", p, ptr(self._pos), ptr(self._cls), ptr(self._g_sigma), None,
              ptr(out), stream_ptr(stream))
 
     def advance_to(self, k, transform=None, stream=None):

@@ -74,4 +74,4 @@ def test_struct_sizes_match_c_layout():
     assert ctypes.sizeof(_lib.StepParams) == 136
     assert ctypes.sizeof(_lib.SplatParams) == 80
     assert ctypes.sizeof(_lib.CameraParams) == 112
-    assert ctypes.sizeof(_lib.DiffuseParams) == 208
+    assert ctypes.sizeof(_lib.DiffuseParams) == 224

@@ -287,6 +287,17 @@ int sc_gauss_backward(const ScGaussParams *p, const float *d_emit, const float *
                       const void *d_ws, size_t ws_bytes, const float *d_grad_mu,
                       float *d_grad_emit, float *d_grad_sigma_e, void *stream);
 
+/* Spot fits for n_blobs blobs (d_blobs: [n][3] x, y, r in pixels) in a
+ * double image [nw][nh]: the region of +-roi_size pixels around each blob,
+ * a least-squares plane through its four edges, and a 2-D Gaussian
+ * a1 exp(-((x - a2)^2 + (y - a3)^2) / a4) fitted to the remainder from the
+ * reference's start.  d_out[n][8] = (centre x, centre y, intensity,
+ * background, a1, a4, status, 0); status 0 is a spot, 1 a region summing to
+ * <= 0, 2 a failed fit, 3 a centre outside the region.  Replaces
+ * spot_detection with given blobs (src/scopyon/analysis/spot_detection.py:49-173). */
+int sc_spot_fit(const double *d_image, int nw, int nh, const double *d_blobs, int n_blobs,
+                double roi_size, double *d_out, void *stream);
+
 /* Bytes of scratch the two reductions below need for n_seg segments of
  * seg_len values (partial sums of up to 64 CTAs per segment).               */
 size_t sc_reduce_scratch_bytes(int64_t seg_len, int n_seg);

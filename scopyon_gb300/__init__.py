@@ -11,12 +11,12 @@ from .image import Image
 from .base import (EPIFMSimulator, EnvironSettings, InjectedDraws, create_simulator, form_image,
                    generate_images)
 from .sampling import DeviceTrajectories, concatenate, sample_inputs, sample_points
-from . import sampling2
+from . import analysis, sampling2
 from .sampling2 import StateTrajectories, sample
 
 __all__ = ["Configuration", "DefaultConfiguration", "Quantity", "DimensionalityError", "Image",
            "EPIFMSimulator", "EnvironSettings", "InjectedDraws", "create_simulator", "form_image",
            "generate_images", "sample_inputs", "sample_points", "DeviceTrajectories",
-           "concatenate", "sample", "sampling2", "StateTrajectories"]
+           "concatenate", "sample", "sampling2", "StateTrajectories", "analysis"]
 
 __version__ = "0.1.0"

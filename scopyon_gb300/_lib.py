@@ -111,6 +111,7 @@ _SIG = {
     "sc_gauss_nll": (_I, [_P, _P, ctypes.c_int64, _P, _D, _P, ctypes.c_size_t, _P, _P, _P]),
     "sc_diffusion_dD": (_I, [_P, _P, _I, _I, _P, _P, _P, ctypes.c_size_t, _P, _P]),
     "sc_segment_sum": (_I, [_P, ctypes.c_int64, _I, _P, ctypes.c_size_t, _P, _P]),
+    "sc_spot_fit": (_I, [_P, _I, _I, _P, _I, _D, _P, _P]),
     "sc_poisson_nll": (_I, [_P, _P, ctypes.c_int64, _I, _P, ctypes.c_size_t, _P, _P, _P]),
 }
 

@@ -167,6 +167,24 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def replica_barrier(world):
+    """All replicas reach this point (one process per GPU; no data exchange)."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(value, world, dev):
+    """The largest of every replica's value (their timed regions' maximum)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def gb300_arm(args, rank, world):
     import torch
     import scopyon_gb300 as sg
@@ -220,8 +238,7 @@ def gb300_arm(args, rank, world):
         fg.step()
     torch.cuda.synchronize()
     pipe.check_status()
-    if world > 1:
-        torch.distributed.barrier()
+    replica_barrier(world)
     live0 = float((pipe.budget[:N_EMIT] > 0).float().mean())
     clocks = ClockSampler(dev.index)
     clocks.start()
@@ -233,8 +250,7 @@ def gb300_arm(args, rank, world):
         fg.step()
     end.record()
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    replica_barrier(world)
     live1 = float((pipe.budget[:N_EMIT] > 0).float().mean())
     elapsed_ms = start.elapsed_time(end)
     # the splat's own duration: the frames right after the timed ones, launched
@@ -262,10 +278,7 @@ def gb300_arm(args, rank, world):
         torch.cuda.synchronize()
     clk = clocks.stop()
     pipe.check_status()
-    if world > 1:
-        tt = torch.tensor([elapsed_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(tt.item())
+    elapsed_ms = max_over_ranks(elapsed_ms, world, dev)
     ms_per_step = elapsed_ms / args.steps
     value = world * args.steps / (elapsed_ms / 1e3)
 
@@ -343,18 +356,13 @@ def e2e_arm(args, cfg, dev, rank, world):
     for _ in range(args.warmup):
         next(gen)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    replica_barrier(world)
     t0 = time.perf_counter()
     for _ in range(steps):
         img = next(gen)
         img.as_array()
     torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([dt], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dt = float(t.item())
+    dt = max_over_ranks(time.perf_counter() - t0, world, dev)
     return {"value": world * steps / dt, "unit": "frames/s", "frames": steps,
             "h2d_bytes_per_step": SUBSTEPS * N_EMIT * 5 * 8 + SUBSTEPS * 8,
             "d2h_bytes_per_step": IMAGE * IMAGE * 8 + 16}

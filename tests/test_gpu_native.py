@@ -248,3 +248,26 @@ def test_fused_native_physics_matches_separate_pass(sg):
     sep = [info["expectation"] for _, info in sim.generate_images(traj.copy(), 4, full_output=True)]
     for a, b in zip(fused, sep):
         numpy.testing.assert_array_equal(a.reshape(40, 40).astype(float), b)
+
+
+def test_host_inputs_fast_path_matches_general_path(sg):
+    """Host trajectories with the same ids at every sub-step are staged by host
+    threads (full_output=False); the frames equal those of the general path
+    (full_output=True), with bleaching on."""
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {
+        "magnification": 100,
+        "detector": {"type": "EMCCD", "image_size": [48, 40], "exposure_time": 0.004},
+        "effects": {"photo_bleaching": {"switch": True, "half_life": 0.01}}}})
+    t = numpy.arange(5 * 4 + 1) * 1e-3
+    inputs = [(float(a), p) for a, p in sg.sampling.sample_inputs(
+        t, N=150, lower=[-3e-6, -3e-6, -0.2e-6], upper=[3e-6, 3e-6, 0.2e-6], D=0.3e-12, ndim=3,
+        rng=numpy.random.RandomState(2), exact=True)]
+    outs = []
+    for full in (True, False):
+        gen = sg.generate_images(inputs, 5, config=cfg, rng=numpy.random.RandomState(9),
+                                 full_output=full)
+        frames = [(img if not full else img[0]).as_array() for img in gen]
+        outs.append(numpy.array(frames))
+    numpy.testing.assert_array_equal(outs[0], outs[1])
+    assert outs[0].std(axis=0).max() > 0

@@ -737,10 +737,11 @@ def main():
     ap.add_argument("--warps", type=int, default=4, help="warps per splat tile with --tile")
     ap.add_argument("--stages", type=int, default=4,
                     help="box-table block copies in flight per splat warp with --tile")
-    ap.add_argument("--case", choices=["dgrad", "batched"], default=None,
+    ap.add_argument("--case", choices=["dgrad", "batched", "fwdbwd"], default=None,
                     help="profiling: run one workload alone and print its result object "
                          "(dgrad: dL/dD at 100k emitters x 100 sub-steps on 2048^2 px; "
-                         "batched: the 256-field canvas without the per-field loop)")
+                         "batched: the 256-field canvas without the per-field loop; "
+                         "fwdbwd: the differentiable image at 512^2 px, 20k emitters)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: depth range +-0.1 um between reflecting walls and "
                          "D = 0.01 um^2/s for all emitters (102 PSF keys, 2.9 GB of tables), "
@@ -760,6 +761,9 @@ def main():
         torch.cuda.set_device(dev)
         if args.case == "dgrad":
             res = diffusion_grad_case(dev, 100000, 2048, 100, args.steps, args.warmup, 9)
+        elif args.case == "fwdbwd":
+            res = fwd_bwd_case(dev, 1, N_EMIT, IMAGE, 90e-9, math.inf, 1e-6, args.steps,
+                               args.warmup, 5)
         else:
             res = batched_arm(args, dev, loop=False)
         print(json.dumps(res), flush=True)

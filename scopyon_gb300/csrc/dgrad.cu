@@ -54,7 +54,7 @@ __global__ void diffusion_positions_kernel(const float4 *__restrict__ emit, int 
 }
 
 constexpr int kThreads = 256;
-constexpr int kChunk = 8192;
+constexpr int kChunk = 1024;
 constexpr int kMaxParts = 1216;  // 8 CTAs on each of 152 SMs
 
 __device__ __forceinline__ double block_sum(double acc, double *part) {

@@ -538,7 +538,7 @@ void launch_tile_splat(int P, int grid, cudaStream_t st, const ScStepRec *recs,
 bool tile_path(const GaussConsts &c) { return c.R <= 7; }
 
 constexpr int kSumThreads = 256;
-constexpr int kSumChunk = 8192;    // values per CTA and pass
+constexpr int kSumChunk = 1024;    // values per CTA and pass
 constexpr int kSumMaxParts = 1216; // CTAs per segment (8 on each of 152 SMs)
 
 __device__ __forceinline__ double block_sum(double acc, double *part) {

@@ -285,11 +285,12 @@ def gb300_arm(args, rank, world):
     e2e = None if args.small else e2e_arm(args, cfg, dev, rank, world)
     fwd_bwd = None if args.small else fwd_bwd_arm(args, dev)
     batched = None if args.small else batched_arm(args, dev)
+    peak, peak_kind = load_peaks()
+    large_stages = None if args.small else hbm_stages(dev, peak)
 
     splat_avg_ms = sum(splat_ms) / len(splat_ms)
     n_rec = sum(splat_recs) / len(splat_recs)
     alg = splat_algorithmic_bytes(n_rec, pipe.tile, pipe.halo)
-    peak, peak_kind = load_peaks()
     achieved = alg / (splat_avg_ms / 1e3) / 1e9
     tables_gb = (pipe.psf.tables.numel() + (pipe.psf.box.numel() if pipe.psf.box is not None
                                             else 0)) * 4 / 1e9
@@ -333,7 +334,8 @@ def gb300_arm(args, rank, world):
                      "algorithmic_bytes": alg, "records": n_rec,
                      "avg_launch_ms": splat_avg_ms,
                      "timed_on": "%d eager frames after the timed graph replays" % n_timing,
-                     "stages": stage_rooflines(stage_ms, pipe, SUBSTEPS * N_EMIT, peak)},
+                     "stages": stage_rooflines(stage_ms, pipe, SUBSTEPS * N_EMIT, peak),
+                     "stages_beyond_l2": large_stages},
     }
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline()
@@ -518,19 +520,114 @@ def stage_rooflines(stage_ms, pipe, n_rec, peak):
     durations on the same eager frames.  Algorithmic bytes: the records stage
     reads and writes each emitter's FP64 position (48 B), photon budget
     (16 B) and class (4 B) and writes each record (64 B) with its bin and rank
-    (8 B); the camera reads each pixel's photons and read-noise sigma (8 B)
-    and writes the expectation (4 B) and the FP64 ADC count (8 B)."""
+    (8 B); the camera reads each pixel's photons (4 B), offset and 1/gain
+    (8 B, with fixed-pattern noise) and read-noise sigma (4 B, sCMOS) and
+    writes the expectation (4 B) and the FP64 ADC count (8 B)."""
     n_px = pipe.nw * pipe.nh
     out = {}
     for name, alg, bound in (
             ("records", N_EMIT * 68 + n_rec * 72,
              "FP64 position chains and footprint arithmetic (FP64 pipe), not HBM"),
-            ("camera", n_px * (8 + (4 if pipe.sigma is not None else 0) + 8),
+            ("camera", n_px * (8 + (8 if pipe.pixel_maps else 0) +
+                               (4 if pipe.sigma is not None else 0) + 8),
              "per-pixel Poisson and normal draws (FP32 and SFU pipes), not HBM")):
         ms = stage_ms[name]
         gbs = alg / (ms / 1e3) / 1e9
         out[name] = {"avg_launch_ms": ms, "algorithmic_bytes": alg, "achieved": gbs,
                      "unit": "GB/s", "frac": gbs / peak, "limited_by": bound}
+    return out
+
+
+def _event_ms(fn, steps, warmup):
+    """Average CUDA-event time of fn() (launches on the current stream)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def hbm_stages(dev, peak, steps=20, warmup=3, n_emit=1 << 22, edge=8192, seed=5):
+    """The diffusion kernel (sc_diffuse_steps) and the camera kernel (sc_camera)
+    alone, each on a workload far larger than L2 (129 MB), so that their HBM
+    rooflines mean something (a 512^2 frame moves only a few MB per stage).
+
+    Diffusion: n_emit emitters, reflecting walls, SUBSTEPS Philox sub-steps per
+    launch; per emitter it reads and writes the FP64 position (48 B) and reads
+    the class (4 B), per emitter-step it writes the formatted [depth, x, y, id,
+    state] row (40 B).  Camera: the workload's sCMOS camera on an edge^2 frame;
+    per pixel it reads photons, offset, 1/gain and readout sigma (16 B) and
+    writes the expectation (4 B) and the FP64 ADC count (8 B)."""
+    import torch
+    import scopyon_gb300 as sg
+    from scopyon_gb300 import _lib
+    from scopyon_gb300._lib import call, ptr, stream_ptr
+    gen = torch.Generator(dev).manual_seed(seed)
+    out = {}
+
+    # diffusion: uniform time grid, device frame counter advanced between launches
+    rng = numpy.random.RandomState(seed)
+    dt = EXPOSURE / SUBSTEPS
+    t = numpy.arange(4 * SUBSTEPS + 1) * dt
+    traj = sg.sample_inputs(t, N=n_emit, D=D_FAST, rng=rng, lower=[-HALF, -HALF, -Z_HALF],
+                            upper=[HALF, HALF, Z_HALF], ndim=3, device=dev,
+                            boundary="reflecting")
+    traj.prepare_uniform(SUBSTEPS)
+    frame = torch.zeros(1, dtype=torch.int64, device=dev)
+    rows = torch.empty(SUBSTEPS * n_emit * 5, dtype=torch.float64, device=dev)
+
+    def diffuse():
+        traj.launch_frame(SUBSTEPS, rows, frame)
+        call("sc_counter_add", ptr(frame), 1, stream_ptr())
+
+    ms = _event_ms(diffuse, steps, warmup)
+    alg = n_emit * (48 + 4) + n_emit * SUBSTEPS * 40
+    gbs = alg / (ms / 1e3) / 1e9
+    out["diffusion"] = {"kernel": "diffuse_kernel (sc_diffuse_steps)", "emitters": n_emit,
+                        "substeps": SUBSTEPS, "avg_launch_ms": ms, "algorithmic_bytes": alg,
+                        "achieved": gbs, "unit": "GB/s", "frac": gbs / peak,
+                        "timing": "includes one 1-thread frame-counter launch per step"}
+    del rows, traj
+    torch.cuda.empty_cache()
+
+    # camera: the workload's sCMOS model on an edge x edge frame
+    n = edge * edge
+    photons = torch.rand(n, device=dev, generator=gen) * 200.0
+    offset_f = torch.round(100.0 + 5.0 * torch.randn(n, device=dev, generator=gen))
+    inv_gain_f = (4096.0 - offset_f) / 30000.0
+    sigma = torch.exp(math.log(1.5) + 0.4 * torch.randn(n, device=dev, generator=gen))
+    expect = torch.empty(n, dtype=torch.float32, device=dev)
+    adc = torch.empty(n, dtype=torch.float64, device=dev)
+    status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
+    cp = _lib.CameraParams()
+    cp.nw = cp.nh = edge
+    cp.camera, cp.exact, cp.rounding, cp.bit = _lib.CAM_SCMOS, 0, 0, 12
+    cp.qe, cp.background, cp.readout_noise, cp.emgain = 0.73, 0.0, 1.5, 1.0
+    cp.fullwell, cp.offset0, cp.gain0 = 30000.0, 100.0, 30000.0 / 3996.0
+    cp.seed = seed
+    counter = [0]
+
+    def camera():
+        counter[0] += 1
+        cp.counter = counter[0]
+        call("sc_camera", cp, ptr(photons), None, None, ptr(offset_f), ptr(inv_gain_f),
+             ptr(sigma), None, None, None, None, None, ptr(expect), ptr(adc), None, ptr(status),
+             stream_ptr())
+
+    ms = _event_ms(camera, steps, warmup)
+    if int(status[0]):
+        raise RuntimeError("camera status %d" % int(status[0]))
+    alg = n * (16 + 4 + 8)
+    gbs = alg / (ms / 1e3) / 1e9
+    out["camera"] = {"kernel": "camera_kernel (sc_camera, sCMOS)", "image": [edge, edge],
+                     "avg_launch_ms": ms, "algorithmic_bytes": alg, "achieved": gbs,
+                     "unit": "GB/s", "frac": gbs / peak}
     return out
 
 
@@ -551,7 +648,7 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=
     D = numpy.exp(rng.uniform(math.log(1e-3), math.log(1.0), n_fields)) * 1e-12
     cfg = config1()
     t0 = time.time()
-    per_step = 2  # two canvas frames per replay, the second frame's records beside the first splat
+    per_step = 4  # four canvas frames per replay, each frame's records beside the previous splat
     bf = BatchedFields(cfg, sizes, counts, D, frames, substeps, seed=seed, device=dev,
                        frames_per_step=per_step)
     if args.tile:
@@ -737,11 +834,12 @@ def main():
     ap.add_argument("--warps", type=int, default=4, help="warps per splat tile with --tile")
     ap.add_argument("--stages", type=int, default=4,
                     help="box-table block copies in flight per splat warp with --tile")
-    ap.add_argument("--case", choices=["dgrad", "batched", "fwdbwd"], default=None,
+    ap.add_argument("--case", choices=["dgrad", "batched", "fwdbwd", "stages"], default=None,
                     help="profiling: run one workload alone and print its result object "
                          "(dgrad: dL/dD at 100k emitters x 100 sub-steps on 2048^2 px; "
                          "batched: the 256-field canvas without the per-field loop; "
-                         "fwdbwd: the differentiable image at 512^2 px, 20k emitters)")
+                         "fwdbwd: the differentiable image at 512^2 px, 20k emitters; "
+                         "stages: the diffusion and camera kernels alone beyond L2)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: depth range +-0.1 um between reflecting walls and "
                          "D = 0.01 um^2/s for all emitters (102 PSF keys, 2.9 GB of tables), "
@@ -761,6 +859,8 @@ def main():
         torch.cuda.set_device(dev)
         if args.case == "dgrad":
             res = diffusion_grad_case(dev, 100000, 2048, 100, args.steps, args.warmup, 9)
+        elif args.case == "stages":
+            res = hbm_stages(dev, load_peaks()[0], args.steps, args.warmup)
         elif args.case == "fwdbwd":
             res = fwd_bwd_case(dev, 1, N_EMIT, IMAGE, 90e-9, math.inf, 1e-6, args.steps,
                                args.warmup, 5)

@@ -27,7 +27,11 @@ struct CamConsts {
 // Poisson variate.  Small means: sequential inversion.  Large means: the
 // transformed rejection method PTRS (W. Hormann, "The transformed rejection
 // method for generating Poisson random variables", Insurance: Mathematics and
-// Economics 12 (1993) 39-45), with log(k!) from Stirling's series.
+// Economics 12 (1993) 39-45), with log(k!) from Stirling's series.  Divisions
+// and the logarithms of the acceptance test use the approximate intrinsics
+// (relative error ~1e-7): they move the accepted distribution by far less
+// than any test of a frame's counts can see, and a pixel's draw costs about
+// half the instructions of the IEEE forms.
 __device__ float poisson(sc::rng_stream &rs, float lam, int32_t *status) {
     if (!(lam > 0.f)) return 0.f;
     if (lam < 12.f) {
@@ -36,30 +40,32 @@ __device__ float poisson(sc::rng_stream &rs, float lam, int32_t *status) {
         int k = 0;
         while (u > s && k < 200) {
             ++k;
-            p *= lam / (float)k;
+            p *= __fdividef(lam, (float)k);
             s += p;
         }
         return (float)k;
     }
-    const float slam = sqrtf(lam), loglam = logf(lam);
+    const float slam = sqrtf(lam), inv_lam = __fdividef(1.f, lam);
     const float b = 0.931f + 2.53f * slam;
     const float a = -0.059f + 0.02483f * b;
-    const float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
-    const float vr = 0.9277f - 3.6224f / (b - 2.f);
+    const float invalpha = 1.1239f + __fdividef(1.1328f, b - 3.4f);
+    const float vr = 0.9277f - __fdividef(3.6224f, b - 2.f);
     for (int it = 0; it < 64; ++it) {
         const float U = rs.uniform() - 0.5f;
         const float V = rs.uniform();
         const float us = 0.5f - fabsf(U);
-        const float k = floorf((2.f * a / us + b) * U + lam + 0.43f);
+        const float k = floorf((__fdividef(2.f * a, us) + b) * U + lam + 0.43f);
         if (us >= 0.07f && V <= vr) return k;
         if (k < 0.f || (us < 0.013f && V > us)) continue;
         // -lam + k log(lam) - log(k!) via Stirling, written relative to k - lam
         const float kk = fmaxf(k, 1.f);
-        const float d = (k - lam) / lam;
-        const float lfact_rel = (k - lam) - k * log1pf(d) - 0.5f * logf(6.2831853f * kk) -
-                                1.f / (12.f * kk) + 1.f / (360.f * kk * kk * kk);
+        const float ikk = __fdividef(1.f, kk);
+        const float d = (k - lam) * inv_lam;
+        const float lfact_rel = (k - lam) - k * log1pf(d) - 0.5f * __logf(6.2831853f * kk) -
+                                ikk * (1.f / 12.f) + ikk * ikk * ikk * (1.f / 360.f);
         const float rhs = k == 0.f ? -lam : lfact_rel;
-        if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <= rhs) return k;
+        // log(V / alpha / (a / us^2 + b)) <= rhs
+        if (__logf(__fdividef(V * invalpha, __fdividef(a, us * us) + b)) <= rhs) return k;
     }
     sc::flag_status(status, 3, 0, 0, 0);
     return rintf(lam);
@@ -158,7 +164,7 @@ __global__ void camera_kernel(CamConsts c, const float *__restrict__ photons,
         v = fminf(fmaxf(v, 0.f), c.adc_max_f);
         if (c.rounding) v = rintf(v);
         if (adc32) adc32[p] = v;
-        if (adc64) adc64[p] = (double)v;
+        if (adc64) adc64[p] = sc::f2d_exact(v);
     }
 }
 

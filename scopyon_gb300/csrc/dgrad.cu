@@ -90,7 +90,7 @@ gauss_nll_kernel(const float *__restrict__ mu, const float *__restrict__ k, int6
             const float v = m + (r2_map ? r2_map[q] : r2);
             const float iv = 1.f / v, hr = 0.5f * r * r * iv;
             // each pixel's term in FP32 (within a few ulp), summed in FP64
-            acc += (double)hr + 0.5 * (double)logf(v);
+            acc += sc::f2d_exact(hr) + 0.5 * sc::f2d_exact(logf(v));
             if (grad) grad[q] = -r * iv - hr * iv + 0.5f * iv;
         }
     }
@@ -110,7 +110,8 @@ dD_partial_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ emi
         int e = (int)((c0 + threadIdx.x) % n);  // emitter of value q (q = t n + e)
         for (int64_t q = c0 + threadIdx.x; q < c1; q += kThreads) {
             const float4 p = pos[q], g = grad[q], p0 = emit[e];
-            acc += (double)g.x * (double)(p.x - p0.x) + (double)g.y * (double)(p.y - p0.y);
+            acc += sc::f2d_exact(g.x) * sc::f2d_exact(p.x - p0.x) +
+                   sc::f2d_exact(g.y) * sc::f2d_exact(p.y - p0.y);
             e += kThreads;
             while (e >= n) e -= n;
         }

@@ -48,6 +48,9 @@ __device__ __forceinline__ double wrap_axis(double x, double lo, double hi, int 
         return r + lo;
     }
     if (boundary == 2) {  // reflecting walls at lo and hi
+        // inside: decided on the integer pipes (order_key), else in FP64
+        const long long kx = sc::order_key(x);
+        if (kx >= sc::order_key(lo) && kx <= sc::order_key(hi)) return x;
         if (x >= lo && x <= hi) return x;
         for (int it = 0; it < 64 && (x < lo || x > hi); ++it) x = x < lo ? 2 * lo - x : 2 * hi - x;
         return fmin(fmax(x, lo), hi);
@@ -122,6 +125,7 @@ __global__ void diffuse_kernel(DiffConsts c, double *pos, int32_t *klass,
     double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
     int k = klass ? klass[i] : 0;
     const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
+    const double id = (double)i;
     for (int s = 0; s < c.n_sub; ++s) {
         const size_t idx = (size_t)s * c.n + i;
         double *q = particles + idx * 5;
@@ -130,7 +134,7 @@ __global__ void diffuse_kernel(DiffConsts c, double *pos, int32_t *klass,
         q[0] = f[0];
         q[1] = f[1];
         q[2] = f[2];
-        q[3] = (double)i;
+        q[3] = id;
         q[4] = 1.0;
         // one Brownian step: x_d += sigma_d * n_d (the reference's 0.0 + sigma * gauss)
         const double *sg = sigma + ((size_t)s * c.n_class + k) * 3;
@@ -140,7 +144,7 @@ __global__ void diffuse_kernel(DiffConsts c, double *pos, int32_t *klass,
         } else {
             float nrm[3];
             philox_normals(c, i, (uint64_t)(step0 + s), nrm);
-            for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], (double)nrm[d], p[d]);
+            for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], sc::f2d_exact(nrm[d]), p[d]);
         }
         if (c.boundary)
             for (int d = 0; d < c.ndim; ++d) {
@@ -277,7 +281,7 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                     for (int d = 0; d < c.ndim; ++d) p[d] += __dmul_rn(sg[d], nv[d]);
                 } else {
                     const float *nr = s_nrm + (j * 32 + lane) * 3;
-                    for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], (double)nr[d], p[d]);
+                    for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], sc::f2d_exact(nr[d]), p[d]);
                 }
                 if (c.boundary)
                     for (int d = 0; d < c.ndim; ++d) {

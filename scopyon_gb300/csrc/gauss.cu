@@ -571,10 +571,10 @@ partial_sum_kernel(const float *__restrict__ x, const float *__restrict__ counts
                 const float kk = counts[base + q];
                 // logf is within an ulp; the FP64 accumulation is what a
                 // sum over millions of pixels needs
-                acc += (double)m - (double)kk * (double)logf(m);
+                acc += sc::f2d_exact(m) - sc::f2d_exact(kk) * sc::f2d_exact(logf(m));
                 if (grad) grad[base + q] = 1.f - kk / m;
             } else {
-                acc += (double)m;
+                acc += sc::f2d_exact(m);
             }
         }
     }

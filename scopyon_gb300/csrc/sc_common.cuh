@@ -104,6 +104,32 @@ __device__ __forceinline__ void df_acc(float &s, float &e, float hi, float lo, f
     e += err + sign * lo;
 }
 
+// ------------------------------------------- FP64 work on the integer pipes
+// GB300 runs FP64 instructions (arithmetic, compares, conversions) at about
+// 1/64 of the FP32 rate; these two replace a conversion and a compare that
+// the Brownian sub-step loops would otherwise issue to the FP64 pipe.
+
+// float -> double, exactly as the conversion instruction gives it: sign, the
+// exponent rebiased by 1023 - 127 = 896, the 23 fraction bits moved to the top
+// of the 52.  Zero, subnormals, infinities and NaN take the conversion.
+__device__ __forceinline__ double f2d_exact(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)f;
+    const uint64_t bits = ((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                          ((uint64_t)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
+// A signed integer that orders doubles as their values do, except that -0.0
+// comes before +0.0 and NaNs fall outside [-inf, +inf]: so key(lo) <= key(x) <=
+// key(hi) implies lo <= x <= hi (the converse fails only for signed zeros and
+// NaN, which callers send down their FP64 path).
+__device__ __forceinline__ long long order_key(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
 // ------------------------------------------------------------------ Philox
 struct u4 {
     uint32_t x, y, z, w;
@@ -167,10 +193,12 @@ struct rng_stream {
         uint32_t a = next();
         return u01d(a, next());
     }
-    // standard normal, Box-Muller on two uniforms
+    // standard normal, Box-Muller on two uniforms (u1 >= 2^-25: the
+    // approximate logarithm's relative error, ~2^-22, is far below what any
+    // test of the draws resolves)
     __device__ float normal() {
         float u1 = uniform(), u2 = uniform();
-        float r = sqrtf(-2.0f * logf(u1));
+        float r = sqrtf(-2.0f * __logf(u1));
         float s, c;
         sincospif(2.0f * u2, &s, &c);
         return r * c;

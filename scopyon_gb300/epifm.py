@@ -358,6 +358,9 @@ class FramePipeline:
         self.gain = torch.from_numpy(numpy.ascontiguousarray(cfg.gain, dtype=float)).to(dev).reshape(-1)
         self.offset_f = self.offset.float()
         self.inv_gain_f = (1.0 / self.gain).float()
+        # without fixed-pattern noise every pixel has the same offset and gain:
+        # the camera takes them from its parameters instead of reading two maps
+        self.pixel_maps = cfg.fpn_type != "none"
         self.sigma = None
         self.table_value = self.table_cdf = None
         n_signal = 2 * self.psf.n_r - 1
@@ -577,8 +580,10 @@ class FramePipeline:
             self.load_cmos_table(self.cfg.cmos_table)
             cp.table_n = self.table_value.numel()
         with self.timed("camera", stream):
-            call("sc_camera", cp, ptr(photons), ptr(self.offset), ptr(self.gain),
-                 ptr(self.offset_f), ptr(self.inv_gain_f), ptr(self.sigma), ptr(self.table_value),
+            maps = self.pixel_maps
+            call("sc_camera", cp, ptr(photons), ptr(self.offset) if maps else None,
+                 ptr(self.gain) if maps else None, ptr(self.offset_f) if maps else None,
+                 ptr(self.inv_gain_f) if maps else None, ptr(self.sigma), ptr(self.table_value),
                  ptr(self.table_cdf), ptr(inj_noise), ptr(inj_signal), ptr(inj_uniform),
                  ptr(expect), ptr(adc64), ptr(adc32), ptr(self.status), s)
 

@@ -860,7 +860,10 @@ def main():
         if args.case == "dgrad":
             res = diffusion_grad_case(dev, 100000, 2048, 100, args.steps, args.warmup, 9)
         elif args.case == "stages":
-            res = hbm_stages(dev, load_peaks()[0], args.steps, args.warmup)
+            # --small: 1M emitters and a 4096^2 frame (still beyond L2), for ncu
+            res = hbm_stages(dev, load_peaks()[0], args.steps, args.warmup,
+                             n_emit=1 << (20 if args.small else 22),
+                             edge=4096 if args.small else 8192)
         elif args.case == "fwdbwd":
             res = fwd_bwd_case(dev, 1, N_EMIT, IMAGE, 90e-9, math.inf, 1e-6, args.steps,
                                args.warmup, 5)

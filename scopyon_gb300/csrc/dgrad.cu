@@ -23,7 +23,7 @@ __device__ __forceinline__ float2 step_normals(uint64_t seed, int e, int t) {
     const float u1 = sc::u01f(r.x), u2 = sc::u01f(r.y);
     const float rad = sqrtf(-2.f * __logf(u1));
     float sn, cs;
-    sincospif(2.f * u2, &sn, &cs);
+    sc::sincos_2pi(u2, &sn, &cs);
     return make_float2(rad * cs, rad * sn);
 }
 

@@ -39,6 +39,14 @@ __device__ __forceinline__ void class_walls(const DiffConsts &c, int cls, int d,
     }
 }
 
+// Reflections of a point outside [lo, hi] (a call, so that the compiler does
+// not evaluate these FP64 compares for the points inside).
+__device__ __noinline__ double reflect_outside(double x, double lo, double hi) {
+    if (x >= lo && x <= hi) return x;
+    for (int it = 0; it < 64 && (x < lo || x > hi); ++it) x = x < lo ? 2 * lo - x : 2 * hi - x;
+    return fmin(fmax(x, lo), hi);
+}
+
 __device__ __forceinline__ double wrap_axis(double x, double lo, double hi, int boundary) {
     if (boundary == 1) {  // periodic: (x - lo) mod (hi - lo) + lo, result in [lo, hi)
         const double len = hi - lo;
@@ -48,12 +56,10 @@ __device__ __forceinline__ double wrap_axis(double x, double lo, double hi, int 
         return r + lo;
     }
     if (boundary == 2) {  // reflecting walls at lo and hi
-        // inside: decided on the integer pipes (order_key), else in FP64
+        // inside: decided on the integer pipes (order_key); else the FP64 path
         const long long kx = sc::order_key(x);
         if (kx >= sc::order_key(lo) && kx <= sc::order_key(hi)) return x;
-        if (x >= lo && x <= hi) return x;
-        for (int it = 0; it < 64 && (x < lo || x > hi); ++it) x = x < lo ? 2 * lo - x : 2 * hi - x;
-        return fmin(fmax(x, lo), hi);
+        return reflect_outside(x, lo, hi);
     }
     return x;
 }
@@ -87,8 +93,8 @@ __device__ __forceinline__ void philox_normals(const DiffConsts &c, int i, uint6
     const float u1 = sc::u01f(r.x), u2 = sc::u01f(r.y), u3 = sc::u01f(r.z), u4 = sc::u01f(r.w);
     const float ra = sqrtf(-2.f * __logf(u1)), rb = sqrtf(-2.f * __logf(u3));
     float sa, ca, sb, cb;
-    sincospif(2.f * u2, &sa, &ca);
-    sincospif(2.f * u4, &sb, &cb);
+    sc::sincos_2pi(u2, &sa, &ca);
+    sc::sincos_2pi(u4, &sb, &cb);
     nrm[0] = ra * ca;
     nrm[1] = ra * sa;
     nrm[2] = rb * cb;
@@ -117,43 +123,86 @@ __device__ __forceinline__ int transition(const DiffConsts &c, int cls, int i, i
     return next_class(c.trans + ((size_t)s * c.n_class + cls) * c.n_class, c.n_class, u);
 }
 
-// One thread per particle, sub-steps in order.
-__global__ void diffuse_kernel(DiffConsts c, double *pos, int32_t *klass,
-                               const double *sigma, const double *normals, double *particles) {
+// One sub-step of a particle: x_d += sigma_d * n_d on every axis (the
+// reference's 0.0 + sigma * gauss; normals from the caller's nv, else the
+// FP32 Philox normals nrm), then the walls.  The axes are independent, so
+// moving and wrapping one axis at a time equals moving all, then wrapping.
+// The loop runs over a fixed 3 (ndim is 2 or 3) so that p stays in registers.
+// kInjected selects the normals at compile time: as a run-time test the
+// compiler predicates both forms, and the FP64 pipe (about 1/64 of the FP32
+// rate on GB300) then issues the injected form's multiply and add as well.
+template <bool kInjected>
+__device__ __forceinline__ void move_point(const DiffConsts &c, double *p, int cls,
+                                           const double *sg, const double *nv, const float *nrm) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (d >= c.ndim) break;
+        if (kInjected) p[d] += __dmul_rn(sg[d], nv[d]);
+        else p[d] = fma(sg[d], sc::f2d_exact(nrm[d]), p[d]);
+        if (c.boundary) {
+            double lo, hi;
+            class_walls(c, cls, d, lo, hi);
+            p[d] = wrap_axis(p[d], lo, hi, c.boundary);
+        }
+    }
+}
+
+constexpr int kDiffThreads = 128;
+
+// One thread per particle, sub-steps in order.  Each warp stages its 32 rows
+// of a sub-step ([depth, x, y, id, state], 40 B each) in shared memory and
+// writes the 1280 contiguous bytes with five coalesced 8-byte stores per
+// lane: 40 full sectors per warp and sub-step, where a row per lane would
+// touch 32 sectors with each of its five stores.
+template <bool kInjected>
+__global__ void __launch_bounds__(kDiffThreads)
+diffuse_kernel(DiffConsts c, double *pos, int32_t *klass, const double *sigma,
+               const double *normals, double *particles) {
+    __shared__ double rows[kDiffThreads * 5];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= c.n) return;
-    double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
-    int k = klass ? klass[i] : 0;
+    const int lane = threadIdx.x & 31;
+    const int first = i - lane;  // this warp's first particle
+    if (first >= c.n) return;    // whole warps only: the staging below is warp-wide
+    const bool live = i < c.n;
+    const int n_rows = min(32, c.n - first);
+    double *stage = rows + (threadIdx.x - lane) * 5;
+    double p[3] = {0.0, 0.0, 0.0};
+    int k = 0;
+    if (live) {
+        p[0] = pos[3 * i];
+        p[1] = pos[3 * i + 1];
+        p[2] = pos[3 * i + 2];
+        k = klass ? klass[i] : 0;
+    }
     const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
     const double id = (double)i;
     for (int s = 0; s < c.n_sub; ++s) {
         const size_t idx = (size_t)s * c.n + i;
-        double *q = particles + idx * 5;
         double f[3];
         format_point(c, p, f);
+        double *q = stage + lane * 5;
         q[0] = f[0];
         q[1] = f[1];
         q[2] = f[2];
         q[3] = id;
         q[4] = 1.0;
-        // one Brownian step: x_d += sigma_d * n_d (the reference's 0.0 + sigma * gauss)
-        const double *sg = sigma + ((size_t)s * c.n_class + k) * 3;
-        if (normals) {
-            const double *nv = normals + idx * c.ndim;
-            for (int d = 0; d < c.ndim; ++d) p[d] += __dmul_rn(sg[d], nv[d]);
-        } else {
-            float nrm[3];
-            philox_normals(c, i, (uint64_t)(step0 + s), nrm);
-            for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], sc::f2d_exact(nrm[d]), p[d]);
+        __syncwarp();
+        double *dst = particles + ((size_t)s * c.n + first) * 5;
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+            const int e = lane + 32 * r;
+            if (e < n_rows * 5) dst[e] = stage[e];
         }
-        if (c.boundary)
-            for (int d = 0; d < c.ndim; ++d) {
-                double lo, hi;
-                class_walls(c, k, d, lo, hi);
-                p[d] = wrap_axis(p[d], lo, hi, c.boundary);
-            }
+        __syncwarp();
+        if (!live) continue;
+        // one Brownian step
+        const double *sg = sigma + ((size_t)s * c.n_class + k) * 3;
+        float nrm[3] = {0.f, 0.f, 0.f};
+        if (!kInjected) philox_normals(c, i, (uint64_t)(step0 + s), nrm);
+        move_point<kInjected>(c, p, k, sg, kInjected ? normals + idx * c.ndim : nullptr, nrm);
         if (c.trans) k = transition(c, k, i, s, (uint64_t)(step0 + s));
     }
+    if (!live) return;
     pos[3 * i] = p[0];
     pos[3 * i + 1] = p[1];
     pos[3 * i + 2] = p[2];
@@ -184,7 +233,11 @@ inline size_t rec_shared_bytes(int chunk) {
                             32 * 3 * sizeof(float));
 }
 
-__global__ void __launch_bounds__(kRecWarps * 32, 8)
+#ifndef SC_REC_MIN_BLOCKS
+#define SC_REC_MIN_BLOCKS 6
+#endif
+template <bool kInjected>
+__global__ void __launch_bounds__(kRecWarps * 32, SC_REC_MIN_BLOCKS)
 native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                       int32_t *klass, const double *sigma, const double *normals,
                       const double *unit_time, double *budget, const int32_t *key_slot,
@@ -217,7 +270,7 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
     for (int s0 = 0; s0 < c.n_sub; s0 += chunk) {
         const int ns = min(chunk, c.n_sub - s0);
         // 1. normals; per-sub-step photons and normalisation under EPI
-        if (!normals) {
+        if (!kInjected) {
             for (int j = warp; j < ns; j += kRecWarps) {
                 float nrm[3] = {0.f, 0.f, 0.f};
                 if (live) philox_normals(c, i, (uint64_t)(step0 + s0 + j), nrm);
@@ -276,19 +329,9 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                 // p_state = 0 gives norm_coeff * (0 / 4 pi) = 0: no record
                 s_norm[j * 32 + lane] = !alive ? 0.0 : (epi ? s_norm1[j] : norm_prev);
                 const double *sg = sigma + ((size_t)s * c.n_class + cls) * 3;
-                if (normals) {
-                    const double *nv = normals + ((size_t)s * c.n + i) * c.ndim;
-                    for (int d = 0; d < c.ndim; ++d) p[d] += __dmul_rn(sg[d], nv[d]);
-                } else {
-                    const float *nr = s_nrm + (j * 32 + lane) * 3;
-                    for (int d = 0; d < c.ndim; ++d) p[d] = fma(sg[d], sc::f2d_exact(nr[d]), p[d]);
-                }
-                if (c.boundary)
-                    for (int d = 0; d < c.ndim; ++d) {
-                        double lo, hi;
-                        class_walls(c, cls, d, lo, hi);
-                        p[d] = wrap_axis(p[d], lo, hi, c.boundary);
-                    }
+                move_point<kInjected>(c, p, cls, sg,
+                                      kInjected ? normals + ((size_t)s * c.n + i) * c.ndim : nullptr,
+                                      s_nrm + (j * 32 + lane) * 3);
                 if (c.trans) cls = transition(c, cls, i, s, (uint64_t)(step0 + s));
             }
         }
@@ -376,9 +419,14 @@ extern "C" int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, int32_t
     if (c.n == 0 || c.n_sub == 0) return SC_OK;
     SC_REQUIRE(d_pos && d_sigma && d_particles, "sc_diffuse_steps: NULL pointer");
     SC_REQUIRE(!p->d_trans || d_class, "sc_diffuse_steps: transitions need the class array");
-    const int block = 128;
-    diffuse_kernel<<<(c.n + block - 1) / block, block, 0, sc::as_stream(stream)>>>(
-        c, d_pos, d_class, d_sigma, d_normals, d_particles);
+    const int block = kDiffThreads;
+    const int grid = (c.n + block - 1) / block;
+    if (d_normals)
+        diffuse_kernel<true><<<grid, block, 0, sc::as_stream(stream)>>>(
+            c, d_pos, d_class, d_sigma, d_normals, d_particles);
+    else
+        diffuse_kernel<false><<<grid, block, 0, sc::as_stream(stream)>>>(
+            c, d_pos, d_class, d_sigma, d_normals, d_particles);
     return sc::launch_status("sc_diffuse_steps");
 }
 
@@ -417,8 +465,13 @@ extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *s
     }
     const int chunk = c.n_sub < 32 ? c.n_sub : 32;
     const size_t smem = rec_shared_bytes(chunk);
-    native_records_kernel<<<(c.n + 31) / 32, kRecWarps * 32, smem, sc::as_stream(stream)>>>(
-        c, k, chunk, d_pos, d_class, d_sigma, d_normals, d_unit_time, d_budget, d_key_slot, d_recs,
-        g, bl, d_status);
+    if (d_normals)
+        native_records_kernel<true><<<(c.n + 31) / 32, kRecWarps * 32, smem, sc::as_stream(stream)>>>(
+            c, k, chunk, d_pos, d_class, d_sigma, d_normals, d_unit_time, d_budget, d_key_slot,
+            d_recs, g, bl, d_status);
+    else
+        native_records_kernel<false><<<(c.n + 31) / 32, kRecWarps * 32, smem, sc::as_stream(stream)>>>(
+            c, k, chunk, d_pos, d_class, d_sigma, d_normals, d_unit_time, d_budget, d_key_slot,
+            d_recs, g, bl, d_status);
     return sc::launch_status("sc_native_records");
 }

@@ -109,15 +109,30 @@ __device__ __forceinline__ void df_acc(float &s, float &e, float hi, float lo, f
 // 1/64 of the FP32 rate; these two replace a conversion and a compare that
 // the Brownian sub-step loops would otherwise issue to the FP64 pipe.
 
-// float -> double, exactly as the conversion instruction gives it: sign, the
-// exponent rebiased by 1023 - 127 = 896, the 23 fraction bits moved to the top
-// of the 52.  Zero, subnormals, infinities and NaN take the conversion.
+// float -> double on the integer pipes: sign, the exponent rebiased by
+// 1023 - 127 = 896, the 23 fraction bits moved to the top of the 52.
+// Subnormals are normalised (top set bit t of the fraction: exponent field
+// t + 874); zeros and infinities keep their sign; a NaN becomes a quiet NaN
+// with its payload.  Equal, bit for bit, to the conversion instruction for
+// every non-NaN float.
 __device__ __forceinline__ double f2d_exact(float f) {
     const uint32_t u = __float_as_uint(f);
-    const uint32_t e = (u >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)f;
-    const uint64_t bits = ((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
-                          ((uint64_t)(u & 0x7fffffu) << 29);
+    const uint32_t e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    const uint64_t sign = (uint64_t)(u >> 31) << 63;
+    uint64_t bits;
+    if (e == 0u) {
+        if (m == 0u) {
+            bits = sign;
+        } else {
+            const int t = 31 - __clz((int)m);
+            bits = sign | ((uint64_t)(t + 874) << 52) |
+                   (((uint64_t)m << (52 - t)) & 0xfffffffffffffull);
+        }
+    } else if (e == 0xffu) {
+        bits = sign | (0x7ffull << 52) | ((uint64_t)(m ? (m | 0x400000u) : 0u) << 29);
+    } else {
+        bits = sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)m << 29);
+    }
     return __longlong_as_double((long long)bits);
 }
 
@@ -152,6 +167,17 @@ __device__ __forceinline__ u4 philox4x32_10(u4 ctr, uint32_t k0, uint32_t k1) {
         k1 += W1;
     }
     return ctr;
+}
+
+// (sin, cos) of 2 pi u for u in (0, 1), the Box-Muller angle: the hardware's
+// approximate sine and cosine of 2 pi (u - 1/2), in [-pi, pi) where their
+// absolute error is about 5e-7, negated.  All on the FP32 and SFU pipes (the
+// angle needs no more accuracy than this for standard normals).
+__device__ __forceinline__ void sincos_2pi(float u, float *s, float *c) {
+    float sn, cs;
+    __sincosf(6.28318530718f * (u - 0.5f), &sn, &cs);
+    *s = -sn;
+    *c = -cs;
 }
 
 // uniform in (0, 1) from 32 bits
@@ -200,7 +226,7 @@ struct rng_stream {
         float u1 = uniform(), u2 = uniform();
         float r = sqrtf(-2.0f * __logf(u1));
         float s, c;
-        sincospif(2.0f * u2, &s, &c);
+        sincos_2pi(u2, &s, &c);
         return r * c;
     }
 };

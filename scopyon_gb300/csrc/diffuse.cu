@@ -39,11 +39,31 @@ __device__ __forceinline__ void class_walls(const DiffConsts &c, int cls, int d,
     }
 }
 
-// Reflections of a point outside [lo, hi] (a call, so that the compiler does
-// not evaluate these FP64 compares for the points inside).
-__device__ __noinline__ double reflect_outside(double x, double lo, double hi) {
-    if (x >= lo && x <= hi) return x;
-    for (int it = 0; it < 64 && (x < lo || x > hi); ++it) x = x < lo ? 2 * lo - x : 2 * hi - x;
+// a < b as the FP64 compare gives it, from the order keys ka, kb: two zeros
+// are equal whatever their signs (NaN aside, which the clamp below handles).
+__device__ __forceinline__ bool key_less(long long ka, long long kb, double a, double b) {
+    return ka < kb &&
+           ((__double_as_longlong(a) | __double_as_longlong(b)) & 0x7fffffffffffffffLL) != 0;
+}
+
+// Reflecting walls at lo and hi: a point inside is returned as it is; one
+// outside is mirrored in the wall it crossed until it is inside (at most 64
+// times), then clamped.  The compares run on the integer pipes (order keys):
+// GB300 issues FP64 instructions at about 1/64 of the FP32 rate, and a
+// predicated-off FP64 instruction costs as much as an executed one, so the
+// only FP64 work is one fused multiply-add per reflection and the clamp.
+__device__ __forceinline__ double reflect_walls(double x, double lo, double hi) {
+    const long long klo = sc::order_key(lo), khi = sc::order_key(hi);
+    long long kx = sc::order_key(x);
+    bool below = key_less(kx, klo, x, lo), above = key_less(khi, kx, hi, x);
+    if (!below && !above) return x;
+    for (int it = 0; it < 64 && (below || above); ++it) {
+        const double wall = below ? lo : hi;
+        x = 2 * wall - x;
+        kx = sc::order_key(x);
+        below = key_less(kx, klo, x, lo);
+        above = key_less(khi, kx, hi, x);
+    }
     return fmin(fmax(x, lo), hi);
 }
 
@@ -55,12 +75,7 @@ __device__ __forceinline__ double wrap_axis(double x, double lo, double hi, int 
         if (r < 0) r += len;
         return r + lo;
     }
-    if (boundary == 2) {  // reflecting walls at lo and hi
-        // inside: decided on the integer pipes (order_key); else the FP64 path
-        const long long kx = sc::order_key(x);
-        if (kx >= sc::order_key(lo) && kx <= sc::order_key(hi)) return x;
-        return reflect_outside(x, lo, hi);
-    }
+    if (boundary == 2) return reflect_walls(x, lo, hi);
     return x;
 }
 

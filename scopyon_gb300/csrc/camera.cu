@@ -101,70 +101,164 @@ __device__ __forceinline__ int table_index(const double *cdf, int n, double u) {
     return lo < n ? lo : n - 1;
 }
 
-__global__ void camera_kernel(CamConsts c, const float *__restrict__ photons,
-                              const double *__restrict__ offset, const double *__restrict__ gain,
-                              const float *__restrict__ offset_f, const float *__restrict__ inv_gain_f,
-                              const float *__restrict__ sigma, const double *__restrict__ table_value,
-                              const double *__restrict__ table_cdf, const double *__restrict__ inj_noise,
-                              const double *__restrict__ inj_signal, const double *__restrict__ inj_uniform,
-                              float *__restrict__ expect, double *__restrict__ adc64,
-                              float *__restrict__ adc32, int32_t *status) {
+// One pixel's native draws (Philox stream keyed by the seed and the pixel, at
+// the frame's counter; FP32 throughout, GB300's FP64 rate being ~1/64 of
+// FP32) and its ADC count.
+__device__ __forceinline__ void native_pixel(const CamConsts &c, int p, float ef, uint64_t counter,
+                                             const float *__restrict__ offset_f,
+                                             const float *__restrict__ inv_gain_f,
+                                             const float *__restrict__ sigma,
+                                             const double *__restrict__ table_value,
+                                             const double *__restrict__ table_cdf,
+                                             double *__restrict__ adc64, float *__restrict__ adc32,
+                                             int32_t *status) {
+    sc::rng_stream rs(c.seed, (uint32_t)p, (uint32_t)counter, (uint32_t)(counter >> 32));
+    float signal, noise;
+    switch (c.camera) {
+        case SC_CAM_EMCCD: {
+            const float n_in = poisson(rs, ef, status);
+            signal = n_in > 0.f ? rintf(c.emgain_f * gamma_ge1(rs, n_in, status)) : 0.f;
+            noise = c.readout_f > 0.f ? c.readout_f * rs.normal() : 0.f;
+            break;
+        }
+        case SC_CAM_CCD:
+            signal = poisson(rs, ef, status);
+            noise = c.readout_f > 0.f ? c.readout_f * rs.normal() : 0.f;
+            break;
+        case SC_CAM_CMOS_TABLE:
+            noise = (float)table_value[table_index(table_cdf, c.table_n, rs.uniform_d())];
+            signal = poisson(rs, ef, status);
+            break;
+        default:  // SC_CAM_SCMOS
+            signal = poisson(rs, ef, status);
+            noise = (sigma ? sigma[p] : c.readout_f) * rs.normal();
+            break;
+    }
+    float v = fminf(signal + noise, c.fullwell_f);
+    v = v * (inv_gain_f ? inv_gain_f[p] : c.inv_gain0_f) + (offset_f ? offset_f[p] : c.offset0_f);
+    v = fminf(fmaxf(v, 0.f), c.adc_max_f);
+    if (c.rounding) v = rintf(v);
+    if (adc32) adc32[p] = v;
+    if (adc64) adc64[p] = sc::f2d_exact(v);
+}
+
+// Injected draws: the reference's FP64 arithmetic on the caller's draws.
+__global__ void camera_exact_kernel(CamConsts c, const float *__restrict__ photons,
+                                    const double *__restrict__ offset, const double *__restrict__ gain,
+                                    const double *__restrict__ table_value,
+                                    const double *__restrict__ table_cdf,
+                                    const double *__restrict__ inj_noise,
+                                    const double *__restrict__ inj_signal,
+                                    const double *__restrict__ inj_uniform,
+                                    float *__restrict__ expect, double *__restrict__ adc64,
+                                    float *__restrict__ adc32) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.n; p += stride) {
+        // E = QE (photons + background) with the reference's FP64 rounding
+        const double ph = (double)photons[p] + c.background;
+        const double e = __dmul_rn(c.qe, ph);
+        if (expect) expect[p] = (float)e;
+        double noise, signal;
+        if (c.camera == SC_CAM_CMOS_TABLE && inj_uniform)
+            noise = table_value[table_index(table_cdf, c.table_n, inj_uniform[p])];
+        else
+            noise = inj_noise ? inj_noise[p] : 0.0;
+        signal = inj_signal ? inj_signal[p] : 0.0;
+        double v = signal + noise;
+        if (v > c.fullwell) v = c.fullwell;
+        v /= gain ? gain[p] : c.gain0;
+        v += offset ? offset[p] : c.offset0;
+        if (v > c.adc_max) v = c.adc_max;
+        if (v < 0) v = 0;
+        if (c.rounding) v = rint(v);
+        if (adc64) adc64[p] = v;
+        if (adc32) adc32[p] = (float)v;
+    }
+}
+
+// Native draws, a pixel per thread (frames of a few hundred thousand pixels,
+// which need every resident warp).
+__global__ void camera_pixel_kernel(CamConsts c, const float *__restrict__ photons,
+                                    const float *__restrict__ offset_f,
+                                    const float *__restrict__ inv_gain_f,
+                                    const float *__restrict__ sigma,
+                                    const double *__restrict__ table_value,
+                                    const double *__restrict__ table_cdf,
+                                    float *__restrict__ expect, double *__restrict__ adc64,
+                                    float *__restrict__ adc32, int32_t *status) {
     const int stride = gridDim.x * blockDim.x;
     const uint64_t counter = c.counter + (c.frame ? (uint64_t)*c.frame : 0);
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.n; p += stride) {
-        if (c.exact) {
-            // E = QE (photons + background) with the reference's FP64 rounding
-            const double ph = (double)photons[p] + c.background;
-            const double e = __dmul_rn(c.qe, ph);
-            if (expect) expect[p] = (float)e;
-            double noise, signal;
-            if (c.camera == SC_CAM_CMOS_TABLE && inj_uniform)
-                noise = table_value[table_index(table_cdf, c.table_n, inj_uniform[p])];
-            else
-                noise = inj_noise ? inj_noise[p] : 0.0;
-            signal = inj_signal ? inj_signal[p] : 0.0;
-            double v = signal + noise;
-            if (v > c.fullwell) v = c.fullwell;
-            v /= gain ? gain[p] : c.gain0;
-            v += offset ? offset[p] : c.offset0;
-            if (v > c.adc_max) v = c.adc_max;
-            if (v < 0) v = 0;
-            if (c.rounding) v = rint(v);
-            if (adc64) adc64[p] = v;
-            if (adc32) adc32[p] = (float)v;
-            continue;
-        }
-        // native draws: FP32 throughout (GB300's FP64 rate is ~1/64 of FP32)
         const float ef = c.qe_f * (photons[p] + c.background_f);
         if (expect) expect[p] = ef;
-        sc::rng_stream rs(c.seed, (uint32_t)p, (uint32_t)counter, (uint32_t)(counter >> 32));
-        float signal, noise;
-        switch (c.camera) {
-            case SC_CAM_EMCCD: {
-                const float n_in = poisson(rs, ef, status);
-                signal = n_in > 0.f ? rintf(c.emgain_f * gamma_ge1(rs, n_in, status)) : 0.f;
-                noise = c.readout_f > 0.f ? c.readout_f * rs.normal() : 0.f;
-                break;
+        native_pixel(c, p, ef, counter, offset_f, inv_gain_f, sigma, table_value, table_cdf,
+                     adc64, adc32, status);
+    }
+}
+
+constexpr int kCamThreads = 256;
+constexpr int kCamMaxPer = 8;  // pixels per lane per chunk, at most
+
+// Native draws.  Each warp takes chunks of 32 * per pixels: it writes their
+// expectations, sorts the pixels by the Poisson method they need (inversion
+// below lambda = 12 and empty pixels to the front of a shared list, PTRS to
+// the back) with ballots, then draws them 32 at a time, one list after the
+// other.  A pixel's draws are those of its own Philox stream whichever lane
+// takes it, so the counts do not depend on the grouping; the grouping keeps
+// a warp from running both methods' loops for one set of 32 pixels (6% off
+// an 8192^2 frame).  Frames too small to fill the GPU twice over take
+// camera_pixel_kernel instead.
+__global__ void __launch_bounds__(kCamThreads)
+camera_native_kernel(CamConsts c, int per, const float *__restrict__ photons,
+                     const float *__restrict__ offset_f, const float *__restrict__ inv_gain_f,
+                     const float *__restrict__ sigma, const double *__restrict__ table_value,
+                     const double *__restrict__ table_cdf, float *__restrict__ expect,
+                     double *__restrict__ adc64, float *__restrict__ adc32, int32_t *status) {
+    constexpr int kWarps = kCamThreads / 32, kList = 32 * kCamMaxPer;
+    __shared__ int s_pix[kWarps][kList];
+    __shared__ float s_ef[kWarps][kList];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint64_t counter = c.counter + (c.frame ? (uint64_t)*c.frame : 0);
+    const int chunk = 32 * per;
+    const int64_t warps = (int64_t)gridDim.x * kWarps;
+    int *pix = s_pix[warp];
+    float *efs = s_ef[warp];
+    const unsigned below = (1u << lane) - 1u;
+    for (int64_t base = ((int64_t)blockIdx.x * kWarps + warp) * chunk; base < c.n;
+         base += warps * chunk) {
+        int n_front = 0, n_back = 0;
+        for (int j = 0; j < per; ++j) {
+            const int64_t p = base + j * 32 + lane;
+            const bool valid = p < c.n;
+            float ef = 0.f;
+            if (valid) {
+                ef = c.qe_f * (photons[p] + c.background_f);
+                if (expect) expect[p] = ef;
             }
-            case SC_CAM_CCD:
-                signal = poisson(rs, ef, status);
-                noise = c.readout_f > 0.f ? c.readout_f * rs.normal() : 0.f;
-                break;
-            case SC_CAM_CMOS_TABLE:
-                noise = (float)table_value[table_index(table_cdf, c.table_n, rs.uniform_d())];
-                signal = poisson(rs, ef, status);
-                break;
-            default:  // SC_CAM_SCMOS
-                signal = poisson(rs, ef, status);
-                noise = (sigma ? sigma[p] : c.readout_f) * rs.normal();
-                break;
+            const bool ptrs = valid && ef >= 12.f;  // poisson()'s own threshold
+            const bool front = valid && !ptrs;
+            const unsigned mf = __ballot_sync(~0u, front), mp = __ballot_sync(~0u, ptrs);
+            if (front) {
+                const int k = n_front + __popc(mf & below);
+                pix[k] = (int)p;
+                efs[k] = ef;
+            }
+            if (ptrs) {
+                const int k = kList - 1 - (n_back + __popc(mp & below));
+                pix[k] = (int)p;
+                efs[k] = ef;
+            }
+            n_front += __popc(mf);
+            n_back += __popc(mp);
         }
-        float v = fminf(signal + noise, c.fullwell_f);
-        v = v * (inv_gain_f ? inv_gain_f[p] : c.inv_gain0_f) + (offset_f ? offset_f[p] : c.offset0_f);
-        v = fminf(fmaxf(v, 0.f), c.adc_max_f);
-        if (c.rounding) v = rintf(v);
-        if (adc32) adc32[p] = v;
-        if (adc64) adc64[p] = sc::f2d_exact(v);
+        __syncwarp();
+        for (int k = lane; k < n_front; k += 32)
+            native_pixel(c, pix[k], efs[k], counter, offset_f, inv_gain_f, sigma, table_value,
+                         table_cdf, adc64, adc32, status);
+        for (int k = lane; k < n_back; k += 32)
+            native_pixel(c, pix[kList - 1 - k], efs[kList - 1 - k], counter, offset_f, inv_gain_f,
+                         sigma, table_value, table_cdf, adc64, adc32, status);
+        __syncwarp();
     }
 }
 
@@ -293,13 +387,48 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
     c.seed = p->seed;
     c.counter = p->counter;
     c.frame = p->d_frame;
-    const int block = 256;
-    int grid = (c.n + block - 1) / block;
-    if (grid > 152 * 16) grid = 152 * 16;
-    camera_kernel<<<grid, block, 0, sc::as_stream(stream)>>>(
-        c, d_photons, d_offset, d_gain, d_offset_f, d_inv_gain_f, d_sigma, d_table_value,
-        d_table_cdf, d_inj_noise, d_inj_signal, d_inj_uniform, d_expect, d_adc64, d_adc32,
-        d_status);
+    cudaStream_t st = sc::as_stream(stream);
+    if (p->exact) {
+        const int block = 256;
+        int grid = (c.n + block - 1) / block;
+        if (grid > 152 * 16) grid = 152 * 16;
+        camera_exact_kernel<<<grid, block, 0, st>>>(c, d_photons, d_offset, d_gain, d_table_value,
+                                                    d_table_cdf, d_inj_noise, d_inj_signal,
+                                                    d_inj_uniform, d_expect, d_adc64, d_adc32);
+    } else {
+        // chunks of 32 * per pixels per warp, 8 per lane once the frame fills
+        // the GPU's resident threads (152 SMs x 2048) 8 times; below twice, a
+        // pixel per thread
+        int per = (int)((int64_t)c.n / (152 * 2048));
+        if (per < 2) {
+            const int block = 256;
+            int grid = (c.n + block - 1) / block;
+            if (grid > 152 * 16) grid = 152 * 16;
+            camera_pixel_kernel<<<grid, block, 0, st>>>(c, d_photons, d_offset_f, d_inv_gain_f,
+                                                        d_sigma, d_table_value, d_table_cdf,
+                                                        d_expect, d_adc64, d_adc32, d_status);
+            return sc::launch_status("sc_camera");
+        }
+        per = per > kCamMaxPer ? kCamMaxPer : per;
+        // at most one wave of resident blocks: the chunks are strided over the
+        // grid, so a second wave would start late and finish late
+        static int resident = 0;
+        if (resident == 0) {
+            int b = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, camera_native_kernel,
+                                                              kCamThreads, 0) != cudaSuccess ||
+                b < 1)
+                b = 1;
+            resident = b;
+        }
+        const int64_t chunks = ((int64_t)c.n + 32 * per - 1) / (32 * per);
+        const int64_t blocks = (chunks + kCamThreads / 32 - 1) / (kCamThreads / 32);
+        const int64_t wave = (int64_t)152 * resident;
+        const int grid = (int)(blocks < wave ? blocks : wave);
+        camera_native_kernel<<<grid, kCamThreads, 0, st>>>(
+            c, per, d_photons, d_offset_f, d_inv_gain_f, d_sigma, d_table_value, d_table_cdf,
+            d_expect, d_adc64, d_adc32, d_status);
+    }
     return sc::launch_status("sc_camera");
 }
 

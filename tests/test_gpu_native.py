@@ -155,6 +155,61 @@ def test_native_scmos_per_pixel_sigma(sg):
     assert 1.5 < numpy.median(pv) < 3.2
 
 
+@pytest.mark.parametrize("kind", ["EMCCD", "CCD", "CMOS_TABLE", "SCMOS"])
+def test_camera_draws_do_not_depend_on_the_grouping(sg, kind):
+    """A pixel's native draws come from its own Philox stream: a frame small
+    enough for the pixel-per-thread kernel and frames large enough for the
+    grouped kernel (3 and 6 pixels per lane per chunk) give the same counts,
+    bit for bit, on the pixels they share.  Photons mix empty pixels, means
+    below the PTRS threshold and bright pixels."""
+    from scopyon_gb300 import _lib
+    from scopyon_gb300._lib import call, ptr, stream_ptr
+    dev = torch.device("cuda")
+    nh = 1024
+    n_big = 2048 * nh
+    g = torch.Generator(dev).manual_seed(11)
+    u = torch.rand(n_big, device=dev, generator=g)
+    photons = torch.where(u < 0.3, torch.zeros_like(u),
+                          torch.where(u < 0.7, 15.0 * torch.rand(n_big, device=dev, generator=g),
+                                      15.0 + 500.0 * torch.rand(n_big, device=dev, generator=g)))
+    offset_f = torch.round(100.0 + 5.0 * torch.randn(n_big, device=dev, generator=g))
+    inv_gain_f = (4096.0 - offset_f) / 30000.0
+    sigma = torch.exp(0.4 + 0.4 * torch.randn(n_big, device=dev, generator=g))
+    tv = torch.linspace(0.5, 5.0, 16, dtype=torch.float64, device=dev)
+    tc = torch.cumsum(torch.full((16,), 1.0 / 16, dtype=torch.float64, device=dev), 0)
+    tc[-1] = 1.0
+    status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
+    cam = {"EMCCD": _lib.CAM_EMCCD, "CCD": _lib.CAM_CCD, "CMOS_TABLE": _lib.CAM_CMOS_TABLE,
+           "SCMOS": _lib.CAM_SCMOS}[kind]
+
+    def run(nw):
+        n = nw * nh
+        cp = _lib.CameraParams()
+        cp.nw, cp.nh, cp.camera, cp.exact, cp.rounding, cp.bit = nw, nh, cam, 0, 1, 16
+        cp.qe, cp.background, cp.readout_noise = 0.9, 2.0, 3.0
+        cp.emgain, cp.fullwell, cp.offset0, cp.gain0 = 300.0, 6.0e5, 100.0, 10.0
+        cp.table_n = 16 if kind == "CMOS_TABLE" else 0
+        cp.seed, cp.counter = 1234567, 5
+        expect = torch.empty(n, dtype=torch.float32, device=dev)
+        adc = torch.empty(n, dtype=torch.float64, device=dev)
+        call("sc_camera", cp, ptr(photons), None, None, ptr(offset_f), ptr(inv_gain_f),
+             ptr(sigma) if kind == "SCMOS" else None, ptr(tv), ptr(tc), None, None, None,
+             ptr(expect), ptr(adc), None, ptr(status), stream_ptr())
+        torch.cuda.synchronize()
+        return expect.cpu().numpy(), adc.cpu().numpy()
+
+    e_small, a_small = run(300)   # 307,200 px: a pixel per thread
+    e_mid, a_mid = run(1024)      # 1,048,576 px: 3 pixels per lane per chunk
+    e_big, a_big = run(2048)      # 2,097,152 px: 6 pixels per lane per chunk
+    assert int(status[0].item()) == 0
+    k = len(a_small)
+    numpy.testing.assert_array_equal(e_mid[:k], e_small)
+    numpy.testing.assert_array_equal(a_mid[:k], a_small)
+    numpy.testing.assert_array_equal(e_big[:len(e_mid)], e_mid)
+    numpy.testing.assert_array_equal(a_big[:len(a_mid)], a_mid)
+    assert len(numpy.unique(a_big)) > 100
+
+
 def test_poisson_sampler_distribution(sg):
     """Photo-electron counts of the CCD path (read noise off) follow Poisson(E): chi-square."""
     from scipy import stats

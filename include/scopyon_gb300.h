@@ -142,6 +142,18 @@ int sc_get_version(void);
 int sc_counter_add(int64_t *d_counter, int64_t delta, void *stream);
 const char *sc_last_error(void);
 
+/* Host helper of the frame upload (no device work): one pass over a
+ * sub-step's n rows [depth, x, y, id, state] (row-major FP64) that checks
+ * each id against ids[i] (the known slot order), copies the rows to dst (the
+ * pinned staging buffer) and writes the depth range to depth_range[0..1]
+ * (NaN when a depth is NaN).  Returns 1 at the first differing id (the
+ * caller then takes the general path), 0 otherwise.  Replaces the per-frame
+ * stacking of EPIFMSimulator.__format_data's output
+ * (src/scopyon/base.py:61-110) and the depth scan of
+ * _EPIFMSimulator.output_frame (src/scopyon/_epifm.py:1121-1225).          */
+int sc_stage_rows(const double *src, int64_t n, const double *ids, double *dst,
+                  double *depth_range);
+
 /* Radial PSF tables for n_keys depths, n_r radii each (r_i = i * res).
  * Replaces PointSpreadingFunction.get_born_wolf_distribution /
  * get_gaussian_distribution (src/scopyon/_epifm.py:136-213).               */

@@ -79,6 +79,7 @@ _D = ctypes.c_double
 _SIG = {
     "sc_get_version": (_I, []),
     "sc_counter_add": (_I, [_P, ctypes.c_int64, _P]),
+    "sc_stage_rows": (_I, [_P, ctypes.c_int64, _P, _P, _P]),
     "sc_last_error": (ctypes.c_char_p, []),
     "sc_psf_radial": (_I, [_I, _D, _D, _D, _P, _I, _I, _D, _P, _P]),
     "sc_diffuse_steps": (_I, [ctypes.POINTER(DiffuseParams), _P, _P, _P, _P, _P, _P]),

@@ -15,6 +15,7 @@ is given.
 
 import collections.abc
 import concurrent.futures
+import math
 import numbers
 import os
 import warnings
@@ -179,12 +180,26 @@ def _stage_known(arrays, slot_ids_f, staging):
     """Copies each sub-step's array into the pinned staging buffer, on the
     host threads, when every array has exactly the known ids in slot order;
     returns (depth min, depth max), or None when the ids differ (the caller
-    then takes the general path)."""
+    then takes the general path).  Row-major float64 arrays go through
+    ``sc_stage_rows`` (one native pass per sub-step, GIL released); others
+    through numpy."""
     n = len(slot_ids_f)
+    lib = _lib.load()
+    ids = numpy.ascontiguousarray(slot_ids_f, dtype=numpy.float64)
 
     def one(k):
         a = arrays[k]
-        if a.shape != (n, 5) or not numpy.array_equal(a[:, 3], slot_ids_f):
+        if a.shape != (n, 5):
+            return None
+        if a.dtype == numpy.float64 and a.flags.c_contiguous:
+            rng_ = numpy.empty(2)
+            rc = lib.sc_stage_rows(a.ctypes.data, n, ids.ctypes.data, staging[k].ctypes.data,
+                                   rng_.ctypes.data)
+            if rc == 1:
+                return None
+            _lib.check(rc, "sc_stage_rows")
+            return float(rng_[0]), float(rng_[1])
+        if not numpy.array_equal(a[:, 3], slot_ids_f):
             return None
         numpy.copyto(staging[k], a)
         d = staging[k, :, 0]
@@ -193,6 +208,8 @@ def _stage_known(arrays, slot_ids_f, staging):
     res = list(_host_pool().map(one, range(len(arrays))))
     if any(r is None for r in res):
         return None
+    if any(math.isnan(r[0]) or math.isnan(r[1]) for r in res):
+        return math.nan, math.nan  # refused by ensure_depth_range
     return min(r[0] for r in res), max(r[1] for r in res)
 
 

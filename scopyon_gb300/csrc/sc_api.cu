@@ -38,3 +38,39 @@ extern "C" int sc_counter_add(int64_t *d_counter, int64_t delta, void *stream) {
     counter_add_kernel<<<1, 1, 0, sc::as_stream(stream)>>>(d_counter, delta);
     return sc::launch_status("sc_counter_add");
 }
+
+// Host side of the frame upload: one pass over a sub-step's (n x 5) rows
+// [depth, x, y, id, state] that checks the ids against the known slot order,
+// copies the rows into the (pinned) staging buffer and takes the depth range.
+// Returns 1 at the first id that differs (dst then partly written), else 0.
+extern "C" int sc_stage_rows(const double *src, int64_t n, const double *ids, double *dst,
+                             double *depth_range) {
+    if (n < 0 || (n > 0 && (!src || !ids || !dst)) || !depth_range) {
+        sc::set_error("sc_stage_rows: bad arguments");
+        return SC_ERR_ARG;
+    }
+    double lo = 0.0, hi = 0.0;
+    bool nan_seen = false;
+    for (int64_t i = 0; i < n; ++i) {
+        const double *r = src + 5 * i;
+        if (!(r[3] == ids[i])) return 1;  // a NaN id differs too
+        double *d = dst + 5 * i;
+        d[0] = r[0];
+        d[1] = r[1];
+        d[2] = r[2];
+        d[3] = r[3];
+        d[4] = r[4];
+        const double z = r[0];
+        if (z != z) nan_seen = true;
+        if (i == 0) {
+            lo = hi = z;
+        } else {
+            lo = z < lo ? z : lo;
+            hi = z > hi ? z : hi;
+        }
+    }
+    const double nan = __builtin_nan("");
+    depth_range[0] = nan_seen ? nan : lo;
+    depth_range[1] = nan_seen ? nan : hi;
+    return 0;
+}

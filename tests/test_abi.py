@@ -75,3 +75,54 @@ def test_struct_sizes_match_c_layout():
     assert ctypes.sizeof(_lib.SplatParams) == 80
     assert ctypes.sizeof(_lib.CameraParams) == 112
     assert ctypes.sizeof(_lib.DiffuseParams) == 224
+
+
+def test_stage_rows_host_helper():
+    """sc_stage_rows (host only): copies the rows, returns the depth range,
+    flags the first id that differs, and propagates a NaN depth."""
+    import numpy
+    from scopyon_gb300 import _build, _lib
+    _build.build()
+    L = _lib.load()
+    rng = numpy.random.RandomState(2)
+    n = 1000
+    a = numpy.column_stack([rng.uniform(-1e-6, 1e-6, (n, 3)), numpy.arange(n, dtype=float),
+                            numpy.ones(n)])
+    ids = numpy.arange(n, dtype=float)
+    dst = numpy.zeros((n, 5))
+    out = numpy.zeros(2)
+    assert L.sc_stage_rows(a.ctypes.data, n, ids.ctypes.data, dst.ctypes.data, out.ctypes.data) == 0
+    numpy.testing.assert_array_equal(dst, a)
+    assert (out[0], out[1]) == (a[:, 0].min(), a[:, 0].max())
+    b = a.copy()
+    b[700, 3] = 5.0
+    assert L.sc_stage_rows(b.ctypes.data, n, ids.ctypes.data, dst.ctypes.data, out.ctypes.data) == 1
+    b = a.copy()
+    b[3, 0] = numpy.nan
+    assert L.sc_stage_rows(b.ctypes.data, n, ids.ctypes.data, dst.ctypes.data, out.ctypes.data) == 0
+    assert numpy.isnan(out).all()
+    assert L.sc_stage_rows(None, n, ids.ctypes.data, dst.ctypes.data, out.ctypes.data) == \
+        _lib.SC_ERR_ARG
+
+
+def test_stage_known_matches_numpy():
+    """The host fast path's staging: native rows for row-major float64
+    arrays, numpy for the rest, the same staging and range either way."""
+    import numpy
+    from scopyon_gb300 import _build
+    _build.build()
+    from scopyon_gb300.base import _stage_known
+    rng = numpy.random.RandomState(5)
+    n, S = 500, 6
+    ids = numpy.arange(n, dtype=float)
+    arrays = [numpy.column_stack([rng.uniform(-2e-6, 2e-6, (n, 3)), ids, numpy.ones(n)])
+              for _ in range(S)]
+    arrays[2] = numpy.asfortranarray(arrays[2])  # takes the numpy form
+    staging = numpy.zeros((S, n, 5))
+    rng_ = _stage_known(arrays, ids, staging)
+    numpy.testing.assert_array_equal(staging, numpy.stack(arrays))
+    allz = numpy.concatenate([a[:, 0] for a in arrays])
+    assert rng_ == (allz.min(), allz.max())
+    arrays[4] = arrays[4].copy()
+    arrays[4][10, 3] = -1.0
+    assert _stage_known(arrays, ids, staging) is None

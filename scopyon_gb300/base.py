@@ -176,6 +176,18 @@ def _host_pool():
     return _POOL
 
 
+_AHEAD = None
+
+
+def _ahead_pool():
+    """One thread that stages the next frame's inputs (it fans out to
+    _host_pool) while the current frame runs on the device."""
+    global _AHEAD
+    if _AHEAD is None:
+        _AHEAD = concurrent.futures.ThreadPoolExecutor(max_workers=1)
+    return _AHEAD
+
+
 def _stage_known(arrays, slot_ids_f, staging):
     """Copies each sub-step's array into the pinned staging buffer, on the
     host threads, when every array has exactly the known ids in slot order;
@@ -236,15 +248,24 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
     focal0 = cfg.focal_point[0]
     nw, nh = cfg.image_size
     slot_ids_f = None
+    pending = None  # (frame, staging, future): the next frame's inputs, staged ahead
     for f in range(num_frames):
+        ahead = None
+        if pending is not None:
+            ahead = (pending[1], pending[2].result()) if pending[0] == f else None
+            pending = None
         windows, exp_eff = frame_windows(times, len(data), start_time, exposure, f, shutter)
         arrays = [data[i][1] for i, _ in windows]
         uts = numpy.array([ut for _, ut in windows], dtype=float)
         if arrays and slot_ids_f is not None and not full_output:
             # the usual case: the same particles in the same order at every
-            # sub-step; staged on the host threads, no per-frame id scan
-            staging = pipe.host_staging((len(arrays), len(slot_ids_f), 5))
-            rng_ = _stage_known(arrays, slot_ids_f, staging)
+            # sub-step; staged on the host threads (while the previous frame
+            # ran), no per-frame id scan
+            if ahead is not None:
+                staging, rng_ = ahead
+            else:
+                staging = pipe.host_staging((len(arrays), len(slot_ids_f), 5), slot=f % 2)
+                rng_ = _stage_known(arrays, slot_ids_f, staging)
             if rng_ is not None:
                 pipe.ensure_slots(len(slot_ids_f))
                 pipe.psf.ensure_depth_range(rng_[0] - focal0, rng_[1] - focal0)
@@ -254,6 +275,16 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
                 expect, adc, opt = pipe.run_frame(staging, uts, with_optinfo=False,
                                                   draws=frame_draws, seed=seed, counter=f,
                                                   present=None, bleaching=bleaching)
+                if f + 1 < num_frames:
+                    w_next, _ = frame_windows(times, len(data), start_time, exposure, f + 1,
+                                              shutter)
+                    a_next = [data[i][1] for i, _ in w_next]
+                    if a_next:
+                        # the other slot's last upload (frame f - 1) is complete
+                        st_next = pipe.host_staging((len(a_next), len(slot_ids_f), 5),
+                                                    slot=(f + 1) % 2)
+                        pending = (f + 1, st_next,
+                                   _ahead_pool().submit(_stage_known, a_next, slot_ids_f, st_next))
                 pipe.check_status()
                 yield Image(adc.cpu().numpy().reshape(nw, nh).copy()), {}
                 continue

@@ -431,16 +431,19 @@ class FramePipeline:
             self._cap[name] = t
         return t
 
-    def host_staging(self, shape):
-        """A pinned host array of ``shape`` (float64) for the next upload."""
+    def host_staging(self, shape, slot=0):
+        """A pinned host array of ``shape`` (float64) for an upload; two slots
+        let one frame's inputs be staged while the other's are uploaded."""
         numel = int(numpy.prod(shape))
-        ev = self._cap.get("staging_event")
-        if ev is not None:
-            ev.synchronize()  # the previous upload from this buffer has finished
-        t = self._cap.get("staging")
+        name = "staging%d" % slot
+        t = self._cap.get(name)
+        if t is not None:
+            ev = self._cap.get("upload_events", {}).get(t.data_ptr())
+            if ev is not None:
+                ev.synchronize()  # the previous upload from this buffer has finished
         if t is None or t.numel() < numel:
             t = torch.empty(max(numel, 1), dtype=torch.float64, pin_memory=True)
-            self._cap["staging"] = t
+            self._cap[name] = t
         return t[:numel].numpy().reshape(shape)
 
     def ensure_slots(self, n_slots, initial=None):
@@ -625,7 +628,7 @@ class FramePipeline:
         if host.is_pinned():
             ev = torch.cuda.Event()
             ev.record()
-            self._cap["staging_event"] = ev
+            self._cap.setdefault("upload_events", {})[host.data_ptr()] = ev
         ut = torch.from_numpy(numpy.ascontiguousarray(unit_times, dtype=float)).to(dev)
         pres = None
         if present is not None:

@@ -38,7 +38,8 @@ extern "C" {
 /* Status word written by kernels into a caller buffer (int[4]):
  * [0] error flags (bit0 bad PSF key, bit1 missing table, bit2 bounds overflow,
  *     bit3 RNG loop bound hit, bit4 capacity, bit5 a bounded wait for an
- *     asynchronous copy ran out), [1..3] first offending index. */
+ *     asynchronous copy ran out, bit6 a caller-built record with a negative
+ *     first pixel, which is not binned), [1..3] first offending index. */
 #define SC_STATUS_WORDS 4
 
 /* One emitter during one exposure sub-step, ready to be splatted (64 bytes).
@@ -364,6 +365,9 @@ int sc_diffusion_dD(const float *d_pos, const float *d_emit, int n, int T,
  * output buffers, or a frame loop that must not allocate -- it calls no
  * allocator.  The first call on a device looks up the array's address with
  * that device current; make that first call before any stream capture.  The
+ * address is kept for the life of the process, so the device's primary
+ * context must not be reset (cudaDeviceReset) while the library is loaded.
+ * Records with a negative first pixel are not binned and set status bit 6.  The
  * array is shared by every call on a device: calls that overlap in time (on
  * different streams or host threads) race on it and must be serialised.
  * No counterpart in the reference, which bins nothing

@@ -24,8 +24,11 @@ namespace {
 // thousands of bins, so contention is low).  With rank, each record's bin and
 // rank within the bin are kept for the placement pass.
 __global__ void bin_count_kernel(const ScStepRec *recs, int n_rec, sc::TileGeom g,
-                                 int32_t *tile_count, int32_t *rec_bin, int32_t *rec_rank) {
+                                 int32_t *tile_count, int32_t *rec_bin, int32_t *rec_rank,
+                                 int32_t *status) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rec; r += gridDim.x * blockDim.x) {
+        if (sc::record_malformed(recs[r]))
+            sc::flag_status(status, 6, r, recs[r].i_start, recs[r].j_start);
         if (rec_bin)
             sc::bin_record(g, recs[r], r, tile_count, rec_bin, rec_rank);
         else {
@@ -614,7 +617,6 @@ extern "C" int sc_bin_finish(int n_rec, const ScSplatParams *p, void *d_ws, size
 extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatParams *p,
                             void *d_ws, size_t ws_bytes, int32_t *d_tile_start, int32_t *d_items,
                             int32_t *d_status, void *stream) {
-    (void)d_status;
     sc::TileGeom g;
     int rc = sc::tile_geom(p, g);
     if (rc) return rc;
@@ -640,7 +642,7 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
     int grid = (n_rec + 255) / 256;
     if (grid > 152 * 8) grid = 152 * 8;
     bin_count_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.count, b.rec_bin,
-                                          sc::rank_array(b));
+                                          sc::rank_array(b), d_status);
     if (b.rec_bin) return bin_finish(n_rec, g, b.count, b.rec_bin, b, d_tile_start, d_items, s);
     bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(b.count, n_bins, d_tile_start, b.cursor);
     bin_scatter_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.cursor, d_items);

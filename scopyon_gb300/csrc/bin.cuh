@@ -26,13 +26,25 @@ constexpr int kRadixMinRecords = 1 << 20;
 int bin_layout(const TileGeom &g, int n_rec, void *d_ws, size_t ws_bytes, BinLayout &b);
 
 // Bin of a record: the tile holding its first footprint pixel, plus n_tiles
-// for records that take the summed-area path; -1 when it has no pixels.
+// for records that take the summed-area path; -1 when it has no pixels or
+// its first pixel lies outside the image (the engine's producers clamp the
+// first pixel to >= 0; a caller-built record with a negative start is
+// dropped, and record_malformed() tells the counting pass to report it).
 __device__ __forceinline__ int record_tile(const ScStepRec &rec, int r, const TileGeom &g) {
     if (rec.n_i < 2 || rec.n_j < 2 || rec.slot < 0) return -1;
     const int img = g.rec_per_image > 0 ? r / g.rec_per_image : 0;
-    if (img >= g.n_images || rec.i_start >= g.nw || rec.j_start >= g.nh) return -1;
+    if (img >= g.n_images || rec.i_start < 0 || rec.j_start < 0 || rec.i_start >= g.nw ||
+        rec.j_start >= g.nh)
+        return -1;
     const int t = img * g.tiles_per_image + (rec.i_start / g.tile) * g.tiles_y + rec.j_start / g.tile;
     return rec.box ? t : t + g.n_tiles;
+}
+
+// A record with pixels to splat whose first pixel has a negative index: no
+// producer of this library writes one, so it came from a caller and is
+// reported (status bit 6) instead of being filed under a tile.
+__device__ __forceinline__ bool record_malformed(const ScStepRec &rec) {
+    return rec.n_i >= 2 && rec.n_j >= 2 && rec.slot >= 0 && (rec.i_start < 0 || rec.j_start < 0);
 }
 
 // Counts record r into its bin and keeps its bin and, when rec_rank is given,

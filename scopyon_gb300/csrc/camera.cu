@@ -3,12 +3,17 @@
 // Reference: _EPIFMSimulator.__detector_output and
 // __get_analog_to_digital_converter_counts (src/scopyon/_epifm.py:1430-1484),
 // with the detector classes EMCCD / CCD / CMOS (:329-433):
-//   expected = QE * (photons + background)
+//   photons += background_mean when the background switch is on (:1437-1438;
+//   the caller passes background = 0 otherwise), then expected = QE * photons
+//   (:1441), so expected = QE * (photons + background)
 //   EMCCD: signal ~ compound Poisson-Gamma (EM gain), noise ~ N(0, readout)
 //   CCD:   signal ~ Poisson(expected), noise ~ N(0, readout)
 //   CMOS:  signal ~ Poisson(expected), noise ~ tabulated distribution (additive)
 //   sCMOS (this engine only): noise ~ N(0, sigma_ij) with a per-pixel sigma map
 //   ADC = clip(min(signal + noise, fullwell) / gain + offset, 0, 2^bit - 1)
+//   (rounding the ADC count to an integer is an option of this engine only;
+//   the reference's ADC count is an unrounded float, and parity runs keep
+//   the option off)
 // Draws come either from Philox4x32-10 (native, one counter stream per pixel)
 // or from caller arrays recorded from the reference (injected), in which case
 // the ADC arithmetic is the reference's FP64 sequence.

@@ -36,6 +36,7 @@ struct SplatConsts {
     const float *box;  // box tables (NULL when px / res is not an integer)
     int box_nq;        // rows and columns of a box table block
     int box_p;         // grid rows per pixel of the box tables
+    int64_t box_floats;  // floats held in the box tables (every slot)
 };
 
 // Footprint bound k of one axis: ceil(((start + k) * px - origin) / res) with
@@ -165,7 +166,12 @@ splat_box_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__
             }
             const float w = __int_as_float(hb.x);
             // pixel (i_start + a, j_start + b) is entry box_off + a * NQ + b
-            const float *B = c.box + (((int64_t)ha.y << 32) | (uint32_t)ha.x);
+            const int64_t off = ((int64_t)ha.y << 32) | (uint32_t)ha.x;
+            if (off < 0 || off + (int64_t)(ni - 1) * nq + nj > c.box_floats) {
+                if (lane == 0) sc::flag_status(status, 2, (int)(off >> 32), (int)off, tile);
+                continue;
+            }
+            const float *B = c.box + off;
             float *D = my_acc + ox * E + oy;
             for (int cb = 0; cb < nj; cb += 16) {
                 const int b = cb + col;
@@ -603,6 +609,7 @@ int splat_consts(const ScSplatParams *p, const sc::TileGeom &g, SplatConsts &c) 
     c.box = nullptr;
     c.box_nq = 0;
     c.box_p = 0;
+    c.box_floats = 0;
     return SC_OK;
 }
 
@@ -635,6 +642,8 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
         c.box = d_box;
         c.box_nq = p->box_nq;
         c.box_p = p->box_p;
+        c.box_floats = (int64_t)p->n_slots * p->box_p * p->box_p *
+                       (((int64_t)p->box_nq * p->box_nq + 3) & ~3LL);
     }
     const float2 *sat = reinterpret_cast<const float2 *>(d_sat);
     cudaStream_t s = sc::as_stream(stream);

@@ -609,7 +609,10 @@ class FramePipeline:
                 msgs.append("bin capacity exceeded (%d entries)" % st[1])
             if bits & 32:
                 msgs.append("bounded wait for an asynchronous copy ran out (tile %d)" % st[3])
-            code = _lib.SC_ERR_TIMEOUT if bits == 32 else _lib.SC_ERR_CAPACITY
+            if bits & 64:
+                msgs.append("record %d has a negative first pixel (%d, %d)" % (st[1], st[2], st[3]))
+            code = (_lib.SC_ERR_TIMEOUT if bits == 32 else _lib.SC_ERR_ARG if bits == 64
+                    else _lib.SC_ERR_CAPACITY)
             raise _lib.ScopyonGPUError(code, "; ".join(msgs))
 
     def run_frame(self, particles, unit_times, with_optinfo=True, draws=None, seed=0, counter=0,

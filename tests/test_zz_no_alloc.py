@@ -36,10 +36,13 @@ def params(lib, nw, nh, tile=8, n_images=1, rec_per_image=0):
     return p
 
 
-def random_records(rng, n, nw, nh):
+def random_records(rng, n, nw, nh, negative=False):
+    """Records spread over the image; some past its edge (no bin), and with
+    ``negative`` some with a negative first pixel (no bin, status bit 6)."""
     r = numpy.zeros(n, REC)
-    r["i_start"] = rng.randint(0, nw + 4, n)  # past the image: no bin
-    r["j_start"] = rng.randint(0, nh + 4, n)
+    lo = -20 if negative else 0
+    r["i_start"] = rng.randint(lo, nw + 4, n)  # past the image: no bin
+    r["j_start"] = rng.randint(lo, nh + 4, n)
     r["n_i"] = rng.randint(0, 30, n)  # fewer than 2 pixels: no bin
     r["n_j"] = rng.randint(0, 30, n)
     r["slot"] = numpy.where(rng.rand(n) < 0.05, -1, 0)
@@ -53,6 +56,7 @@ def numpy_bins(r, p):
     img = idx // p.rec_per_image if p.rec_per_image > 0 else numpy.zeros(len(r), int)
     n_tiles = p.tiles_x * p.tiles_y * p.n_images
     ok = ((r["n_i"] >= 2) & (r["n_j"] >= 2) & (r["slot"] >= 0) & (img < p.n_images)
+          & (r["i_start"] >= 0) & (r["j_start"] >= 0)
           & (r["i_start"] < p.nw) & (r["j_start"] < p.nh))
     i0, j0 = r["i_start"].astype(numpy.int64), r["j_start"].astype(numpy.int64)
     t = img * p.tiles_x * p.tiles_y + (i0 // p.tile) * p.tiles_y + j0 // p.tile
@@ -62,6 +66,12 @@ def numpy_bins(r, p):
     start = numpy.concatenate([[0], numpy.cumsum(counts)]).astype(numpy.int32)
     order = idx[ok][numpy.argsort(b[ok], kind="stable")].astype(numpy.int32)
     return start, order
+
+
+def malformed(r):
+    """Records the counting pass reports: pixels to splat, negative first pixel."""
+    return ((r["n_i"] >= 2) & (r["n_j"] >= 2) & (r["slot"] >= 0)
+            & ((r["i_start"] < 0) | (r["j_start"] < 0)))
 
 
 def run(lib, fn, recs_h, p, counts_only=False):
@@ -85,6 +95,11 @@ def run(lib, fn, recs_h, p, counts_only=False):
     assert rc == 0, L.sc_last_error().decode()
     torch.cuda.synchronize()
     start = start.cpu().numpy()
+    st = status.cpu().numpy()
+    bad = malformed(recs_h)
+    assert bool(st[0] & 64) == bool(bad.any()), st
+    if bad.any():
+        assert bad[st[1]], st  # the flagged record is one of the malformed ones
     return start, items.cpu().numpy()[:start[-1]]
 
 
@@ -96,7 +111,7 @@ def test_static_matches_workspace_entry_point(lib, shape):
         n = 20000 + 3001 * call
         rpi = -(-n // n_images) if n_images > 1 else 0
         p = params(lib, nw, nh, n_images=n_images, rec_per_image=rpi)
-        r = random_records(rng, n, nw, nh)
+        r = random_records(rng, n, nw, nh, negative=call == 1)
         s_start, s_items = run(lib, "static", r, p)
         w_start, w_items = run(lib, "workspace", r, p)
         numpy.testing.assert_array_equal(s_start, w_start)
@@ -107,6 +122,27 @@ def test_static_matches_workspace_entry_point(lib, shape):
         e_start, e_items = numpy_bins(r, p)
         numpy.testing.assert_array_equal(s_start, e_start)
         numpy.testing.assert_array_equal(s_items, e_items)
+
+
+def test_static_counts_only_fallback(lib):
+    """With more records than the fixed array has room for (bins and ranks
+    of every record), sc_bin_steps_static takes the counts-only path: atomic
+    cursors, then a sort of each bin.  Same lists as the workspace path and
+    numpy, two calls in a row."""
+    L = lib.load()
+    rng = numpy.random.RandomState(23)
+    p = params(lib, 512, 512)
+    n_tiles = p.tiles_x * p.tiles_y
+    for call in range(2):
+        n = 300000 + 17 * call
+        assert L.sc_bin_workspace_bytes(n, n_tiles) > 1 << 20  # beyond the fixed array
+        r = random_records(rng, n, 512, 512, negative=call == 0)
+        s_start, s_items = run(lib, "static", r, p)
+        e_start, e_items = numpy_bins(r, p)
+        numpy.testing.assert_array_equal(s_start, e_start)
+        numpy.testing.assert_array_equal(s_items, e_items)
+        w_start, w_items = run(lib, "workspace", r, p)
+        numpy.testing.assert_array_equal(s_items, w_items)
 
 
 @pytest.mark.parametrize("shape", [(4096, 2048, 1), (256, 256, 1), (1024, 512, 3)])

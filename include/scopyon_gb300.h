@@ -112,6 +112,8 @@ typedef struct {
     uint64_t seed;           /* Philox key for native draws                                */
     uint64_t counter;        /* Philox counter base (e.g. frame index)                     */
     const int64_t *d_frame;  /* optional device counter f added to counter (graph replay)   */
+    const double *d_photons64; /* exact mode: FP64 photons read in place of d_photons       */
+    double *d_expect64;      /* exact mode: FP64 expectation QE*(photons+background) out    */
 } ScCameraParams;
 
 typedef struct {
@@ -209,14 +211,16 @@ int sc_psf_box_table(const float *d_sat, int n_keys, int n_r, int sat_pitch, int
  * absent at a sub-step; d_budget holds the
  * photon budget per particle slot (initialised by the caller at first sight,
  * carried across frames); d_optinfo receives the per-slot 8-vector sums of
- * the frame (may be NULL when with_optinfo is 0).  Replaces
+ * the frame (may be NULL when with_optinfo is 0); d_norm, when not NULL,
+ * receives each record's FP64 normalisation ([n_sub][n_particles]; 0: nothing
+ * to splat), which sc_splat_fp64 reads.  Replaces
  * _EPIFMSimulator.__overlay_molecule_plane and get_emit_photons
  * (src/scopyon/_epifm.py:1267-1360).                                       */
 int sc_emitter_steps(const ScStepParams *p, const double *d_particles,
                      const double *d_unit_time, const uint8_t *d_present,
                      const int32_t *d_key_slot,
                      double *d_budget, double *d_optinfo, ScStepRec *d_recs,
-                     int32_t *d_status, void *stream);
+                     double *d_norm, int32_t *d_status, void *stream);
 
 /* Native frame records: sc_diffuse_steps and sc_emitter_steps in one pass
  * for trajectories that live on the device.  For every (sub-step, particle)
@@ -376,6 +380,19 @@ int sc_bin_steps_static(const ScStepRec *d_recs, int n_rec, const ScSplatParams 
                         int32_t *d_tile_start, int32_t *d_items, int32_t *d_status,
                         void *stream);
 
+/* FP64 splat for the injected-draws parity mode: every record's footprint,
+ * each pixel's slice sum from the double-float quadrant tables evaluated in
+ * FP64, times res^2 and the record's FP64 normalisation d_norm[r] (from
+ * sc_emitter_steps), added to d_image (n_images x nw x nh FP64, zeroed by
+ * the caller) with FP64 atomic adds when the slice sum is positive.  A warp
+ * per record, no binning; records need not be sorted.  The expected image
+ * then matches an FP64 evaluation of overlay_signal_
+ * (src/scopyon/_epifm.py:224-282) to ~1e-13 relative, so that draws the
+ * camera takes from the expectation (the EMCCD inverse CDF) are the
+ * reference's.                                                              */
+int sc_splat_fp64(const ScStepRec *d_recs, const double *d_norm, int n_rec, const float *d_sat,
+                  const ScSplatParams *p, double *d_image, int32_t *d_status, void *stream);
+
 /* Bytes of scratch sc_splat needs: one FP32 (tile + halo)^2 buffer per tile. */
 size_t sc_splat_workspace_bytes(const ScSplatParams *p);
 
@@ -410,7 +427,7 @@ int sc_camera(const ScCameraParams *p, const float *d_photons,
 /* Exact EMCCD draw: the reference's discrete distribution over integer
  * output electrons, inverse CDF at the given uniform, per pixel
  * (EMCCD.probability_distribution / draw_signal, src/scopyon/_epifm.py:365-400). */
-int sc_emccd_exact(const float *d_photons, double qe, double background,
+int sc_emccd_exact(const double *d_photons, double qe, double background,
                    const double *d_uniform, int n_pixels, double emgain,
                    double *d_signal, int32_t *d_status, void *stream);
 

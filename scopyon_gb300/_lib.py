@@ -52,7 +52,8 @@ class CameraParams(ctypes.Structure):
                 ("fullwell", ctypes.c_double), ("offset0", ctypes.c_double),
                 ("gain0", ctypes.c_double), ("table_n", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("counter", ctypes.c_uint64),
-                ("d_frame", ctypes.c_void_p)]
+                ("d_frame", ctypes.c_void_p), ("d_photons64", ctypes.c_void_p),
+                ("d_expect64", ctypes.c_void_p)]
 
 
 class DiffuseParams(ctypes.Structure):
@@ -88,13 +89,15 @@ _SIG = {
                                ctypes.c_size_t, _P, _P]),
     "sc_psf_quadrant_sat": (_I, [_P, _I, _I, _D, _P, _I, _P]),
     "sc_psf_box_table": (_I, [_P, _I, _I, _I, _I, _P, _P]),
-    "sc_emitter_steps": (_I, [ctypes.POINTER(StepParams), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "sc_emitter_steps": (_I, [ctypes.POINTER(StepParams), _P, _P, _P, _P, _P, _P, _P, _P, _P,
+                              _P]),
     "sc_bin_workspace_bytes": (ctypes.c_size_t, [_I, _I]),
     "sc_bin_reset": (_I, [ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P]),
     "sc_bin_finish": (_I, [_I, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P, _P, _P]),
     "sc_bin_steps": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P, _P, _P,
                           _P]),
     "sc_bin_steps_static": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, _P, _P, _P]),
+    "sc_splat_fp64": (_I, [_P, _P, _I, _P, ctypes.POINTER(SplatParams), _P, _P, _P]),
     "sc_splat_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(SplatParams)]),
     "sc_splat": (_I, [_P, _P, _P, _P, _P, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P,
                       _P, _P]),

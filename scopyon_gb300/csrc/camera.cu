@@ -27,6 +27,8 @@ struct CamConsts {
     float qe_f, background_f, readout_f, emgain_f, fullwell_f, adc_max_f, offset0_f, inv_gain0_f;
     uint64_t seed, counter;
     const int64_t *frame;
+    const double *photons64;  // exact mode: FP64 photons in place of the FP32 ones
+    double *expect64;         // exact mode: FP64 expectation out
 };
 
 // Poisson variate.  Small means: sequential inversion.  Large means: the
@@ -160,9 +162,10 @@ __global__ void camera_exact_kernel(CamConsts c, const float *__restrict__ photo
     const int stride = gridDim.x * blockDim.x;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.n; p += stride) {
         // E = QE (photons + background) with the reference's FP64 rounding
-        const double ph = (double)photons[p] + c.background;
+        const double ph = (c.photons64 ? c.photons64[p] : (double)photons[p]) + c.background;
         const double e = __dmul_rn(c.qe, ph);
         if (expect) expect[p] = (float)e;
+        if (c.expect64) c.expect64[p] = e;
         double noise, signal;
         if (c.camera == SC_CAM_CMOS_TABLE && inj_uniform)
             noise = table_value[table_index(table_cdf, c.table_n, inj_uniform[p])];
@@ -285,13 +288,13 @@ __device__ double i1e_d(double y) {
 // One warp per pixel: support [s_min, s_max), weights p(S) with the exponent
 // shifted by E (the continuous maximum, so nothing overflows), total, then
 // the first S whose cumulative weight exceeds u * total.
-__global__ void emccd_exact_kernel(const float *photons, double qe, double background,
+__global__ void emccd_exact_kernel(const double *photons, double qe, double background,
                                    const double *uniform, int n, double g, double *signal,
                                    int32_t *status) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
     for (int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < n; p += warps) {
-        const double e = qe * ((double)photons[p] + background);
+        const double e = __dmul_rn(qe, photons[p] + background);
         if (!(e > 0.0)) {
             if (lane == 0) signal[p] = 0.0;
             continue;
@@ -358,7 +361,11 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
     SC_REQUIRE(p->camera >= SC_CAM_EMCCD && p->camera <= SC_CAM_SCMOS, "sc_camera: camera %d",
                p->camera);
     SC_REQUIRE(p->bit > 0 && p->bit <= 32, "sc_camera: bit=%d", p->bit);
-    SC_REQUIRE(d_photons != nullptr && (d_adc64 || d_adc32), "sc_camera: NULL input/output");
+    SC_REQUIRE((d_photons != nullptr || (p->exact && p->d_photons64 != nullptr)) &&
+                   (d_adc64 || d_adc32),
+               "sc_camera: NULL input/output");
+    SC_REQUIRE(p->exact || (p->d_photons64 == nullptr && p->d_expect64 == nullptr),
+               "sc_camera: FP64 photons and expectation are exact-mode buffers");
     if (p->camera == SC_CAM_CMOS_TABLE)
         SC_REQUIRE(p->table_n > 0 && d_table_value && d_table_cdf,
                    "sc_camera: CMOS table mode needs the noise table");
@@ -392,6 +399,8 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
     c.seed = p->seed;
     c.counter = p->counter;
     c.frame = p->d_frame;
+    c.photons64 = p->d_photons64;
+    c.expect64 = p->d_expect64;
     cudaStream_t st = sc::as_stream(stream);
     if (p->exact) {
         const int block = 256;
@@ -437,7 +446,7 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
     return sc::launch_status("sc_camera");
 }
 
-extern "C" int sc_emccd_exact(const float *d_photons, double qe, double background,
+extern "C" int sc_emccd_exact(const double *d_photons, double qe, double background,
                               const double *d_uniform, int n_pixels, double emgain,
                               double *d_signal, int32_t *d_status, void *stream) {
     SC_REQUIRE(n_pixels >= 0, "sc_emccd_exact: n_pixels=%d", n_pixels);

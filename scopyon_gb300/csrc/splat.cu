@@ -512,6 +512,71 @@ splat_sat_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__
     }
 }
 
+// FP64 splat (injected-draws parity mode): a warp per record, no bins.  The
+// footprint bounds are axis_bound's (the reference's ceil decisions), each
+// pixel's slice sum is the signed quadrant-table combination with every hi
+// and lo term taken in FP64, and the pixel gets (sum * res^2) * norm by an
+// FP64 atomic add when the sum is positive (_epifm.py:277-282).
+__global__ void splat_fp64_kernel(const ScStepRec *__restrict__ recs,
+                                  const double *__restrict__ norm, int n_rec,
+                                  const float2 *__restrict__ sat, SplatConsts c, int n_images,
+                                  int rec_per_image, int n_slots, int max_bounds,
+                                  double *__restrict__ image, int32_t *status) {
+    extern __shared__ int bnd64[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int *bx = bnd64 + warp * 2 * max_bounds;
+    int *by = bx + max_bounds;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    const double unit_area = c.res * c.res;
+    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_rec; r += warps) {
+        const ScStepRec rec = recs[r];
+        const double w = norm[r];
+        if (rec.n_i < 2 || rec.n_j < 2 || rec.slot < 0 || !(w > 0.0)) continue;
+        const int img = rec_per_image > 0 ? r / rec_per_image : 0;
+        if (rec.n_i > max_bounds || rec.n_j > max_bounds || rec.slot >= n_slots ||
+            img >= n_images || rec.i_start < 0 || rec.j_start < 0 ||
+            rec.i_start + rec.n_i - 1 > c.nw || rec.j_start + rec.n_j - 1 > c.nh) {
+            if (lane == 0) sc::flag_status(status, 2, r, rec.i_start, rec.j_start);
+            continue;
+        }
+        for (int b = lane; b < rec.n_i + rec.n_j; b += 32) {
+            if (b < rec.n_i)
+                bx[b] = axis_bound(b, rec.n_i, rec.i_start, rec.ax_hi, rec.ax_lo, rec.x0, c);
+            else
+                by[b - rec.n_i] = axis_bound(b - rec.n_i, rec.n_j, rec.j_start, rec.ay_hi,
+                                             rec.ay_lo, rec.y0, c);
+        }
+        __syncwarp();
+        const float2 *G = sat + (int64_t)rec.slot * c.table_stride;
+        const int ni = rec.n_i - 1, nj = rec.n_j - 1;
+        double *out = image + (int64_t)img * c.nw * c.nh;
+        for (int q = lane; q < ni * nj; q += 32) {
+            const int a = q / nj, bj = q - (q / nj) * nj;
+            int a0 = bx[a], a1 = bx[a + 1], b0 = by[bj], b1 = by[bj + 1];
+            sc::slice_bounds(a0, a1, c.n_signal);
+            sc::slice_bounds(b0, b1, c.n_signal);
+            if (a1 <= a0 || b1 <= b0) continue;
+            int uu[3], vv[3];
+            float us[3], vs[3];
+            const int nu = sc::fold(a0, a1, c.n_r, uu, us);
+            const int nv = sc::fold(b0, b1, c.n_r, vv, vs);
+            double sum = 0.0;
+            for (int iu = 0; iu < nu; ++iu) {
+                const float2 *row = G + (int64_t)uu[iu] * c.pitch;
+                for (int iv = 0; iv < nv; ++iv) {
+                    const float2 gv = __ldg(row + vv[iv]);
+                    sum += (double)(us[iu] * vs[iv]) * ((double)gv.x + (double)gv.y);
+                }
+            }
+            const double photons = sum * unit_area;
+            if (photons > 0.0)
+                atomicAdd(out + (int64_t)(rec.i_start + a) * c.nh + (rec.j_start + bj),
+                          photons * w);
+        }
+        __syncwarp();
+    }
+}
+
 // Per pixel: the tile buffers that cover it, summed in a fixed order.
 __global__ void splat_merge_kernel(const float *__restrict__ ws, SplatConsts c, int n_images,
                                    float *__restrict__ image) {
@@ -614,6 +679,44 @@ int splat_consts(const ScSplatParams *p, const sc::TileGeom &g, SplatConsts &c) 
 }
 
 }  // namespace
+
+extern "C" int sc_splat_fp64(const ScStepRec *d_recs, const double *d_norm, int n_rec,
+                             const float *d_sat, const ScSplatParams *p, double *d_image,
+                             int32_t *d_status, void *stream) {
+    SC_REQUIRE(p != nullptr, "sc_splat_fp64: params are NULL");
+    SC_REQUIRE(p->nw > 0 && p->nh > 0 && p->n_images >= 1, "sc_splat_fp64: image %dx%d x %d",
+               p->nw, p->nh, p->n_images);
+    SC_REQUIRE(n_rec >= 0, "sc_splat_fp64: n_rec=%d", n_rec);
+    SC_REQUIRE(p->n_slots >= 1, "sc_splat_fp64: n_slots=%d", p->n_slots);
+    if (n_rec == 0) return SC_OK;
+    SC_REQUIRE(d_recs && d_norm && d_sat && d_image, "sc_splat_fp64: NULL pointer");
+    SC_REQUIRE(p->rec_per_image >= 0 &&
+                   (p->rec_per_image == 0 || (int64_t)p->rec_per_image * p->n_images >= n_rec),
+               "sc_splat_fp64: rec_per_image too small for n_rec");
+    sc::TileGeom g;
+    g.tile = 1;
+    g.halo = 0;
+    g.edge = 1;
+    g.tiles_per_image = 1;
+    g.tiles_y = 1;
+    g.nw = p->nw;
+    g.nh = p->nh;
+    SplatConsts c;
+    int rc = splat_consts(p, g, c);
+    if (rc) return rc;
+    // bounds per axis: the pixels a footprint spans (ceil(sw / px) + 1) and one more
+    const int max_bounds = (int)ceil(p->res * (double)(c.n_signal - 1) / p->px) + 3;
+    const int threads = 256;
+    const size_t smem = (size_t)(threads / 32) * 2 * max_bounds * sizeof(int);
+    SC_REQUIRE(smem <= 48 * 1024, "sc_splat_fp64: footprints of %d bounds are too wide",
+               max_bounds);
+    int64_t blocks = ((int64_t)n_rec * 32 + threads - 1) / threads;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    splat_fp64_kernel<<<(int)blocks, threads, smem, sc::as_stream(stream)>>>(
+        d_recs, d_norm, n_rec, reinterpret_cast<const float2 *>(d_sat), c, p->n_images,
+        p->rec_per_image, p->n_slots, max_bounds, d_image, d_status);
+    return sc::launch_status("sc_splat_fp64");
+}
 
 extern "C" size_t sc_splat_workspace_bytes(const ScSplatParams *p) {
     sc::TileGeom g;

@@ -75,10 +75,11 @@ __global__ void emitter_physics_kernel(sc::StepConsts c, const double *particles
 // Pass 2, one thread per (sub-step, slot): depth key and footprint.
 __global__ void emitter_footprint_kernel(sc::StepConsts c, const double *particles,
                                          const int32_t *key_slot, ScStepRec *recs,
-                                         int32_t *status) {
+                                         double *norm_out, int32_t *status) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= (int64_t)c.n_sub * c.n_particles) return;
     const double norm = recs[idx].x0;
+    if (norm_out) norm_out[idx] = norm;
     const double *q = particles + idx * 5;
     ScStepRec rec;
     const int i = (int)(idx % c.n_particles), s = (int)(idx / c.n_particles);
@@ -153,7 +154,7 @@ extern "C" int sc_emitter_steps(const ScStepParams *p, const double *d_particles
                                 const double *d_unit_time, const uint8_t *d_present,
                                 const int32_t *d_key_slot,
                                 double *d_budget, double *d_optinfo, ScStepRec *d_recs,
-                                int32_t *d_status, void *stream) {
+                                double *d_norm, int32_t *d_status, void *stream) {
     sc::StepConsts c;
     int rc = sc::step_consts(p, c);
     if (rc) return rc;
@@ -167,6 +168,6 @@ extern "C" int sc_emitter_steps(const ScStepParams *p, const double *d_particles
         c, d_particles, d_unit_time, d_present, d_budget, d_optinfo, d_recs);
     const int64_t n_rec = (int64_t)c.n_sub * c.n_particles;
     emitter_footprint_kernel<<<(unsigned)((n_rec + 255) / 256), 256, 0, st>>>(
-        c, d_particles, d_key_slot, d_recs, d_status);
+        c, d_particles, d_key_slot, d_recs, d_norm, d_status);
     return sc::launch_status("sc_emitter_steps");
 }

@@ -543,8 +543,10 @@ class FramePipeline:
         ev.setdefault(name, []).append((e0, e1))
 
     def camera(self, photons, expect, adc64, adc32=None, seed=0, counter=0, draws=None,
-               stream=None, d_frame=None):
-        """Camera model + ADC on one frame (photons: float32 W*H on the device)."""
+               stream=None, d_frame=None, photons64=None, expect64=None):
+        """Camera model + ADC on one frame (photons: float32 W*H on the device;
+        with injected draws, photons64 / expect64 are the FP64 photons read and
+        the FP64 expectation written in their place)."""
         cfg = self.cfg
         s = stream_ptr(stream)
         cp = _lib.CameraParams()
@@ -561,6 +563,9 @@ class FramePipeline:
         cp.table_n = 0 if self.table_value is None else self.table_value.numel()
         cp.seed, cp.counter = int(seed) & (2 ** 64 - 1), int(counter) & (2 ** 64 - 1)
         cp.d_frame = None if d_frame is None else d_frame.data_ptr()
+        if draws is not None:
+            cp.d_photons64 = None if photons64 is None else photons64.data_ptr()
+            cp.d_expect64 = None if expect64 is None else expect64.data_ptr()
         inj_noise = inj_signal = inj_uniform = None
         if draws is not None:
             dev = self.device
@@ -575,7 +580,9 @@ class FramePipeline:
                 inj_uniform = dev64(numpy.nan_to_num(numpy.asarray(draws["uniform"], float)))
             if inj_signal is None and self.camera_kind == _lib.CAM_EMCCD:
                 inj_signal = self._buf("emccd_sig", self.n_pix, torch.float64)
-                call("sc_emccd_exact", ptr(photons), float(cfg.qe), cp.background,
+                if photons64 is None:
+                    photons64 = photons.double()
+                call("sc_emccd_exact", ptr(photons64), float(cfg.qe), cp.background,
                      ptr(inj_uniform), self.n_pix, float(cfg.emgain), ptr(inj_signal),
                      ptr(self.status), s)
                 inj_uniform = None
@@ -647,16 +654,32 @@ class FramePipeline:
         n_rec = n_sub * n
         recs = self._buf("recs", max(n_rec, 1) * (_lib.STEP_REC_BYTES // 4), torch.int32)
         optinfo = self._buf("optinfo", n * 8, torch.float64) if with_optinfo else None
+        # injected draws: the reference-parity mode, with the expected image
+        # accumulated in FP64 (sc_splat_fp64) so that draws taken from it are
+        # the reference's
+        exact = draws is not None
+        norm = self._buf("norm64", max(n_rec, 1), torch.float64) if exact else None
         if n_rec:
             sp = self.step_params(n_sub, n, with_optinfo)
             if bleaching is not None:
                 sp.bleaching = 1 if bleaching else 0
             call("sc_emitter_steps", sp, ptr(part), ptr(ut), ptr(present), ptr(self.psf.key_slot),
-                 ptr(self.budget), ptr(optinfo), ptr(recs), ptr(self.status), s)
+                 ptr(self.budget), ptr(optinfo), ptr(recs), ptr(norm), ptr(self.status), s)
+        opt = optinfo[: n * 8].view(n, 8) if with_optinfo else None
+        if exact:
+            image64 = self._buf("image64", self.n_pix, torch.float64)[: self.n_pix]
+            expect64 = self._buf("expect64", self.n_pix, torch.float64)[: self.n_pix]
+            image64.zero_()
+            if n_rec:
+                call("sc_splat_fp64", ptr(recs), ptr(norm), n_rec, ptr(self.psf.tables),
+                     self.splat_params(), ptr(image64), ptr(self.status), s)
+            self.camera(None, None, self.adc, seed=seed, counter=counter, draws=draws,
+                        stream=stream, d_frame=d_frame, photons64=image64, expect64=expect64)
+            return expect64, self.adc, opt
         self.splat_records(recs, n_rec, self.image, stream=stream)
         self.camera(self.image, self.expect, self.adc, seed=seed, counter=counter, draws=draws,
                     stream=stream, d_frame=d_frame)
-        return self.expect, self.adc, (optinfo[: n * 8].view(n, 8) if with_optinfo else None)
+        return self.expect, self.adc, opt
 
 
 TILE_CANDIDATES = ((8, 4, 4), (8, 4, 8), (8, 2, 6), (16, 4, 4), (16, 8, 4), (16, 4, 8))

@@ -73,7 +73,7 @@ def test_struct_sizes_match_c_layout():
     from scopyon_gb300 import _lib
     assert ctypes.sizeof(_lib.StepParams) == 136
     assert ctypes.sizeof(_lib.SplatParams) == 80
-    assert ctypes.sizeof(_lib.CameraParams) == 112
+    assert ctypes.sizeof(_lib.CameraParams) == 128
     assert ctypes.sizeof(_lib.DiffuseParams) == 224
 
 

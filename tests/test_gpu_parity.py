@@ -207,7 +207,7 @@ def test_emccd_exact_matches_oracle(lib):
     e = numpy.concatenate([[0.0, 0.01, 0.5, 3.7, 55.0, 333.3, 700.0, 1200.0],
                            rng.uniform(0, 800, 56)])
     u = rng.uniform(size=e.size)
-    photons = _dev(e.astype(numpy.float32), torch.float32)
+    photons = _dev(e.astype(numpy.float32).astype(numpy.float64))
     out = torch.empty(e.size, dtype=torch.float64, device="cuda")
     status = torch.zeros(4, dtype=torch.int32, device="cuda")
     lib.call("sc_emccd_exact", lib.ptr(photons), 1.0, 0.0, lib.ptr(_dev(u)), e.size, 300.0,

@@ -42,6 +42,17 @@ METRIC = "frames/s, 512^2 px 20k emitters (EPIFM defocus, sCMOS)"
 WORKLOAD = "epifm_defocus_512px_20k_emitters_20substeps_scmos"
 
 
+def workload_dict():
+    """The ``config`` object of the JSON line (the same in both arms)."""
+    return {"workload": WORKLOAD + ("_z0.1um_profiling" if Z_HALF < 1e-6 else ""),
+            "n_emitters": N_EMIT, "image": [IMAGE, IMAGE], "substeps": SUBSTEPS,
+            "exposure_s": EXPOSURE, "pixel_nm": PX * 1e9,
+            "camera": "sCMOS per-pixel sigma, 12-bit", "psf": "Born-Wolf TRITC",
+            "depth_range_um": [-Z_HALF * 1e6, Z_HALF * 1e6],
+            "D_um2_per_s": [0.01, D_FAST * 1e12], "bleaching_mean_lifetime_s": 2.0,
+            "l2": "inputs larger than L2 (PSF tables of every depth key, several GB)"}
+
+
 def workload_config():
     import scopyon_gb300 as sg
     cfg = sg.DefaultConfiguration()
@@ -283,6 +294,7 @@ def gb300_arm(args, rank, world):
     value = world * args.steps / (elapsed_ms / 1e3)
 
     e2e = None if args.small else e2e_arm(args, cfg, dev, rank, world)
+    cfg1 = None if args.small else config1_arm(args, dev)
     fwd_bwd = None if args.small else fwd_bwd_arm(args, dev)
     batched = None if args.small else batched_arm(args, dev)
     peak, peak_kind = load_peaks()
@@ -299,27 +311,23 @@ def gb300_arm(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded uniform initial positions, Philox Brownian steps on the GPU)",
-        "config": {"workload": WORKLOAD + ("_z0.1um_profiling" if args.small else ""),
-                   "n_emitters": N_EMIT, "image": [IMAGE, IMAGE], "substeps": SUBSTEPS,
-                   "exposure_s": EXPOSURE, "pixel_nm": PX * 1e9,
-                   "camera": "sCMOS per-pixel sigma, 12-bit",
-                   "psf": "Born-Wolf TRITC, %d depth keys" % len(pipe.psf.slot_of),
-                   "tile": pipe.tile, "warps_per_tile": pipe.warps,
-                   "stages": pipe.stages,
-                   "tile_autotune_ms_per_frame": {"%dx%d/%dw/%ds" % (t, t, w, st): round(ms, 4)
-                                                  for (t, w, st), ms in tune.items()},
-                   "step": "one frame: Brownian sub-steps, physics, binning, splat, camera; "
-                           "%d frame(s) per CUDA graph replay%s" % (
-                               fps, ", each frame's records kernel (side stream) overlapping "
-                                    "the previous frame's binning, splat and camera"
-                               if fps > 1 else ""),
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (PSF tables %.1f GB)" % tables_gb,
-                   "boundary": "reflecting",
-                   "timed_frames": [args.warmup, args.warmup + args.steps],
-                   "live_emitters": [round(live0, 4), round(live1, 4)],
-                   "psf_build_s": round(psf_build_s, 3)},
+        "config": workload_dict(),
+        "run": {"depth_keys": len(pipe.psf.slot_of), "psf_tables_gb": round(tables_gb, 2),
+                "tile": pipe.tile, "warps_per_tile": pipe.warps, "stages": pipe.stages,
+                "tile_autotune_ms_per_frame": {"%dx%d/%dw/%ds" % (t, t, w, st): round(ms, 4)
+                                               for (t, w, st), ms in tune.items()},
+                "step": "one frame: Brownian sub-steps, physics, binning, splat, camera; "
+                        "%d frame(s) per CUDA graph replay%s" % (
+                            fps, ", each frame's records kernel (side stream) overlapping "
+                                 "the previous frame's binning, splat and camera"
+                            if fps > 1 else ""),
+                "parallelism": "replicas" if world > 1 else "single",
+                "boundary": "reflecting",
+                "timed_frames": [args.warmup, args.warmup + args.steps],
+                "live_emitters": [round(live0, 4), round(live1, 4)],
+                "psf_build_s": round(psf_build_s, 3)},
         "e2e": e2e,
+        "config1_plain_tirf": cfg1,
         "fwd_bwd": fwd_bwd,
         "batched": batched,
         "gpu_launches": fg.launches_per_frame * args.steps,
@@ -338,8 +346,39 @@ def gb300_arm(args, rank, world):
                      "stages_beyond_l2": large_stages},
     }
     if rank == 0 and not args.no_cpu:
-        result["cpu_baseline"] = cpu_baseline()
+        result["cpu_baseline"], result["rel_err"] = cpu_baseline_and_accuracy(dev)
+    result["summary"] = summary(result)
     return result
+
+
+def summary(r):
+    """The headline figures in a few words (printed last, so they survive a
+    truncated log)."""
+    out = {"frames_per_s": round(r["value"], 1),
+           "e2e_frames_per_s": round(r["e2e"]["value"], 1) if r.get("e2e") else None,
+           "splat_frac": round(r["roofline"]["frac"], 3)}
+    if r.get("rel_err"):
+        out["rel_err_per_pixel"] = r["rel_err"]["per_pixel"]
+        out["rel_err_norm"] = r["rel_err"]["norm"]
+    c1 = r.get("config1_plain_tirf")
+    if c1:
+        out["config1_frames_per_s"] = round(c1["value"], 1)
+        out["config1_e2e_frames_per_s"] = round(c1["e2e"]["value"], 1)
+    fb = r.get("fwd_bwd")
+    if fb:
+        out["fwd_bwd_gaussian_model_512px_20k"] = {
+            "frames_per_s": round(fb["value"], 1),
+            "over_forward": round(fb["headline"]["fwd_bwd_over_forward"], 2)}
+        out["dL_dD_100k_T100_over_forward"] = round(
+            fb["diffusion_dD_100k_2048px_T100"]["fwd_bwd_over_forward"], 2)
+    bt = r.get("batched")
+    if bt:
+        out["batched_over_per_field_loop"] = round(bt["batched_over_plain_loop"], 2)
+    st = r["roofline"].get("stages_beyond_l2")
+    if st:
+        out["diffusion_frac_beyond_l2"] = round(st["diffusion"]["frac"], 3)
+        out["camera_frac_beyond_l2"] = round(st["camera"]["frac"], 3)
+    return out
 
 
 def e2e_arm(args, cfg, dev, rank, world):
@@ -490,6 +529,8 @@ def fwd_bwd_arm(args, dev):
     batch = fwd_bwd_case(dev, 64, 200, 128, 120e-9, 300e-9, 0.5e-6, steps, args.warmup, 6)
     dgrad = diffusion_grad_case(dev, 100000, 2048, 100, max(5, args.steps // 4), args.warmup, 9)
     return {"value": headline["fwd_bwd_frames_per_s"], "unit": "frames/s",
+            "model": "the differentiable Gaussian-PSF model (pixel-integrated Gaussians, "
+                     "TIRF depth factor), not the Born-Wolf frame path",
             "workload": "differentiable Gaussian-PSF image, 512^2 px, 20k emitters: forward, "
                         "FP64 Poisson NLL, adjoint (dL/dx, dy, dz, dI, dbg, dsigma); one CUDA "
                         "graph replay per step",
@@ -512,6 +553,74 @@ def config1(exposure=0.030):
         "light_source": {"flux_density": 1.1745e7},
         "effects": {"photo_bleaching": {"switch": False}}}})
     return cfg
+
+
+def config1_arm(args, dev, n_emit=1000, substeps=10, seed=17):
+    """Frames/s of the plain TIRF workload the reference runs on the CPU: 1,000
+    emitters over a 25.6 um field at z = 0, D = 0.1 um^2/s with no boundary
+    (the reference's sample_inputs), 30 ms frames in 10 sub-steps, 160^2 px
+    EMCCD, 100 photons per emitter per ms.  Device-resident frames replayed
+    from CUDA graphs, and frames through ``generate_images`` with host
+    trajectories (e2e)."""
+    import torch
+    import scopyon_gb300 as sg
+    from scopyon_gb300.base import _psf_for
+    from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
+    cfg = config1()
+    cfg.update({"default": {"detector": {"image_size": [160, 160]}}})
+    rng = numpy.random.RandomState(seed)
+    eng = EngineConfig(cfg["default"], rng=rng)
+    pipe = FramePipeline(eng, dev, psf=_psf_for(eng, dev))
+    pipe.psf.ensure([0])
+    dt = eng.exposure_time / substeps
+    steps = max(40, 4 * args.steps)
+    n_frames = 4 * (args.warmup + steps) + 16
+    half = 80 * PX
+    traj = sg.sample_inputs(numpy.arange(n_frames * substeps + 1) * dt, N=n_emit, D=0.1e-12,
+                            rng=rng, lower=-half, upper=half, ndim=2, device=dev)
+    fg = FrameGraph(pipe, traj, substeps, dt, seed=seed, frames_per_step=4)
+    fg.capture()
+    for _ in range(-(-args.warmup // 4)):
+        fg.step()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record()
+    for _ in range(steps // 4):
+        fg.step()
+    b.record()
+    torch.cuda.synchronize()
+    pipe.check_status()
+    ms = a.elapsed_time(b) / (4 * (steps // 4))
+    # e2e: the public API on host trajectories (the reference's sample_inputs layout)
+    e2e_frames = 20
+    t_host = numpy.arange((args.warmup + e2e_frames) * substeps + 1) * dt
+    hrng = numpy.random.RandomState(seed + 1)
+    pts = numpy.zeros((n_emit, 4))
+    pts[:, :2] = hrng.uniform(-half, half, (n_emit, 2))
+    pts[:, 2] = numpy.arange(n_emit)
+    pts[:, 3] = 1.0
+    inputs = []
+    for k, t in enumerate(t_host):
+        if k:
+            pts = pts.copy()
+            pts[:, :2] += math.sqrt(2 * 0.1e-12 * dt) * hrng.standard_normal((n_emit, 2))
+        inputs.append((float(t), pts))
+    gen = sg.generate_images(inputs, args.warmup + e2e_frames, config=cfg,
+                             rng=numpy.random.RandomState(seed + 2), device=dev)
+    for _ in range(args.warmup):
+        next(gen).as_array()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_frames):
+        next(gen).as_array()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_frames
+    return {"workload": "plain TIRF: 1,000 emitters, 160^2 px EMCCD, 10 sub-steps of 3 ms, "
+                        "100 photons/emitter/ms, D = 0.1 um^2/s",
+            "value": 1e3 / ms, "unit": "frames/s", "ms_per_frame": ms, "frames": steps,
+            "e2e": {"value": 1.0 / e2e_s, "unit": "frames/s", "frames": e2e_frames,
+                    "h2d_bytes_per_step": substeps * n_emit * 5 * 8 + substeps * 8,
+                    "d2h_bytes_per_step": 160 * 160 * 8 + 16}}
 
 
 def stage_rooflines(stage_ms, pipe, n_rec, peak):
@@ -728,94 +837,183 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=
 
 
 # ---------------------------------------------------------------- CPU baseline
-_WORKER_PSF = {}
+def _cmos_table():
+    """The reference's CMOS read-noise table (RNDist_F40), from the committed
+    reference goldens."""
+    g = numpy.load(os.path.join(ROOT, "tests", "golden", "reference_goldens.npz"))
+    return numpy.asarray(g["cmos_table"])
 
 
-def _cpu_worker(job):
-    """Times the oracle on one bounded sample: footprint sums of ``n_steps``
-    emitter-steps over ``n_keys`` depth keys (tables built once per process,
-    untimed) and the CMOS camera on a 64 x 64 patch (per-pixel table choice
-    plus Poisson draw, the reference's CMOS loop)."""
-    n_steps, n_keys, seed = job
+def _oracle_params(cfg, rng):
+    import oracle as O
+    import scopyon_gb300 as sg
+    from __graft_entry__ import _si_tree
+    eng = sg.EPIFMSimulator(cfg, rng=numpy.random.RandomState(0)).base()
+    return O.Params(_si_tree(cfg.yaml)["default"], float(eng.psf_wavelength),
+                    eng.norm_coeff / eng.psf_normalization, rng=rng, na=eng.na,
+                    cmos_table=_cmos_table())
+
+
+def cpu_baseline_and_accuracy(dev, seed=61):
+    """The CPU leg: the FP64 oracle forms one whole frame of the workload on
+    the host cores (timed), and that frame checks the GPU's.
+
+    Frame: the workload's first frame from host trajectories (20,000 emitters,
+    20 sub-steps, depths in +-1 um), bleaching times drawn once and given to
+    both sides.  GPU: ``generate_images`` with those inputs, native camera, so
+    the expectation comes from the production FP32 path (records, box tables,
+    tile bins, splat).  Oracle: the vectorised FP64 frame (a prefix sum per
+    depth key, the keys spread over spawned processes) plus the reference's
+    CMOS camera law vectorised (table read noise, Poisson signal).  Returns
+    (cpu_baseline, rel_err)."""
+    import multiprocessing as mp
+    import torch
+    import oracle as O
+    from oracle import frames as F
+    import scopyon_gb300 as sg
+    times, pos = trajectories(1, seed=seed)
+    ids = numpy.arange(N_EMIT, dtype=float)
+    inputs = [(float(t), numpy.hstack([pos[k], ids[:, None], numpy.ones((N_EMIT, 1))]))
+              for k, t in enumerate(times)]
+    rng = numpy.random.RandomState(seed)
+    bleach = dict(zip(range(N_EMIT), rng.exponential(2.0, N_EMIT)))
+    cfg = workload_config()
+    _, info = next(sg.generate_images(inputs, 1, config=cfg, rng=numpy.random.RandomState(seed),
+                                      full_output=True, device=dev,
+                                      draws=sg.InjectedDraws(bleach=bleach)))
+    torch.cuda.synchronize()
+    e_gpu = info["expectation"]
+    workers = max(1, min(os.cpu_count() or 1, 64))
+    params = _oracle_params(cfg, numpy.random.RandomState(seed))
+    params.detector_type = "CMOS"
+    data = [(t, O.format_data(p)) for t, p in inputs]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        pool.map(abs, range(workers))  # workers started before the clock
+        t0 = time.perf_counter()
+        cam, _ = F.output_frame_fast(params, data, O.InjectedDraws(bleach, []), 0, states={},
+                                     camera=False, pool=pool, workers=workers)
+        t1 = time.perf_counter()
+    e_ref = cam[:, :, 0]
+    crng = numpy.random.RandomState(seed + 1)
+    noise = O.cmos_table_draw_array(params.cmos_table, crng.random_sample(e_ref.shape))
+    adc = O.adc_counts(crng.poisson(e_ref) + noise, params.fullwell, params.gain, params.offset,
+                       params.bit)
+    t2 = time.perf_counter()
+    assert adc.shape == e_ref.shape
+    big = e_ref > 1e-6 * e_ref.max()
+    rel = {"per_pixel": float((numpy.abs(e_gpu - e_ref)[big] / e_ref[big]).max()),
+           "norm": float(numpy.abs(e_gpu - e_ref).sum() / e_ref.sum()),
+           "floor": "pixels above 1e-6 of the frame maximum (%d of %d)" % (int(big.sum()),
+                                                                          big.size),
+           "frame": "the workload's first frame: generate_images on host trajectories, "
+                    "production FP32 path, against the FP64 oracle"}
+    base = {"value": 1.0 / (t2 - t0), "unit": "frames/s", "cores": workers, "kind": "port",
+            "sample": "one whole frame of the workload, not extrapolated: the FP64 oracle's "
+                      "expectation (%d records over %d depth keys, %.2f s on %d processes) "
+                      "and the CMOS camera (%.2f s)"
+                      % (len(data[0][1]) * SUBSTEPS,
+                         len(numpy.unique(F.depth_keys(pos[:-1, :, 2]))), t1 - t0, workers,
+                         t2 - t1)}
+    return base, rel
+
+
+def _ref_worker(job):
+    """One process's share of a reference-arm step: the reference's own
+    per-element algorithms on a bounded sample, each timed per unit.
+
+    * footprints: ``overlay_signal_`` slice sums of 1999^2 FP64 grids, one
+      emitter-step at a time (``_epifm.py:224-282``), on depth keys built
+      beforehand;
+    * a depth key's grid: Born-Wolf radial table and ``radial_to_cartesian``
+      (``_epifm.py:99-126``, ``:181-213``);
+    * camera: the CMOS model pixel by pixel, a table draw then a Poisson draw
+      (``_epifm.py:332-353``), with the RNDist_F40 table;
+    * diffusion: ``move_points``' scalar normal per particle and axis
+      (``sampling.py:115-119``)."""
+    n_steps, n_keys, n_px, n_move, seed, table = job
     if ROOT not in sys.path:
         sys.path.insert(0, ROOT)
     import oracle as O
     from scopyon_gb300._catalog import psf_wavelength_and_norm
     rng = numpy.random.RandomState(seed)
-    z = numpy.random.RandomState(seed % 1000).uniform(-1e-6, 1e-6, size=n_keys)
-    psf = _WORKER_PSF.get("psf")
-    if psf is None:
-        wl, _ = psf_wavelength_and_norm("Tetramethylrhodamine(TRITC)")
-        psf = _WORKER_PSF["psf"] = O.PSFCache("Born-Wolf", wl)
+    wl, _ = psf_wavelength_and_norm("Tetramethylrhodamine(TRITC)")
+    psf = O.PSFCache("Born-Wolf", wl)
+    z = rng.uniform(-1e-6, 1e-6, size=n_keys)
+    t0 = time.perf_counter()
     for d in z:
         psf.get(d)
+    t_key = (time.perf_counter() - t0) / n_keys
     xy = rng.uniform(-HALF, HALF, size=(n_steps, 2))
     img = numpy.zeros((IMAGE, IMAGE))
     t0 = time.perf_counter()
     for k in range(n_steps):
         O.overlay_signal(img, psf.get(z[k % n_keys]), [0.0, xy[k, 0], xy[k, 1]], PX, 1.0)
     t_splat = (time.perf_counter() - t0) / n_steps
-    table = numpy.column_stack([numpy.linspace(0.6, 19.9, 194),
-                                numpy.exp(-numpy.linspace(0, 8, 194))])
 
     class P:
         detector_type = "CMOS"
         cmos_table = table
 
-    patch = rng.uniform(0, 20, size=(64, 64))
+    side = int(round(math.sqrt(n_px)))
+    patch = rng.uniform(0, 20, size=(side, side))
     t0 = time.perf_counter()
     O.NumpyDraws(rng).camera(P, patch)
-    t_cam = (time.perf_counter() - t0) / patch.size
-    return t_splat, t_cam
-
-
-def _rate(res, threads):
-    t_splat = statistics.mean(r[0] for r in res)
-    t_cam = statistics.mean(r[1] for r in res)
-    sec_per_frame = (t_splat * SUBSTEPS * N_EMIT + t_cam * IMAGE * IMAGE) / threads
-    return 1.0 / sec_per_frame, t_splat, t_cam
-
-
-def cpu_baseline(n_steps=300, n_keys=6):
-    """Oracle frames/s on one host core (bounded sample, extrapolated)."""
+    t_px = (time.perf_counter() - t0) / patch.size
+    pts = rng.uniform(-HALF, HALF, size=(n_move, 3))
     t0 = time.perf_counter()
-    res = [_cpu_worker((n_steps, n_keys, 100))]
-    wall = time.perf_counter() - t0
-    value, t_splat, t_cam = _rate(res, 1)
-    return {"value": value, "unit": "frames/s", "cores": 1, "kind": "port",
-            "sample": "%d emitter-step footprint sums (exact 1-nm slice sums over %d depth "
-                      "keys, tables built untimed) + CMOS table/Poisson camera on 64x64 px, "
-                      "extrapolated linearly to 400k emitter-steps and 512^2 px per frame "
-                      "(%.2f ms/step, %.1f us/px; %.1f s wall)"
-                      % (n_steps, n_keys, t_splat * 1e3, t_cam * 1e6, wall)}
+    for i in range(n_move):
+        for d in range(3):
+            pts[i, d] += rng.normal(0.0, 1e-8)
+    t_draw = (time.perf_counter() - t0) / (3 * n_move)
+    return t_splat, t_px, t_draw, t_key
 
 
 def reference_arm(args, rank, world):
-    """The oracle port on all host cores; each step is one bounded sample."""
+    """The reference's own CPU algorithms (ported, per element, as the reference
+    runs them) on all host cores.  Each step: every process times a bounded
+    sample of footprint sums, camera pixels, diffusion draws and one depth-key
+    grid.  ``value`` extrapolates the per-unit times to one frame of the
+    workload (400k emitter-steps, 512^2 pixels, 1.2M diffusion draws) divided
+    over the processes; ``ms_per_step`` is the wall time of the timed sample."""
     if rank != 0:
         return None
     import multiprocessing as mp
     threads = max(1, min(os.cpu_count() or 1, 64))
-    n_steps, n_keys = 40, 2
-    times_ = []
+    table = _cmos_table()
+    n_steps, n_keys, n_px, n_move = 40, 2, 1024, 2000
+    res, walls = [], []
     with mp.get_context("spawn").Pool(threads) as pool:
         for k in range(args.warmup + args.steps):
             t0 = time.perf_counter()
-            res = pool.map(_cpu_worker, [(n_steps, n_keys, 1000 * k + w) for w in range(threads)])
+            out = pool.map(_ref_worker, [(n_steps, n_keys, n_px, n_move, 1000 * k + w, table)
+                                         for w in range(threads)])
             if k >= args.warmup:
-                times_.append((res, time.perf_counter() - t0))
-    all_res = [r for res, _ in times_ for r in res]
-    value, t_splat, t_cam = _rate(all_res, threads)
-    sample = ("%d processes x %d emitter-step footprint sums (%d depth keys) + 64x64 px CMOS "
-              "camera per step; extrapolated to 400k emitter-steps and 512^2 px per frame "
-              "(%.2f ms/step, %.1f us/px per process)" % (threads, n_steps, n_keys,
-                                                         t_splat * 1e3, t_cam * 1e6))
+                res += out
+                walls.append(time.perf_counter() - t0)
+    t_splat, t_px, t_draw, t_key = (statistics.mean(r[i] for r in res) for i in range(4))
+    parts = {"footprints_s": t_splat * SUBSTEPS * N_EMIT,
+             "camera_s": t_px * IMAGE * IMAGE,
+             "diffusion_s": t_draw * SUBSTEPS * N_EMIT * 3}
+    sec_per_frame = sum(parts.values()) / threads
+    value = 1.0 / sec_per_frame
+    n_keys_frame = int(round(Z_HALF / 1e-9)) + 2  # keys 0..Z/1nm and the key past the cutoff
+    sample = ("%d processes, each step per process: %d emitter-step footprint sums (1-nm slice "
+              "sums of 1999^2 FP64 grids), %d CMOS camera pixels (RNDist_F40 table, Poisson), "
+              "%d diffusion draws, %d depth-key grids; per unit %.2f ms / footprint, %.1f us / "
+              "pixel, %.2f us / draw, %.0f ms / key" % (threads, n_steps, n_px, 3 * n_move,
+                                                       n_keys, t_splat * 1e3, t_px * 1e6,
+                                                       t_draw * 1e6, t_key * 1e3))
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_emitters": N_EMIT, "image": [IMAGE, IMAGE],
-                       "substeps": SUBSTEPS},
+            "ms_per_step": 1e3 * statistics.mean(walls), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_dict(),
+            "extrapolated": True,
+            "extrapolation": "value = 1 / (per-frame work / processes): per-unit times of the "
+                             "timed samples times one frame's units; ms_per_step is the wall "
+                             "time of one timed sample step, not of a frame",
+            "frame_seconds_one_process": {k: round(v, 2) for k, v in parts.items()},
+            "psf_warmup_s_one_process": round(t_key * n_keys_frame, 1),
             "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads,
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0,

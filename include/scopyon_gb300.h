@@ -39,7 +39,8 @@ extern "C" {
  * [0] error flags (bit0 bad PSF key, bit1 missing table, bit2 bounds overflow,
  *     bit3 RNG loop bound hit, bit4 capacity, bit5 a bounded wait for an
  *     asynchronous copy ran out, bit6 a caller-built record with a negative
- *     first pixel, which is not binned), [1..3] first offending index. */
+ *     first pixel, which is not binned, bit7 a non-finite emitter position or
+ *     normalisation), [1..3] first offending index. */
 #define SC_STATUS_WORDS 4
 
 /* One emitter during one exposure sub-step, ready to be splatted (64 bytes).
@@ -97,6 +98,10 @@ typedef struct {
     int32_t box_p, box_nq;   /* box tables: P rows per pixel and NQ pixel offsets, or 0     */
     int32_t n_slots;         /* depth-key tables held in d_sat / d_box                      */
     int32_t box_stages;      /* block copies in flight per splat warp (1..8; 0: 4)          */
+    int32_t first_wait_polls;/* test hook: polls allowed for each splat warp's first block  */
+                             /* wait; 0: the normal bound (4096), -1: none, so that wait    */
+                             /* runs out at once (status bit 5) while the copies in flight  */
+                             /* are still drained under the normal bound                   */
     double px, res;
 } ScSplatParams;
 

@@ -41,6 +41,7 @@ class SplatParams(ctypes.Structure):
                 ("n_images", ctypes.c_int32), ("rec_per_image", ctypes.c_int32),
                 ("box_p", ctypes.c_int32), ("box_nq", ctypes.c_int32),
                 ("n_slots", ctypes.c_int32), ("box_stages", ctypes.c_int32),
+                ("first_wait_polls", ctypes.c_int32),
                 ("px", ctypes.c_double), ("res", ctypes.c_double)]
 
 
@@ -126,6 +127,11 @@ class ScopyonGPUError(RuntimeError):
     def __init__(self, code, message):
         super().__init__(message)
         self.code = code
+
+
+class ScopyonInputError(ScopyonGPUError, ValueError):
+    """Invalid input found on the device (a non-finite position, a malformed
+    record): a ValueError, as the reference raises for the same inputs."""
 
 
 _lock = threading.Lock()

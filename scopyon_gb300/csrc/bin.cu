@@ -586,7 +586,7 @@ extern "C" int sc_bin_reset(const ScSplatParams *p, void *d_ws, size_t ws_bytes,
     sc::TileGeom g;
     int rc = sc::tile_geom(p, g);
     if (rc) return rc;
-    SC_REQUIRE(d_ws && ws_bytes >= bin_counts_bytes(g.n_tiles), "sc_bin_reset: workspace %zu < %zu",
+    SC_REQUIRE_CAP(d_ws && ws_bytes >= bin_counts_bytes(g.n_tiles), "sc_bin_reset: workspace %zu < %zu",
                ws_bytes, bin_counts_bytes(g.n_tiles));
     return sc::cuda_status(cudaMemsetAsync(d_ws, 0, sizeof(int32_t) * 2 * g.n_tiles,
                                            sc::as_stream(stream)),
@@ -606,7 +606,7 @@ extern "C" int sc_bin_finish(int n_rec, const ScSplatParams *p, void *d_ws, size
             cudaMemsetAsync(d_tile_start, 0, sizeof(int32_t) * (2 * g.n_tiles + 1), s),
             "sc_bin_finish");
     SC_REQUIRE(d_ws && d_items, "sc_bin_finish: NULL pointer");
-    SC_REQUIRE(ws_bytes >= sc_bin_workspace_bytes(n_rec, g.n_tiles),
+    SC_REQUIRE_CAP(ws_bytes >= sc_bin_workspace_bytes(n_rec, g.n_tiles),
                "sc_bin_finish: workspace %zu < %zu bytes (counts, bins and ranks)", ws_bytes,
                sc_bin_workspace_bytes(n_rec, g.n_tiles));
     sc::BinLayout b;
@@ -629,7 +629,7 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
             "sc_bin_steps");
     }
     SC_REQUIRE(d_recs && d_items && d_ws, "sc_bin_steps: NULL pointer");
-    SC_REQUIRE(ws_bytes >= bin_counts_bytes(g.n_tiles), "sc_bin_steps: workspace %zu < %zu bytes",
+    SC_REQUIRE_CAP(ws_bytes >= bin_counts_bytes(g.n_tiles), "sc_bin_steps: workspace %zu < %zu bytes",
                ws_bytes, bin_counts_bytes(g.n_tiles));
     SC_REQUIRE(g.rec_per_image == 0 || (int64_t)g.rec_per_image * g.n_images >= n_rec,
                "sc_bin_steps: rec_per_image too small for n_rec");

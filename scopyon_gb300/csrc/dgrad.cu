@@ -157,7 +157,7 @@ extern "C" int sc_gauss_nll(const float *d_mu, const float *d_counts, int64_t n,
     SC_REQUIRE(n > 0, "sc_gauss_nll: n=%lld", (long long)n);
     SC_REQUIRE(d_mu && d_counts && d_loss, "sc_gauss_nll: NULL pointer");
     const int parts = parts_of(n);
-    SC_REQUIRE(d_scratch && scratch_bytes >= (size_t)parts * sizeof(double),
+    SC_REQUIRE_CAP(d_scratch && scratch_bytes >= (size_t)parts * sizeof(double),
                "sc_gauss_nll: scratch %zu < %zu bytes", scratch_bytes, (size_t)parts * sizeof(double));
     cudaStream_t s = sc::as_stream(stream);
     double *partial = static_cast<double *>(d_scratch);
@@ -174,7 +174,7 @@ extern "C" int sc_diffusion_dD(const float *d_pos, const float *d_emit, int n, i
     SC_REQUIRE(d_pos && d_emit && d_grad_pos && d_D && d_dD, "sc_diffusion_dD: NULL pointer");
     const int64_t total = (int64_t)n * T;
     const int parts = parts_of(total);
-    SC_REQUIRE(d_scratch && scratch_bytes >= (size_t)parts * sizeof(double),
+    SC_REQUIRE_CAP(d_scratch && scratch_bytes >= (size_t)parts * sizeof(double),
                "sc_diffusion_dD: scratch %zu < %zu bytes", scratch_bytes,
                (size_t)parts * sizeof(double));
     cudaStream_t s = sc::as_stream(stream);

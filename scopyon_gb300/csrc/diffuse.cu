@@ -473,7 +473,7 @@ extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *s
         SC_REQUIRE(n_rec < (1ll << 31), "sc_native_records: %lld records", (long long)n_rec);
         SC_REQUIRE(g.n_images == 1 && g.nw == k.nw && g.nh == k.nh,
                    "sc_native_records: bin geometry is not the frame's");
-        SC_REQUIRE(d_bin_ws && bin_ws_bytes >= sc_bin_workspace_bytes((int)n_rec, g.n_tiles),
+        SC_REQUIRE_CAP(d_bin_ws && bin_ws_bytes >= sc_bin_workspace_bytes((int)n_rec, g.n_tiles),
                    "sc_native_records: bin workspace %zu < %zu bytes", bin_ws_bytes,
                    sc_bin_workspace_bytes((int)n_rec, g.n_tiles));
         sc::bin_layout(g, (int)n_rec, d_bin_ws, bin_ws_bytes, bl);

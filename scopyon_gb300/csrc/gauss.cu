@@ -610,7 +610,7 @@ int launch_reduce(const float *x, const float *counts, int64_t seg_len, int n_se
     SC_REQUIRE(n_seg <= 65535, "n_seg=%d exceeds 65535", n_seg);
     SC_REQUIRE(out && (seg_len == 0 || x), "NULL pointer");
     const int parts = sum_parts(seg_len);
-    SC_REQUIRE(scratch && scratch_bytes >= (size_t)parts * n_seg * sizeof(double),
+    SC_REQUIRE_CAP(scratch && scratch_bytes >= (size_t)parts * n_seg * sizeof(double),
                "reduction scratch %zu < %zu bytes", scratch_bytes,
                (size_t)parts * n_seg * sizeof(double));
     double *partial = static_cast<double *>(scratch);
@@ -712,7 +712,7 @@ extern "C" int sc_gauss_forward(const ScGaussParams *p, const float *d_emit, con
     SC_REQUIRE(d_sigma && d_mu && d_ws, "sc_gauss_forward: NULL pointer");
     SC_REQUIRE(c.n_emit == 0 || d_emit, "sc_gauss_forward: emitters are NULL");
     const GaussWorkspace w = gauss_workspace(p, d_ws);
-    SC_REQUIRE(ws_bytes >= w.total, "sc_gauss_forward: workspace %zu < %zu bytes", ws_bytes, w.total);
+    SC_REQUIRE_CAP(ws_bytes >= w.total, "sc_gauss_forward: workspace %zu < %zu bytes", ws_bytes, w.total);
     cudaStream_t s = sc::as_stream(stream);
     const ScSplatParams sp = gauss_splat_params(p);
     sc::TileGeom g;
@@ -781,7 +781,7 @@ extern "C" int sc_gauss_backward(const ScGaussParams *p, const float *d_emit, co
     // the records and bins sc_gauss_forward left in the workspace
     SC_REQUIRE(d_ws, "sc_gauss_backward: the forward's workspace is NULL");
     const GaussWorkspace w = gauss_workspace(p, const_cast<void *>(d_ws));
-    SC_REQUIRE(ws_bytes >= w.total, "sc_gauss_backward: workspace %zu < %zu bytes", ws_bytes,
+    SC_REQUIRE_CAP(ws_bytes >= w.total, "sc_gauss_backward: workspace %zu < %zu bytes", ws_bytes,
                w.total);
     const ScSplatParams sp = gauss_splat_params(p);
     sc::TileGeom g;

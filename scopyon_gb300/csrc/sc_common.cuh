@@ -25,6 +25,15 @@ int launch_status(const char *what);
         }                                \
     } while (0)
 
+// A caller buffer (workspace, scratch) smaller than the call needs.
+#define SC_REQUIRE_CAP(cond, ...)        \
+    do {                                 \
+        if (!(cond)) {                   \
+            ::sc::set_error(__VA_ARGS__); \
+            return SC_ERR_CAPACITY;      \
+        }                                \
+    } while (0)
+
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // status word helpers (device): first error wins the index slots

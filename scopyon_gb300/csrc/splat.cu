@@ -37,6 +37,7 @@ struct SplatConsts {
     int box_nq;        // rows and columns of a box table block
     int box_p;         // grid rows per pixel of the box tables
     int64_t box_floats;  // floats held in the box tables (every slot)
+    uint32_t first_wait_tries;  // polls of each bulk-copy warp's first wait
 };
 
 // Footprint bound k of one axis: ceil(((start + k) * px - origin) / res) with
@@ -247,12 +248,13 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
                  : "memory");
 }
 
-// Waits until the phase of this parity has completed: at most kWaitTries
+// Waits until the phase of this parity has completed: at most max_tries
 // polls, each suspending the thread until completion or kSuspendNs.  The
 // result is uniform across the warp.
-__device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity,
+                                          uint32_t max_tries = kWaitTries) {
     uint32_t ok = 0;
-    for (uint32_t tries = 0; tries < kWaitTries && !ok; ++tries) {
+    for (uint32_t tries = 0; tries < max_tries && !ok; ++tries) {
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
             "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
@@ -371,7 +373,7 @@ splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restr
                                   table_floats, NB, nxt_src, status, tile);
             __syncwarp();
         }
-        if (!warp_wait(my_bars + s, parity)) {
+        if (!warp_wait(my_bars + s, parity, k == 0 ? c.first_wait_tries : kWaitTries)) {
             if (lane == 0) sc::flag_status(status, 5, k, warp, tile);
             break;
         }
@@ -675,6 +677,9 @@ int splat_consts(const ScSplatParams *p, const sc::TileGeom &g, SplatConsts &c) 
     c.box_nq = 0;
     c.box_p = 0;
     c.box_floats = 0;
+    c.first_wait_tries = p->first_wait_polls < 0 ? 0u
+                         : p->first_wait_polls == 0 ? kWaitTries
+                                                    : (uint32_t)p->first_wait_polls;
     return SC_OK;
 }
 
@@ -737,7 +742,7 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
     SC_REQUIRE(d_tile_start && d_image && d_ws, "sc_splat: NULL pointer");
     SC_REQUIRE(p->box_stages >= 0 && p->box_stages <= 8, "sc_splat: box_stages=%d not in 0..8",
                p->box_stages);
-    SC_REQUIRE(ws_bytes >= sc_splat_workspace_bytes(p), "sc_splat: workspace %zu < %zu bytes",
+    SC_REQUIRE_CAP(ws_bytes >= sc_splat_workspace_bytes(p), "sc_splat: workspace %zu < %zu bytes",
                ws_bytes, sc_splat_workspace_bytes(p));
     if (d_box) {
         SC_REQUIRE(p->box_p >= 1 && p->box_nq == (c.n_signal + p->box_p - 1) / p->box_p + 1,

@@ -101,6 +101,12 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
     rec.slot = -1;
     rec.w = 0.f;
     if (norm <= 0.0) return;  // overlay_signal returns early (_epifm.py:216-217)
+    // a non-finite position or normalisation: the reference's math.floor
+    // raises ValueError (_epifm.py:233); reported here (status bit 7)
+    if (!isfinite(rel1) || !isfinite(rel2) || !isfinite(norm)) {
+        flag_status(status, 7, i, s, 0);
+        return;
+    }
     // depth key: int(|depth| / res) inside depth_cutoff + res, else -1 (_epifm.py:76-88)
     const double depth = fabs(rel0);
     const float df32 = __double2float_rn(depth);

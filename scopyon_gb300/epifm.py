@@ -83,6 +83,7 @@ class EngineConfig:
         adc = conf.analog_to_digital_converter
         self.bit = int(adc.bit)
         self.fullwell = adc.fullwell
+        self._validate()
         self.fpn_type, self.fpn_count = adc.type, adc.count
         self.offset, self.gain = self._adc_maps(adc.offset, rng)
 
@@ -121,6 +122,33 @@ class EngineConfig:
         self.catalog_dir = _gpu_opt(raw, "catalog_dir")
         table = _gpu_opt(raw, "cmos_table")
         self.cmos_table = None if table is None else numpy.asarray(table, dtype=float)
+
+    def _validate(self):
+        """Reject a corrupt detector or ADC section before anything reaches the
+        device (the reference fails later, inside numpy, on the same values)."""
+        def finite_pos(name, v):
+            try:
+                ok = math.isfinite(float(v)) and float(v) > 0
+            except (TypeError, ValueError):
+                ok = False
+            if not ok:
+                raise ValueError("%s must be a finite positive number (got %r)" % (name, v))
+        if len(self.image_size) != 2 or not all(0 < v < 32767 for v in self.image_size):
+            raise ValueError("detector.image_size must be two sizes in 1..32766 (got %r)"
+                             % (self.image_size,))
+        finite_pos("detector.pixel_length", self.pixel_length)
+        finite_pos("magnification", self.magnification)
+        finite_pos("detector.exposure_time", self.exposure_time)
+        finite_pos("analog_to_digital_converter.fullwell", self.fullwell)
+        if not 1 <= self.bit <= 32:
+            raise ValueError("analog_to_digital_converter.bit must be in 1..32 (got %r)"
+                             % self.bit)
+        try:
+            qe = float(self.qe)
+        except (TypeError, ValueError):
+            qe = float("nan")
+        if not 0.0 <= qe <= 1.0:
+            raise ValueError("detector.QE must be in [0, 1] (got %r)" % (self.qe,))
 
     @property
     def px(self):
@@ -377,6 +405,9 @@ class FramePipeline:
         self.camera_kind = self._camera_kind()
         # name -> [(start, end) CUDA events]; set to a dict to time kernels in place
         self.kernel_events = None
+        # test hook: polls of each splat warp's first block wait (0: the normal
+        # bound; -1: none, so that the wait runs out and the frame reports it)
+        self.first_wait_polls = 0
 
     def set_tiles(self, tile, warps, stages=4):
         """Use tiles of tile x tile pixels, `warps` warps per splat CTA and
@@ -481,6 +512,7 @@ class FramePipeline:
         p.box_p, p.box_nq = self.psf.box_p, self.psf.box_nq
         p.n_slots = self.psf.capacity
         p.box_stages = self.stages
+        p.first_wait_polls = int(self.first_wait_polls)
         p.px, p.res = self.cfg.px, PSF_RES
         return p
 
@@ -618,8 +650,13 @@ class FramePipeline:
                 msgs.append("bounded wait for an asynchronous copy ran out (tile %d)" % st[3])
             if bits & 64:
                 msgs.append("record %d has a negative first pixel (%d, %d)" % (st[1], st[2], st[3]))
-            code = (_lib.SC_ERR_TIMEOUT if bits == 32 else _lib.SC_ERR_ARG if bits == 64
-                    else _lib.SC_ERR_CAPACITY)
+            if bits & 128:
+                msgs.append("non-finite emitter position or normalisation (particle %d, "
+                            "sub-step %d)" % (st[1], st[2]))
+            if bits & ~(64 | 128) == 0:
+                raise _lib.ScopyonInputError(
+                    _lib.SC_ERR_NAN if bits & 128 else _lib.SC_ERR_ARG, "; ".join(msgs))
+            code = _lib.SC_ERR_TIMEOUT if bits == 32 else _lib.SC_ERR_CAPACITY
             raise _lib.ScopyonGPUError(code, "; ".join(msgs))
 
     def run_frame(self, particles, unit_times, with_optinfo=True, draws=None, seed=0, counter=0,

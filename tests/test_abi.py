@@ -126,3 +126,28 @@ def test_stage_known_matches_numpy():
     arrays[4] = arrays[4].copy()
     arrays[4][10, 3] = -1.0
     assert _stage_known(arrays, ids, staging) is None
+
+
+def test_undersized_workspace_is_a_capacity_error():
+    """A caller workspace smaller than the call needs: SC_ERR_CAPACITY, found
+    before anything is launched (the pointers are never dereferenced)."""
+    from scopyon_gb300 import _build, _lib
+    _build.build()
+    L = _lib.load()
+    P = ctypes.c_void_p
+    fake = P(1 << 20)  # non-NULL, never dereferenced: validation fails first
+    p = _lib.SplatParams(nw=64, nh=64, tile=8, halo=14, warps=4, tiles_x=8, tiles_y=8, n_r=1000,
+                         sat_pitch=1004, n_images=1, rec_per_image=0, px=1.6e-7, res=1e-9)
+    need = L.sc_bin_workspace_bytes(1000, 64)
+    rc = L.sc_bin_steps(fake, 1000, ctypes.byref(p), fake, 16, fake, fake, None, None)
+    assert rc == _lib.SC_ERR_CAPACITY
+    assert b"workspace" in L.sc_last_error()
+    rc = L.sc_bin_finish(1000, ctypes.byref(p), fake, need - 4, fake, fake, None)
+    assert rc == _lib.SC_ERR_CAPACITY
+    rc = L.sc_splat(fake, fake, fake, fake, None, ctypes.byref(p), fake,
+                    L.sc_splat_workspace_bytes(ctypes.byref(p)) - 4, fake, None, None)
+    assert rc == _lib.SC_ERR_CAPACITY
+    with pytest.raises(_lib.ScopyonGPUError) as err:
+        _lib.call("sc_splat", fake, fake, fake, fake, None, ctypes.byref(p), fake, 0, fake,
+                  None, None)
+    assert err.value.code == _lib.SC_ERR_CAPACITY

@@ -90,3 +90,17 @@ def test_unknown_detector_and_type():
     cfg.update({"default": {"type": "lscm"}})
     with pytest.raises(ValueError):
         EngineConfig(cfg["default"])
+
+
+@pytest.mark.parametrize("section,key,value", [
+    ("detector", "image_size", [0, 64]), ("detector", "image_size", [64, 40000]),
+    ("detector", "pixel_length", -16e-6), ("detector", "exposure_time", 0.0),
+    ("detector", "QE", 1.5), ("analog_to_digital_converter", "bit", 0),
+    ("analog_to_digital_converter", "bit", 40),
+    ("analog_to_digital_converter", "fullwell", float("nan"))])
+def test_corrupt_config_is_rejected_on_the_host(section, key, value):
+    """A corrupt detector / ADC section raises ValueError before any launch."""
+    cfg = DefaultConfiguration()
+    cfg.update({"default": {section: {key: value}}})
+    with pytest.raises(ValueError, match=key):
+        EngineConfig(cfg["default"], rng=numpy.random.RandomState(0))

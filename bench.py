@@ -406,7 +406,7 @@ def e2e_arm(args, cfg, dev, rank, world):
     dt = max_over_ranks(time.perf_counter() - t0, world, dev)
     return {"value": world * steps / dt, "unit": "frames/s", "frames": steps,
             "h2d_bytes_per_step": SUBSTEPS * N_EMIT * 5 * 8 + SUBSTEPS * 8,
-            "d2h_bytes_per_step": IMAGE * IMAGE * 8 + 16}
+            "d2h_bytes_per_step": IMAGE * IMAGE * 4 + 16}
 
 
 # ------------------------------------------------------- differentiable form
@@ -620,7 +620,7 @@ def config1_arm(args, dev, n_emit=1000, substeps=10, seed=17):
             "value": 1e3 / ms, "unit": "frames/s", "ms_per_frame": ms, "frames": steps,
             "e2e": {"value": 1.0 / e2e_s, "unit": "frames/s", "frames": e2e_frames,
                     "h2d_bytes_per_step": substeps * n_emit * 5 * 8 + substeps * 8,
-                    "d2h_bytes_per_step": 160 * 160 * 8 + 16}}
+                    "d2h_bytes_per_step": 160 * 160 * 4 + 16}}
 
 
 def stage_rooflines(stage_ms, pipe, n_rec, peak):
@@ -631,14 +631,14 @@ def stage_rooflines(stage_ms, pipe, n_rec, peak):
     (16 B) and class (4 B) and writes each record (64 B) with its bin and rank
     (8 B); the camera reads each pixel's photons (4 B), offset and 1/gain
     (8 B, with fixed-pattern noise) and read-noise sigma (4 B, sCMOS) and
-    writes the expectation (4 B) and the FP64 ADC count (8 B)."""
+    writes the expectation (4 B) and the FP32 ADC count (4 B)."""
     n_px = pipe.nw * pipe.nh
     out = {}
     for name, alg, bound in (
             ("records", N_EMIT * 68 + n_rec * 72,
              "FP64 position chains and footprint arithmetic (FP64 pipe), not HBM"),
             ("camera", n_px * (8 + (8 if pipe.pixel_maps else 0) +
-                               (4 if pipe.sigma is not None else 0) + 8),
+                               (4 if pipe.sigma is not None else 0) + 4),
              "per-pixel Poisson and normal draws (FP32 and SFU pipes), not HBM")):
         ms = stage_ms[name]
         gbs = alg / (ms / 1e3) / 1e9
@@ -672,7 +672,7 @@ def hbm_stages(dev, peak, steps=20, warmup=3, n_emit=1 << 22, edge=8192, seed=5)
     the class (4 B), per emitter-step it writes the formatted [depth, x, y, id,
     state] row (40 B).  Camera: the workload's sCMOS camera on an edge^2 frame;
     per pixel it reads photons, offset, 1/gain and readout sigma (16 B) and
-    writes the expectation (4 B) and the FP64 ADC count (8 B)."""
+    writes the expectation (4 B) and the FP32 ADC count (4 B)."""
     import torch
     import scopyon_gb300 as sg
     from scopyon_gb300 import _lib
@@ -712,9 +712,10 @@ def hbm_stages(dev, peak, steps=20, warmup=3, n_emit=1 << 22, edge=8192, seed=5)
     inv_gain_f = (4096.0 - offset_f) / 30000.0
     sigma = torch.exp(math.log(1.5) + 0.4 * torch.randn(n, device=dev, generator=gen))
     expect = torch.empty(n, dtype=torch.float32, device=dev)
-    adc = torch.empty(n, dtype=torch.float64, device=dev)
+    adc = torch.empty(n, dtype=torch.float32, device=dev)
     status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
     cp = _lib.CameraParams()
+    cp.d_poisson_table = _lib.poisson_table(dev).data_ptr()
     cp.nw = cp.nh = edge
     cp.camera, cp.exact, cp.rounding, cp.bit = _lib.CAM_SCMOS, 0, 0, 12
     cp.qe, cp.background, cp.readout_noise, cp.emgain = 0.73, 0.0, 1.5, 1.0
@@ -726,13 +727,13 @@ def hbm_stages(dev, peak, steps=20, warmup=3, n_emit=1 << 22, edge=8192, seed=5)
         counter[0] += 1
         cp.counter = counter[0]
         call("sc_camera", cp, ptr(photons), None, None, ptr(offset_f), ptr(inv_gain_f),
-             ptr(sigma), None, None, None, None, None, ptr(expect), ptr(adc), None, ptr(status),
+             ptr(sigma), None, None, None, None, None, ptr(expect), None, ptr(adc), ptr(status),
              stream_ptr())
 
     ms = _event_ms(camera, steps, warmup)
     if int(status[0]):
         raise RuntimeError("camera status %d" % int(status[0]))
-    alg = n * (16 + 4 + 8)
+    alg = n * (16 + 4 + 4)
     gbs = alg / (ms / 1e3) / 1e9
     out["camera"] = {"kernel": "camera_native_kernel (sc_camera, sCMOS)", "image": [edge, edge],
                      "avg_launch_ms": ms, "algorithmic_bytes": alg, "achieved": gbs,

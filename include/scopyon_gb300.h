@@ -119,6 +119,7 @@ typedef struct {
     const int64_t *d_frame;  /* optional device counter f added to counter (graph replay)   */
     const double *d_photons64; /* exact mode: FP64 photons read in place of d_photons       */
     double *d_expect64;      /* exact mode: FP64 expectation QE*(photons+background) out    */
+    const void *d_poisson_table; /* native mode: the tables of sc_poisson_table (required)   */
 } ScCameraParams;
 
 typedef struct {
@@ -144,6 +145,11 @@ typedef struct {
 } ScDiffuseParams;
 
 int sc_get_version(void);
+
+/* sizeof of the ABI structs as this library was compiled: out[0..5] =
+ * ScStepRec, ScStepParams, ScSplatParams, ScCameraParams, ScDiffuseParams,
+ * ScGaussParams (n >= 6), so that a binding can check its layouts.          */
+int sc_struct_sizes(size_t *out, int n);
 
 /* *d_counter += delta on the stream: advances the device frame counter read by
  * sc_diffuse_steps and sc_camera, so that a captured frame can be replayed. */
@@ -415,7 +421,10 @@ int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
  * EMCCD / CCD / CMOS classes and __get_analog_to_digital_converter_counts
  * (src/scopyon/_epifm.py:329-433, :1430-1484).
  * Native mode (p->exact == 0): Philox draws, FP32 arithmetic with the float
- * maps d_offset_f / d_inv_gain_f (NULL: constants offset0 / 1/gain0).
+ * maps d_offset_f / d_inv_gain_f (NULL: constants offset0 / 1/gain0).  The
+ * Poisson draw takes no rejection below a mean of 256 (table inversion of
+ * the integer part plus sequential inversion of the fraction); the EMCCD
+ * output follows the reference's truncated discrete law.
  * Exact mode (p->exact == 1): draws injected by the caller — d_inj_signal
  * (electrons) and d_inj_noise (electrons) or, for the CMOS table,
  * d_inj_uniform — and the reference's FP64 ADC sequence with d_offset /
@@ -428,6 +437,16 @@ int sc_camera(const ScCameraParams *p, const float *d_photons,
               const double *d_inj_noise, const double *d_inj_signal,
               const double *d_inj_uniform, float *d_expect, double *d_adc64,
               float *d_adc32, int32_t *d_status, void *stream);
+
+/* Poisson tables for the camera's native draws: for every integer mean j <
+ * 256, the Poisson(j) CDF in FP32 (summed in FP64) and a guide of starting
+ * points for its inversion.  Built once per device into a caller buffer of
+ * sc_poisson_table_bytes() bytes (16-byte aligned), read by sc_camera
+ * (ScCameraParams.d_poisson_table).  Replaces the Poisson draws of
+ * CCD / CMOS get_signal and the photo-electron count inside the EMCCD law
+ * (src/scopyon/_epifm.py:348-353, :365-400, :428-433).                      */
+size_t sc_poisson_table_bytes(void);
+int sc_poisson_table(void *d_table, size_t bytes, void *stream);
 
 /* Exact EMCCD draw: the reference's discrete distribution over integer
  * output electrons, inverse CDF at the given uniform, per pixel

@@ -54,7 +54,7 @@ class CameraParams(ctypes.Structure):
                 ("gain0", ctypes.c_double), ("table_n", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("counter", ctypes.c_uint64),
                 ("d_frame", ctypes.c_void_p), ("d_photons64", ctypes.c_void_p),
-                ("d_expect64", ctypes.c_void_p)]
+                ("d_expect64", ctypes.c_void_p), ("d_poisson_table", ctypes.c_void_p)]
 
 
 class DiffuseParams(ctypes.Structure):
@@ -80,6 +80,7 @@ _I = ctypes.c_int
 _D = ctypes.c_double
 _SIG = {
     "sc_get_version": (_I, []),
+    "sc_struct_sizes": (_I, [_P, _I]),
     "sc_counter_add": (_I, [_P, ctypes.c_int64, _P]),
     "sc_stage_rows": (_I, [_P, ctypes.c_int64, _P, _P, _P]),
     "sc_last_error": (ctypes.c_char_p, []),
@@ -105,6 +106,8 @@ _SIG = {
     "sc_camera": (_I, [ctypes.POINTER(CameraParams), _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                        _P, _P, _P, _P, _P]),
     "sc_emccd_exact": (_I, [_P, _D, _D, _P, _I, _D, _P, _P, _P]),
+    "sc_poisson_table_bytes": (ctypes.c_size_t, []),
+    "sc_poisson_table": (_I, [_P, ctypes.c_size_t, _P]),
     "sc_gauss_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(GaussParams)]),
     "sc_gauss_forward": (_I, [ctypes.POINTER(GaussParams), _P, _P, _P, _P, ctypes.c_size_t, _P,
                               _P, _P]),
@@ -180,6 +183,25 @@ def call(name, *args):
     rc = getattr(load(), name)(*args)
     check(rc, name)
     return rc
+
+
+_POISSON = {}
+
+
+def poisson_table(device):
+    """The camera's Poisson tables on ``device`` (built once per device)."""
+    import torch
+    dev = torch.device(device)
+    key = (dev.type, dev.index if dev.index is not None else torch.cuda.current_device())
+    t = _POISSON.get(key)
+    if t is None:
+        nbytes = load().sc_poisson_table_bytes()
+        t = torch.empty((nbytes + 15) // 16 * 4, dtype=torch.int32, device=dev)
+        with torch.cuda.device(dev):
+            call("sc_poisson_table", ptr(t), t.numel() * 4, stream_ptr())
+            torch.cuda.current_stream().synchronize()  # ready for every stream
+        _POISSON[key] = t
+    return t
 
 
 def ptr(t):

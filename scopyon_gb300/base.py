@@ -286,7 +286,7 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
                         pending = (f + 1, st_next,
                                    _ahead_pool().submit(_stage_known, a_next, slot_ids_f, st_next))
                 pipe.check_status()
-                yield Image(adc.cpu().numpy().reshape(nw, nh).copy()), {}
+                yield Image(adc.cpu().numpy().reshape(nw, nh).astype(numpy.float64)), {}
                 continue
         new_ids = []
         id_cols = [a[:, 3].astype(numpy.int64) for a in arrays]
@@ -338,7 +338,7 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
                                           draws=frame_draws, seed=seed, counter=f,
                                           present=present, bleaching=bleaching)
         pipe.check_status()
-        adc_np = adc.cpu().numpy().reshape(nw, nh).copy()
+        adc_np = adc.cpu().numpy().reshape(nw, nh).astype(numpy.float64)
         info = {}
         if full_output:
             info["expectation"] = expect.cpu().numpy().astype(float).reshape(nw, nh)
@@ -402,7 +402,7 @@ def _DeviceFrames(sim, cfg, pipe, traj, num_frames, start_time, exposure_time, b
                                                  draws=frame_draws, seed=seed, counter=f,
                                                  bleaching=bleaching)
         pipe.check_status()
-        adc_np = adc.cpu().numpy().reshape(nw, nh).copy()
+        adc_np = adc.cpu().numpy().reshape(nw, nh).astype(numpy.float64)
         info = {}
         if full_output:
             info["expectation"] = expect.cpu().numpy().astype(float).reshape(nw, nh)

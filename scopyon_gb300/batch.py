@@ -135,7 +135,7 @@ class BatchedFields:
     def field_image(self, k, what="adc"):
         """Frame of field k from the last step: 'adc' counts or 'expect' photons."""
         W, H = self.canvas
-        src = self.pipe.adc if what == "adc" else self.pipe.expect
+        src = self.pipe.adc32 if what == "adc" else self.pipe.expect
         i0, j0 = self.origins[k]
         s = self.sizes[k]
         return src.view(W, H)[i0:i0 + s, j0:j0 + s]

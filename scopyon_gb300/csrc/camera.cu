@@ -108,47 +108,6 @@ __device__ __forceinline__ int table_index(const double *cdf, int n, double u) {
     return lo < n ? lo : n - 1;
 }
 
-// One pixel's native draws (Philox stream keyed by the seed and the pixel, at
-// the frame's counter; FP32 throughout, GB300's FP64 rate being ~1/64 of
-// FP32) and its ADC count.
-__device__ __forceinline__ void native_pixel(const CamConsts &c, int p, float ef, uint64_t counter,
-                                             const float *__restrict__ offset_f,
-                                             const float *__restrict__ inv_gain_f,
-                                             const float *__restrict__ sigma,
-                                             const double *__restrict__ table_value,
-                                             const double *__restrict__ table_cdf,
-                                             double *__restrict__ adc64, float *__restrict__ adc32,
-                                             int32_t *status) {
-    sc::rng_stream rs(c.seed, (uint32_t)p, (uint32_t)counter, (uint32_t)(counter >> 32));
-    float signal, noise;
-    switch (c.camera) {
-        case SC_CAM_EMCCD: {
-            const float n_in = poisson(rs, ef, status);
-            signal = n_in > 0.f ? rintf(c.emgain_f * gamma_ge1(rs, n_in, status)) : 0.f;
-            noise = c.readout_f > 0.f ? c.readout_f * rs.normal() : 0.f;
-            break;
-        }
-        case SC_CAM_CCD:
-            signal = poisson(rs, ef, status);
-            noise = c.readout_f > 0.f ? c.readout_f * rs.normal() : 0.f;
-            break;
-        case SC_CAM_CMOS_TABLE:
-            noise = (float)table_value[table_index(table_cdf, c.table_n, rs.uniform_d())];
-            signal = poisson(rs, ef, status);
-            break;
-        default:  // SC_CAM_SCMOS
-            signal = poisson(rs, ef, status);
-            noise = (sigma ? sigma[p] : c.readout_f) * rs.normal();
-            break;
-    }
-    float v = fminf(signal + noise, c.fullwell_f);
-    v = v * (inv_gain_f ? inv_gain_f[p] : c.inv_gain0_f) + (offset_f ? offset_f[p] : c.offset0_f);
-    v = fminf(fmaxf(v, 0.f), c.adc_max_f);
-    if (c.rounding) v = rintf(v);
-    if (adc32) adc32[p] = v;
-    if (adc64) adc64[p] = sc::f2d_exact(v);
-}
-
 // Injected draws: the reference's FP64 arithmetic on the caller's draws.
 __global__ void camera_exact_kernel(CamConsts c, const float *__restrict__ photons,
                                     const double *__restrict__ offset, const double *__restrict__ gain,
@@ -184,89 +143,183 @@ __global__ void camera_exact_kernel(CamConsts c, const float *__restrict__ photo
     }
 }
 
-// Native draws, a pixel per thread (frames of a few hundred thousand pixels,
-// which need every resident warp).
-__global__ void camera_pixel_kernel(CamConsts c, const float *__restrict__ photons,
-                                    const float *__restrict__ offset_f,
-                                    const float *__restrict__ inv_gain_f,
-                                    const float *__restrict__ sigma,
-                                    const double *__restrict__ table_value,
-                                    const double *__restrict__ table_cdf,
-                                    float *__restrict__ expect, double *__restrict__ adc64,
-                                    float *__restrict__ adc32, int32_t *status) {
-    const int stride = gridDim.x * blockDim.x;
-    const uint64_t counter = c.counter + (c.frame ? (uint64_t)*c.frame : 0);
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < c.n; p += stride) {
-        const float ef = c.qe_f * (photons[p] + c.background_f);
-        if (expect) expect[p] = ef;
-        native_pixel(c, p, ef, counter, offset_f, inv_gain_f, sigma, table_value, table_cdf,
-                     adc64, adc32, status);
+// ------------------------------------------------ Poisson inverse-CDF tables
+// Poisson(j) for j = 0 .. kPoisJ - 1: the CDF over k = 0 .. K_j - 1 in FP32
+// (each entry the FP64 sum rounded once; the last entry is exactly 1) and,
+// per j, kPoisG starting points for the search (the first k whose CDF
+// reaches g / kPoisG).  Layout of the caller's buffer: int32 offsets
+// [kPoisJ + 1], uint16 guide [kPoisJ][kPoisG], float CDF [sum K_j].
+constexpr int kPoisJ = 256, kPoisG = 64;
+constexpr size_t kPoisGuideAt = ((sizeof(int32_t) * (kPoisJ + 1) + 15) / 16) * 16;
+constexpr size_t kPoisCdfAt = kPoisGuideAt + sizeof(uint16_t) * kPoisJ * kPoisG;
+
+// Support of the Poisson(j) table: j + 10 sqrt(j) + 12 values (the mass past
+// it is far below the FP32 rounding of the CDF).
+__host__ __device__ __forceinline__ int pois_support(int j) {
+    return j + (int)ceil(10.0 * sqrt((double)j)) + 12;
+}
+
+int64_t pois_entries() {
+    int64_t n = 0;
+    for (int j = 0; j < kPoisJ; ++j) n += pois_support(j);
+    return n;
+}
+
+struct PoisTab {
+    const int32_t *off;
+    const uint16_t *guide;
+    const float *cdf;
+};
+
+__device__ __forceinline__ PoisTab pois_tab(const void *base) {
+    const char *b = static_cast<const char *>(base);
+    return PoisTab{reinterpret_cast<const int32_t *>(b),
+                   reinterpret_cast<const uint16_t *>(b + kPoisGuideAt),
+                   reinterpret_cast<const float *>(b + kPoisCdfAt)};
+}
+
+// One thread per j: offsets, then the CDF summed in FP64 from
+// p_k = exp(k log j - j - log k!).
+__global__ void pois_cdf_kernel(void *base) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= kPoisJ) return;
+    char *b = static_cast<char *>(base);
+    int32_t *off = reinterpret_cast<int32_t *>(b);
+    float *cdf = reinterpret_cast<float *>(b + kPoisCdfAt);
+    int o = 0;
+    for (int i = 0; i < j; ++i) o += pois_support(i);
+    off[j] = o;
+    const int K = pois_support(j);
+    if (j == kPoisJ - 1) off[kPoisJ] = o + K;
+    const double lj = j > 0 ? log((double)j) : 0.0;
+    double F = 0.0;
+    for (int k = 0; k < K; ++k) {
+        const double pk = j == 0 ? (k == 0 ? 1.0 : 0.0)
+                                 : exp((double)k * lj - (double)j - lgamma((double)k + 1.0));
+        F += pk;
+        cdf[o + k] = k == K - 1 ? 1.0f : (float)fmin(F, 1.0);
     }
 }
 
-constexpr int kCamThreads = 256;
-constexpr int kCamMaxPer = 8;  // pixels per lane per chunk, at most
+// One thread per (j, g): the first k whose CDF reaches g / kPoisG.
+__global__ void pois_guide_kernel(void *base) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= kPoisJ * kPoisG) return;
+    const int j = idx / kPoisG, g = idx % kPoisG;
+    char *b = static_cast<char *>(base);
+    const int32_t *off = reinterpret_cast<const int32_t *>(b);
+    uint16_t *guide = reinterpret_cast<uint16_t *>(b + kPoisGuideAt);
+    const float *cdf = reinterpret_cast<const float *>(b + kPoisCdfAt);
+    const float target = (float)g / (float)kPoisG;
+    const int K = off[j + 1] - off[j];
+    int k = 0;
+    while (k < K - 1 && cdf[off[j] + k] < target) ++k;
+    guide[idx] = (uint16_t)k;
+}
 
-// Native draws.  Each warp takes chunks of 32 * per pixels: it writes their
-// expectations, sorts the pixels by the Poisson method they need (inversion
-// below lambda = 12 and empty pixels to the front of a shared list, PTRS to
-// the back) with ballots, then draws them 32 at a time, one list after the
-// other.  A pixel's draws are those of its own Philox stream whichever lane
-// takes it, so the counts do not depend on the grouping; the grouping keeps
-// a warp from running both methods' loops for one set of 32 pixels (6% off
-// an 8192^2 frame).  Frames too small to fill the GPU twice over take
-// camera_pixel_kernel instead.
-__global__ void __launch_bounds__(kCamThreads)
-camera_native_kernel(CamConsts c, int per, const float *__restrict__ photons,
+// Poisson(lam) from two uniforms, with no rejection: Poisson(j) by table
+// inversion at u0 plus Poisson(lam - j) by sequential inversion at u1,
+// j = floor(lam) (a sum of independent Poisson variates is Poisson with the
+// summed mean).  Means of kPoisJ and more take PTRS on the pixel's stream.
+__device__ __forceinline__ float poisson_tab(const PoisTab &t, float lam, float u0, float u1,
+                                             sc::rng_stream &rs, int32_t *status) {
+    if (!(lam > 0.f)) return 0.f;
+    if (!(lam < (float)kPoisJ)) return poisson(rs, lam, status);
+    const int j = (int)lam;
+    const float r = lam - (float)j;
+    int k = 0;
+    if (j > 0) {
+        const int base = __ldg(t.off + j), last = __ldg(t.off + j + 1) - 1 - base;
+        k = __ldg(t.guide + j * kPoisG + min((int)(u0 * (float)kPoisG), kPoisG - 1));
+        while (k < last && u0 > __ldg(t.cdf + base + k)) ++k;
+    }
+    // Poisson(r), r in [0, 1): P(X >= 16) < 1e-13
+    float p = expf(-r), s = p;
+    int m = 0;
+    while (u1 > s && m < 16) {
+        ++m;
+        p *= __fdividef(r, (float)m);
+        s += p;
+    }
+    return (float)(k + m);
+}
+
+// Standard normal from two 32-bit words (Box-Muller, the cosine branch).
+__device__ __forceinline__ float bm_normal(uint32_t a, uint32_t b) {
+    const float r = sqrtf(-2.0f * __logf(sc::u01f(a)));
+    float sn, cs;
+    sc::sincos_2pi(sc::u01f(b), &sn, &cs);
+    return r * cs;
+}
+
+// EMCCD output electrons with the reference's law (EMCCD.probability_
+// distribution, _epifm.py:365-400): S = 0 with the weight of no
+// photo-electron, S >= 1 with weight proportional to the Poisson-gamma density
+// at S, on the support [g floor(E - sigma), g floor(E + sigma)), sigma =
+// 5 sqrt(E) + 10.  Drawn as n ~ Poisson(E), S = rint(g Gamma(n)) for n > 0,
+// and drawn again when S leaves the support or rounds to 0 with n > 0 (the
+// law has no density mass below S = 1/2 beside the atom at 0).
+__device__ float emccd_native(const PoisTab &t, float e, float g, float u0, float u1,
+                              sc::rng_stream &rs, int32_t *status) {
+    if (!(e > 0.f)) return 0.f;
+    const float sig = sqrtf(e) * 5.f + 10.f;
+    const float s_min = fmaxf(0.f, g * truncf(e - sig)), s_max = g * truncf(e + sig);
+    for (int it = 0; it < 32; ++it) {
+        const float n = it == 0 ? poisson_tab(t, e, u0, u1, rs, status)
+                                : poisson_tab(t, e, rs.uniform(), rs.uniform(), rs, status);
+        const float s = n > 0.f ? rintf(g * gamma_ge1(rs, n, status)) : 0.f;
+        if (n > 0.f && s < 1.f) continue;
+        if (s >= s_min && s < s_max) return s;
+    }
+    sc::flag_status(status, 3, 2, 0, 0);
+    return rintf(g * e);
+}
+
+// Native draws, a pixel per thread.  Pixel p's draws come from its own
+// Philox stream (key: seed; counter: p and the frame counter): block 0's
+// four words give the Poisson draw (two) and the read noise (two); block 1
+// on feeds the rare fallbacks (PTRS above kPoisJ, the EMCCD gain and its
+// redraws).  No lane loops on a rejection in the common case, so a warp's
+// lanes stay together; the counts do not depend on the launch shape.
+template <int CAM>
+__global__ void __launch_bounds__(256)
+camera_native_kernel(CamConsts c, const void *__restrict__ ptab, const float *__restrict__ photons,
                      const float *__restrict__ offset_f, const float *__restrict__ inv_gain_f,
                      const float *__restrict__ sigma, const double *__restrict__ table_value,
                      const double *__restrict__ table_cdf, float *__restrict__ expect,
                      double *__restrict__ adc64, float *__restrict__ adc32, int32_t *status) {
-    constexpr int kWarps = kCamThreads / 32, kList = 32 * kCamMaxPer;
-    __shared__ int s_pix[kWarps][kList];
-    __shared__ float s_ef[kWarps][kList];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const PoisTab t = pois_tab(ptab);
     const uint64_t counter = c.counter + (c.frame ? (uint64_t)*c.frame : 0);
-    const int chunk = 32 * per;
-    const int64_t warps = (int64_t)gridDim.x * kWarps;
-    int *pix = s_pix[warp];
-    float *efs = s_ef[warp];
-    const unsigned below = (1u << lane) - 1u;
-    for (int64_t base = ((int64_t)blockIdx.x * kWarps + warp) * chunk; base < c.n;
-         base += warps * chunk) {
-        int n_front = 0, n_back = 0;
-        for (int j = 0; j < per; ++j) {
-            const int64_t p = base + j * 32 + lane;
-            const bool valid = p < c.n;
-            float ef = 0.f;
-            if (valid) {
-                ef = c.qe_f * (photons[p] + c.background_f);
-                if (expect) expect[p] = ef;
-            }
-            const bool ptrs = valid && ef >= 12.f;  // poisson()'s own threshold
-            const bool front = valid && !ptrs;
-            const unsigned mf = __ballot_sync(~0u, front), mp = __ballot_sync(~0u, ptrs);
-            if (front) {
-                const int k = n_front + __popc(mf & below);
-                pix[k] = (int)p;
-                efs[k] = ef;
-            }
-            if (ptrs) {
-                const int k = kList - 1 - (n_back + __popc(mp & below));
-                pix[k] = (int)p;
-                efs[k] = ef;
-            }
-            n_front += __popc(mf);
-            n_back += __popc(mp);
+    const uint32_t c0 = (uint32_t)counter, c1 = (uint32_t)(counter >> 32);
+    const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < c.n; q += stride) {
+        const int p = (int)q;
+        const float ef = c.qe_f * (__ldg(photons + p) + c.background_f);
+        if (expect) expect[p] = ef;
+        const sc::u4 r = sc::philox4x32_10(sc::u4{(uint32_t)p, c0, c1, 0u}, k0, k1);
+        sc::rng_stream rs(c.seed, (uint32_t)p, c0, c1);
+        rs.ctr.w = 1;
+        const float u0 = sc::u01f(r.x), u1 = sc::u01f(r.y);
+        float signal, noise;
+        if (CAM == SC_CAM_EMCCD) {
+            signal = emccd_native(t, ef, c.emgain_f, u0, u1, rs, status);
+            noise = c.readout_f > 0.f ? c.readout_f * bm_normal(r.z, r.w) : 0.f;
+        } else if (CAM == SC_CAM_CMOS_TABLE) {
+            noise = (float)table_value[table_index(table_cdf, c.table_n, sc::u01d(r.z, r.w))];
+            signal = poisson_tab(t, ef, u0, u1, rs, status);
+        } else {
+            signal = poisson_tab(t, ef, u0, u1, rs, status);
+            const float sg = (CAM == SC_CAM_SCMOS && sigma) ? __ldg(sigma + p) : c.readout_f;
+            noise = sg * bm_normal(r.z, r.w);
         }
-        __syncwarp();
-        for (int k = lane; k < n_front; k += 32)
-            native_pixel(c, pix[k], efs[k], counter, offset_f, inv_gain_f, sigma, table_value,
-                         table_cdf, adc64, adc32, status);
-        for (int k = lane; k < n_back; k += 32)
-            native_pixel(c, pix[kList - 1 - k], efs[kList - 1 - k], counter, offset_f, inv_gain_f,
-                         sigma, table_value, table_cdf, adc64, adc32, status);
-        __syncwarp();
+        float v = fminf(signal + noise, c.fullwell_f);
+        v = v * (inv_gain_f ? __ldg(inv_gain_f + p) : c.inv_gain0_f) +
+            (offset_f ? __ldg(offset_f + p) : c.offset0_f);
+        v = fminf(fmaxf(v, 0.f), c.adc_max_f);
+        if (c.rounding) v = rintf(v);
+        if (adc32) adc32[p] = v;
+        if (adc64) adc64[p] = sc::f2d_exact(v);
     }
 }
 
@@ -369,6 +422,9 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
     if (p->camera == SC_CAM_CMOS_TABLE)
         SC_REQUIRE(p->table_n > 0 && d_table_value && d_table_cdf,
                    "sc_camera: CMOS table mode needs the noise table");
+    if (!p->exact)
+        SC_REQUIRE(p->d_poisson_table != nullptr,
+                   "sc_camera: native draws need the Poisson tables (sc_poisson_table)");
     if (p->exact) {
         SC_REQUIRE(d_inj_signal != nullptr, "sc_camera: exact mode needs injected signal");
         SC_REQUIRE(p->camera == SC_CAM_CMOS_TABLE ? (d_inj_uniform || d_inj_noise) : true,
@@ -410,38 +466,22 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
                                                     d_table_cdf, d_inj_noise, d_inj_signal,
                                                     d_inj_uniform, d_expect, d_adc64, d_adc32);
     } else {
-        // chunks of 32 * per pixels per warp, 8 per lane once the frame fills
-        // the GPU's resident threads (152 SMs x 2048) 8 times; below twice, a
-        // pixel per thread
-        int per = (int)((int64_t)c.n / (152 * 2048));
-        if (per < 2) {
-            const int block = 256;
-            int grid = (c.n + block - 1) / block;
-            if (grid > 152 * 16) grid = 152 * 16;
-            camera_pixel_kernel<<<grid, block, 0, st>>>(c, d_photons, d_offset_f, d_inv_gain_f,
-                                                        d_sigma, d_table_value, d_table_cdf,
-                                                        d_expect, d_adc64, d_adc32, d_status);
-            return sc::launch_status("sc_camera");
+        const int block = 256;
+        int64_t grid = ((int64_t)c.n + block - 1) / block;
+        if (grid > 152 * 8) grid = 152 * 8;
+        switch (c.camera) {
+#define SC_CAM_LAUNCH(K)                                                                        \
+    case K:                                                                                     \
+        camera_native_kernel<K><<<(int)grid, block, 0, st>>>(                                   \
+            c, p->d_poisson_table, d_photons, d_offset_f, d_inv_gain_f, d_sigma, d_table_value, \
+            d_table_cdf, d_expect, d_adc64, d_adc32, d_status);                                 \
+        break;
+            SC_CAM_LAUNCH(SC_CAM_EMCCD)
+            SC_CAM_LAUNCH(SC_CAM_CCD)
+            SC_CAM_LAUNCH(SC_CAM_CMOS_TABLE)
+            SC_CAM_LAUNCH(SC_CAM_SCMOS)
+#undef SC_CAM_LAUNCH
         }
-        per = per > kCamMaxPer ? kCamMaxPer : per;
-        // at most one wave of resident blocks: the chunks are strided over the
-        // grid, so a second wave would start late and finish late
-        static int resident = 0;
-        if (resident == 0) {
-            int b = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, camera_native_kernel,
-                                                              kCamThreads, 0) != cudaSuccess ||
-                b < 1)
-                b = 1;
-            resident = b;
-        }
-        const int64_t chunks = ((int64_t)c.n + 32 * per - 1) / (32 * per);
-        const int64_t blocks = (chunks + kCamThreads / 32 - 1) / (kCamThreads / 32);
-        const int64_t wave = (int64_t)152 * resident;
-        const int grid = (int)(blocks < wave ? blocks : wave);
-        camera_native_kernel<<<grid, kCamThreads, 0, st>>>(
-            c, per, d_photons, d_offset_f, d_inv_gain_f, d_sigma, d_table_value, d_table_cdf,
-            d_expect, d_adc64, d_adc32, d_status);
     }
     return sc::launch_status("sc_camera");
 }
@@ -461,4 +501,19 @@ extern "C" int sc_emccd_exact(const double *d_photons, double qe, double backgro
                                                                   d_uniform, n_pixels, emgain,
                                                                   d_signal, d_status);
     return sc::launch_status("sc_emccd_exact");
+}
+
+extern "C" size_t sc_poisson_table_bytes(void) {
+    return kPoisCdfAt + sizeof(float) * (size_t)pois_entries();
+}
+
+extern "C" int sc_poisson_table(void *d_table, size_t bytes, void *stream) {
+    SC_REQUIRE(d_table != nullptr, "sc_poisson_table: NULL buffer");
+    SC_REQUIRE_CAP(bytes >= sc_poisson_table_bytes(), "sc_poisson_table: buffer %zu < %zu bytes",
+                   bytes, sc_poisson_table_bytes());
+    SC_REQUIRE(((uintptr_t)d_table & 15) == 0, "sc_poisson_table: buffer not 16-byte aligned");
+    cudaStream_t st = sc::as_stream(stream);
+    pois_cdf_kernel<<<1, kPoisJ, 0, st>>>(d_table);
+    pois_guide_kernel<<<(kPoisJ * kPoisG + 255) / 256, 256, 0, st>>>(d_table);
+    return sc::launch_status("sc_poisson_table");
 }

@@ -27,6 +27,17 @@ int launch_status(const char *what) { return cuda_status(cudaGetLastError(), wha
 
 extern "C" int sc_get_version(void) { return 1; }
 
+extern "C" int sc_struct_sizes(size_t *out, int n) {
+    SC_REQUIRE(out != nullptr && n >= 6, "sc_struct_sizes: need room for 6 sizes");
+    out[0] = sizeof(ScStepRec);
+    out[1] = sizeof(ScStepParams);
+    out[2] = sizeof(ScSplatParams);
+    out[3] = sizeof(ScCameraParams);
+    out[4] = sizeof(ScDiffuseParams);
+    out[5] = sizeof(ScGaussParams);
+    return SC_OK;
+}
+
 extern "C" const char *sc_last_error(void) { return sc::g_last_error; }
 
 namespace {

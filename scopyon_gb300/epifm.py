@@ -381,7 +381,9 @@ class FramePipeline:
         self.status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
         self.image = torch.empty(self.n_pix, dtype=torch.float32, device=dev)
         self.expect = torch.empty(self.n_pix, dtype=torch.float32, device=dev)
-        self.adc = torch.empty(self.n_pix, dtype=torch.float64, device=dev)
+        self.adc = torch.empty(self.n_pix, dtype=torch.float64, device=dev)  # injected draws
+        self.adc32 = torch.empty(self.n_pix, dtype=torch.float32, device=dev)  # native draws
+        self.poisson = _lib.poisson_table(dev)
         self.offset = torch.from_numpy(numpy.ascontiguousarray(cfg.offset, dtype=float)).to(dev).reshape(-1)
         self.gain = torch.from_numpy(numpy.ascontiguousarray(cfg.gain, dtype=float)).to(dev).reshape(-1)
         self.offset_f = self.offset.float()
@@ -595,6 +597,7 @@ class FramePipeline:
         cp.table_n = 0 if self.table_value is None else self.table_value.numel()
         cp.seed, cp.counter = int(seed) & (2 ** 64 - 1), int(counter) & (2 ** 64 - 1)
         cp.d_frame = None if d_frame is None else d_frame.data_ptr()
+        cp.d_poisson_table = self.poisson.data_ptr()
         if draws is not None:
             cp.d_photons64 = None if photons64 is None else photons64.data_ptr()
             cp.d_expect64 = None if expect64 is None else expect64.data_ptr()
@@ -714,9 +717,9 @@ class FramePipeline:
                         stream=stream, d_frame=d_frame, photons64=image64, expect64=expect64)
             return expect64, self.adc, opt
         self.splat_records(recs, n_rec, self.image, stream=stream)
-        self.camera(self.image, self.expect, self.adc, seed=seed, counter=counter, draws=draws,
-                    stream=stream, d_frame=d_frame)
-        return self.expect, self.adc, opt
+        self.camera(self.image, self.expect, None, self.adc32, seed=seed, counter=counter,
+                    draws=draws, stream=stream, d_frame=d_frame)
+        return self.expect, self.adc32, opt
 
 
 TILE_CANDIDATES = ((8, 4, 4), (8, 4, 8), (8, 2, 6), (16, 4, 4), (16, 8, 4), (16, 4, 8))
@@ -778,7 +781,7 @@ class FrameGraph:
     the only per-frame quantity, the frame index that offsets the Philox
     counters, lives in device memory and is advanced by the graph itself.
     Launch cost per frame is one graph launch.  Outputs (``pipe.expect``,
-    ``pipe.adc``) are overwritten by each frame.
+    ``pipe.adc32``) are overwritten by each frame.
 
     frames_per_step=k > 1 runs k consecutive frames per step (per graph
     replay) as a pipeline: the records kernels (which need only the positions
@@ -837,8 +840,8 @@ class FrameGraph:
         recs, bufs = recs
         pipe.splat_records(recs, self.n_sub * self.n, pipe.image, tag=tag, binned=True,
                            bufs=bufs)
-        pipe.camera(pipe.image, pipe.expect, pipe.adc, seed=self.seed, counter=frame_offset,
-                    d_frame=self.frame)
+        pipe.camera(pipe.image, pipe.expect, None, pipe.adc32, seed=self.seed,
+                    counter=frame_offset, d_frame=self.frame)
 
     def _launch(self):
         s = stream_ptr()

@@ -70,11 +70,14 @@ def test_host_side_validation_needs_no_gpu():
 
 
 def test_struct_sizes_match_c_layout():
-    from scopyon_gb300 import _lib
-    assert ctypes.sizeof(_lib.StepParams) == 136
-    assert ctypes.sizeof(_lib.SplatParams) == 80
-    assert ctypes.sizeof(_lib.CameraParams) == 128
-    assert ctypes.sizeof(_lib.DiffuseParams) == 224
+    """The ctypes structs have the sizes the C compiler gave the header's."""
+    from scopyon_gb300 import _build, _lib
+    _build.build()
+    out = (ctypes.c_size_t * 6)()
+    assert _lib.load().sc_struct_sizes(ctypes.addressof(out), 6) == 0
+    assert list(out) == [_lib.STEP_REC_BYTES, ctypes.sizeof(_lib.StepParams),
+                         ctypes.sizeof(_lib.SplatParams), ctypes.sizeof(_lib.CameraParams),
+                         ctypes.sizeof(_lib.DiffuseParams), ctypes.sizeof(_lib.GaussParams)]
 
 
 def test_stage_rows_host_helper():

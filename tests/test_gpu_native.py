@@ -157,11 +157,11 @@ def test_native_scmos_per_pixel_sigma(sg):
 
 @pytest.mark.parametrize("kind", ["EMCCD", "CCD", "CMOS_TABLE", "SCMOS"])
 def test_camera_draws_do_not_depend_on_the_grouping(sg, kind):
-    """A pixel's native draws come from its own Philox stream: a frame small
-    enough for the pixel-per-thread kernel and frames large enough for the
-    grouped kernel (3 and 6 pixels per lane per chunk) give the same counts,
-    bit for bit, on the pixels they share.  Photons mix empty pixels, means
-    below the PTRS threshold and bright pixels."""
+    """A pixel's native draws come from its own Philox stream: frames of
+    different sizes (so the grid-stride loop hands each pixel to a different
+    thread and iteration) give the same counts, bit for bit, on the pixels
+    they share.  Photons mix empty pixels, table means (below 256) and bright
+    pixels on the PTRS fallback."""
     from scopyon_gb300 import _lib
     from scopyon_gb300._lib import call, ptr, stream_ptr
     dev = torch.device("cuda")
@@ -190,6 +190,7 @@ def test_camera_draws_do_not_depend_on_the_grouping(sg, kind):
         cp.emgain, cp.fullwell, cp.offset0, cp.gain0 = 300.0, 6.0e5, 100.0, 10.0
         cp.table_n = 16 if kind == "CMOS_TABLE" else 0
         cp.seed, cp.counter = 1234567, 5
+        cp.d_poisson_table = _lib.poisson_table(dev).data_ptr()
         expect = torch.empty(n, dtype=torch.float32, device=dev)
         adc = torch.empty(n, dtype=torch.float64, device=dev)
         call("sc_camera", cp, ptr(photons), None, None, ptr(offset_f), ptr(inv_gain_f),
@@ -198,9 +199,9 @@ def test_camera_draws_do_not_depend_on_the_grouping(sg, kind):
         torch.cuda.synchronize()
         return expect.cpu().numpy(), adc.cpu().numpy()
 
-    e_small, a_small = run(300)   # 307,200 px: a pixel per thread
-    e_mid, a_mid = run(1024)      # 1,048,576 px: 3 pixels per lane per chunk
-    e_big, a_big = run(2048)      # 2,097,152 px: 6 pixels per lane per chunk
+    e_small, a_small = run(300)   # 307,200 px: about one pixel per thread
+    e_mid, a_mid = run(1024)      # 1,048,576 px: several pixels per thread
+    e_big, a_big = run(2048)      # 2,097,152 px
     assert int(status[0].item()) == 0
     k = len(a_small)
     numpy.testing.assert_array_equal(e_mid[:k], e_small)

@@ -455,6 +455,24 @@ int sc_emccd_exact(const double *d_photons, double qe, double background,
                    const double *d_uniform, int n_pixels, double emgain,
                    double *d_signal, int32_t *d_status, void *stream);
 
+/* Laplacian-of-Gaussian scale space for blob detection (the blob_log search
+ * of spot_detection, src/scopyon/analysis/spot_detection.py:14-46).  For
+ * scale s: d_cube[(i * nh + j) * n_scales + s] = -sigma_s^2 times the sum
+ * over both axes of (second-derivative kernel along that axis, Gaussian
+ * kernel along the other) applied to d_img (nw x nh FP64), with the kernels
+ * d_phi / d_d2 of scale s at d_tap_off[s] .. + 2 d_radius[s] and scipy.ndimage's
+ * 'reflect' edges; FP64.  d_work: 2 * nw * nh * n_scales doubles.           */
+int sc_log_cube(const double *d_img, int nw, int nh, const double *d_phi, const double *d_d2,
+                const int32_t *d_tap_off, const int32_t *d_radius, const double *d_sigma,
+                int n_scales, double *d_work, size_t work_bytes, double *d_cube, void *stream);
+
+/* Blobs of the scale space: cells above threshold that are the maximum of
+ * their 3 x 3 x 3 neighbourhood, written as (i, j, s) int32 triples to
+ * d_peaks (at most capacity; *d_count receives how many were found, in no
+ * particular order).                                                        */
+int sc_log_peaks(const double *d_cube, int nw, int nh, int n_scales, double threshold,
+                 int32_t *d_count, int32_t *d_peaks, int capacity, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

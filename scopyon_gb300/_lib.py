@@ -106,6 +106,8 @@ _SIG = {
     "sc_camera": (_I, [ctypes.POINTER(CameraParams), _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                        _P, _P, _P, _P, _P]),
     "sc_emccd_exact": (_I, [_P, _D, _D, _P, _I, _D, _P, _P, _P]),
+    "sc_log_cube": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _I, _P, ctypes.c_size_t, _P, _P]),
+    "sc_log_peaks": (_I, [_P, _I, _I, _I, _D, _P, _P, _I, _P]),
     "sc_poisson_table_bytes": (ctypes.c_size_t, []),
     "sc_poisson_table": (_I, [_P, ctypes.c_size_t, _P]),
     "sc_gauss_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(GaussParams)]),

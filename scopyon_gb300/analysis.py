@@ -12,9 +12,11 @@ where it is not (a region without a spot) they may stop in different places.
 
 ``blob_detection`` is the Laplacian-of-Gaussian scale-space search the
 reference takes from scikit-image (``blob_log``, :14-46): the scale-normalised
-LoG of the image at ``num_sigma`` scales on the GPU, maxima over 3 x 3 x 3
-neighbourhoods above ``threshold``, overlapping blobs pruned.  It is written
-from the published method, not from scikit-image (absent here).
+LoG of the image at ``num_sigma`` scales (``sc_log_cube``, FP64 separable
+passes with scipy.ndimage's kernels and edges), maxima over 3 x 3 x 3
+neighbourhoods above ``threshold`` (``sc_log_peaks``), overlapping blobs
+pruned on the host.  It is written from the published method, not from
+scikit-image (absent here).
 """
 
 import math
@@ -25,7 +27,7 @@ import torch
 from . import _lib
 from ._lib import call, ptr, stream_ptr
 
-__all__ = ["spot_detection", "blob_detection", "spot_fits"]
+__all__ = ["spot_detection", "blob_detection", "spot_fits", "log_cube"]
 
 
 def _device():
@@ -74,36 +76,58 @@ def _gauss_kernels(sigma, truncate=4.0):
     return phi, d2
 
 
-def _conv1d(img, k, dim):
-    """Correlation with a symmetric kernel along ``dim`` with scipy.ndimage's
-    'reflect' edges (d c b a | a b c d | d c b a, repeated as needed)."""
-    r = (len(k) - 1) // 2
-    kt = torch.as_tensor(k, dtype=img.dtype, device=img.device).flip(0)
-    x = img.transpose(0, 1) if dim == 0 else img
-    n = x.shape[1]
-    q = torch.arange(-r, n + r, device=img.device) % (2 * n)
-    src = torch.where(q < n, q, 2 * n - 1 - q)
-    y = torch.nn.functional.conv1d(x[:, src].unsqueeze(1), kt.view(1, 1, -1)).squeeze(1)
-    return y.transpose(0, 1) if dim == 0 else y
+def log_cube(data, sigmas):
+    """Scale-normalised LoG of ``data`` (W x H) at each of ``sigmas``: a
+    W x H x len(sigmas) FP64 tensor on the GPU (``sc_log_cube``)."""
+    data = numpy.asarray(data, dtype=float)
+    if data.ndim != 2:
+        raise ValueError("data must be a 2-D image")
+    dev = _device()
+    nw, nh = data.shape
+    phis, d2s, off, rad = [], [], [], []
+    o = 0
+    for s in sigmas:
+        phi, d2 = _gauss_kernels(s)
+        phis.append(phi)
+        d2s.append(d2)
+        off.append(o)
+        rad.append((len(phi) - 1) // 2)
+        o += len(phi)
+    ns = len(sigmas)
+
+    def dev_t(a, dtype):
+        return torch.as_tensor(numpy.ascontiguousarray(a), dtype=dtype, device=dev)
+
+    img = dev_t(data, torch.float64)
+    phi_t = dev_t(numpy.concatenate(phis), torch.float64)
+    d2_t = dev_t(numpy.concatenate(d2s), torch.float64)
+    off_t = dev_t(numpy.array(off, dtype=numpy.int32), torch.int32)
+    rad_t = dev_t(numpy.array(rad, dtype=numpy.int32), torch.int32)
+    sig_t = dev_t(numpy.asarray(sigmas, dtype=float), torch.float64)
+    work = torch.empty(2 * nw * nh * ns, dtype=torch.float64, device=dev)
+    cube = torch.empty((nw, nh, ns), dtype=torch.float64, device=dev)
+    call("sc_log_cube", ptr(img), nw, nh, ptr(phi_t), ptr(d2_t), ptr(off_t), ptr(rad_t),
+         ptr(sig_t), ns, ptr(work), work.numel() * 8, ptr(cube), stream_ptr())
+    return cube
 
 
 def blob_detection(data, min_sigma=1, max_sigma=50, num_sigma=10, threshold=0.2, overlap=0.5):
     """Blobs (n x 3: x, y, r = sigma sqrt 2) in ``data`` by the scale-normalised
     Laplacian of Gaussian (the reference's defaults)."""
     data = numpy.asarray(data, dtype=float)
-    dev = _device()
-    img = torch.from_numpy(numpy.ascontiguousarray(data)).to(dev)
     sigmas = numpy.linspace(min_sigma, max_sigma, num_sigma)
-    cube = []
-    for s in sigmas:
-        phi, d2 = _gauss_kernels(s)
-        lap = (_conv1d(_conv1d(img, d2, 0), phi, 1) + _conv1d(_conv1d(img, phi, 0), d2, 1))
-        cube.append(-lap * s * s)
-    cube = torch.stack(cube, 2)  # W x H x scales
-    mx = torch.nn.functional.max_pool3d(cube[None, None], 3, stride=1, padding=1)[0, 0]
-    peaks = torch.nonzero((cube == mx) & (cube > threshold)).cpu().numpy()
-    if len(peaks) == 0:
+    cube = log_cube(data, sigmas)
+    nw, nh, ns = cube.shape
+    cap = nw * nh * ns
+    count = torch.zeros(1, dtype=torch.int32, device=cube.device)
+    found = torch.empty(3 * cap, dtype=torch.int32, device=cube.device)
+    call("sc_log_peaks", ptr(cube), nw, nh, ns, float(threshold), ptr(count), ptr(found), cap,
+         stream_ptr())
+    n = int(count.item())
+    if n == 0:
         return numpy.zeros((0, 3))
+    peaks = found[: 3 * n].view(n, 3).cpu().numpy()
+    peaks = peaks[numpy.lexsort((peaks[:, 2], peaks[:, 1], peaks[:, 0]))]  # (i, j, s) order
     blobs = numpy.column_stack([peaks[:, 0].astype(float), peaks[:, 1].astype(float),
                                 sigmas[peaks[:, 2]]])
     blobs = _prune(blobs, overlap)

@@ -32,18 +32,69 @@ def test_oracle_matches_reference(golden, roi):
     numpy.testing.assert_array_equal(got, golden["roi%d_spots" % roi])
 
 
-def test_log_filter_matches_scipy():
-    torch = pytest.importorskip("torch")
+def test_log_kernels_match_scipy():
+    """The Gaussian and second-derivative kernels the LoG kernel is given are
+    scipy.ndimage's: separable 'reflect' correlations with them equal
+    gaussian_laplace."""
     import scipy.ndimage as ndi
     from scopyon_gb300 import analysis as A
     img = numpy.random.RandomState(0).rand(37, 23)
     for s in (1.0, 2.5, 9.0, 30.0):
         phi, d2 = A._gauss_kernels(s)
-        t = torch.from_numpy(img)
-        lap = (A._conv1d(A._conv1d(t, d2, 0), phi, 1) +
-               A._conv1d(A._conv1d(t, phi, 0), d2, 1)).numpy()
+        c = ndi.correlate1d
+        lap = (c(c(img, d2, 0, mode="reflect"), phi, 1, mode="reflect") +
+               c(c(img, phi, 0, mode="reflect"), d2, 1, mode="reflect"))
         ref = ndi.gaussian_laplace(img, s)
         assert numpy.abs(lap - ref).max() <= 1e-12 * numpy.abs(ref).max()
+
+
+@pytest.mark.gpu
+def test_gpu_log_cube_matches_scipy():
+    """sc_log_cube against scipy.ndimage.gaussian_laplace (times -sigma^2),
+    including kernels wider than the image (repeated reflection)."""
+    import scipy.ndimage as ndi
+    from scopyon_gb300 import _build
+    _build.build()
+    from scopyon_gb300 import analysis as A
+    img = numpy.random.RandomState(0).rand(37, 23) * 100.0
+    sigmas = numpy.array([1.0, 2.5, 9.0, 30.0])
+    cube = A.log_cube(img, sigmas).cpu().numpy()
+    for k, s in enumerate(sigmas):
+        ref = -ndi.gaussian_laplace(img, s) * s * s
+        assert numpy.abs(cube[:, :, k] - ref).max() <= 1e-12 * numpy.abs(ref).max()
+
+
+@pytest.mark.gpu
+def test_gpu_log_peaks_match_maximum_filter():
+    """sc_log_peaks finds exactly the cells a 3 x 3 x 3 maximum filter (edges
+    ignored) and the threshold select, on the GPU's own scale space."""
+    import scipy.ndimage as ndi
+    import torch
+    from scopyon_gb300 import _build
+    _build.build()
+    from scopyon_gb300 import analysis as A
+    from scopyon_gb300._lib import call, ptr, stream_ptr
+    rng = numpy.random.RandomState(3)
+    img = rng.poisson(5.0, (96, 80)).astype(float)
+    X, Y = numpy.indices(img.shape)
+    for cx, cy, a in ((20, 30, 200), (50, 61, 120), (80, 12, 90), (51, 63, 60)):
+        img += a * numpy.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / 6.0)
+    sigmas = numpy.linspace(1, 5, 6)
+    cube = A.log_cube(img, sigmas)
+    nw, nh, ns = cube.shape
+    for threshold in (0.5, 5.0, 40.0):
+        count = torch.zeros(1, dtype=torch.int32, device="cuda")
+        found = torch.empty(3 * nw * nh * ns, dtype=torch.int32, device="cuda")
+        call("sc_log_peaks", ptr(cube), nw, nh, ns, threshold, ptr(count), ptr(found),
+             nw * nh * ns, stream_ptr())
+        n = int(count.item())
+        got = found[: 3 * n].view(n, 3).cpu().numpy()
+        got = got[numpy.lexsort((got[:, 2], got[:, 1], got[:, 0]))]
+        c = cube.cpu().numpy()
+        mx = ndi.maximum_filter(c, size=3, mode="constant", cval=-numpy.inf)
+        ref = numpy.argwhere((c == mx) & (c > threshold))
+        numpy.testing.assert_array_equal(got, ref)
+        assert n > 0
 
 
 def test_prune_keeps_the_larger_of_overlapping_blobs():

@@ -84,10 +84,12 @@ __global__ void emitter_footprint_kernel(sc::StepConsts c, const double *particl
     ScStepRec rec;
     const int i = (int)(idx % c.n_particles), s = (int)(idx / c.n_particles);
     if (c.focal_zero)
-        sc::make_record(c, q[0], q[1], q[2], norm, key_slot, status, i, s, rec);
+        sc::make_record(c, q[0], q[1], q[2], norm, key_slot, status, i, s, rec,
+                        norm_out != nullptr);
     else
         sc::make_record(c, q[0] - c.focal[0], q[1] - c.focal[1], q[2] - c.focal[2], norm,
-                        key_slot, status, i, s, rec);
+                        key_slot, status, i, s, rec,
+                        norm_out != nullptr);
     recs[idx] = rec;
 }
 

@@ -88,9 +88,12 @@ __device__ __forceinline__ bool axis_footprint(const StepConsts &c, double half_
 // footprint along x and y, box-table entry when the pixel bounds are a fixed
 // stride apart, and the weight w = norm * res^2.  rel0..2 are the emitter's
 // depth, x and y relative to the focal point.
+// origins: also give box-path records their FP64 footprint origins (x0, y0),
+// which the FP64 splat's exact bound decisions read.
 __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, double rel1,
                                             double rel2, double norm, const int32_t *key_slot,
-                                            int32_t *status, int i, int s, ScStepRec &rec) {
+                                            int32_t *status, int i, int s, ScStepRec &rec,
+                                            bool origins = false) {
     rec.box_off = 0;
     rec.x0 = rec.y0 = 0.0;
     rec.ax_hi = rec.ax_lo = rec.ay_hi = rec.ay_lo = 0.f;
@@ -149,6 +152,10 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
         rec.box_local = ((mx / P) << 16) | (my / P);
         rec.box_off = (int64_t)slot * ((int64_t)P * P * NB) + (int64_t)phase * NB +
                       (mx / P) * NQ + my / P;
+        if (origins) {
+            rec.x0 = (c.half_w + rel1) - c.half_sig;
+            rec.y0 = (c.half_h + rel2) - c.half_sig;
+        }
     } else {
         rec.x0 = (c.half_w + rel1) - c.half_sig;
         rec.y0 = (c.half_h + rel2) - c.half_sig;

@@ -265,7 +265,7 @@ def test_frame_graph_replay_matches_eager(sg):
         for _ in range(6 // per_step):
             fg.step()
             # a two-frame step leaves the second frame's outputs
-            frames.append(pipe.adc.cpu().numpy().copy())
+            frames.append(pipe.adc32.cpu().numpy().copy())
         pipe.check_status()
         pos = traj._pos.cpu().numpy().copy()
         outs.append((numpy.array(frames), pos))

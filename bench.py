@@ -896,7 +896,7 @@ def cpu_baseline_and_accuracy(dev, seed=61):
         t1 = time.perf_counter()
     e_ref = cam[:, :, 0]
     crng = numpy.random.RandomState(seed + 1)
-    noise = O.cmos_table_draw_array(params.cmos_table, crng.random_sample(e_ref.shape))
+    noise = O.cmos_table_draw(params.cmos_table, crng.random_sample(e_ref.shape))
     adc = O.adc_counts(crng.poisson(e_ref) + noise, params.fullwell, params.gain, params.offset,
                        params.bit)
     t2 = time.perf_counter()

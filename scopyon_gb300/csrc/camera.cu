@@ -149,7 +149,7 @@ __global__ void camera_exact_kernel(CamConsts c, const float *__restrict__ photo
 // per j, kPoisG starting points for the search (the first k whose CDF
 // reaches g / kPoisG).  Layout of the caller's buffer: int32 offsets
 // [kPoisJ + 1], uint16 guide [kPoisJ][kPoisG], float CDF [sum K_j].
-constexpr int kPoisJ = 256, kPoisG = 64;
+constexpr int kPoisJ = 256, kPoisG = 256;
 constexpr size_t kPoisGuideAt = ((sizeof(int32_t) * (kPoisJ + 1) + 15) / 16) * 16;
 constexpr size_t kPoisCdfAt = kPoisGuideAt + sizeof(uint16_t) * kPoisJ * kPoisG;
 
@@ -233,13 +233,28 @@ __device__ __forceinline__ float poisson_tab(const PoisTab &t, float lam, float 
         k = __ldg(t.guide + j * kPoisG + min((int)(u0 * (float)kPoisG), kPoisG - 1));
         while (k < last && u0 > __ldg(t.cdf + base + k)) ++k;
     }
-    // Poisson(r), r in [0, 1): P(X >= 16) < 1e-13
+    // Poisson(r), r in [0, 1): the first four cumulative sums without a
+    // branch (u1 lies past the fourth with probability below 2%), then the
+    // sequential search (P(X >= 16) < 1e-13)
     float p = expf(-r), s = p;
-    int m = 0;
-    while (u1 > s && m < 16) {
-        ++m;
-        p *= __fdividef(r, (float)m);
+    int m = u1 > s;
+    p *= r;
+    s += p;
+    m += u1 > s;
+    p *= 0.5f * r;
+    s += p;
+    m += u1 > s;
+    p *= (1.f / 3.f) * r;
+    s += p;
+    if (u1 > s) {
+        m = 4;
+        p *= 0.25f * r;
         s += p;
+        while (u1 > s && m < 16) {
+            ++m;
+            p *= __fdividef(r, (float)m);
+            s += p;
+        }
     }
     return (float)(k + m);
 }
@@ -467,12 +482,13 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
                                                     d_inj_uniform, d_expect, d_adc64, d_adc32);
     } else {
         const int block = 256;
-        int64_t grid = ((int64_t)c.n + block - 1) / block;
-        if (grid > 152 * 8) grid = 152 * 8;
+        const int64_t want = ((int64_t)c.n + block - 1) / block;
         switch (c.camera) {
 #define SC_CAM_LAUNCH(K)                                                                        \
     case K:                                                                                     \
-        camera_native_kernel<K><<<(int)grid, block, 0, st>>>(                                   \
+        camera_native_kernel<K><<<sc::resident_grid((const void *)camera_native_kernel<K>,      \
+                                                    block, 0, want),                            \
+                                   block, 0, st>>>(                                             \
             c, p->d_poisson_table, d_photons, d_offset_f, d_inv_gain_f, d_sigma, d_table_value, \
             d_table_cdf, d_expect, d_adc64, d_adc32, d_status);                                 \
         break;

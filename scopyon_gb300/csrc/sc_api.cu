@@ -85,3 +85,21 @@ extern "C" int sc_stage_rows(const double *src, int64_t n, const double *ids, do
     depth_range[1] = nan_seen ? nan : hi;
     return 0;
 }
+
+namespace sc {
+
+int resident_grid(const void *fn, int block, size_t smem, int64_t want) {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms < 1)
+        sms = 152;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    const int64_t wave = (int64_t)sms * per_sm;
+    if (want < 1) want = 1;
+    return (int)(want < wave ? want : wave);
+}
+
+}  // namespace sc

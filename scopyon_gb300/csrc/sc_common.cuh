@@ -34,6 +34,11 @@ int launch_status(const char *what);
         }                                \
     } while (0)
 
+// Blocks for a grid-stride kernel: `want` blocks, at most one full wave of
+// resident blocks on the current device (occupancy of `fn` at `block`
+// threads and `smem` dynamic bytes), so that no block starts a second wave.
+int resident_grid(const void *fn, int block, size_t smem, int64_t want);
+
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // status word helpers (device): first error wins the index slots

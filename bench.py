@@ -374,6 +374,8 @@ def summary(r):
     bt = r.get("batched")
     if bt:
         out["batched_over_per_field_loop"] = round(bt["batched_over_plain_loop"], 2)
+        out["persistent_batched_over_per_field_loop"] = round(
+            bt["persistent"]["over_plain_loop"], 2)
     st = r["roofline"].get("stages_beyond_l2")
     if st:
         out["diffusion_frac_beyond_l2"] = round(st["diffusion"]["frac"], 3)
@@ -757,34 +759,41 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=
     counts = numpy.exp(rng.uniform(math.log(10), math.log(50000), n_fields)).astype(int)
     D = numpy.exp(rng.uniform(math.log(1e-3), math.log(1.0), n_fields)) * 1e-12
     cfg = config1()
-    t0 = time.time()
     per_step = 4  # four canvas frames per replay, each frame's records beside the previous splat
-    bf = BatchedFields(cfg, sizes, counts, D, frames, substeps, seed=seed, device=dev,
-                       frames_per_step=per_step)
-    if args.tile:
-        bf.pipe.set_tiles(args.tile, args.warps, args.stages)
-        tune = {}
-    else:
-        tune = bf.autotune(frames=1)
-    bf.step()  # capture
-    for _ in range(args.warmup):
-        bf.step()
-    steps = max(1, min(args.steps, frames - 2 - args.warmup) // per_step)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    a.record()
-    for _ in range(steps):
-        bf.step()
-    b.record()
-    torch.cuda.synchronize()
-    bf.pipe.check_status()
-    batch_ms = a.elapsed_time(b) / (steps * per_step)
-    setup_s = time.time() - t0
-    del bf
-    torch.cuda.empty_cache()
+
+    def run(persistent):
+        t0 = time.time()
+        bf = BatchedFields(cfg, sizes, counts, D, frames, substeps, seed=seed, device=dev,
+                           frames_per_step=per_step, persistent=persistent)
+        if args.tile:
+            bf.pipe.set_tiles(args.tile, args.warps, args.stages)
+            tune = {}
+        else:
+            tune = bf.autotune(frames=1)
+        bf.step()  # capture
+        for _ in range(args.warmup):
+            bf.step()
+        steps = max(1, min(args.steps, frames - 2 - args.warmup) // per_step)
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(steps):
+            bf.step()
+        b.record()
+        torch.cuda.synchronize()
+        bf.pipe.check_status()
+        ms = a.elapsed_time(b) / (steps * per_step)
+        setup = time.time() - t0
+        del bf
+        torch.cuda.empty_cache()
+        return ms, tune, setup
+
+    batch_ms, tune, setup_s = run(False)
+    pers_ms, pers_tune, _ = run(True)
     if not loop:
         return {"value": n_fields / (batch_ms / 1e3), "unit": "field-frames/s",
-                "batched_ms_per_frame_of_all_fields": batch_ms, "setup_s": setup_s}
+                "batched_ms_per_frame_of_all_fields": batch_ms,
+                "persistent_ms_per_frame_of_all_fields": pers_ms, "setup_s": setup_s}
 
     # the plain method, one field at a time: a pipeline, trajectories and frame per field
     fields = []
@@ -828,6 +837,15 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=
                         "%d sub-steps per 30 ms frame, TIRF EGFP, EMCCD camera"
                         % (n_fields, int(counts.sum()), substeps),
             "batched_ms_per_frame_of_all_fields": batch_ms,
+            "persistent": {
+                "form": "one persistent launch per canvas frame (sc_batch_frame): resident "
+                        "blocks take tiles and camera chunks from a work list, heaviest "
+                        "fields first, each chunk waiting (bounded) for its field's tiles",
+                "ms_per_frame_of_all_fields": pers_ms,
+                "field_frames_per_s": n_fields / (pers_ms / 1e3),
+                "over_plain_loop": plain_eager_ms / pers_ms,
+                "autotune_ms_per_frame": {"%dx%d/%dw/%ds" % (t, t, w, st): ms
+                                          for (t, w, st), ms in pers_tune.items()}},
             "plain_per_field_loop_ms": plain_eager_ms,
             "plain_per_field_graphs_ms": plain_graph_ms,
             "batched_over_plain_loop": plain_eager_ms / batch_ms,

@@ -404,6 +404,50 @@ int sc_bin_steps_static(const ScStepRec *d_recs, int n_rec, const ScSplatParams 
 int sc_splat_fp64(const ScStepRec *d_recs, const double *d_norm, int n_rec, const float *d_sat,
                   const ScSplatParams *p, double *d_image, int32_t *d_status, void *stream);
 
+/* Work plan of the persistent batched frame (sc_batch_frame): fields of view
+ * packed into one canvas, and the order in which the launch's blocks take
+ * work.  A work entry w >= 0 is tile w (its box and summed-area records
+ * into its tile buffer); w < 0 is camera chunk -w - 1 (chunk_pixels pixels
+ * of one field: the merge of the covering tile buffers, the expectation and
+ * the native camera draws).  Every tile a field's pixels read must come
+ * before that field's chunks in the list.                                   */
+typedef struct {
+    const int32_t *d_work;          /* [n_work] tile indices and -(chunk + 1)         */
+    const int32_t *d_tile_field_off;/* [n_tiles + 1] CSR: fields whose pixels read   */
+    const int32_t *d_tile_field;    /*   tile t's buffer (their counters it advances) */
+    const int32_t *d_field;         /* [n_fields][4]: first pixel i0, j0, edge, and   */
+                                    /*   the number of tiles its pixels read          */
+    const int32_t *d_chunk;         /* [n_chunks][2]: field, first pixel in the field */
+    int32_t *d_counters;            /* [2 + n_fields]: next work entry, stop flag,    */
+                                    /*   tiles done per field; zeroed by the call     */
+    int32_t n_work, n_fields, n_chunks, chunk_pixels;
+    int32_t spin_limit;             /* polls of a chunk's wait for its tiles (0: about */
+                                    /*   a second's worth)                            */
+    int32_t target_extra;           /* test hook: added to every field's tile count,  */
+                                    /*   so that the waits run out (status bit 5)     */
+} ScBatchPlan;
+
+/* Persistent batched frame: one launch of resident blocks that take work
+ * entries in plan order from a device counter.  A tile entry splats the
+ * tile's box records (bulk copies, as sc_splat) and summed-area records into
+ * its tile buffer in d_ws (sc_splat_workspace_bytes) and advances the tile
+ * counters of the fields that read it; a chunk entry waits (bounded poll)
+ * until its field's tiles are done, then merges, forms the expectation and
+ * draws the native camera (d_poisson_table required) for its pixels.  The
+ * wait always ends: a field's tiles are taken before its chunks, and a
+ * block that took a tile finishes it without waiting on anything.  Per
+ * pixel, the results equal sc_splat followed by sc_camera on the canvas
+ * (same sums in the same order, same draws); pixels outside the fields are
+ * not written.  Replaces the per-field loop of generate_frames
+ * (src/scopyon/_epifm.py:1045-1049) for many fields.  Box tables with 12..16
+ * pixel offsets per axis only (else SC_ERR_ARG).                            */
+int sc_batch_frame(const ScStepRec *d_recs, const int32_t *d_tile_start, const int32_t *d_items,
+                   const float *d_sat, const float *d_box, const ScSplatParams *sp,
+                   const ScBatchPlan *plan, const ScCameraParams *cp, const float *d_offset_f,
+                   const float *d_inv_gain_f, const float *d_sigma, const double *d_table_value,
+                   const double *d_table_cdf, void *d_ws, size_t ws_bytes, float *d_expect,
+                   float *d_adc32, int32_t *d_status, void *stream);
+
 /* Bytes of scratch sc_splat needs: one FP32 (tile + halo)^2 buffer per tile. */
 size_t sc_splat_workspace_bytes(const ScSplatParams *p);
 

@@ -57,6 +57,15 @@ class CameraParams(ctypes.Structure):
                 ("d_expect64", ctypes.c_void_p), ("d_poisson_table", ctypes.c_void_p)]
 
 
+class BatchPlan(ctypes.Structure):
+    _fields_ = [("d_work", ctypes.c_void_p), ("d_tile_field_off", ctypes.c_void_p),
+                ("d_tile_field", ctypes.c_void_p), ("d_field", ctypes.c_void_p),
+                ("d_chunk", ctypes.c_void_p), ("d_counters", ctypes.c_void_p),
+                ("n_work", ctypes.c_int32), ("n_fields", ctypes.c_int32),
+                ("n_chunks", ctypes.c_int32), ("chunk_pixels", ctypes.c_int32),
+                ("spin_limit", ctypes.c_int32), ("target_extra", ctypes.c_int32)]
+
+
 class DiffuseParams(ctypes.Structure):
     _fields_ = [("n_particles", ctypes.c_int32), ("n_sub", ctypes.c_int32),
                 ("ndim", ctypes.c_int32), ("boundary", ctypes.c_int32),
@@ -101,6 +110,9 @@ _SIG = {
     "sc_bin_steps_static": (_I, [_P, _I, ctypes.POINTER(SplatParams), _P, _P, _P, _P]),
     "sc_splat_fp64": (_I, [_P, _P, _I, _P, ctypes.POINTER(SplatParams), _P, _P, _P]),
     "sc_splat_workspace_bytes": (ctypes.c_size_t, [ctypes.POINTER(SplatParams)]),
+    "sc_batch_frame": (_I, [_P, _P, _P, _P, _P, ctypes.POINTER(SplatParams),
+                            ctypes.POINTER(BatchPlan), ctypes.POINTER(CameraParams), _P, _P, _P,
+                            _P, _P, _P, ctypes.c_size_t, _P, _P, _P, _P]),
     "sc_splat": (_I, [_P, _P, _P, _P, _P, ctypes.POINTER(SplatParams), _P, ctypes.c_size_t, _P,
                       _P, _P]),
     "sc_camera": (_I, [ctypes.POINTER(CameraParams), _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,

@@ -31,6 +31,74 @@ from .epifm import TILE_CANDIDATES, EngineConfig, FrameGraph, FramePipeline, tun
 from .sampling import DeviceTrajectories
 
 GAP = 16
+CHUNK_PIXELS = 4096  # pixels of one camera work entry of the persistent frame
+
+
+def batch_plan(canvas, tile, halo, origins, sizes, counts, chunk_pixels=CHUNK_PIXELS):
+    """Work list of the persistent batched frame (``sc_batch_frame``).
+
+    Fields are taken heaviest first (by emitters); each field contributes the
+    tiles its pixels read that no earlier field queued, then its camera
+    chunks, so every chunk comes after the tiles it waits for.  A pixel (i, j)
+    reads the tile buffers (tx, ty) with tx * tile <= i < tx * tile + edge,
+    edge = tile + halo (and the same along j).  Returns numpy arrays: work,
+    tile_field_off, tile_field, field [n][4] (i0, j0, size, tiles read),
+    chunk [m][2] (field, first pixel)."""
+    W, H = canvas
+    T, E = int(tile), int(tile) + int(halo)
+    tiles_y = -(-H // T)
+    n_tiles = (-(-W // T)) * tiles_y
+    queued = numpy.zeros(n_tiles, dtype=bool)
+    readers = [[] for _ in range(n_tiles)]
+    work, chunks = [], []
+    field = numpy.zeros((len(sizes), 4), dtype=numpy.int32)
+    for f in sorted(range(len(sizes)), key=lambda k: -int(counts[k])):
+        i0, j0 = origins[f]
+        s = int(sizes[f])
+        tx = numpy.arange(max(0, (i0 - E) // T + 1), (i0 + s - 1) // T + 1)
+        ty = numpy.arange(max(0, (j0 - E) // T + 1), (j0 + s - 1) // T + 1)
+        tiles = (tx[:, None] * tiles_y + ty[None, :]).ravel()
+        for t in tiles.tolist():
+            readers[t].append(f)
+            if not queued[t]:
+                queued[t] = True
+                work.append(t)
+        field[f] = (i0, j0, s, len(tiles))
+        for first in range(0, s * s, chunk_pixels):
+            chunks.append((f, first))
+            work.append(-len(chunks))
+    off = numpy.zeros(n_tiles + 1, dtype=numpy.int32)
+    off[1:] = numpy.cumsum([len(r) for r in readers])
+    flat = numpy.array([f for r in readers for f in r], dtype=numpy.int32)
+    return (numpy.array(work, dtype=numpy.int32), off, flat, field,
+            numpy.array(chunks, dtype=numpy.int32).reshape(-1, 2))
+
+
+class _PersistentFrames(FrameGraph):
+    """FrameGraph whose splat and camera are one persistent launch per frame
+    (``sc_batch_frame``) over the batch's work list."""
+
+    def __init__(self, batch, *args, **kwargs):
+        self.batch = batch
+        super().__init__(*args, **kwargs)
+
+    def _image(self, recs, tag, frame_offset):
+        pipe = self.pipe
+        recs, bufs = recs
+        sp = bufs[0]
+        plan = self.batch.plan_for(pipe)
+        sws_bytes = _lib.load().sc_splat_workspace_bytes(sp)
+        sws = pipe._buf("splat_ws", (sws_bytes + 3) // 4, torch.float32)
+        cp = pipe.camera_params(self.seed, frame_offset, self.frame)
+        maps = pipe.pixel_maps
+        with pipe.timed("batch_frame"):
+            _lib.call("sc_batch_frame", _lib.ptr(recs), _lib.ptr(bufs[4]), _lib.ptr(bufs[3]),
+                      _lib.ptr(pipe.psf.tables), _lib.ptr(pipe.psf.box), sp, plan, cp,
+                      _lib.ptr(pipe.offset_f) if maps else None,
+                      _lib.ptr(pipe.inv_gain_f) if maps else None, _lib.ptr(pipe.sigma),
+                      _lib.ptr(pipe.table_value), _lib.ptr(pipe.table_cdf), _lib.ptr(sws),
+                      sws_bytes, _lib.ptr(pipe.expect), _lib.ptr(pipe.adc32),
+                      _lib.ptr(pipe.status), _lib.stream_ptr())
 
 
 def pack_fields(sizes, gap=GAP, width=8192):
@@ -69,7 +137,7 @@ class BatchedFields:
     """
 
     def __init__(self, config, sizes, counts, D, frames, substeps, seed=0, device=None,
-                 frames_per_step=1):
+                 frames_per_step=1, persistent=False):
         self.device = torch.device(device or "cuda")
         self.sizes = [int(s) for s in sizes]
         self.counts = [int(c) for c in counts]
@@ -112,9 +180,46 @@ class BatchedFields:
             beta = self.eng.half_life / math.log(2.0)
             self.pipe.budget[:self.n_emit].copy_(torch.from_numpy(
                 rng.exponential(beta, self.n_emit) * self.eng.n_emit0))
-        self.graph = FrameGraph(self.pipe, self.traj, self.substeps, self.dt,
-                                seed=int(rng.randint(0, 2 ** 31)), frames_per_step=frames_per_step)
+        graph_seed = int(rng.randint(0, 2 ** 31))
+        self.persistent = bool(persistent)
+        self._plan = None  # (tile, halo, ScBatchPlan, device arrays)
+        self.spin_limit, self.target_extra = 0, 0  # test hooks of the persistent launch
+        if self.persistent:
+            if not 12 <= self.pipe.psf.box_nq <= 16:
+                raise ValueError("the persistent batched frame needs box tables with 12..16 "
+                                 "pixel offsets per axis (160 nm pixels give 14)")
+            self.graph = _PersistentFrames(self, self.pipe, self.traj, self.substeps, self.dt,
+                                           seed=graph_seed, frames_per_step=frames_per_step)
+        else:
+            self.graph = FrameGraph(self.pipe, self.traj, self.substeps, self.dt,
+                                    seed=graph_seed, frames_per_step=frames_per_step)
         self.tuning = None
+
+    def plan_for(self, pipe):
+        """The persistent launch's plan for the pipeline's current tile shape."""
+        key = (pipe.tile, pipe.halo, self.spin_limit, self.target_extra)
+        if self._plan is None or self._plan[0] != key:
+            work, off, flat, field, chunk = batch_plan(self.canvas, pipe.tile, pipe.halo,
+                                                       self.origins, self.sizes, self.counts)
+            dev = self.device
+
+            def dt(a):
+                return torch.from_numpy(numpy.ascontiguousarray(a, dtype=numpy.int32)
+                                        .reshape(-1)).to(dev)
+
+            arrays = dict(work=dt(work), off=dt(off), flat=dt(numpy.append(flat, 0)),
+                          field=dt(field), chunk=dt(chunk),
+                          counters=torch.zeros(2 + len(self.sizes), dtype=torch.int32,
+                                               device=dev))
+            plan = _lib.BatchPlan()
+            plan.d_work, plan.d_tile_field_off = arrays["work"].data_ptr(), arrays["off"].data_ptr()
+            plan.d_tile_field, plan.d_field = arrays["flat"].data_ptr(), arrays["field"].data_ptr()
+            plan.d_chunk, plan.d_counters = arrays["chunk"].data_ptr(), arrays["counters"].data_ptr()
+            plan.n_work, plan.n_fields = len(work), len(self.sizes)
+            plan.n_chunks, plan.chunk_pixels = len(chunk), CHUNK_PIXELS
+            plan.spin_limit, plan.target_extra = int(self.spin_limit), int(self.target_extra)
+            self._plan = (key, plan, arrays)
+        return self._plan[1]
 
     # ------------------------------------------------------------------
     def autotune(self, candidates=TILE_CANDIDATES, frames=2):

@@ -18,95 +18,11 @@
 // or from caller arrays recorded from the reference (injected), in which case
 // the ADC arithmetic is the reference's FP64 sequence.
 #include "sc_common.cuh"
+#include "camera.cuh"
 
 namespace {
 
-struct CamConsts {
-    int n, camera, exact, rounding, table_n;
-    double qe, background, readout, emgain, fullwell, adc_max, offset0, gain0;
-    float qe_f, background_f, readout_f, emgain_f, fullwell_f, adc_max_f, offset0_f, inv_gain0_f;
-    uint64_t seed, counter;
-    const int64_t *frame;
-    const double *photons64;  // exact mode: FP64 photons in place of the FP32 ones
-    double *expect64;         // exact mode: FP64 expectation out
-};
-
-// Poisson variate.  Small means: sequential inversion.  Large means: the
-// transformed rejection method PTRS (W. Hormann, "The transformed rejection
-// method for generating Poisson random variables", Insurance: Mathematics and
-// Economics 12 (1993) 39-45), with log(k!) from Stirling's series.  Divisions
-// and the logarithms of the acceptance test use the approximate intrinsics
-// (relative error ~1e-7): they move the accepted distribution by far less
-// than any test of a frame's counts can see, and a pixel's draw costs about
-// half the instructions of the IEEE forms.
-__device__ float poisson(sc::rng_stream &rs, float lam, int32_t *status) {
-    if (!(lam > 0.f)) return 0.f;
-    if (lam < 12.f) {
-        const float u = rs.uniform();
-        float p = expf(-lam), s = p;
-        int k = 0;
-        while (u > s && k < 200) {
-            ++k;
-            p *= __fdividef(lam, (float)k);
-            s += p;
-        }
-        return (float)k;
-    }
-    const float slam = sqrtf(lam), inv_lam = __fdividef(1.f, lam);
-    const float b = 0.931f + 2.53f * slam;
-    const float a = -0.059f + 0.02483f * b;
-    const float invalpha = 1.1239f + __fdividef(1.1328f, b - 3.4f);
-    const float vr = 0.9277f - __fdividef(3.6224f, b - 2.f);
-    for (int it = 0; it < 64; ++it) {
-        const float U = rs.uniform() - 0.5f;
-        const float V = rs.uniform();
-        const float us = 0.5f - fabsf(U);
-        const float k = floorf((__fdividef(2.f * a, us) + b) * U + lam + 0.43f);
-        if (us >= 0.07f && V <= vr) return k;
-        if (k < 0.f || (us < 0.013f && V > us)) continue;
-        // -lam + k log(lam) - log(k!) via Stirling, written relative to k - lam
-        const float kk = fmaxf(k, 1.f);
-        const float ikk = __fdividef(1.f, kk);
-        const float d = (k - lam) * inv_lam;
-        const float lfact_rel = (k - lam) - k * log1pf(d) - 0.5f * __logf(6.2831853f * kk) -
-                                ikk * (1.f / 12.f) + ikk * ikk * ikk * (1.f / 360.f);
-        const float rhs = k == 0.f ? -lam : lfact_rel;
-        // log(V / alpha / (a / us^2 + b)) <= rhs
-        if (__logf(__fdividef(V * invalpha, __fdividef(a, us * us) + b)) <= rhs) return k;
-    }
-    sc::flag_status(status, 3, 0, 0, 0);
-    return rintf(lam);
-}
-
-// Gamma(shape, 1) for shape >= 1: G. Marsaglia and W. W. Tsang, "A simple
-// method for generating gamma variables", ACM TOMS 26 (2000) 363-372.
-__device__ float gamma_ge1(sc::rng_stream &rs, float shape, int32_t *status) {
-    const float d = shape - 1.f / 3.f;
-    const float c = rsqrtf(9.f * d);
-    for (int it = 0; it < 64; ++it) {
-        const float x = rs.normal();
-        const float t = c * x;
-        if (t <= -1.f) continue;
-        const float u = rs.uniform();
-        const float vm1 = t * (3.f + t * (3.f + t));  // (1 + t)^3 - 1
-        const float x2 = x * x;
-        if (u < 1.f - 0.0331f * x2 * x2) return d * (1.f + vm1);
-        if (logf(u) < 0.5f * x2 + d * (3.f * log1pf(t) - vm1)) return d * (1.f + vm1);
-    }
-    sc::flag_status(status, 3, 1, 0, 0);
-    return shape;
-}
-
-__device__ __forceinline__ int table_index(const double *cdf, int n, double u) {
-    // searchsorted(cdf, u, side='right')
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (cdf[mid] <= u) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo < n ? lo : n - 1;
-}
+using namespace sc::cam;
 
 // Injected draws: the reference's FP64 arithmetic on the caller's draws.
 __global__ void camera_exact_kernel(CamConsts c, const float *__restrict__ photons,
@@ -143,39 +59,10 @@ __global__ void camera_exact_kernel(CamConsts c, const float *__restrict__ photo
     }
 }
 
-// ------------------------------------------------ Poisson inverse-CDF tables
-// Poisson(j) for j = 0 .. kPoisJ - 1: the CDF over k = 0 .. K_j - 1 in FP32
-// (each entry the FP64 sum rounded once; the last entry is exactly 1) and,
-// per j, kPoisG starting points for the search (the first k whose CDF
-// reaches g / kPoisG).  Layout of the caller's buffer: int32 offsets
-// [kPoisJ + 1], uint16 guide [kPoisJ][kPoisG], float CDF [sum K_j].
-constexpr int kPoisJ = 256, kPoisG = 256;
-constexpr size_t kPoisGuideAt = ((sizeof(int32_t) * (kPoisJ + 1) + 15) / 16) * 16;
-constexpr size_t kPoisCdfAt = kPoisGuideAt + sizeof(uint16_t) * kPoisJ * kPoisG;
-
-// Support of the Poisson(j) table: j + 10 sqrt(j) + 12 values (the mass past
-// it is far below the FP32 rounding of the CDF).
-__host__ __device__ __forceinline__ int pois_support(int j) {
-    return j + (int)ceil(10.0 * sqrt((double)j)) + 12;
-}
-
 int64_t pois_entries() {
     int64_t n = 0;
     for (int j = 0; j < kPoisJ; ++j) n += pois_support(j);
     return n;
-}
-
-struct PoisTab {
-    const int32_t *off;
-    const uint16_t *guide;
-    const float *cdf;
-};
-
-__device__ __forceinline__ PoisTab pois_tab(const void *base) {
-    const char *b = static_cast<const char *>(base);
-    return PoisTab{reinterpret_cast<const int32_t *>(b),
-                   reinterpret_cast<const uint16_t *>(b + kPoisGuideAt),
-                   reinterpret_cast<const float *>(b + kPoisCdfAt)};
 }
 
 // One thread per j: offsets, then the CDF summed in FP64 from
@@ -217,79 +104,6 @@ __global__ void pois_guide_kernel(void *base) {
     guide[idx] = (uint16_t)k;
 }
 
-// Poisson(lam) from two uniforms, with no rejection: Poisson(j) by table
-// inversion at u0 plus Poisson(lam - j) by sequential inversion at u1,
-// j = floor(lam) (a sum of independent Poisson variates is Poisson with the
-// summed mean).  Means of kPoisJ and more take PTRS on the pixel's stream.
-__device__ __forceinline__ float poisson_tab(const PoisTab &t, float lam, float u0, float u1,
-                                             sc::rng_stream &rs, int32_t *status) {
-    if (!(lam > 0.f)) return 0.f;
-    if (!(lam < (float)kPoisJ)) return poisson(rs, lam, status);
-    const int j = (int)lam;
-    const float r = lam - (float)j;
-    int k = 0;
-    if (j > 0) {
-        const int base = __ldg(t.off + j), last = __ldg(t.off + j + 1) - 1 - base;
-        k = __ldg(t.guide + j * kPoisG + min((int)(u0 * (float)kPoisG), kPoisG - 1));
-        while (k < last && u0 > __ldg(t.cdf + base + k)) ++k;
-    }
-    // Poisson(r), r in [0, 1): the first four cumulative sums without a
-    // branch (u1 lies past the fourth with probability below 2%), then the
-    // sequential search (P(X >= 16) < 1e-13)
-    float p = expf(-r), s = p;
-    int m = u1 > s;
-    p *= r;
-    s += p;
-    m += u1 > s;
-    p *= 0.5f * r;
-    s += p;
-    m += u1 > s;
-    p *= (1.f / 3.f) * r;
-    s += p;
-    if (u1 > s) {
-        m = 4;
-        p *= 0.25f * r;
-        s += p;
-        while (u1 > s && m < 16) {
-            ++m;
-            p *= __fdividef(r, (float)m);
-            s += p;
-        }
-    }
-    return (float)(k + m);
-}
-
-// Standard normal from two 32-bit words (Box-Muller, the cosine branch).
-__device__ __forceinline__ float bm_normal(uint32_t a, uint32_t b) {
-    const float r = sqrtf(-2.0f * __logf(sc::u01f(a)));
-    float sn, cs;
-    sc::sincos_2pi(sc::u01f(b), &sn, &cs);
-    return r * cs;
-}
-
-// EMCCD output electrons with the reference's law (EMCCD.probability_
-// distribution, _epifm.py:365-400): S = 0 with the weight of no
-// photo-electron, S >= 1 with weight proportional to the Poisson-gamma density
-// at S, on the support [g floor(E - sigma), g floor(E + sigma)), sigma =
-// 5 sqrt(E) + 10.  Drawn as n ~ Poisson(E), S = rint(g Gamma(n)) for n > 0,
-// and drawn again when S leaves the support or rounds to 0 with n > 0 (the
-// law has no density mass below S = 1/2 beside the atom at 0).
-__device__ float emccd_native(const PoisTab &t, float e, float g, float u0, float u1,
-                              sc::rng_stream &rs, int32_t *status) {
-    if (!(e > 0.f)) return 0.f;
-    const float sig = sqrtf(e) * 5.f + 10.f;
-    const float s_min = fmaxf(0.f, g * truncf(e - sig)), s_max = g * truncf(e + sig);
-    for (int it = 0; it < 32; ++it) {
-        const float n = it == 0 ? poisson_tab(t, e, u0, u1, rs, status)
-                                : poisson_tab(t, e, rs.uniform(), rs.uniform(), rs, status);
-        const float s = n > 0.f ? rintf(g * gamma_ge1(rs, n, status)) : 0.f;
-        if (n > 0.f && s < 1.f) continue;
-        if (s >= s_min && s < s_max) return s;
-    }
-    sc::flag_status(status, 3, 2, 0, 0);
-    return rintf(g * e);
-}
-
 // Native draws, a pixel per thread.  Pixel p's draws come from its own
 // Philox stream (key: seed; counter: p and the frame counter): block 0's
 // four words give the Poisson draw (two) and the read noise (two); block 1
@@ -305,34 +119,16 @@ camera_native_kernel(CamConsts c, const void *__restrict__ ptab, const float *__
                      double *__restrict__ adc64, float *__restrict__ adc32, int32_t *status) {
     const PoisTab t = pois_tab(ptab);
     const uint64_t counter = c.counter + (c.frame ? (uint64_t)*c.frame : 0);
-    const uint32_t c0 = (uint32_t)counter, c1 = (uint32_t)(counter >> 32);
-    const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < c.n; q += stride) {
         const int p = (int)q;
         const float ef = c.qe_f * (__ldg(photons + p) + c.background_f);
         if (expect) expect[p] = ef;
-        const sc::u4 r = sc::philox4x32_10(sc::u4{(uint32_t)p, c0, c1, 0u}, k0, k1);
-        sc::rng_stream rs(c.seed, (uint32_t)p, c0, c1);
-        rs.ctr.w = 1;
-        const float u0 = sc::u01f(r.x), u1 = sc::u01f(r.y);
-        float signal, noise;
-        if (CAM == SC_CAM_EMCCD) {
-            signal = emccd_native(t, ef, c.emgain_f, u0, u1, rs, status);
-            noise = c.readout_f > 0.f ? c.readout_f * bm_normal(r.z, r.w) : 0.f;
-        } else if (CAM == SC_CAM_CMOS_TABLE) {
-            noise = (float)table_value[table_index(table_cdf, c.table_n, sc::u01d(r.z, r.w))];
-            signal = poisson_tab(t, ef, u0, u1, rs, status);
-        } else {
-            signal = poisson_tab(t, ef, u0, u1, rs, status);
-            const float sg = (CAM == SC_CAM_SCMOS && sigma) ? __ldg(sigma + p) : c.readout_f;
-            noise = sg * bm_normal(r.z, r.w);
-        }
-        float v = fminf(signal + noise, c.fullwell_f);
-        v = v * (inv_gain_f ? __ldg(inv_gain_f + p) : c.inv_gain0_f) +
-            (offset_f ? __ldg(offset_f + p) : c.offset0_f);
-        v = fminf(fmaxf(v, 0.f), c.adc_max_f);
-        if (c.rounding) v = rintf(v);
+        const float sg = (CAM == SC_CAM_SCMOS && sigma) ? __ldg(sigma + p) : c.readout_f;
+        const float g = inv_gain_f ? __ldg(inv_gain_f + p) : c.inv_gain0_f;
+        const float o = offset_f ? __ldg(offset_f + p) : c.offset0_f;
+        const float v = native_adc<CAM>(c, t, p, ef, sg, g, o, counter, table_value, table_cdf,
+                                        status);
         if (adc32) adc32[p] = v;
         if (adc64) adc64[p] = sc::f2d_exact(v);
     }
@@ -418,6 +214,44 @@ __global__ void emccd_exact_kernel(const double *photons, double qe, double back
 
 }  // namespace
 
+namespace sc {
+namespace cam {
+
+int cam_consts(const ScCameraParams *p, CamConsts &c) {
+    SC_REQUIRE(p != nullptr, "camera params are NULL");
+    SC_REQUIRE(p->bit > 0 && p->bit <= 32, "camera: bit=%d", p->bit);
+    c.n = p->nw * p->nh;
+    c.camera = p->camera;
+    c.exact = p->exact;
+    c.rounding = p->rounding;
+    c.table_n = p->table_n;
+    c.qe = p->qe;
+    c.background = p->background;
+    c.readout = p->readout_noise;
+    c.emgain = p->emgain;
+    c.fullwell = p->fullwell;
+    c.adc_max = (double)((1ull << p->bit) - 1);
+    c.offset0 = p->offset0;
+    c.gain0 = p->gain0;
+    c.qe_f = (float)p->qe;
+    c.background_f = (float)p->background;
+    c.readout_f = (float)p->readout_noise;
+    c.emgain_f = (float)p->emgain;
+    c.fullwell_f = (float)p->fullwell;
+    c.adc_max_f = (float)c.adc_max;
+    c.offset0_f = (float)p->offset0;
+    c.inv_gain0_f = (float)(1.0 / p->gain0);
+    c.seed = p->seed;
+    c.counter = p->counter;
+    c.frame = p->d_frame;
+    c.photons64 = p->d_photons64;
+    c.expect64 = p->d_expect64;
+    return SC_OK;
+}
+
+}  // namespace cam
+}  // namespace sc
+
 extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const double *d_offset,
                          const double *d_gain, const float *d_offset_f, const float *d_inv_gain_f,
                          const float *d_sigma, const double *d_table_value,
@@ -446,32 +280,8 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
                    "sc_camera: CMOS exact mode needs injected uniforms or noise");
     }
     CamConsts c;
-    c.n = p->nw * p->nh;
-    c.camera = p->camera;
-    c.exact = p->exact;
-    c.rounding = p->rounding;
-    c.table_n = p->table_n;
-    c.qe = p->qe;
-    c.background = p->background;
-    c.readout = p->readout_noise;
-    c.emgain = p->emgain;
-    c.fullwell = p->fullwell;
-    c.adc_max = (double)((1ull << p->bit) - 1);
-    c.offset0 = p->offset0;
-    c.gain0 = p->gain0;
-    c.qe_f = (float)p->qe;
-    c.background_f = (float)p->background;
-    c.readout_f = (float)p->readout_noise;
-    c.emgain_f = (float)p->emgain;
-    c.fullwell_f = (float)p->fullwell;
-    c.adc_max_f = (float)c.adc_max;
-    c.offset0_f = (float)p->offset0;
-    c.inv_gain0_f = (float)(1.0 / p->gain0);
-    c.seed = p->seed;
-    c.counter = p->counter;
-    c.frame = p->d_frame;
-    c.photons64 = p->d_photons64;
-    c.expect64 = p->d_expect64;
+    int rc = sc::cam::cam_consts(p, c);
+    if (rc) return rc;
     cudaStream_t st = sc::as_stream(stream);
     if (p->exact) {
         const int block = 256;

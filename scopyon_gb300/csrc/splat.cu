@@ -21,9 +21,12 @@
 //    evaluated exactly whenever the estimate is within 1e-6 of an integer),
 //    and each pixel's sum folds onto at most 3 x 3 quadrant-table entries of
 //    the mirror-symmetric grid, held as double-float pairs (~2^-48 relative).
+#include <climits>
+
 #include "sc_common.cuh"
 #include "bin.cuh"
 #include "fold.cuh"
+#include "camera.cuh"
 
 
 namespace {
@@ -313,40 +316,26 @@ __device__ __forceinline__ int4 decode_record(const ScStepRec *recs, const int32
     return make_int4(b.x, (dr + 128) | ((dc + 128) << 8), qlo | (qhi << 8), flags);
 }
 
+// One tile's box-path records through the calling warp's ring of block
+// copies (`stages` buffers with one mbarrier each): the warp takes records
+// it0 + warp + NW k of the tile's list.  Every copy a call issues is waited
+// for before it returns, so the ring is empty between calls; `phase` holds
+// each buffer's next wait parity (bit b for buffer b) and carries over.
+// Returns false when a wait ran out (after draining the copies in flight).
 template <int NW, int NQ>
-__global__ void __launch_bounds__(NW * 32, 20 / NW)
-splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
-                      const int32_t *__restrict__ items, SplatConsts c, int stages, int half_rows,
-                      int64_t table_floats, float *__restrict__ ws, int32_t *status) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ bool bulk_tile_records(
+    const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
+    const int32_t *__restrict__ items, const SplatConsts &c, int stages, int HB,
+    int64_t table_floats, int tile, int x0, int y0, float *my_acc, int4 *my_desc,
+    float *my_stage, uint64_t *my_bars, uint32_t &phase, uint32_t first_tries,
+    int32_t *status) {
     constexpr int BSR = kBulkBsr;
-    constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;  // stage buffer floats
+    constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;
     constexpr int NB = SC_BOX_BLOCK_FLOATS(NQ);
-    const int E = c.edge, EE = c.edge * c.edge;
-    const int HB = half_rows * BSR + 16;  // odd half starts 16 banks after the even half
-    const int BS = (2 * HB + 31) & ~31;
-    float *acc = reinterpret_cast<float *>(smem_raw);                   // [NW][BS]
-    int4 *descs = reinterpret_cast<int4 *>(acc + NW * BS);              // [NW][2][32]
-    float *stage = reinterpret_cast<float *>(descs + NW * 64);          // [NW][stages][SB]
-    uint64_t *bars = reinterpret_cast<uint64_t *>(stage + NW * stages * SB);  // [NW][stages]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tile = blockIdx.x;
-    const int t = tile % c.tiles_per_image;
-    const int x0 = (t / c.tiles_y) * c.tile, y0 = (t % c.tiles_y) * c.tile;
-    for (int i = threadIdx.x; i < NW * BS; i += blockDim.x) acc[i] = 0.f;
-    for (int i = threadIdx.x; i < NW * stages * SB; i += blockDim.x) stage[i] = 0.f;
-    if (threadIdx.x < NW * stages) mbar_init(bars + threadIdx.x, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    __syncthreads();
-
     const int it0 = tile_start[tile], it1 = tile_start[tile + 1];
     // records of this warp: m_k = it0 + warp + NW k, k < K
     const int K = it1 - it0 > warp ? (it1 - it0 - warp + NW - 1) / NW : 0;
-    // buffer (r, c) is half (r + 1) & 1, entry ((r + 1) >> 1) * BSR + c + 1
-    float *my_acc = acc + warp * BS;
-    int4 *my_desc = descs + warp * 64;
-    float *my_stage = stage + warp * stages * SB;
-    uint64_t *my_bars = bars + warp * stages;
     constexpr uint32_t bytes = NB * 4u;
     const int col = lane & 15, rsel = lane >> 4;
 
@@ -361,7 +350,6 @@ splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restr
     __syncwarp();
     if (lane < min(stages, K)) bulk_copy(my_stage + lane * SB, cur_src, bytes, my_bars + lane);
     int s = 0;
-    uint32_t parity = 0;
     int k = 0;
     for (; k < K; ++k) {
         if (k > 0 && (k & 31) == 0) {
@@ -373,7 +361,7 @@ splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restr
                                   table_floats, NB, nxt_src, status, tile);
             __syncwarp();
         }
-        if (!warp_wait(my_bars + s, parity, k == 0 ? c.first_wait_tries : kWaitTries)) {
+        if (!warp_wait(my_bars + s, (phase >> s) & 1u, k == 0 ? first_tries : kWaitTries)) {
             if (lane == 0) sc::flag_status(status, 5, k, warp, tile);
             break;
         }
@@ -408,17 +396,53 @@ splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restr
         if (kn < K && lane == (kn & 31))
             bulk_copy(my_stage + s * SB, ((kn >> 5) == (k >> 5)) ? cur_src : nxt_src, bytes,
                       my_bars + s);
-        if (++s == stages) {
-            s = 0;
-            parity ^= 1u;
-        }
+        phase ^= 1u << s;
+        if (++s == stages) s = 0;
     }
     if (k < K) {
         // a wait ran out: wait (bounded) for every copy still in flight before
         // the CTA's shared memory is released
         const int last = min(K, k + stages);
-        for (int j = k; j < last; ++j) warp_wait(my_bars + j % stages, (uint32_t)((j / stages) & 1));
+        for (int j = k; j < last; ++j) {
+            const int bj = j % stages;
+            warp_wait(my_bars + bj, (phase >> bj) & 1u);
+        }
+        return false;
     }
+    return true;
+}
+
+template <int NW, int NQ>
+__global__ void __launch_bounds__(NW * 32, 20 / NW)
+splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
+                      const int32_t *__restrict__ items, SplatConsts c, int stages, int half_rows,
+                      int64_t table_floats, float *__restrict__ ws, int32_t *status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int BSR = kBulkBsr;
+    constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;  // stage buffer floats
+    constexpr int NB = SC_BOX_BLOCK_FLOATS(NQ);
+    const int E = c.edge, EE = c.edge * c.edge;
+    const int HB = half_rows * BSR + 16;  // odd half starts 16 banks after the even half
+    const int BS = (2 * HB + 31) & ~31;
+    float *acc = reinterpret_cast<float *>(smem_raw);                   // [NW][BS]
+    int4 *descs = reinterpret_cast<int4 *>(acc + NW * BS);              // [NW][2][32]
+    float *stage = reinterpret_cast<float *>(descs + NW * 64);          // [NW][stages][SB]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(stage + NW * stages * SB);  // [NW][stages]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x;
+    const int t = tile % c.tiles_per_image;
+    const int x0 = (t / c.tiles_y) * c.tile, y0 = (t % c.tiles_y) * c.tile;
+    for (int i = threadIdx.x; i < NW * BS; i += blockDim.x) acc[i] = 0.f;
+    for (int i = threadIdx.x; i < NW * stages * SB; i += blockDim.x) stage[i] = 0.f;
+    if (threadIdx.x < NW * stages) mbar_init(bars + threadIdx.x, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+
+    // buffer (r, c) is half (r + 1) & 1, entry ((r + 1) >> 1) * BSR + c + 1
+    uint32_t phase = 0;
+    bulk_tile_records<NW, NQ>(recs, tile_start, items, c, stages, HB, table_floats, tile, x0, y0,
+                              acc + warp * BS, descs + warp * 64, stage + warp * stages * SB,
+                              bars + warp * stages, phase, c.first_wait_tries, status);
     __syncthreads();
     float *out = ws + (size_t)tile * EE;
     for (int p = threadIdx.x; p < EE; p += blockDim.x) {
@@ -653,6 +677,245 @@ int launch_splat(const ScStepRec *recs, const int32_t *tile_start, const int32_t
     return sc::launch_status("sc_splat summed-area");
 }
 
+// ------------------------------------------------- persistent batched frame
+struct BatchPlanDev {
+    const int32_t *work, *tile_field_off, *tile_field, *field, *chunk;
+    int32_t *counters;  // [0] next work entry, [1] stop, [2 + f] tiles done of field f
+    int n_work, n_fields, n_chunks, chunk_pixels;
+    uint32_t spin_limit;
+    int target_extra;
+};
+
+struct BatchCam {
+    sc::cam::CamConsts c;
+    const void *ptab;
+    const float *offset_f, *inv_gain_f, *sigma;
+    const double *table_value, *table_cdf;
+    float *expect, *adc32;
+};
+
+__device__ __forceinline__ int ld_acquire(const int32_t *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Canvas pixel (i, j): the tile buffers that cover it, summed in
+// splat_merge_kernel's order (read through L2: they were written by other
+// blocks of the same launch).
+__device__ __forceinline__ float merge_pixel(const float *ws, const SplatConsts &c, int i, int j) {
+    const int E = c.edge, EE = c.edge * c.edge;
+    const int tx = i / c.tile, ty = j / c.tile;
+    float sum = 0.f;
+    for (int a = 0; a <= tx; ++a) {
+        const int li = i - (tx - a) * c.tile;
+        if (li >= E) break;
+        for (int b = 0; b <= ty; ++b) {
+            const int lj = j - (ty - b) * c.tile;
+            if (lj >= E) break;
+            sum += __ldcg(ws + (size_t)((tx - a) * c.tiles_y + (ty - b)) * EE + li * E + lj);
+        }
+    }
+    return sum;
+}
+
+// The native camera of one pixel (the camera kind is uniform across a launch).
+__device__ __forceinline__ float batch_adc(const BatchCam &bc, const sc::cam::PoisTab &t, int p,
+                                           float ef, uint64_t counter, int32_t *status) {
+    using namespace sc::cam;
+    const CamConsts &c = bc.c;
+    const float sg = (c.camera == SC_CAM_SCMOS && bc.sigma) ? __ldg(bc.sigma + p) : c.readout_f;
+    const float g = bc.inv_gain_f ? __ldg(bc.inv_gain_f + p) : c.inv_gain0_f;
+    const float o = bc.offset_f ? __ldg(bc.offset_f + p) : c.offset0_f;
+    switch (c.camera) {
+        case SC_CAM_EMCCD:
+            return native_adc<SC_CAM_EMCCD>(c, t, p, ef, sg, g, o, counter, bc.table_value,
+                                            bc.table_cdf, status);
+        case SC_CAM_CCD:
+            return native_adc<SC_CAM_CCD>(c, t, p, ef, sg, g, o, counter, bc.table_value,
+                                          bc.table_cdf, status);
+        case SC_CAM_CMOS_TABLE:
+            return native_adc<SC_CAM_CMOS_TABLE>(c, t, p, ef, sg, g, o, counter, bc.table_value,
+                                                 bc.table_cdf, status);
+        default:
+            return native_adc<SC_CAM_SCMOS>(c, t, p, ef, sg, g, o, counter, bc.table_value,
+                                            bc.table_cdf, status);
+    }
+}
+
+// Resident blocks take work entries in plan order from b.counters[0] until
+// the list is done.  Tile entry: the tile's box records through each warp's
+// copy ring (the ring and its mbarriers live for the whole launch), the
+// buffer written, then the tile's summed-area records added (both sums as
+// splat_box_bulk_kernel and splat_sat_kernel form them), then the tile
+// counters of the fields that read it advanced.  Chunk entry: thread 0 polls
+// the field's counter (bounded; running out sets status bit 5 and stops the
+// launch), then every thread merges, images and draws its pixels.
+template <int NW, int NQ>
+__global__ void __launch_bounds__(NW * 32, 20 / NW)
+batch_frame_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
+                   const int32_t *__restrict__ items, const float2 *__restrict__ sat,
+                   SplatConsts c, int n_tiles, int stages, int half_rows, int64_t table_floats,
+                   float *__restrict__ ws, BatchPlanDev b, BatchCam bc, int32_t *status) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int sh_work, sh_stop;
+    constexpr int BSR = kBulkBsr;
+    constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;
+    const int E = c.edge, EE = c.edge * c.edge;
+    const int HB = half_rows * BSR + 16;
+    const int BS = (2 * HB + 31) & ~31;
+    const int SBS = (EE + 31) & ~31;  // summed-area buffers (E-stride), in the same space
+    float *acc = reinterpret_cast<float *>(smem_raw);                         // [NW][BS]
+    int4 *descs = reinterpret_cast<int4 *>(acc + NW * BS);                    // [NW][2][32]
+    float *stage = reinterpret_cast<float *>(descs + NW * 64);                // [NW][stages][SB]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(stage + NW * stages * SB);  // [NW][stages]
+    int *bnd = reinterpret_cast<int *>(bars + NW * stages);                   // [NW][2][E + 2]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < NW * stages * SB; i += blockDim.x) stage[i] = 0.f;
+    if (threadIdx.x < NW * stages) mbar_init(bars + threadIdx.x, 1);
+    if (threadIdx.x == 0) sh_stop = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+    const sc::cam::PoisTab ptab = sc::cam::pois_tab(bc.ptab);
+    const uint64_t counter = bc.c.counter + (bc.c.frame ? (uint64_t)*bc.c.frame : 0);
+    uint32_t phase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int w = atomicAdd(b.counters, 1);
+            if (w < b.n_work && ld_acquire(b.counters + 1)) w = b.n_work;  // stopped
+            sh_work = w < b.n_work ? b.work[w] : INT_MIN;
+        }
+        __syncthreads();
+        const int w = sh_work;
+        __syncthreads();
+        if (w == INT_MIN) break;
+        if (w >= 0) {
+            const int tile = w;
+            const int t = tile % c.tiles_per_image;
+            const int x0 = (t / c.tiles_y) * c.tile, y0 = (t % c.tiles_y) * c.tile;
+            for (int i = threadIdx.x; i < NW * BS; i += blockDim.x) acc[i] = 0.f;
+            __syncthreads();
+            if (!bulk_tile_records<NW, NQ>(recs, tile_start, items, c, stages, HB, table_floats,
+                                           tile, x0, y0, acc + warp * BS, descs + warp * 64,
+                                           stage + warp * stages * SB, bars + warp * stages,
+                                           phase, kWaitTries, status))
+                sh_stop = 1;
+            __syncthreads();
+            float *out = ws + (size_t)tile * EE;
+            for (int p = threadIdx.x; p < EE; p += blockDim.x) {
+                const int r = p / E, cc = p - (p / E) * E;
+                const int off = ((r + 1) & 1) * HB + ((r + 1) >> 1) * BSR + cc + 1;
+                float sum = 0.f;
+#pragma unroll
+                for (int v = 0; v < NW; ++v) sum += acc[v * BS + off];
+                out[p] = sum;
+            }
+            const int s0 = tile_start[n_tiles + tile], s1 = tile_start[n_tiles + tile + 1];
+            if (s1 > s0 && !sh_stop) {
+                __syncthreads();
+                for (int i = threadIdx.x; i < NW * SBS; i += blockDim.x) acc[i] = 0.f;
+                __syncthreads();
+                int *bx = bnd + warp * 2 * (E + 2);
+                int *by = bx + (E + 2);
+                for (int m = s0 + warp; m < s1; m += NW) {
+                    const ScStepRec &rec = recs[__ldg(items + m)];
+                    const int ni = rec.n_i - 1, nj = rec.n_j - 1;
+                    const int ox = rec.i_start - x0, oy = rec.j_start - y0;
+                    if (!in_buffer(ox, oy, ni, nj, E)) {
+                        if (lane == 0) sc::flag_status(status, 2, rec.i_start, rec.j_start, tile);
+                        continue;
+                    }
+                    splat_sat_record(rec, ox * E + oy, sat, c, bx, by, acc + warp * SBS, lane);
+                }
+                __syncthreads();
+                for (int p = threadIdx.x; p < EE; p += blockDim.x) {
+                    float sum = 0.f;
+#pragma unroll
+                    for (int v = 0; v < NW; ++v) sum += acc[v * SBS + p];
+                    out[p] = out[p] + sum;
+                }
+            }
+            __threadfence();
+            __syncthreads();
+            if (sh_stop) {
+                if (threadIdx.x == 0) atomicExch(b.counters + 1, 1);
+                break;
+            }
+            if (threadIdx.x == 0)
+                for (int q = b.tile_field_off[tile]; q < b.tile_field_off[tile + 1]; ++q)
+                    atomicAdd(b.counters + 2 + b.tile_field[q], 1);
+        } else {
+            const int k = -w - 1;
+            const int f = b.chunk[2 * k], first = b.chunk[2 * k + 1];
+            const int i0 = b.field[4 * f], j0 = b.field[4 * f + 1], edge = b.field[4 * f + 2];
+            if (threadIdx.x == 0) {
+                const int target = b.field[4 * f + 3] + b.target_extra;
+                uint32_t it = 0;
+                bool ok = true;
+                while (ld_acquire(b.counters + 2 + f) < target) {
+                    if (++it > b.spin_limit) {
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(256);
+                }
+                if (!ok) {
+                    sc::flag_status(status, 5, k, f, -1);
+                    atomicExch(b.counters + 1, 1);
+                }
+                sh_stop = ok ? 0 : 1;
+                __threadfence();
+            }
+            __syncthreads();
+            if (sh_stop) break;
+            const int last = min(first + b.chunk_pixels, edge * edge);
+            for (int q = first + threadIdx.x; q < last; q += blockDim.x) {
+                const int li = q / edge;
+                const int i = i0 + li, j = j0 + (q - li * edge);
+                const int p = i * c.nh + j;
+                const float ph = merge_pixel(ws, c, i, j);
+                const float ef = bc.c.qe_f * (ph + bc.c.background_f);
+                if (bc.expect) bc.expect[p] = ef;
+                bc.adc32[p] = batch_adc(bc, ptab, p, ef, counter, status);
+            }
+        }
+    }
+}
+
+template <int NW, int NQ>
+int launch_batch(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
+                 const float2 *sat, const SplatConsts &c, int n_tiles, int n_slots,
+                 int want_stages, float *ws, const BatchPlanDev &b, const BatchCam &bc,
+                 int32_t *status, cudaStream_t s) {
+    constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;
+    constexpr int NB = SC_BOX_BLOCK_FLOATS(NQ);
+    SC_REQUIRE(c.tile + 15 <= kBulkBsr && c.edge + 1 <= kBulkBsr,
+               "sc_batch_frame: tile %d + halo %d does not fit the bulk-copy buffers", c.tile,
+               c.halo);
+    const int rows = max(c.edge, c.tile + 2 * PAIRS - 1) + 1;
+    const int half_rows = ((rows + 1) / 2 + 3) & ~3;
+    const int64_t table_floats = (int64_t)n_slots * c.box_p * c.box_p * NB;
+    const size_t fixed = (size_t)NW * ((2 * (half_rows * kBulkBsr + 16) + 31) & ~31) * sizeof(float) +
+                         (size_t)NW * 64 * sizeof(int4);
+    auto smem_for = [&](int st) {
+        return fixed + (size_t)NW * st * SB * sizeof(float) + (size_t)NW * st * sizeof(uint64_t) +
+               (size_t)NW * 2 * (c.edge + 2) * sizeof(int);
+    };
+    int stages = want_stages > 0 ? want_stages : 4;
+    while (stages > 1 && smem_for(stages) > 160 * 1024) --stages;
+    const size_t smem = smem_for(stages);
+    SC_REQUIRE(smem <= 160 * 1024, "sc_batch_frame: %zu bytes of shared memory", smem);
+    cudaError_t e = cudaFuncSetAttribute(batch_frame_kernel<NW, NQ>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return sc::cuda_status(e, "sc_batch_frame: smem attribute");
+    const int grid = sc::resident_grid((const void *)batch_frame_kernel<NW, NQ>, NW * 32, smem,
+                                       (int64_t)b.n_work);
+    batch_frame_kernel<NW, NQ><<<grid, NW * 32, smem, s>>>(recs, tile_start, items, sat, c,
+                                                           n_tiles, stages, half_rows,
+                                                           table_floats, ws, b, bc, status);
+    return sc::launch_status("sc_batch_frame");
+}
+
 int splat_consts(const ScSplatParams *p, const sc::TileGeom &g, SplatConsts &c) {
     SC_REQUIRE(p->n_r >= 2 && p->sat_pitch >= p->n_r + 1, "sc_splat: n_r=%d pitch=%d", p->n_r,
                p->sat_pitch);
@@ -769,4 +1032,94 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
     if (grid > 152 * 32) grid = 152 * 32;
     splat_merge_kernel<<<grid, 256, 0, s>>>(ws, c, g.n_images, d_image);
     return sc::launch_status("sc_splat merge");
+}
+
+extern "C" int sc_batch_frame(const ScStepRec *d_recs, const int32_t *d_tile_start,
+                              const int32_t *d_items, const float *d_sat, const float *d_box,
+                              const ScSplatParams *sp, const ScBatchPlan *plan,
+                              const ScCameraParams *cp, const float *d_offset_f,
+                              const float *d_inv_gain_f, const float *d_sigma,
+                              const double *d_table_value, const double *d_table_cdf,
+                              void *d_ws, size_t ws_bytes, float *d_expect, float *d_adc32,
+                              int32_t *d_status, void *stream) {
+    sc::TileGeom g;
+    int rc = sc::tile_geom(sp, g);
+    if (rc) return rc;
+    SC_REQUIRE(g.n_images == 1, "sc_batch_frame: one canvas image per call");
+    SplatConsts c;
+    rc = splat_consts(sp, g, c);
+    if (rc) return rc;
+    SC_REQUIRE(plan && cp, "sc_batch_frame: NULL plan or camera params");
+    SC_REQUIRE(d_tile_start && d_items && d_sat && d_box && d_adc32 && d_ws,
+               "sc_batch_frame: NULL pointer");
+    SC_REQUIRE(plan->d_work && plan->d_tile_field_off && plan->d_field && plan->d_counters &&
+                   plan->n_work >= 0 && plan->n_fields >= 1 && plan->chunk_pixels >= 1 &&
+                   (plan->n_chunks == 0 || plan->d_chunk),
+               "sc_batch_frame: incomplete plan");
+    SC_REQUIRE(!cp->exact && cp->d_poisson_table, "sc_batch_frame: native camera draws only");
+    SC_REQUIRE(cp->nw == sp->nw && cp->nh == sp->nh, "sc_batch_frame: camera %dx%d, canvas %dx%d",
+               cp->nw, cp->nh, sp->nw, sp->nh);
+    if (cp->camera == SC_CAM_CMOS_TABLE)
+        SC_REQUIRE(cp->table_n > 0 && d_table_value && d_table_cdf,
+                   "sc_batch_frame: CMOS table mode needs the noise table");
+    SC_REQUIRE(sp->box_p >= 1 && sp->box_nq >= 12 && sp->box_nq <= 16,
+               "sc_batch_frame: box tables with 12..16 offsets per axis (got %d)", sp->box_nq);
+    SC_REQUIRE_CAP(ws_bytes >= sc_splat_workspace_bytes(sp), "sc_batch_frame: workspace %zu < %zu",
+                   ws_bytes, sc_splat_workspace_bytes(sp));
+    c.box = d_box;
+    c.box_nq = sp->box_nq;
+    c.box_p = sp->box_p;
+    c.box_floats = (int64_t)sp->n_slots * sp->box_p * sp->box_p *
+                   (((int64_t)sp->box_nq * sp->box_nq + 3) & ~3LL);
+    BatchPlanDev b;
+    b.work = plan->d_work;
+    b.tile_field_off = plan->d_tile_field_off;
+    b.tile_field = plan->d_tile_field;
+    b.field = plan->d_field;
+    b.chunk = plan->d_chunk;
+    b.counters = plan->d_counters;
+    b.n_work = plan->n_work;
+    b.n_fields = plan->n_fields;
+    b.n_chunks = plan->n_chunks;
+    b.chunk_pixels = plan->chunk_pixels;
+    b.spin_limit = plan->spin_limit > 0 ? (uint32_t)plan->spin_limit : (1u << 22);
+    b.target_extra = plan->target_extra;
+    BatchCam bc;
+    rc = sc::cam::cam_consts(cp, bc.c);
+    if (rc) return rc;
+    bc.ptab = cp->d_poisson_table;
+    bc.offset_f = d_offset_f;
+    bc.inv_gain_f = d_inv_gain_f;
+    bc.sigma = d_sigma;
+    bc.table_value = d_table_value;
+    bc.table_cdf = d_table_cdf;
+    bc.expect = d_expect;
+    bc.adc32 = d_adc32;
+    cudaStream_t s = sc::as_stream(stream);
+    rc = sc::cuda_status(cudaMemsetAsync(plan->d_counters, 0,
+                                         sizeof(int32_t) * (2 + (size_t)plan->n_fields), s),
+                         "sc_batch_frame: counters");
+    if (rc) return rc;
+    if (plan->n_work == 0) return SC_OK;
+    const float2 *sat = reinterpret_cast<const float2 *>(d_sat);
+    float *ws = static_cast<float *>(d_ws);
+#define SC_BATCH_NQ(NW)                                                                         \
+    switch (c.box_nq) {                                                                         \
+        case 12: return launch_batch<NW, 12>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles,  \
+                                             sp->n_slots, sp->box_stages, ws, b, bc, d_status, s); \
+        case 13: return launch_batch<NW, 13>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles,  \
+                                             sp->n_slots, sp->box_stages, ws, b, bc, d_status, s); \
+        case 14: return launch_batch<NW, 14>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles,  \
+                                             sp->n_slots, sp->box_stages, ws, b, bc, d_status, s); \
+        case 15: return launch_batch<NW, 15>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles,  \
+                                             sp->n_slots, sp->box_stages, ws, b, bc, d_status, s); \
+        default: return launch_batch<NW, 16>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, \
+                                             sp->n_slots, sp->box_stages, ws, b, bc, d_status, s); \
+    }
+    switch (g.warps) {
+        case 2: SC_BATCH_NQ(2)
+        case 4: SC_BATCH_NQ(4)
+        default: SC_BATCH_NQ(8)
+    }
+#undef SC_BATCH_NQ
 }

@@ -576,16 +576,14 @@ class FramePipeline:
         e1.record(st)
         ev.setdefault(name, []).append((e0, e1))
 
-    def camera(self, photons, expect, adc64, adc32=None, seed=0, counter=0, draws=None,
-               stream=None, d_frame=None, photons64=None, expect64=None):
-        """Camera model + ADC on one frame (photons: float32 W*H on the device;
-        with injected draws, photons64 / expect64 are the FP64 photons read and
-        the FP64 expectation written in their place)."""
+    def camera_params(self, seed=0, counter=0, d_frame=None, exact=False):
+        """The camera's parameter block (loads the CMOS noise table when needed)."""
         cfg = self.cfg
-        s = stream_ptr(stream)
+        if self.camera_kind == _lib.CAM_CMOS_TABLE and self.table_value is None:
+            self.load_cmos_table(self.cfg.cmos_table)
         cp = _lib.CameraParams()
         cp.nw, cp.nh, cp.camera = self.nw, self.nh, self.camera_kind
-        cp.exact = 1 if draws is not None else 0
+        cp.exact = 1 if exact else 0
         cp.rounding = 1 if cfg.adc_rounding else 0
         cp.bit = cfg.bit
         cp.qe = float(cfg.qe)
@@ -598,6 +596,16 @@ class FramePipeline:
         cp.seed, cp.counter = int(seed) & (2 ** 64 - 1), int(counter) & (2 ** 64 - 1)
         cp.d_frame = None if d_frame is None else d_frame.data_ptr()
         cp.d_poisson_table = self.poisson.data_ptr()
+        return cp
+
+    def camera(self, photons, expect, adc64, adc32=None, seed=0, counter=0, draws=None,
+               stream=None, d_frame=None, photons64=None, expect64=None):
+        """Camera model + ADC on one frame (photons: float32 W*H on the device;
+        with injected draws, photons64 / expect64 are the FP64 photons read and
+        the FP64 expectation written in their place)."""
+        cfg = self.cfg
+        s = stream_ptr(stream)
+        cp = self.camera_params(seed, counter, d_frame, exact=draws is not None)
         if draws is not None:
             cp.d_photons64 = None if photons64 is None else photons64.data_ptr()
             cp.d_expect64 = None if expect64 is None else expect64.data_ptr()
@@ -621,9 +629,6 @@ class FramePipeline:
                      ptr(inj_uniform), self.n_pix, float(cfg.emgain), ptr(inj_signal),
                      ptr(self.status), s)
                 inj_uniform = None
-        if self.camera_kind == _lib.CAM_CMOS_TABLE and self.table_value is None:
-            self.load_cmos_table(self.cfg.cmos_table)
-            cp.table_n = self.table_value.numel()
         with self.timed("camera", stream):
             maps = self.pixel_maps
             call("sc_camera", cp, ptr(photons), ptr(self.offset) if maps else None,

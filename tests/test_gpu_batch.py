@@ -182,3 +182,68 @@ def test_dense_field_accumulation_within_1e5_of_fp64(sg):
     ref = eng.qe * ref
     rel = numpy.abs(got - ref).max() / numpy.abs(ref).max()
     assert rel <= 1e-5, rel
+
+
+def _batch_pair(sg, fps, **kw):
+    from scopyon_gb300.batch import BatchedFields
+    sizes = [128, 256, 128, 512, 128, 256]
+    counts = [4000, 20, 0, 30000, 900, 7000]
+    D = [1e-15, 1e-12, 3e-13, 5e-14, 1e-13, 1e-12]
+    cfg = config1(sg)
+    out = []
+    for persistent in (False, True):
+        bf = BatchedFields(cfg, sizes, counts, D, frames=12, substeps=5, seed=8,
+                           frames_per_step=fps, persistent=persistent, **kw)
+        bf.pipe.set_tiles(16, 4, 4)
+        out.append(bf)
+    return out
+
+
+@pytest.mark.parametrize("fps,graph", [(1, False), (2, True)])
+def test_persistent_batch_frame_equals_canvas_form(sg, fps, graph):
+    """The persistent launch (work list over tiles and camera chunks, bounded
+    waits for each field's tiles) gives every field's expectation and ADC
+    counts bit for bit as the canvas form (splat, merge, camera launches)."""
+    canvas, persistent = _batch_pair(sg, fps)
+    for bf in (canvas, persistent):
+        bf.graph.use_graph = graph
+    for step in range(3):
+        canvas.step()
+        persistent.step()
+        torch.cuda.synchronize()
+        canvas.pipe.check_status()
+        persistent.pipe.check_status()
+        for k in range(len(canvas.sizes)):
+            for what in ("expect", "adc"):
+                a = canvas.field_image(k, what).cpu().numpy()
+                b = persistent.field_image(k, what).cpu().numpy()
+                numpy.testing.assert_array_equal(a, b, err_msg="field %d %s step %d" % (k, what,
+                                                                                         step))
+    assert persistent.field_image(3, "expect").sum() > 0
+
+
+def test_persistent_batch_wait_runs_out_and_is_reported(sg):
+    """With a field tile count that no tile can reach (test hook) every
+    chunk's bounded wait runs out: status bit 5, SC_ERR_TIMEOUT on the host,
+    and the launch stops; with the hook off the next frame is correct."""
+    from scopyon_gb300 import _lib
+    canvas, persistent = _batch_pair(sg, 1)
+    for bf in (canvas, persistent):
+        bf.graph.use_graph = False
+    persistent.target_extra, persistent.spin_limit = 1, 200
+    persistent.step()
+    torch.cuda.synchronize()
+    assert persistent.pipe.status.cpu().numpy()[0] & 32
+    with pytest.raises(_lib.ScopyonGPUError) as err:
+        persistent.pipe.check_status()
+    assert err.value.code == _lib.SC_ERR_TIMEOUT
+    persistent.target_extra, persistent.spin_limit = 0, 0
+    canvas.step()
+    canvas.step()
+    persistent.step()
+    torch.cuda.synchronize()
+    canvas.pipe.check_status()
+    persistent.pipe.check_status()
+    for k in range(len(canvas.sizes)):
+        numpy.testing.assert_array_equal(canvas.field_image(k, "adc").cpu().numpy(),
+                                         persistent.field_image(k, "adc").cpu().numpy())

@@ -743,6 +743,12 @@ def hbm_stages(dev, peak, steps=20, warmup=3, n_emit=1 << 22, edge=8192, seed=5)
     return out
 
 
+def _tune_names(tune):
+    """Autotuner results keyed by readable names."""
+    return {("%dx%d/%dw/%ds" % (k[0], k[0], k[1], k[2]) if len(k) == 3 else "%s=%s" % k): ms
+            for k, ms in tune.items()}
+
+
 def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=True):
     """field-frames/s of 256 fields (edges 128/256/512 px, emitters log-uniform
     in [10, 50000], D log-uniform in [0.001, 1] um^2/s) batched in one canvas,
@@ -844,14 +850,12 @@ def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=
                 "ms_per_frame_of_all_fields": pers_ms,
                 "field_frames_per_s": n_fields / (pers_ms / 1e3),
                 "over_plain_loop": plain_eager_ms / pers_ms,
-                "autotune_ms_per_frame": {"%dx%d/%dw/%ds" % (t, t, w, st): ms
-                                          for (t, w, st), ms in pers_tune.items()}},
+                "autotune_ms_per_frame": _tune_names(pers_tune)},
             "plain_per_field_loop_ms": plain_eager_ms,
             "plain_per_field_graphs_ms": plain_graph_ms,
             "batched_over_plain_loop": plain_eager_ms / batch_ms,
             "batched_over_plain_graphs": plain_graph_ms / batch_ms,
-            "autotune_ms_per_frame": {"%dx%d/%dw/%ds" % (t, t, w, st): ms
-                                      for (t, w, st), ms in tune.items()},
+            "autotune_ms_per_frame": _tune_names(tune),
             "setup_s": setup_s}
 
 

@@ -425,6 +425,9 @@ typedef struct {
                                     /*   a second's worth)                            */
     int32_t target_extra;           /* test hook: added to every field's tile count,  */
                                     /*   so that the waits run out (status bit 5)     */
+    int32_t blocks_per_sm;          /* resident blocks per SM (0: as many as fit);    */
+                                    /*   fewer leave room for work on other streams   */
+    int32_t pad;
 } ScBatchPlan;
 
 /* Persistent batched frame: one launch of resident blocks that take work

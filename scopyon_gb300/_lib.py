@@ -63,7 +63,8 @@ class BatchPlan(ctypes.Structure):
                 ("d_chunk", ctypes.c_void_p), ("d_counters", ctypes.c_void_p),
                 ("n_work", ctypes.c_int32), ("n_fields", ctypes.c_int32),
                 ("n_chunks", ctypes.c_int32), ("chunk_pixels", ctypes.c_int32),
-                ("spin_limit", ctypes.c_int32), ("target_extra", ctypes.c_int32)]
+                ("spin_limit", ctypes.c_int32), ("target_extra", ctypes.c_int32),
+                ("blocks_per_sm", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class DiffuseParams(ctypes.Structure):

@@ -184,6 +184,7 @@ class BatchedFields:
         self.persistent = bool(persistent)
         self._plan = None  # (tile, halo, ScBatchPlan, device arrays)
         self.spin_limit, self.target_extra = 0, 0  # test hooks of the persistent launch
+        self.blocks_per_sm = 0  # persistent launch: resident blocks per SM (0: all that fit)
         if self.persistent:
             if not 12 <= self.pipe.psf.box_nq <= 16:
                 raise ValueError("the persistent batched frame needs box tables with 12..16 "
@@ -197,7 +198,7 @@ class BatchedFields:
 
     def plan_for(self, pipe):
         """The persistent launch's plan for the pipeline's current tile shape."""
-        key = (pipe.tile, pipe.halo, self.spin_limit, self.target_extra)
+        key = (pipe.tile, pipe.halo, self.spin_limit, self.target_extra, self.blocks_per_sm)
         if self._plan is None or self._plan[0] != key:
             work, off, flat, field, chunk = batch_plan(self.canvas, pipe.tile, pipe.halo,
                                                        self.origins, self.sizes, self.counts)
@@ -218,18 +219,33 @@ class BatchedFields:
             plan.n_work, plan.n_fields = len(work), len(self.sizes)
             plan.n_chunks, plan.chunk_pixels = len(chunk), CHUNK_PIXELS
             plan.spin_limit, plan.target_extra = int(self.spin_limit), int(self.target_extra)
+            plan.blocks_per_sm = int(self.blocks_per_sm)
             self._plan = (key, plan, arrays)
         return self._plan[1]
 
     # ------------------------------------------------------------------
-    def autotune(self, candidates=TILE_CANDIDATES, frames=2):
-        """Time whole batch frames (graph replays) for each (tile, warps)
-        choice; keep the fastest.  Returns {(tile, warps): ms per frame}."""
+    def autotune(self, candidates=TILE_CANDIDATES, frames=2, blocks_per_sm=(0, 4, 3, 2)):
+        """Time whole batch frames (graph replays) for each (tile, warps,
+        copies in flight) choice and keep the fastest; the persistent form then
+        times the launch's resident blocks per SM (fewer leave room for the
+        next frame's records on the side stream).  Returns {choice: ms per
+        frame}, a choice being (tile, warps, stages) or ('blocks_per_sm', n)."""
         times = tune_tiles(self.graph, candidates, frames)
         name = "%dx%d tiles, %d warps, %d stages"
         self.tuning = {name % (t, t, w, st): ms for (t, w, st), ms in times.items()}
         self.tuning["chosen"] = name % (self.pipe.tile, self.pipe.tile, self.pipe.warps,
                                         self.pipe.stages)
+        if self.persistent and len(blocks_per_sm) > 1:
+            per = {}
+            for n in blocks_per_sm:
+                self.blocks_per_sm = n
+                per[n] = tune_tiles(self.graph, [(self.pipe.tile, self.pipe.warps,
+                                                  self.pipe.stages)], frames)[
+                    (self.pipe.tile, self.pipe.warps, self.pipe.stages)]
+                times[("blocks_per_sm", n)] = per[n]
+            self.blocks_per_sm = min(per, key=per.get)
+            self.tuning["blocks_per_sm"] = {str(k): v for k, v in per.items()}
+            self.tuning["chosen_blocks_per_sm"] = self.blocks_per_sm
         return times
 
     def step(self):

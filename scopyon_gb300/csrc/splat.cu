@@ -683,7 +683,7 @@ struct BatchPlanDev {
     int32_t *counters;  // [0] next work entry, [1] stop, [2 + f] tiles done of field f
     int n_work, n_fields, n_chunks, chunk_pixels;
     uint32_t spin_limit;
-    int target_extra;
+    int target_extra, blocks_per_sm;
 };
 
 struct BatchCam {
@@ -908,8 +908,14 @@ int launch_batch(const ScStepRec *recs, const int32_t *tile_start, const int32_t
     cudaError_t e = cudaFuncSetAttribute(batch_frame_kernel<NW, NQ>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return sc::cuda_status(e, "sc_batch_frame: smem attribute");
-    const int grid = sc::resident_grid((const void *)batch_frame_kernel<NW, NQ>, NW * 32, smem,
-                                       (int64_t)b.n_work);
+    int grid = sc::resident_grid((const void *)batch_frame_kernel<NW, NQ>, NW * 32, smem,
+                                 (int64_t)b.n_work);
+    if (b.blocks_per_sm > 0) {
+        int dev = 0, sms = 152;
+        if (cudaGetDevice(&dev) == cudaSuccess)
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        grid = min(grid, max(1, sms * b.blocks_per_sm));
+    }
     batch_frame_kernel<NW, NQ><<<grid, NW * 32, smem, s>>>(recs, tile_start, items, sat, c,
                                                            n_tiles, stages, half_rows,
                                                            table_floats, ws, b, bc, status);
@@ -1084,6 +1090,7 @@ extern "C" int sc_batch_frame(const ScStepRec *d_recs, const int32_t *d_tile_sta
     b.chunk_pixels = plan->chunk_pixels;
     b.spin_limit = plan->spin_limit > 0 ? (uint32_t)plan->spin_limit : (1u << 22);
     b.target_extra = plan->target_extra;
+    b.blocks_per_sm = plan->blocks_per_sm;
     BatchCam bc;
     rc = sc::cam::cam_consts(cp, bc.c);
     if (rc) return rc;

@@ -407,10 +407,9 @@ int sc_splat_fp64(const ScStepRec *d_recs, const double *d_norm, int n_rec, cons
 /* Work plan of the persistent batched frame (sc_batch_frame): fields of view
  * packed into one canvas, and the order in which the launch's blocks take
  * work.  A work entry w >= 0 is tile w (its box and summed-area records
- * into its tile buffer); w < 0 is camera chunk -w - 1 (chunk_pixels pixels
- * of one field: the merge of the covering tile buffers, the expectation and
- * the native camera draws).  Every tile a field's pixels read must come
- * before that field's chunks in the list.                                   */
+ * into its tile buffer); w < 0 is chunk -w - 1 (chunk_pixels pixels of one
+ * field: the merge of the covering tile buffers).  Every tile a field's
+ * pixels read must come before that field's chunks in the list.             */
 typedef struct {
     const int32_t *d_work;          /* [n_work] tile indices and -(chunk + 1)         */
     const int32_t *d_tile_field_off;/* [n_tiles + 1] CSR: fields whose pixels read   */
@@ -435,8 +434,9 @@ typedef struct {
  * tile's box records (bulk copies, as sc_splat) and summed-area records into
  * its tile buffer in d_ws (sc_splat_workspace_bytes) and advances the tile
  * counters of the fields that read it; a chunk entry waits (bounded poll)
- * until its field's tiles are done, then merges, forms the expectation and
- * draws the native camera (d_poisson_table required) for its pixels.  The
+ * until its field's tiles are done, then merges its pixels into d_expect.
+ * A second launch then draws the native camera (d_poisson_table required)
+ * on the fields' pixels, the expectation replacing the photons.  The
  * wait always ends: a field's tiles are taken before its chunks, and a
  * block that took a tile finishes it without waiting on anything.  Per
  * pixel, the results equal sc_splat followed by sc_camera on the canvas

@@ -719,32 +719,10 @@ __device__ __forceinline__ float merge_pixel(const float *ws, const SplatConsts 
     return sum;
 }
 
-// The native camera of one pixel (the camera kind is uniform across a launch).
-__device__ __forceinline__ float batch_adc(const BatchCam &bc, const sc::cam::PoisTab &t, int p,
-                                           float ef, uint64_t counter, int32_t *status) {
-    using namespace sc::cam;
-    const CamConsts &c = bc.c;
-    const float sg = (c.camera == SC_CAM_SCMOS && bc.sigma) ? __ldg(bc.sigma + p) : c.readout_f;
-    const float g = bc.inv_gain_f ? __ldg(bc.inv_gain_f + p) : c.inv_gain0_f;
-    const float o = bc.offset_f ? __ldg(bc.offset_f + p) : c.offset0_f;
-    switch (c.camera) {
-        case SC_CAM_EMCCD:
-            return native_adc<SC_CAM_EMCCD>(c, t, p, ef, sg, g, o, counter, bc.table_value,
-                                            bc.table_cdf, status);
-        case SC_CAM_CCD:
-            return native_adc<SC_CAM_CCD>(c, t, p, ef, sg, g, o, counter, bc.table_value,
-                                          bc.table_cdf, status);
-        case SC_CAM_CMOS_TABLE:
-            return native_adc<SC_CAM_CMOS_TABLE>(c, t, p, ef, sg, g, o, counter, bc.table_value,
-                                                 bc.table_cdf, status);
-        default:
-            return native_adc<SC_CAM_SCMOS>(c, t, p, ef, sg, g, o, counter, bc.table_value,
-                                            bc.table_cdf, status);
-    }
-}
-
 // Resident blocks take work entries in plan order from b.counters[0] until
-// the list is done.  Tile entry: the tile's box records through each warp's
+// the list is done.  An entry is claimed only when the block is free to work
+// on it (claiming the next one ahead would let a block hold a tile that other
+// blocks' chunks wait for while it is busy, measured 4x slower).  Tile entry: the tile's box records through each warp's
 // copy ring (the ring and its mbarriers live for the whole launch), the
 // buffer written, then the tile's summed-area records added (both sums as
 // splat_box_bulk_kernel and splat_sat_kernel form them), then the tile
@@ -776,8 +754,6 @@ batch_frame_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict
     if (threadIdx.x == 0) sh_stop = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     __syncthreads();
-    const sc::cam::PoisTab ptab = sc::cam::pois_tab(bc.ptab);
-    const uint64_t counter = bc.c.counter + (bc.c.frame ? (uint64_t)*bc.c.frame : 0);
     uint32_t phase = 0;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -868,16 +844,43 @@ batch_frame_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict
             }
             __syncthreads();
             if (sh_stop) break;
+            // the merged photons of the chunk's pixels, into the expectation
+            // buffer; batch_camera_kernel turns them into the expectation and
+            // the ADC counts at full occupancy
             const int last = min(first + b.chunk_pixels, edge * edge);
             for (int q = first + threadIdx.x; q < last; q += blockDim.x) {
                 const int li = q / edge;
                 const int i = i0 + li, j = j0 + (q - li * edge);
-                const int p = i * c.nh + j;
-                const float ph = merge_pixel(ws, c, i, j);
-                const float ef = bc.c.qe_f * (ph + bc.c.background_f);
-                if (bc.expect) bc.expect[p] = ef;
-                bc.adc32[p] = batch_adc(bc, ptab, p, ef, counter, status);
+                bc.expect[i * c.nh + j] = merge_pixel(ws, c, i, j);
             }
+        }
+    }
+}
+
+// The camera of the fields' pixels: a block per chunk, the photons the
+// persistent kernel merged (in the expectation buffer) turned into the
+// expectation and the ADC counts.
+template <int CAM>
+__global__ void __launch_bounds__(256)
+batch_camera_kernel(BatchPlanDev b, BatchCam bc, int nh, int32_t *status) {
+    if (*(volatile const int32_t *)(b.counters + 1)) return;  // the frame was stopped
+    const sc::cam::PoisTab ptab = sc::cam::pois_tab(bc.ptab);
+    const uint64_t counter = bc.c.counter + (bc.c.frame ? (uint64_t)*bc.c.frame : 0);
+    for (int k = blockIdx.x; k < b.n_chunks; k += gridDim.x) {
+        const int f = b.chunk[2 * k], first = b.chunk[2 * k + 1];
+        const int i0 = b.field[4 * f], j0 = b.field[4 * f + 1], edge = b.field[4 * f + 2];
+        const int last = min(first + b.chunk_pixels, edge * edge);
+        for (int q = first + threadIdx.x; q < last; q += blockDim.x) {
+            const int li = q / edge;
+            const int p = (i0 + li) * nh + j0 + (q - li * edge);
+            const float ef = bc.c.qe_f * (bc.expect[p] + bc.c.background_f);
+            bc.expect[p] = ef;
+            const float sg =
+                (CAM == SC_CAM_SCMOS && bc.sigma) ? __ldg(bc.sigma + p) : bc.c.readout_f;
+            const float g = bc.inv_gain_f ? __ldg(bc.inv_gain_f + p) : bc.c.inv_gain0_f;
+            const float o = bc.offset_f ? __ldg(bc.offset_f + p) : bc.c.offset0_f;
+            bc.adc32[p] = sc::cam::native_adc<CAM>(bc.c, ptab, p, ef, sg, g, o, counter,
+                                                   bc.table_value, bc.table_cdf, status);
         }
     }
 }
@@ -919,7 +922,22 @@ int launch_batch(const ScStepRec *recs, const int32_t *tile_start, const int32_t
     batch_frame_kernel<NW, NQ><<<grid, NW * 32, smem, s>>>(recs, tile_start, items, sat, c,
                                                            n_tiles, stages, half_rows,
                                                            table_floats, ws, b, bc, status);
-    return sc::launch_status("sc_batch_frame");
+    int rc = sc::launch_status("sc_batch_frame");
+    if (rc || b.n_chunks == 0) return rc;
+    switch (bc.c.camera) {
+#define SC_BATCH_CAM(K)                                                                         \
+    case K:                                                                                     \
+        batch_camera_kernel<K><<<sc::resident_grid((const void *)batch_camera_kernel<K>, 256, 0, \
+                                                   (int64_t)b.n_chunks),                        \
+                                 256, 0, s>>>(b, bc, c.nh, status);                             \
+        break;
+        SC_BATCH_CAM(SC_CAM_EMCCD)
+        SC_BATCH_CAM(SC_CAM_CCD)
+        SC_BATCH_CAM(SC_CAM_CMOS_TABLE)
+        SC_BATCH_CAM(SC_CAM_SCMOS)
+#undef SC_BATCH_CAM
+    }
+    return sc::launch_status("sc_batch_frame camera");
 }
 
 int splat_consts(const ScSplatParams *p, const sc::TileGeom &g, SplatConsts &c) {
@@ -1056,7 +1074,7 @@ extern "C" int sc_batch_frame(const ScStepRec *d_recs, const int32_t *d_tile_sta
     rc = splat_consts(sp, g, c);
     if (rc) return rc;
     SC_REQUIRE(plan && cp, "sc_batch_frame: NULL plan or camera params");
-    SC_REQUIRE(d_tile_start && d_items && d_sat && d_box && d_adc32 && d_ws,
+    SC_REQUIRE(d_tile_start && d_items && d_sat && d_box && d_adc32 && d_expect && d_ws,
                "sc_batch_frame: NULL pointer");
     SC_REQUIRE(plan->d_work && plan->d_tile_field_off && plan->d_field && plan->d_counters &&
                    plan->n_work >= 0 && plan->n_fields >= 1 && plan->chunk_pixels >= 1 &&

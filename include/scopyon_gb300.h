@@ -370,6 +370,42 @@ int sc_diffusion_dD(const float *d_pos, const float *d_emit, int n, int T,
                     const float *d_grad_pos, const float *d_D, void *d_scratch,
                     size_t scratch_bytes, double *d_dD, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Differentiable Born-Wolf image (new: the reference has no gradients).  The
+ * reference's Born-Wolf image (overlay_signal_ with the 1-nm depth-keyed
+ * grids, src/scopyon/_epifm.py:76-126, :181-213, :224-282) made continuous:
+ * each grid value fills a 1-nm cell and a pixel integrates that
+ * piecewise-constant function exactly (bilinear interpolation of the grid's
+ * 2-D prefix sum at the pixel corners, evaluated in FP64 from the quadrant
+ * tables of sc_psf_quadrant_sat); the two depth keys around
+ * |z - z_focal| / res are blended linearly (the last key, key_hi, beyond the
+ * cutoff); TIRF excitation A(z) = exp(-|z - z_focal| inv_pen) (:1281-1289):
+ *   mu[f][i][j] = bg[f] + sum_e I_e A(z_e) cnorm B_e(i, j).
+ * Emitters are float4 (x, y: metres from the image centre; z; I: photons),
+ * [n_frames][n_emit].                                                        */
+typedef struct {
+    int32_t nw, nh, n_frames, n_emit;
+    int32_t n_r, sat_pitch;  /* quadrant tables: (n_r + 1) rows of sat_pitch float2  */
+    int32_t key_hi;          /* depth keys 0 .. key_hi have tables (key_hi = cutoff / res) */
+    int32_t pad;
+    double px, res, inv_pen, z_focal;
+    double cnorm;            /* psf_normalization * res^2                              */
+    const int32_t *d_key_slot; /* table slot of each depth key (-1: not built)         */
+} ScBWParams;
+
+/* FP64 work buffer of sc_bw_forward: n_frames * nw * nh doubles. */
+size_t sc_bw_work_bytes(const ScBWParams *p);
+
+/* Forward: d_mu [n_frames][nw][nh] FP32 (FP64 accumulation in d_work). */
+int sc_bw_forward(const ScBWParams *p, const float *d_emit, const float *d_bg, const float *d_sat,
+                  void *d_work, size_t work_bytes, float *d_mu, int32_t *d_status, void *stream);
+
+/* Adjoint: d_grad_emit [n_frames][n_emit] float4 = (dL/dx, dL/dy, dL/dz, dL/dI)
+ * from d_grad_mu = dL/dmu; each emitter's sums in a fixed order.  dL/dbg is
+ * the per-frame sum of dL/dmu (sc_segment_sum).                              */
+int sc_bw_backward(const ScBWParams *p, const float *d_emit, const float *d_sat,
+                   const float *d_grad_mu, float *d_grad_emit, int32_t *d_status, void *stream);
+
 /* Largest tile count (tiles per image x images) sc_bin_steps_static takes. */
 #define SC_BIN_STATIC_MAX_TILES 65536
 

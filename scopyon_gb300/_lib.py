@@ -67,6 +67,15 @@ class BatchPlan(ctypes.Structure):
                 ("blocks_per_sm", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
+class BWParams(ctypes.Structure):
+    _fields_ = [("nw", ctypes.c_int32), ("nh", ctypes.c_int32), ("n_frames", ctypes.c_int32),
+                ("n_emit", ctypes.c_int32), ("n_r", ctypes.c_int32), ("sat_pitch", ctypes.c_int32),
+                ("key_hi", ctypes.c_int32), ("pad", ctypes.c_int32), ("px", ctypes.c_double),
+                ("res", ctypes.c_double), ("inv_pen", ctypes.c_double),
+                ("z_focal", ctypes.c_double), ("cnorm", ctypes.c_double),
+                ("d_key_slot", ctypes.c_void_p)]
+
+
 class DiffuseParams(ctypes.Structure):
     _fields_ = [("n_particles", ctypes.c_int32), ("n_sub", ctypes.c_int32),
                 ("ndim", ctypes.c_int32), ("boundary", ctypes.c_int32),
@@ -119,6 +128,10 @@ _SIG = {
     "sc_camera": (_I, [ctypes.POINTER(CameraParams), _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                        _P, _P, _P, _P, _P]),
     "sc_emccd_exact": (_I, [_P, _D, _D, _P, _I, _D, _P, _P, _P]),
+    "sc_bw_work_bytes": (ctypes.c_size_t, [ctypes.POINTER(BWParams)]),
+    "sc_bw_forward": (_I, [ctypes.POINTER(BWParams), _P, _P, _P, _P, ctypes.c_size_t, _P, _P,
+                           _P]),
+    "sc_bw_backward": (_I, [ctypes.POINTER(BWParams), _P, _P, _P, _P, _P, _P]),
     "sc_log_cube": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _I, _P, ctypes.c_size_t, _P, _P]),
     "sc_log_peaks": (_I, [_P, _I, _I, _I, _D, _P, _P, _I, _P]),
     "sc_poisson_table_bytes": (ctypes.c_size_t, []),

@@ -158,7 +158,9 @@ class BornWolfImageModel:
     the exact integral over its extent, and the two depth keys around
     ``|z - z_focal|`` are blended linearly, so that x, y and z all have
     gradients.  It differs from the reference's rounded bounds by a fraction
-    of one 1-nm cell at each pixel edge.
+    of one 1-nm cell at each pixel edge.  Intensities are the photons an
+    emitter in focus puts on its whole 1999-nm grid (the grid keeps the
+    reference's constant floor past the radial cutoff, _epifm.py:123).
     """
 
     def __init__(self, config, device=None):
@@ -180,7 +182,17 @@ class BornWolfImageModel:
         self.z_focal = float(self.eng.focal_point[0])
         self.res = 1e-9
         self.key_hi = int(round(self.eng.depth_cutoff / self.res))
-        self.cnorm = float(self.eng.psf_normalization) * self.res * self.res
+        # intensity = photons of an emitter in focus over its whole 1999-nm
+        # grid: cnorm is one over the in-focus grid's sum (the full-grid prefix
+        # S(n_signal, n_signal) from the quadrant table, 4 G[n][n] - 2 G[n][1]
+        # - 2 G[1][n] + G[1][1] with n = n_r)
+        self.psf.ensure([0])
+        n = self.psf.n_r
+        slot = self.psf.slot_of[0]
+        tab = self.psf.tables[slot * self.psf.table_floats: (slot + 1) * self.psf.table_floats]
+        G = tab.view(n + 1, self.psf.pitch, 2).double().sum(-1)
+        total = float(4 * G[n, n] - 2 * G[n, 1] - 2 * G[1, n] + G[1, 1])
+        self.cnorm = 1.0 / total
 
     def ensure_keys(self, emitters):
         """Build the tables of every depth key the emitters' |z - z_focal| needs."""

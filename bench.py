@@ -371,6 +371,9 @@ def summary(r):
             "over_forward": round(fb["headline"]["fwd_bwd_over_forward"], 2)}
         out["dL_dD_100k_T100_over_forward"] = round(
             fb["diffusion_dD_100k_2048px_T100"]["fwd_bwd_over_forward"], 2)
+        out["fwd_bwd_born_wolf_512px_20k"] = {
+            "frames_per_s": round(fb["born_wolf_512px_20k"]["fwd_bwd_frames_per_s"], 1),
+            "over_forward": round(fb["born_wolf_512px_20k"]["fwd_bwd_over_forward"], 2)}
     bt = r.get("batched")
     if bt:
         out["batched_over_per_field_loop"] = round(bt["batched_over_plain_loop"], 2)
@@ -523,6 +526,45 @@ def diffusion_grad_case(dev, n_emit, image, T, steps, warmup, seed):
             "emitter_steps_per_s_fwd_bwd": n_emit * T / (fb_ms / 1e3)}
 
 
+def born_wolf_fwd_bwd_case(dev, steps, warmup, seed=15, n_emit=N_EMIT):
+    """Forward and forward + Poisson NLL + adjoint of the differentiable
+    Born-Wolf image on the workload's frame: 512^2 px of 160 nm, 20k emitters
+    with z in +-1 um (about 1,000 depth keys), TRITC."""
+    import torch
+    from scopyon_gb300 import differentiable as dm
+    rng = numpy.random.RandomState(seed)
+    model = dm.BornWolfImageModel(workload_config(), device=dev)
+    e = numpy.zeros((1, n_emit, 4), dtype=numpy.float32)
+    e[..., 0] = rng.uniform(-HALF, HALF, (1, n_emit))
+    e[..., 1] = rng.uniform(-HALF, HALF, (1, n_emit))
+    e[..., 2] = rng.uniform(-Z_HALF, Z_HALF, (1, n_emit))
+    e[..., 3] = rng.lognormal(math.log(2000.0), 0.3, (1, n_emit))
+    emit = torch.tensor(e, device=dev).requires_grad_(True)
+    bg = torch.full((1,), 10.0, device=dev).requires_grad_(True)
+    model.ensure_keys(emit.detach())
+    with torch.no_grad():
+        counts = torch.poisson(dm.born_wolf_image(emit, bg, model).double(),
+                               generator=torch.Generator(dev).manual_seed(seed)).float()
+
+    def forward():
+        with torch.no_grad():
+            return dm.born_wolf_image(emit, bg, model)
+
+    def step():
+        loss = dm.poisson_nll(dm.born_wolf_image(emit, bg, model), counts)
+        return torch.autograd.grad(loss, [emit, bg])
+
+    fwd_ms = _event_ms(forward, steps, warmup)
+    fb_ms = _event_ms(step, steps, warmup)
+    return {"model": "differentiable Born-Wolf image (cells integrated over each pixel, "
+                     "adjacent depth keys blended)", "emitters": n_emit,
+            "image": [IMAGE, IMAGE], "forward_ms": fwd_ms, "fwd_bwd_ms": fb_ms,
+            "fwd_bwd_over_forward": fb_ms / fwd_ms,
+            "fwd_bwd_frames_per_s": 1e3 / fb_ms,
+            "timing": "eager launches with CUDA events (the forward checks the depth keys "
+                      "on the host)"}
+
+
 def fwd_bwd_arm(args, dev):
     """fwd+bwd frames/s of the differentiable image at 512^2 px, 20k emitters, and
     on a batch of 64 frames of 128^2 px with 200 emitters each."""
@@ -530,6 +572,7 @@ def fwd_bwd_arm(args, dev):
     headline = fwd_bwd_case(dev, 1, N_EMIT, IMAGE, 90e-9, math.inf, 1e-6, steps, args.warmup, 5)
     batch = fwd_bwd_case(dev, 64, 200, 128, 120e-9, 300e-9, 0.5e-6, steps, args.warmup, 6)
     dgrad = diffusion_grad_case(dev, 100000, 2048, 100, max(5, args.steps // 4), args.warmup, 9)
+    bw = born_wolf_fwd_bwd_case(dev, max(10, args.steps), args.warmup)
     return {"value": headline["fwd_bwd_frames_per_s"], "unit": "frames/s",
             "model": "the differentiable Gaussian-PSF model (pixel-integrated Gaussians, "
                      "TIRF depth factor), not the Born-Wolf frame path",
@@ -537,7 +580,8 @@ def fwd_bwd_arm(args, dev):
                         "FP64 Poisson NLL, adjoint (dL/dx, dy, dz, dI, dbg, dsigma); one CUDA "
                         "graph replay per step",
             "dtype": "f32 (FP64 loss reduction)", "headline": headline,
-            "batch_64x128px_200": batch, "diffusion_dD_100k_2048px_T100": dgrad}
+            "batch_64x128px_200": batch, "diffusion_dD_100k_2048px_T100": dgrad,
+            "born_wolf_512px_20k": bw}
 
 
 # ------------------------------------------------------------- batched form
@@ -1055,12 +1099,14 @@ def main():
     ap.add_argument("--warps", type=int, default=4, help="warps per splat tile with --tile")
     ap.add_argument("--stages", type=int, default=4,
                     help="box-table block copies in flight per splat warp with --tile")
-    ap.add_argument("--case", choices=["dgrad", "batched", "fwdbwd", "stages"], default=None,
+    ap.add_argument("--case", choices=["dgrad", "batched", "fwdbwd", "stages", "bwdiff"],
+                    default=None,
                     help="profiling: run one workload alone and print its result object "
                          "(dgrad: dL/dD at 100k emitters x 100 sub-steps on 2048^2 px; "
                          "batched: the 256-field canvas without the per-field loop; "
                          "fwdbwd: the differentiable image at 512^2 px, 20k emitters; "
-                         "stages: the diffusion and camera kernels alone beyond L2)")
+                         "stages: the diffusion and camera kernels alone beyond L2; "
+                         "bwdiff: the differentiable Born-Wolf image at 512^2 px, 20k emitters)")
     ap.add_argument("--small", action="store_true",
                     help="profiling case: depth range +-0.1 um between reflecting walls and "
                          "D = 0.01 um^2/s for all emitters (102 PSF keys, 2.9 GB of tables), "
@@ -1085,6 +1131,8 @@ def main():
             res = hbm_stages(dev, load_peaks()[0], args.steps, args.warmup,
                              n_emit=1 << (20 if args.small else 22),
                              edge=4096 if args.small else 8192)
+        elif args.case == "bwdiff":
+            res = born_wolf_fwd_bwd_case(dev, args.steps, args.warmup)
         elif args.case == "fwdbwd":
             res = fwd_bwd_case(dev, 1, N_EMIT, IMAGE, 90e-9, math.inf, 1e-6, args.steps,
                                args.warmup, 5)

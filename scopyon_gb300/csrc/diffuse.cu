@@ -138,27 +138,36 @@ __device__ __forceinline__ int transition(const DiffConsts &c, int cls, int i, i
     return next_class(c.trans + ((size_t)s * c.n_class + cls) * c.n_class, c.n_class, u);
 }
 
-// One sub-step of a particle: x_d += sigma_d * n_d on every axis (the
-// reference's 0.0 + sigma * gauss; normals from the caller's nv, else the
-// FP32 Philox normals nrm), then the walls.  The axes are independent, so
-// moving and wrapping one axis at a time equals moving all, then wrapping.
-// The loop runs over a fixed 3 (ndim is 2 or 3) so that p stays in registers.
+// One sub-step of one axis d of a particle: x += sigma_d * n_d (the
+// reference's 0.0 + sigma * gauss; the normal from the caller's nv, else the
+// FP32 Philox normal), then the walls of the particle's class on that axis.
 // kInjected selects the normals at compile time: as a run-time test the
 // compiler predicates both forms, and the FP64 pipe (about 1/64 of the FP32
 // rate on GB300) then issues the injected form's multiply and add as well.
+template <bool kInjected>
+__device__ __forceinline__ double move_axis(const DiffConsts &c, double x, int d, int cls,
+                                            double sg, double nv, float nrm) {
+    if (kInjected) x += __dmul_rn(sg, nv);
+    else x = fma(sg, sc::f2d_exact(nrm), x);
+    if (c.boundary) {
+        double lo, hi;
+        class_walls(c, cls, d, lo, hi);
+        x = wrap_axis(x, lo, hi, c.boundary);
+    }
+    return x;
+}
+
+// One sub-step of a particle on every axis.  The axes are independent, so
+// moving and wrapping one axis at a time equals moving all, then wrapping.
+// The loop runs over a fixed 3 (ndim is 2 or 3) so that p stays in registers.
 template <bool kInjected>
 __device__ __forceinline__ void move_point(const DiffConsts &c, double *p, int cls,
                                            const double *sg, const double *nv, const float *nrm) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         if (d >= c.ndim) break;
-        if (kInjected) p[d] += __dmul_rn(sg[d], nv[d]);
-        else p[d] = fma(sg[d], sc::f2d_exact(nrm[d]), p[d]);
-        if (c.boundary) {
-            double lo, hi;
-            class_walls(c, cls, d, lo, hi);
-            p[d] = wrap_axis(p[d], lo, hi, c.boundary);
-        }
+        p[d] = move_axis<kInjected>(c, p[d], d, cls, sg[d], kInjected ? nv[d] : 0.0,
+                                    kInjected ? 0.f : nrm[d]);
     }
 }
 
@@ -224,25 +233,38 @@ diffuse_kernel(DiffConsts c, double *pos, int32_t *klass, const double *sigma,
     if (c.trans) klass[i] = k;
 }
 
-// Native frame records for 32 particles per CTA, in three phases per chunk of
-// up to 32 sub-steps:
-//   1. all warps draw the Philox normals of every (sub-step, particle); under
-//      EPI (amplitude independent of depth) the emitted photons and the
-//      normalisation of each sub-step are computed once;
-//   2. warp 0, one lane per particle, runs the position chain and the
-//      photon-budget chain in sub-step order with the operations of
-//      diffuse_kernel and emitter_physics_kernel, storing each sub-step's
-//      position and normalisation in shared memory;
-//   3. all warps build the records, a warp per sub-step and a lane per
+// Native frame records for 32 particles per CTA, in phases per chunk of up to
+// 32 sub-steps:
+//   1. all warps draw the Philox normals of every (sub-step, particle); when
+//      the excitation does not depend on the particle (EPI, or a flat field
+//      whose depth is always 0) the last warp computes the emitted photons
+//      and the normalisation of each sub-step once;
+//   2. the position chains, in sub-step order with the operations of
+//      diffuse_kernel, one lane per particle, storing each sub-step's
+//      position in shared memory.  Without class transitions the axes are
+//      independent chains and warp d runs axis d; with transitions warp 0
+//      runs all axes and the class.  When the excitation is uniform the last
+//      warp runs the photon-budget chains meanwhile (one subtraction per
+//      sub-step), zeroing the normalisation of the sub-steps at which a
+//      particle is bleached;
+//   3. otherwise (TIRF with depth) all warps, a warp per sub-step and a lane
+//      per particle, evaluate the excitation, the emitted photons and the
+//      normalisation of every (sub-step, particle): the FP64 exponentials and
+//      divisions, independent of one another, run on every warp instead of
+//      on a chain; then, with bleaching, warp 0 runs the budget chains;
+//   4. all warps build the records, a warp per sub-step and a lane per
 //      particle (32 consecutive records, coalesced stores).
 // The records equal those of sc_diffuse_steps followed by sc_emitter_steps bit
-// for bit.  FP64 work runs with full warps only (GB300's FP64 rate is ~1/64 of
-// FP32, so a warp with a few active lanes wastes it).
+// for bit: every quantity is formed by the same FP64 expression as there.
+// FP64 work runs with full warps only (GB300's FP64 rate is ~1/64 of FP32, so
+// a warp with a few active lanes wastes it).
 constexpr int kRecWarps = 4;
 
 // Shared memory of one CTA for `chunk` sub-steps: positions [chunk][32][3] and
-// normalisations [chunk][32] (FP64), per-sub-step photons and live-emitter
-// normalisation [chunk] (FP64), normals [chunk][32][3] (FP32).
+// normalisations [chunk][32] (FP64), per-sub-step photons and normalisation
+// [chunk] (FP64), normals [chunk][32][3] (FP32).  The emitted photons of each
+// (sub-step, particle) [chunk][32] (FP64, phase 3) reuse the normals' space,
+// which the position chains have consumed by then.
 inline size_t rec_shared_bytes(int chunk) {
     return (size_t)chunk * (32 * 3 * sizeof(double) + 32 * sizeof(double) + 2 * sizeof(double) +
                             32 * 3 * sizeof(float));
@@ -263,28 +285,36 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
     double *s_emit = s_norm + chunk * 32;
     double *s_norm1 = s_emit + chunk;
     float *s_nrm = reinterpret_cast<float *>(s_norm1 + chunk);
+    double *s_e = s_norm1 + chunk;  // [chunk][32], over the normals after phase 2
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * 32 + lane;  // this lane's particle
     const bool live = i < c.n;
     const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
+    // the excitation is the same for every particle: EPI, or a flat field
+    // (format_point gives depth 0.0, so the depth offset is -focal[0])
     const bool epi = isinf(k.penetration);
+    const bool uniform = epi || c.ndim == 2;
+    const bool axis_chains = c.trans == nullptr;
+    const int budget_warp = uniform ? kRecWarps - 1 : 0;
+    // chain state: axis `warp` (axis chains) or every axis and the class (warp
+    // 0 otherwise); the photon budget on budget_warp
     double p[3] = {0.0, 0.0, 0.0}, b = 0.0;
-    // last depth offset and unit time seen by this lane's chain, with their
-    // photons and normalisation: a particle whose depth does not change
-    // (two-dimensional inputs) evaluates the TIRF exponential once
-    double rel_prev = nan(""), ut_prev = nan(""), amp_prev = 0.0, emit_prev = 0.0;
-    double norm_prev = 0.0;
     int cls = 0;
-    if (warp == 0 && live) {
-        p[0] = pos[3 * i];
-        p[1] = pos[3 * i + 1];
-        p[2] = pos[3 * i + 2];
-        b = k.bleaching ? budget[i] : 0.0;
-        cls = klass ? klass[i] : 0;
+    if (live) {
+        if (axis_chains && warp < c.ndim) {
+            p[0] = pos[3 * i + warp];  // an axis chain keeps its coordinate in p[0]
+            cls = klass ? klass[i] : 0;
+        } else if (!axis_chains && warp == 0) {
+            p[0] = pos[3 * i];
+            p[1] = pos[3 * i + 1];
+            p[2] = pos[3 * i + 2];
+            cls = klass[i];
+        }
+        if (warp == budget_warp && k.bleaching) b = budget[i];
     }
     for (int s0 = 0; s0 < c.n_sub; s0 += chunk) {
         const int ns = min(chunk, c.n_sub - s0);
-        // 1. normals; per-sub-step photons and normalisation under EPI
+        // 1. normals; per-sub-step photons and normalisation when uniform
         if (!kInjected) {
             for (int j = warp; j < ns; j += kRecWarps) {
                 float nrm[3] = {0.f, 0.f, 0.f};
@@ -295,68 +325,115 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                 d[2] = nrm[2];
             }
         }
-        if (epi && warp == kRecWarps - 1) {
+        if (uniform && warp == kRecWarps - 1) {
+            const double amp =
+                epi ? k.amplitude0
+                    : __dmul_rn(k.amplitude0, exp(-fabs(0.0 - k.focal[0]) / k.penetration));
             for (int j = lane; j < ns; j += 32) {
-                const double n_emit = sc::emit_photons(k, k.amplitude0, unit_time[s0 + j]);
+                const double n_emit = sc::emit_photons(k, amp, unit_time[s0 + j]);
                 s_emit[j] = n_emit;
                 // p_state = 1: __dmul_rn(1.0, n_emit) is n_emit
                 s_norm1[j] = __dmul_rn(k.norm_coeff, n_emit / (4.0 * M_PI));
             }
         }
         __syncthreads();
-        // 2. the chains, one lane per particle
-        if (warp == 0 && live) {
-            for (int j = 0; j < ns; ++j) {
-                const int s = s0 + j;
-                double *ps = s_pos + (j * 32 + lane) * 3;
-                ps[0] = p[0];
-                ps[1] = p[1];
-                ps[2] = p[2];
-                double n_emit;
-                if (epi) {
-                    n_emit = s_emit[j];
-                } else {
-                    double f[3];
-                    format_point(c, p, f);
-                    const double rel0 = f[0] - k.focal[0];
-                    const double ut = unit_time[s];
-                    if (rel0 != rel_prev) {  // NaN never compares equal: first step
-                        amp_prev = __dmul_rn(k.amplitude0, exp(-fabs(rel0) / k.penetration));
-                        rel_prev = rel0;
-                        ut_prev = nan("");
+        // 2. the position chains (and the budget chains when uniform)
+        if (live) {
+            if (axis_chains && warp < c.ndim) {
+                const int d = warp;
+                double x = p[0];
+                const double *sgd = sigma + (size_t)cls * 3 + d;
+                const size_t sg_step = (size_t)c.n_class * 3;
+                // the next sub-step's sigma and normal are loaded a step ahead
+                double sg = sgd[(size_t)s0 * sg_step];
+                double nv = kInjected ? normals[((size_t)s0 * c.n + i) * c.ndim + d] : 0.0;
+                float nr = kInjected ? 0.f : s_nrm[lane * 3 + d];
+                for (int j = 0; j < ns; ++j) {
+                    const int s = s0 + j;
+                    s_pos[(j * 32 + lane) * 3 + d] = x;
+                    double sg_n = 0.0, nv_n = 0.0;
+                    float nr_n = 0.f;
+                    if (j + 1 < ns) {
+                        sg_n = sgd[(size_t)(s + 1) * sg_step];
+                        if (kInjected) nv_n = normals[((size_t)(s + 1) * c.n + i) * c.ndim + d];
+                        else nr_n = s_nrm[((j + 1) * 32 + lane) * 3 + d];
                     }
-                    if (ut != ut_prev) {
-                        emit_prev = sc::emit_photons(k, amp_prev, ut);
-                        norm_prev = __dmul_rn(k.norm_coeff, emit_prev / (4.0 * M_PI));
-                        ut_prev = ut;
-                    }
-                    n_emit = emit_prev;
+                    x = move_axis<kInjected>(c, x, d, cls, sg, nv, nr);
+                    sg = sg_n;
+                    nv = nv_n;
+                    nr = nr_n;
                 }
-                bool alive = true;
-                if (k.bleaching) {
-                    double nb = b - n_emit;
-                    if (nb <= 0) {
-                        nb = 0;
-                        alive = false;
-                    }
-                    b = nb;
+                p[0] = x;
+            } else if (!axis_chains && warp == 0) {
+                for (int j = 0; j < ns; ++j) {
+                    const int s = s0 + j;
+                    double *ps = s_pos + (j * 32 + lane) * 3;
+                    ps[0] = p[0];
+                    ps[1] = p[1];
+                    ps[2] = p[2];
+                    const double *sg = sigma + ((size_t)s * c.n_class + cls) * 3;
+                    move_point<kInjected>(
+                        c, p, cls, sg, kInjected ? normals + ((size_t)s * c.n + i) * c.ndim : nullptr,
+                        s_nrm + (j * 32 + lane) * 3);
+                    cls = transition(c, cls, i, s, (uint64_t)(step0 + s));
                 }
+            }
+            if (uniform && warp == kRecWarps - 1) {
                 // p_state = 0 gives norm_coeff * (0 / 4 pi) = 0: no record
-                s_norm[j * 32 + lane] = !alive ? 0.0 : (epi ? s_norm1[j] : norm_prev);
-                const double *sg = sigma + ((size_t)s * c.n_class + cls) * 3;
-                move_point<kInjected>(c, p, cls, sg,
-                                      kInjected ? normals + ((size_t)s * c.n + i) * c.ndim : nullptr,
-                                      s_nrm + (j * 32 + lane) * 3);
-                if (c.trans) cls = transition(c, cls, i, s, (uint64_t)(step0 + s));
+                for (int j = 0; j < ns; ++j) {
+                    double norm = s_norm1[j];
+                    if (k.bleaching) {
+                        double nb = b - s_emit[j];
+                        if (nb <= 0) {
+                            nb = 0;
+                            norm = 0.0;
+                        }
+                        b = nb;
+                    }
+                    s_norm[j * 32 + lane] = norm;
+                }
             }
         }
         __syncthreads();
-        // 3. records: warp w takes sub-steps w, w + kRecWarps, ...
+        // 3. excitation, photons and normalisation of every (sub-step,
+        // particle) when they depend on its depth; then the budget chains
+        if (!uniform) {
+            if (live) {
+                for (int j = warp; j < ns; j += kRecWarps) {
+                    const double *ps = s_pos + (j * 32 + lane) * 3;
+                    const double q[3] = {ps[0], ps[1], ps[2]};
+                    double f[3];
+                    format_point(c, q, f);
+                    const double rel0 = f[0] - k.focal[0];
+                    const double amp = __dmul_rn(k.amplitude0, exp(-fabs(rel0) / k.penetration));
+                    const double n_emit = sc::emit_photons(k, amp, unit_time[s0 + j]);
+                    s_e[j * 32 + lane] = n_emit;
+                    s_norm[j * 32 + lane] = __dmul_rn(k.norm_coeff, n_emit / (4.0 * M_PI));
+                }
+            }
+            if (k.bleaching) {
+                __syncthreads();
+                if (warp == 0 && live) {
+                    for (int j = 0; j < ns; ++j) {
+                        double nb = b - s_e[j * 32 + lane];
+                        if (nb <= 0) {
+                            nb = 0;
+                            s_norm[j * 32 + lane] = 0.0;
+                        }
+                        b = nb;
+                    }
+                }
+                __syncthreads();
+            } else {
+                __syncwarp();  // phase 4 reads what phase 3 of the same warp wrote
+            }
+        }
+        // 4. records: warp w takes sub-steps w, w + kRecWarps, ...
         if (live) {
             for (int j = warp; j < ns; j += kRecWarps) {
                 const int s = s0 + j;
                 const double *ps = s_pos + (j * 32 + lane) * 3;
-                const double q[3] = {ps[0], ps[1], ps[2]};
+                const double q[3] = {ps[0], ps[1], c.ndim == 3 ? ps[2] : 0.0};
                 double f[3];
                 format_point(c, q, f);
                 const double norm = s_norm[j * 32 + lane];
@@ -372,12 +449,16 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
         }
         __syncthreads();
     }
-    if (warp == 0 && live) {
-        pos[3 * i] = p[0];
-        pos[3 * i + 1] = p[1];
-        pos[3 * i + 2] = p[2];
-        if (k.bleaching) budget[i] = b;
-        if (c.trans) klass[i] = cls;
+    if (live) {
+        if (axis_chains) {
+            if (warp < c.ndim) pos[3 * i + warp] = p[0];
+        } else if (warp == 0) {
+            pos[3 * i] = p[0];
+            pos[3 * i + 1] = p[1];
+            pos[3 * i + 2] = p[2];
+            klass[i] = cls;
+        }
+        if (warp == budget_warp && k.bleaching) budget[i] = b;
     }
 }
 

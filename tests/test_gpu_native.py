@@ -278,32 +278,55 @@ def test_frame_graph_replay_matches_eager(sg):
         numpy.testing.assert_array_equal(outs[k][1], outs[0][1])
 
 
-def test_fused_native_physics_matches_separate_pass(sg):
+@pytest.mark.parametrize("angle,bleach,ndim", [(None, False, 3), (None, True, 3), (0.0, True, 3),
+                                               (None, True, 2)])
+def test_fused_native_physics_matches_separate_pass(sg, angle, bleach, ndim):
     """sc_native_records (diffusion, physics and footprints in one pass) equals
     sc_diffuse_steps followed by sc_emitter_steps on the same Philox trajectory:
-    identical expectation images."""
+    identical expectation images.  TIRF with depth (the default angle), with and
+    without photobleaching (a half-life short enough that emitters bleach inside
+    the frames), EPI (angle 0) and a flat field (ndim 2: the excitation is the
+    same for every emitter)."""
     from scopyon_gb300.base import _psf_for
     from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
     cfg = sg.DefaultConfiguration()
-    cfg.update({"default": {
-        "magnification": 100,
-        "detector": {"type": "EMCCD", "image_size": [40, 40], "exposure_time": 0.004},
-        "effects": {"photo_bleaching": {"switch": False}}}})
+    upd = {"magnification": 100,
+           "detector": {"type": "EMCCD", "image_size": [40, 40], "exposure_time": 0.004},
+           "effects": {"photo_bleaching": {"switch": bleach, "half_life": 0.006}}}
+    if angle is not None:
+        upd["light_source"] = {"angle": angle}
+    cfg.update({"default": upd})
     t = numpy.arange(4 * 4 + 1) * 1e-3
-    traj = sg.sample_inputs(t, N=200, lower=[-2.5e-6, -2.5e-6, -0.2e-6], upper=[2.5e-6, 2.5e-6, 0.2e-6],
-                            D=0.4e-12, ndim=3, rng=numpy.random.RandomState(12))
+    lo, hi = [-2.5e-6, -2.5e-6, -0.2e-6][:ndim], [2.5e-6, 2.5e-6, 0.2e-6][:ndim]
+    traj = sg.sample_inputs(t, N=200, lower=lo, upper=hi, D=0.4e-12, ndim=ndim,
+                            rng=numpy.random.RandomState(12))
     eng = EngineConfig(cfg["default"])
     pipe = FramePipeline(eng, "cuda", psf=_psf_for(eng, torch.device("cuda")))
     pipe.psf.ensure(list(range(0, 800)))
+    if bleach:  # the budgets the separate pass draws first from its generator
+        beta = eng.half_life / numpy.log(2.0)
+        times_b = numpy.random.RandomState(0).exponential(scale=beta, size=200)
+        pipe.ensure_slots(200)
+        pipe.budget[:200].copy_(torch.from_numpy(times_b * eng.n_emit0))
     fg = FrameGraph(pipe, traj.copy(), 4, 1e-3, seed=3, use_graph=False)
     fused = []
     for _ in range(4):
         fg.step()
         fused.append(pipe.expect.cpu().numpy().copy())
+    budget = pipe.budget[:200].cpu().numpy().copy()
     sim = sg.EPIFMSimulator(cfg, method="default", rng=numpy.random.RandomState(0))
-    sep = [info["expectation"] for _, info in sim.generate_images(traj.copy(), 4, full_output=True)]
-    for a, b in zip(fused, sep):
-        numpy.testing.assert_array_equal(a.reshape(40, 40).astype(float), b)
+    sep = [info for _, info in sim.generate_images(traj.copy(), 4, full_output=True)]
+    for a, info in zip(fused, sep):
+        numpy.testing.assert_array_equal(a.reshape(40, 40).astype(float), info["expectation"])
+    if bleach:
+        # the same emitters bleached; the budgets left agree to rounding (the
+        # frame graph's sub-step length is 1 ms, the generator's the difference
+        # of two sample times)
+        states = sep[-1]["fluorescence_states"]
+        sep_budget = numpy.array([states[m] for m in sorted(states)])
+        numpy.testing.assert_array_equal(budget == 0, sep_budget == 0)
+        numpy.testing.assert_allclose(budget, sep_budget, rtol=1e-12, atol=0)
+        assert (budget == 0).any() and (budget > 0).any()  # some emitters bleached, not all
 
 
 def test_host_inputs_fast_path_matches_general_path(sg):

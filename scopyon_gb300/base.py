@@ -225,6 +225,73 @@ def _stage_known(arrays, slot_ids_f, staging):
     return min(r[0] for r in res), max(r[1] for r in res)
 
 
+_PIN_LIMIT = 8 << 30  # bytes of formatted inputs kept in one pinned host block
+
+
+class _PinnedInputs:
+    """The formatted inputs of a frame sequence in one pinned host block, so
+    that each frame's sub-steps are uploaded straight from it (one
+    asynchronous copy, no host copy per frame).  Built once, on the host
+    threads, when every array is (n, 5) with the same n and the block stays
+    under _PIN_LIMIT bytes.  Per array it keeps the depth range and whether
+    its ids equal the first array's, row for row."""
+
+    def __init__(self, arrays):
+        import torch
+        n = arrays[0].shape[0]
+        self.ids = numpy.ascontiguousarray(arrays[0][:, 3], dtype=numpy.float64)
+        self._t = torch.empty(len(arrays) * n * 5, dtype=torch.float64, pin_memory=True)
+        self.block = self._t.numpy().reshape(len(arrays), n, 5)
+        self.lo = numpy.empty(len(arrays))
+        self.hi = numpy.empty(len(arrays))
+        self.same = numpy.zeros(len(arrays), dtype=bool)
+        lib = _lib.load()
+
+        def one(k):
+            a = numpy.ascontiguousarray(arrays[k], dtype=numpy.float64)
+            rng_ = numpy.empty(2)
+            rc = lib.sc_stage_rows(a.ctypes.data, n, self.ids.ctypes.data,
+                                   self.block[k].ctypes.data, rng_.ctypes.data)
+            if rc == 1:  # other ids: copied without the check
+                numpy.copyto(self.block[k], a)
+                d = a[:, 0]
+                rng_[:] = (d.min(), d.max())  # NaN when a depth is NaN
+            else:
+                _lib.check(rc, "sc_stage_rows")
+                self.same[k] = True
+            self.lo[k], self.hi[k] = rng_
+
+        list(_host_pool().map(one, range(len(arrays))))
+
+    @classmethod
+    def build(cls, data):
+        arrays = [a for _, a in data]
+        if len(arrays) < 2:
+            return None
+        n = arrays[0].shape[0]
+        if n == 0 or any(a.shape != (n, 5) for a in arrays) or len(arrays) * n * 40 > _PIN_LIMIT:
+            return None
+        return cls(arrays)
+
+    def frame(self, idx):
+        """(particles, depth min, depth max) of the arrays idx, a run of
+        consecutive indices that all hold the first array's ids; None
+        otherwise."""
+        i0, i1 = idx[0], idx[-1] + 1
+        if i1 - i0 != len(idx) or not self.same[i0:i1].all():
+            return None
+        return self.block[i0:i1], float(self.lo[i0:i1].min()), float(self.hi[i0:i1].max())
+
+
+def _finish(pipe, out, nw, nh):
+    """The Image of a frame whose counts frame_out is copying to the host:
+    waits for the copy, raises what the frame's status words record."""
+    ev, counts, status = out
+    ev.synchronize()
+    pipe.raise_for_status(status)
+    return Image(counts.reshape(nw, nh).astype(numpy.float64)), {}
+
+
 def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, draws,
             full_output=True):
     """Frame generator: host bookkeeping around FramePipeline.run_frame."""
@@ -249,32 +316,72 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
     nw, nh = cfg.image_size
     slot_ids_f = None
     pending = None  # (frame, staging, future): the next frame's inputs, staged ahead
+    # frames on the fast paths are yielded one frame late: frame f's counts
+    # are read back while frame f + 1 runs on the device
+    out = None
+    pinned = _PinnedInputs.build(data) if num_frames > 1 and not full_output else None
+    if pinned is not None and isinstance(data, list):
+        for k in range(len(data)):  # the formatted arrays live on in the block only
+            data[k] = (data[k][0], pinned.block[k])
+    pinned_ok = None  # the slot order equals the pinned block's ids
     for f in range(num_frames):
         ahead = None
         if pending is not None:
             ahead = (pending[1], pending[2].result()) if pending[0] == f else None
             pending = None
         windows, exp_eff = frame_windows(times, len(data), start_time, exposure, f, shutter)
-        arrays = [data[i][1] for i, _ in windows]
         uts = numpy.array([ut for _, ut in windows], dtype=float)
-        if arrays and slot_ids_f is not None and not full_output:
+        if windows and slot_ids_f is not None and not full_output and pinned is not None:
             # the usual case: the same particles in the same order at every
-            # sub-step; staged on the host threads (while the previous frame
-            # ran), no per-frame id scan
+            # sub-step, uploaded from the pinned block
+            if pinned_ok is None:
+                pinned_ok = numpy.array_equal(slot_ids_f, pinned.ids)
+            got = pinned.frame([i for i, _ in windows]) if pinned_ok else None
+            if got is not None:
+                particles, lo, hi = got
+                try:
+                    pipe.ensure_slots(len(slot_ids_f))
+                    pipe.psf.ensure_depth_range(lo - focal0, hi - focal0)
+                    frame_draws = draws.next_frame() if draws is not None and draws.frames else None
+                    seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | \
+                        int(rng.randint(0, 2 ** 31 - 1)) if frame_draws is None else 0
+                    _, adc, _ = pipe.run_frame(particles, uts, with_optinfo=False,
+                                               draws=frame_draws, seed=seed, counter=f,
+                                               present=None, bleaching=bleaching,
+                                               track_upload=False)
+                    nxt = pipe.frame_out(adc, slot=f % 2)
+                except Exception:
+                    if out is not None:  # the frame before first, then the error
+                        yield _finish(pipe, out, nw, nh)
+                    raise
+                if out is not None:
+                    yield _finish(pipe, out, nw, nh)
+                out = nxt
+                continue
+        arrays = [data[i][1] for i, _ in windows]
+        if arrays and slot_ids_f is not None and not full_output:
+            # the same particles in the same order at every sub-step; staged
+            # on the host threads (while the previous frame ran), no per-frame
+            # id scan
             if ahead is not None:
                 staging, rng_ = ahead
             else:
                 staging = pipe.host_staging((len(arrays), len(slot_ids_f), 5), slot=f % 2)
                 rng_ = _stage_known(arrays, slot_ids_f, staging)
             if rng_ is not None:
-                pipe.ensure_slots(len(slot_ids_f))
-                pipe.psf.ensure_depth_range(rng_[0] - focal0, rng_[1] - focal0)
-                frame_draws = draws.next_frame() if draws is not None and draws.frames else None
-                seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | int(rng.randint(0, 2 ** 31 - 1)) \
-                    if frame_draws is None else 0
-                expect, adc, opt = pipe.run_frame(staging, uts, with_optinfo=False,
-                                                  draws=frame_draws, seed=seed, counter=f,
-                                                  present=None, bleaching=bleaching)
+                try:
+                    pipe.ensure_slots(len(slot_ids_f))
+                    pipe.psf.ensure_depth_range(rng_[0] - focal0, rng_[1] - focal0)
+                    frame_draws = draws.next_frame() if draws is not None and draws.frames else None
+                    seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | \
+                        int(rng.randint(0, 2 ** 31 - 1)) if frame_draws is None else 0
+                    _, adc, _ = pipe.run_frame(staging, uts, with_optinfo=False,
+                                               draws=frame_draws, seed=seed, counter=f,
+                                               present=None, bleaching=bleaching)
+                except Exception:
+                    if out is not None:  # the frame before first, then the error
+                        yield _finish(pipe, out, nw, nh)
+                    raise
                 if f + 1 < num_frames:
                     w_next, _ = frame_windows(times, len(data), start_time, exposure, f + 1,
                                               shutter)
@@ -285,9 +392,14 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
                                                     slot=(f + 1) % 2)
                         pending = (f + 1, st_next,
                                    _ahead_pool().submit(_stage_known, a_next, slot_ids_f, st_next))
-                pipe.check_status()
-                yield Image(adc.cpu().numpy().reshape(nw, nh).astype(numpy.float64)), {}
+                nxt = pipe.frame_out(adc, slot=f % 2)
+                if out is not None:
+                    yield _finish(pipe, out, nw, nh)
+                out = nxt
                 continue
+        if out is not None:
+            yield _finish(pipe, out, nw, nh)
+            out = None
         new_ids = []
         id_cols = [a[:, 3].astype(numpy.int64) for a in arrays]
         same = len(arrays) > 0 and all(ids.shape == id_cols[0].shape and numpy.array_equal(ids, id_cols[0])
@@ -303,6 +415,7 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
             slot_arr = numpy.array(slot_ids, dtype=numpy.int64)
         n_slots = len(slots)
         slot_ids_f = numpy.asarray(slot_ids, dtype=float) if same else None
+        pinned_ok = None
         pipe.ensure_slots(n_slots)
         if bleaching and new_ids:
             times_b = numpy.empty(len(new_ids))
@@ -347,6 +460,8 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
             b = pipe.budget[:n_slots].cpu().numpy()
             info["fluorescence_states"] = {m: float(b[slots[m]]) for m in slot_ids}
         yield Image(adc_np), info
+    if out is not None:
+        yield _finish(pipe, out, nw, nh)
 
 
 def _DeviceFrames(sim, cfg, pipe, traj, num_frames, start_time, exposure_time, bleaching, draws,

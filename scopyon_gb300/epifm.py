@@ -638,7 +638,30 @@ class FramePipeline:
                  ptr(expect), ptr(adc64), ptr(adc32), ptr(self.status), s)
 
     def check_status(self):
-        st = self.status.cpu().numpy()
+        self.raise_for_status(self.status.cpu().numpy())
+
+    def frame_out(self, adc, slot=0):
+        """Enqueues on the current stream the device-to-host copies of a
+        frame's ADC counts and of the status words into pinned buffers (two
+        slots, so that one frame's are read while the next frame's are
+        copied); returns (event, counts, status) with the host arrays valid
+        once the event has completed."""
+        name = "frame_out%d" % slot
+        h = self._cap.get(name)
+        if h is None or h[0].numel() < adc.numel() or h[0].dtype != adc.dtype:
+            h = (torch.empty(adc.numel(), dtype=adc.dtype, pin_memory=True),
+                 torch.empty(self.status.numel(), dtype=torch.int32, pin_memory=True))
+            self._cap[name] = h
+        counts = h[0][: adc.numel()]
+        counts.copy_(adc.reshape(-1), non_blocking=True)
+        h[1].copy_(self.status, non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        return ev, counts.numpy(), h[1].numpy()
+
+    def raise_for_status(self, st):
+        """Raises the error the status words ``st`` (read from the device)
+        record, after clearing them on the device; nothing when clear."""
         if st[0]:
             self.status.zero_()
             bits = int(st[0])
@@ -668,23 +691,28 @@ class FramePipeline:
             raise _lib.ScopyonGPUError(code, "; ".join(msgs))
 
     def run_frame(self, particles, unit_times, with_optinfo=True, draws=None, seed=0, counter=0,
-                  present=None, bleaching=None, stream=None):
+                  present=None, bleaching=None, stream=None, track_upload=True):
         """One frame from host arrays.
 
         particles: (S, N, 5) float64 [depth, x, y, m_id, p_state] per sub-step,
         column n holding particle slot n; unit_times: (S,) float64.
         Returns device tensors (expect f32, adc f64, optinfo f64 (N, 8) or None).
+        Pinned particles are uploaded asynchronously; with track_upload the
+        upload's event is kept for ``host_staging`` (a staging buffer that
+        will be refilled), without it the caller keeps the array unchanged.
         """
         n_sub, n = particles.shape[0], particles.shape[1]
         dev = self.device
         part = self._buf("particles", n_sub * n * 5, torch.float64)[: n_sub * n * 5]
         host = torch.from_numpy(numpy.ascontiguousarray(particles, dtype=float).reshape(-1))
         part.copy_(host, non_blocking=host.is_pinned())
-        if host.is_pinned():
+        if host.is_pinned() and track_upload:
             ev = torch.cuda.Event()
             ev.record()
             self._cap.setdefault("upload_events", {})[host.data_ptr()] = ev
-        ut = torch.from_numpy(numpy.ascontiguousarray(unit_times, dtype=float)).to(dev)
+        # a pinned copy: a pageable upload would wait for all the work queued before it
+        ut = torch.from_numpy(numpy.ascontiguousarray(unit_times, dtype=float)).pin_memory().to(
+            dev, non_blocking=True)
         pres = None
         if present is not None:
             pres = torch.from_numpy(numpy.ascontiguousarray(present, dtype=numpy.uint8).reshape(-1)).to(dev)

@@ -75,6 +75,44 @@ def test_nan_position_raises_value_error(lib):
     numpy.testing.assert_array_equal(again.as_array(), good.as_array())
 
 
+@pytest.mark.parametrize("bad", ["x", "depth"])
+def test_error_surfaces_at_its_frame_in_a_sequence(lib, bad):
+    """generate_images reads each frame back while the next one runs.  A
+    non-finite x at frame 3 (found by the device) or depth at frame 3 (found
+    on the host) still comes out as ValueError at frame 3: frames 0-2 equal
+    those of the clean inputs first."""
+    import scopyon_gb300 as sg
+    cfg = _cfg(edge=48)
+    rng = numpy.random.RandomState(5)
+    n, sub = 40, 4
+    half = 48 * 160e-9 / 2
+    pts = numpy.column_stack([rng.uniform(-half, half, (n, 2)), rng.uniform(-1e-7, 1e-7, n),
+                              numpy.arange(n), numpy.ones(n)])
+    t = numpy.arange(6 * sub + 1) * (0.01 / sub)
+    clean = []
+    for _ in t:
+        pts = pts.copy()
+        pts[:, :2] += 2e-8 * rng.standard_normal((n, 2))
+        clean.append(pts)
+    dirty = [a.copy() for a in clean]
+    dirty[3 * sub + 1][7, 0 if bad == "x" else 2] = numpy.nan
+
+    def frames(arrays, k):
+        gen = sg.generate_images([(float(a), b) for a, b in zip(t, arrays)], 6, config=cfg,
+                                 rng=numpy.random.RandomState(8), device="cuda:0")
+        return gen, [next(gen).as_array() for _ in range(k)]
+
+    _, want = frames(clean, 6)
+    gen, got = frames(dirty, 3)
+    for a, b in zip(got, want):
+        numpy.testing.assert_array_equal(a, b)
+    with pytest.raises(ValueError):
+        next(gen)
+    # the context still gives the clean frames
+    _, again = frames(clean, 6)
+    numpy.testing.assert_array_equal(numpy.array(again), numpy.array(want))
+
+
 def test_splat_wait_runs_out_and_is_reported(lib):
     """The bulk-copy splat (160 nm pixels, box tables) with no polls for each
     warp's first wait: SC_ERR_TIMEOUT through the status word, then a normal

@@ -329,10 +329,16 @@ def test_fused_native_physics_matches_separate_pass(sg, angle, bleach, ndim):
         assert (budget == 0).any() and (budget > 0).any()  # some emitters bleached, not all
 
 
-def test_host_inputs_fast_path_matches_general_path(sg):
-    """Host trajectories with the same ids at every sub-step are staged by host
-    threads (full_output=False); the frames equal those of the general path
-    (full_output=True), with bleaching on."""
+@pytest.mark.parametrize("pin_limit", [None, 0])
+def test_host_inputs_fast_path_matches_general_path(sg, pin_limit, monkeypatch):
+    """Host trajectories with the same ids at every sub-step take a fast path
+    (full_output=False): uploads from one pinned block of all the formatted
+    inputs, or (with no room for the block) per-frame staging on host
+    threads, each frame read back while the next one runs.  The frames equal
+    those of the general path (full_output=True), with bleaching on."""
+    from scopyon_gb300 import base
+    if pin_limit is not None:
+        monkeypatch.setattr(base, "_PIN_LIMIT", pin_limit)
     cfg = sg.DefaultConfiguration()
     cfg.update({"default": {
         "magnification": 100,

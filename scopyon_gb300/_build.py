@@ -37,12 +37,20 @@ def _deps(src):
 
 def _compile(src, extra):
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-    if os.path.exists(obj) and all(os.path.getmtime(d) <= os.path.getmtime(obj) for d in _deps(src)):
-        return obj, None
     cmd = [nvcc()] + ARCH + FLAGS + extra + ["-I", INCLUDE, "-c", src, "-o", obj]
+    # the object is current when it is newer than its sources and was built
+    # with the same command line (extra flags rebuild it)
+    stamp = obj + ".cmd"
+    line = " ".join(cmd)
+    same_cmd = os.path.exists(stamp) and open(stamp).read() == line
+    if (same_cmd and os.path.exists(obj) and
+            all(os.path.getmtime(d) <= os.path.getmtime(obj) for d in _deps(src))):
+        return obj, None
     proc = subprocess.run(cmd, capture_output=True, text=True)
     if proc.returncode != 0:
-        return obj, "%s\n%s%s" % (" ".join(cmd), proc.stdout, proc.stderr)
+        return obj, "%s\n%s%s" % (line, proc.stdout, proc.stderr)
+    with open(stamp, "w") as f:
+        f.write(line)
     return obj, None
 
 

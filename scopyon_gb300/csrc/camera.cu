@@ -14,7 +14,7 @@
 //   (rounding the ADC count to an integer is an option of this engine only;
 //   the reference's ADC count is an unrounded float, and parity runs keep
 //   the option off)
-// Draws come either from Philox4x32-10 (native, one counter stream per pixel)
+// Draws come either from Philox4x32-10 (native, one counter block per pixel pair)
 // or from caller arrays recorded from the reference (injected), in which case
 // the ADC arithmetic is the reference's FP64 sequence.
 #include "sc_common.cuh"
@@ -65,53 +65,93 @@ int64_t pois_entries() {
     return n;
 }
 
-// One thread per j: offsets, then the CDF summed in FP64 from
-// p_k = exp(k log j - j - log k!).
+// One thread per j: the span, then the CDF summed in FP64 from
+// p_k = exp(k log j - j - log k!), as 32-bit fixed point.
 __global__ void pois_cdf_kernel(void *base) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= kPoisJ) return;
     char *b = static_cast<char *>(base);
-    int32_t *off = reinterpret_cast<int32_t *>(b);
-    float *cdf = reinterpret_cast<float *>(b + kPoisCdfAt);
+    int2 *span = reinterpret_cast<int2 *>(b);
+    uint32_t *cdf = reinterpret_cast<uint32_t *>(b + kPoisCdfAt);
     int o = 0;
     for (int i = 0; i < j; ++i) o += pois_support(i);
-    off[j] = o;
     const int K = pois_support(j);
-    if (j == kPoisJ - 1) off[kPoisJ] = o + K;
+    span[j] = make_int2(o, K - 1);
     const double lj = j > 0 ? log((double)j) : 0.0;
     double F = 0.0;
     for (int k = 0; k < K; ++k) {
         const double pk = j == 0 ? (k == 0 ? 1.0 : 0.0)
                                  : exp((double)k * lj - (double)j - lgamma((double)k + 1.0));
         F += pk;
-        cdf[o + k] = k == K - 1 ? 1.0f : (float)fmin(F, 1.0);
+        cdf[o + k] = k == K - 1 ? 0u : (uint32_t)fmin(rint(F * 4294967296.0), 4294967295.0);
     }
 }
 
-// One thread per (j, g): the first k whose CDF reaches g / kPoisG.
+// One thread per (j, g): the first k below K_j - 1 whose upper edge lies
+// above g 2^24, else K_j - 1.
 __global__ void pois_guide_kernel(void *base) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= kPoisJ * kPoisG) return;
     const int j = idx / kPoisG, g = idx % kPoisG;
     char *b = static_cast<char *>(base);
-    const int32_t *off = reinterpret_cast<const int32_t *>(b);
+    const int2 sp = reinterpret_cast<const int2 *>(b)[j];
     uint16_t *guide = reinterpret_cast<uint16_t *>(b + kPoisGuideAt);
-    const float *cdf = reinterpret_cast<const float *>(b + kPoisCdfAt);
-    const float target = (float)g / (float)kPoisG;
-    const int K = off[j + 1] - off[j];
+    const uint32_t *cdf = reinterpret_cast<const uint32_t *>(b + kPoisCdfAt) + sp.x;
+    const uint32_t target = (uint32_t)g << 24;
     int k = 0;
-    while (k < K - 1 && cdf[off[j] + k] < target) ++k;
+    while (k < sp.y && cdf[k] <= target) ++k;
     guide[idx] = (uint16_t)k;
 }
 
-// Native draws, a pixel per thread.  Pixel p's draws come from its own
-// Philox stream (key: seed; counter: p and the frame counter): block 0's
-// four words give the Poisson draw (two) and the read noise (two); block 1
-// on feeds the rare fallbacks (PTRS above kPoisJ, the EMCCD gain and its
-// redraws).  No lane loops on a rejection in the common case, so a warp's
-// lanes stay together; the counts do not depend on the launch shape.
-template <int CAM>
-__global__ void __launch_bounds__(256)
+// The per-pixel inputs of pixel pair q (photons, read-noise sigma, 1/gain,
+// offset): float2 loads when VEC, else two scalar loads (the last pair of an
+// odd frame repeats its one pixel).
+struct PairIn {
+    float2 ph, sg, g, o;
+};
+
+template <int CAM, bool VEC>
+__device__ __forceinline__ PairIn load_pair(const CamConsts &c, int q,
+                                            const float *__restrict__ photons,
+                                            const float *__restrict__ offset_f,
+                                            const float *__restrict__ inv_gain_f,
+                                            const float *__restrict__ sigma) {
+    // streamed once: loaded evict-first, so that the Poisson tables keep L1
+    const bool scmos = CAM == SC_CAM_SCMOS && sigma;
+    PairIn in;
+    if (VEC) {
+        in.ph = __ldcs(reinterpret_cast<const float2 *>(photons) + q);
+        in.sg = scmos ? __ldcs(reinterpret_cast<const float2 *>(sigma) + q)
+                      : make_float2(c.readout_f, c.readout_f);
+        in.g = inv_gain_f ? __ldcs(reinterpret_cast<const float2 *>(inv_gain_f) + q)
+                          : make_float2(c.inv_gain0_f, c.inv_gain0_f);
+        in.o = offset_f ? __ldcs(reinterpret_cast<const float2 *>(offset_f) + q)
+                        : make_float2(c.offset0_f, c.offset0_f);
+    } else {
+        const int p = 2 * q, p1 = min(p + 1, c.n - 1);
+        in.ph = make_float2(__ldcs(photons + p), __ldcs(photons + p1));
+        in.sg = scmos ? make_float2(__ldcs(sigma + p), __ldcs(sigma + p1))
+                      : make_float2(c.readout_f, c.readout_f);
+        in.g = inv_gain_f ? make_float2(__ldcs(inv_gain_f + p), __ldcs(inv_gain_f + p1))
+                          : make_float2(c.inv_gain0_f, c.inv_gain0_f);
+        in.o = offset_f ? make_float2(__ldcs(offset_f + p), __ldcs(offset_f + p1))
+                        : make_float2(c.offset0_f, c.offset0_f);
+    }
+    return in;
+}
+
+// Native draws, a pixel pair per thread (pixels 2q and 2q + 1, one Philox
+// block between them; see pair_draws).  VEC: the per-pixel inputs and the
+// FP32 outputs are 8-byte aligned and the frame has an even pixel count, so
+// a pair's values move as float2.  Each thread loads its next pair's inputs
+// before it draws the current pair, so that a load's DRAM latency overlaps
+// a pair's arithmetic.  No lane loops on a rejection in the common case, so
+// a warp's lanes stay together.
+#ifndef SC_CAM_MIN_BLOCKS
+#define SC_CAM_MIN_BLOCKS 1
+#endif
+template <int CAM, bool VEC>
+__global__ void __launch_bounds__(256, SC_CAM_MIN_BLOCKS)
 camera_native_kernel(CamConsts c, const void *__restrict__ ptab, const float *__restrict__ photons,
                      const float *__restrict__ offset_f, const float *__restrict__ inv_gain_f,
                      const float *__restrict__ sigma, const double *__restrict__ table_value,
@@ -119,18 +159,42 @@ camera_native_kernel(CamConsts c, const void *__restrict__ ptab, const float *__
                      double *__restrict__ adc64, float *__restrict__ adc32, int32_t *status) {
     const PoisTab t = pois_tab(ptab);
     const uint64_t counter = c.counter + (c.frame ? (uint64_t)*c.frame : 0);
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < c.n; q += stride) {
-        const int p = (int)q;
-        const float ef = c.qe_f * (__ldg(photons + p) + c.background_f);
-        if (expect) expect[p] = ef;
-        const float sg = (CAM == SC_CAM_SCMOS && sigma) ? __ldg(sigma + p) : c.readout_f;
-        const float g = inv_gain_f ? __ldg(inv_gain_f + p) : c.inv_gain0_f;
-        const float o = offset_f ? __ldg(offset_f + p) : c.offset0_f;
-        const float v = native_adc<CAM>(c, t, p, ef, sg, g, o, counter, table_value, table_cdf,
-                                        status);
-        if (adc32) adc32[p] = v;
-        if (adc64) adc64[p] = sc::f2d_exact(v);
+    const uint32_t c0 = (uint32_t)counter, c1 = (uint32_t)(counter >> 32);
+    const int n_pairs = (c.n + 1) >> 1;
+    const int stride = gridDim.x * blockDim.x;
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_pairs) return;
+    PairIn in = load_pair<CAM, VEC>(c, q, photons, offset_f, inv_gain_f, sigma);
+    for (; q < n_pairs; q += stride) {
+        const int qn = q + stride;
+        PairIn next = in;
+        if (qn < n_pairs) next = load_pair<CAM, VEC>(c, qn, photons, offset_f, inv_gain_f, sigma);
+        const PairDraws d = pair_draws<CAM>(c, q, c0, c1);
+        const int p = 2 * q;
+        const float e0 = c.qe_f * (in.ph.x + c.background_f);
+        const float e1 = c.qe_f * (in.ph.y + c.background_f);
+        const float v0 = pixel_adc<CAM>(c, t, p, e0, in.sg.x, in.g.x, in.o.x, d, 0, c0, c1,
+                                        table_value, table_cdf, status);
+        const bool two = VEC || p + 1 < c.n;
+        const float v1 = two ? pixel_adc<CAM>(c, t, p + 1, e1, in.sg.y, in.g.y, in.o.y, d, 1, c0,
+                                              c1, table_value, table_cdf, status)
+                             : 0.f;
+        if (VEC) {
+            if (expect) __stcs(reinterpret_cast<float2 *>(expect) + q, make_float2(e0, e1));
+            if (adc32) __stcs(reinterpret_cast<float2 *>(adc32) + q, make_float2(v0, v1));
+        } else {
+            if (expect) expect[p] = e0;
+            if (adc32) adc32[p] = v0;
+            if (two) {
+                if (expect) expect[p + 1] = e1;
+                if (adc32) adc32[p + 1] = v1;
+            }
+        }
+        if (adc64) {
+            adc64[p] = sc::f2d_exact(v0);
+            if (two) adc64[p + 1] = sc::f2d_exact(v1);
+        }
+        in = next;
     }
 }
 
@@ -292,20 +356,27 @@ extern "C" int sc_camera(const ScCameraParams *p, const float *d_photons, const 
                                                     d_inj_uniform, d_expect, d_adc64, d_adc32);
     } else {
         const int block = 256;
-        const int64_t want = ((int64_t)c.n + block - 1) / block;
-        switch (c.camera) {
-#define SC_CAM_LAUNCH(K)                                                                        \
-    case K:                                                                                     \
-        camera_native_kernel<K><<<sc::resident_grid((const void *)camera_native_kernel<K>,      \
-                                                    block, 0, want),                            \
-                                   block, 0, st>>>(                                             \
-            c, p->d_poisson_table, d_photons, d_offset_f, d_inv_gain_f, d_sigma, d_table_value, \
-            d_table_cdf, d_expect, d_adc64, d_adc32, d_status);                                 \
+        const int64_t want = (((int64_t)c.n + 1) / 2 + block - 1) / block;
+        auto al8 = [](const void *ptr) { return ((uintptr_t)ptr & 7) == 0; };
+        const bool vec = (c.n & 1) == 0 && al8(d_photons) && al8(d_offset_f) &&
+                         al8(d_inv_gain_f) && al8(d_sigma) && al8(d_expect) && al8(d_adc32);
+        switch (c.camera * 2 + (vec ? 1 : 0)) {
+#define SC_CAM_LAUNCH(K, V)                                                                       \
+    case K * 2 + V:                                                                             \
+        camera_native_kernel<K, V><<<sc::resident_grid((const void *)camera_native_kernel<K, V>, \
+                                                       block, 0, want),                         \
+                                      block, 0, st>>>(                                          \
+            c, p->d_poisson_table, d_photons, d_offset_f, d_inv_gain_f, d_sigma, d_table_value,   \
+            d_table_cdf, d_expect, d_adc64, d_adc32, d_status);                                   \
         break;
-            SC_CAM_LAUNCH(SC_CAM_EMCCD)
-            SC_CAM_LAUNCH(SC_CAM_CCD)
-            SC_CAM_LAUNCH(SC_CAM_CMOS_TABLE)
-            SC_CAM_LAUNCH(SC_CAM_SCMOS)
+            SC_CAM_LAUNCH(SC_CAM_EMCCD, 0)
+            SC_CAM_LAUNCH(SC_CAM_EMCCD, 1)
+            SC_CAM_LAUNCH(SC_CAM_CCD, 0)
+            SC_CAM_LAUNCH(SC_CAM_CCD, 1)
+            SC_CAM_LAUNCH(SC_CAM_CMOS_TABLE, 0)
+            SC_CAM_LAUNCH(SC_CAM_CMOS_TABLE, 1)
+            SC_CAM_LAUNCH(SC_CAM_SCMOS, 0)
+            SC_CAM_LAUNCH(SC_CAM_SCMOS, 1)
 #undef SC_CAM_LAUNCH
         }
     }
@@ -330,7 +401,7 @@ extern "C" int sc_emccd_exact(const double *d_photons, double qe, double backgro
 }
 
 extern "C" size_t sc_poisson_table_bytes(void) {
-    return kPoisCdfAt + sizeof(float) * (size_t)pois_entries();
+    return kPoisCdfAt + sizeof(uint32_t) * (size_t)pois_entries();
 }
 
 extern "C" int sc_poisson_table(void *d_table, size_t bytes, void *stream) {

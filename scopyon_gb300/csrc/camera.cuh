@@ -96,68 +96,85 @@ __device__ __forceinline__ int table_index(const double *cdf, int n, double u) {
 }
 
 // ------------------------------------------------ Poisson inverse-CDF tables
-// Poisson(j) for j = 0 .. kPoisJ - 1: the CDF over k = 0 .. K_j - 1 in FP32
-// (each entry the FP64 sum rounded once; the last entry is exactly 1) and,
-// per j, kPoisG starting points for the search (the first k whose CDF
-// reaches g / kPoisG).  Layout of the caller's buffer: int32 offsets
-// [kPoisJ + 1], uint16 guide [kPoisJ][kPoisG], float CDF [sum K_j].
+// Poisson(j) for j = 0 .. kPoisJ - 1 over k = 0 .. K_j - 1 as 32-bit fixed
+// point: C_j[k] = F_j(k) 2^32, rounded from the FP64 sum (the last entry,
+// whose upper edge is 2^32, is stored as 0 and never compared), and per j
+// kPoisG starting points for the search (the first k with C_j[k] above
+// g 2^24).  Layout of the caller's buffer: int2 {first entry, K_j - 1}
+// [kPoisJ], uint16 guide [kPoisJ][kPoisG], uint32 CDF [sum K_j].
 constexpr int kPoisJ = 256, kPoisG = 256;
-constexpr size_t kPoisGuideAt = ((sizeof(int32_t) * (kPoisJ + 1) + 15) / 16) * 16;
+constexpr size_t kPoisGuideAt = sizeof(int2) * kPoisJ;
 constexpr size_t kPoisCdfAt = kPoisGuideAt + sizeof(uint16_t) * kPoisJ * kPoisG;
 
 // Support of the Poisson(j) table: j + 10 sqrt(j) + 12 values (the mass past
-// it is far below the FP32 rounding of the CDF).
+// it, below 1e-20, is far below one step of 2^-32).
 __host__ __device__ __forceinline__ int pois_support(int j) {
     return j + (int)ceil(10.0 * sqrt((double)j)) + 12;
 }
 
 struct PoisTab {
-    const int32_t *off;
+    const int2 *span;
     const uint16_t *guide;
-    const float *cdf;
+    const uint32_t *cdf;
 };
 
 __device__ __forceinline__ PoisTab pois_tab(const void *base) {
     const char *b = static_cast<const char *>(base);
-    return PoisTab{reinterpret_cast<const int32_t *>(b),
+    return PoisTab{reinterpret_cast<const int2 *>(b),
                    reinterpret_cast<const uint16_t *>(b + kPoisGuideAt),
-                   reinterpret_cast<const float *>(b + kPoisCdfAt)};
+                   reinterpret_cast<const uint32_t *>(b + kPoisCdfAt)};
 }
 
-// Poisson(lam) from two uniforms, with no rejection: Poisson(j) by table
-// inversion at u0 plus Poisson(lam - j) by sequential inversion at u1,
-// j = floor(lam) (a sum of independent Poisson variates is Poisson with the
-// summed mean).  Means of kPoisJ and more take PTRS on the pixel's stream.
-__device__ __forceinline__ float poisson_tab(const PoisTab &t, float lam, float u0, float u1,
-                                             sc::rng_stream &rs, int32_t *status) {
+// Poisson(lam) from one 32-bit uniform word u, with no rejection.  A sum of
+// independent Poisson variates is Poisson with the summed mean, so the draw
+// is K + M with K ~ Poisson(j), j = floor(lam), and M ~ Poisson(lam - j):
+//   K: inversion of the fixed-point CDF, C_j[K - 1] <= u < C_j[K];
+//   M: sequential inversion at v = (u - C_j[K - 1] + 1/2) / (C_j[K] -
+//      C_j[K - 1]), which, given K, is uniform on (0, 1) and independent of
+//      K, to within one step of the bin's width (a bin of probability p holds
+//      p 2^32 values of u).
+// Means of kPoisJ and more take PTRS on the pixel's fallback stream.
+// The caller takes means of kPoisJ and more (and NaN) elsewhere.
+__device__ __forceinline__ float poisson_u32(const PoisTab &t, float lam, uint32_t u) {
     if (!(lam > 0.f)) return 0.f;
-    if (!(lam < (float)kPoisJ)) return poisson(rs, lam, status);
     const int j = (int)lam;
     const float r = lam - (float)j;
     int k = 0;
+    float v;
     if (j > 0) {
-        const int base = __ldg(t.off + j), last = __ldg(t.off + j + 1) - 1 - base;
-        k = __ldg(t.guide + j * kPoisG + min((int)(u0 * (float)kPoisG), kPoisG - 1));
-        while (k < last && u0 > __ldg(t.cdf + base + k)) ++k;
+        const int2 sp = __ldg(t.span + j);
+        const uint32_t *cdf = t.cdf + sp.x;
+        k = __ldg(t.guide + j * kPoisG + (u >> 24));
+        uint32_t lo = k > 0 ? __ldg(cdf + k - 1) : 0u;
+        uint32_t hi = __ldg(cdf + k);
+        while (k < sp.y && u >= hi) {
+            lo = hi;
+            hi = __ldg(cdf + ++k);
+        }
+        // the bin's width (mod 2^32: the last bin's upper edge 2^32 is stored as 0)
+        const uint32_t w = hi - lo;
+        v = fminf(__fdividef((float)(u - lo) + 0.5f, (float)w), 0.99999994f);
+    } else {
+        v = sc::u01f(u);
     }
     // Poisson(r), r in [0, 1): the first four cumulative sums without a
-    // branch (u1 lies past the fourth with probability below 2%), then the
-    // sequential search (P(X >= 16) < 1e-13)
-    float p = expf(-r), s = p;
-    int m = u1 > s;
+    // branch (v lies past the fourth with probability below 2%), then the
+    // sequential search (P(M >= 16) < 1e-13)
+    float p = __expf(-r), s = p;
+    int m = v > s;
     p *= r;
     s += p;
-    m += u1 > s;
+    m += v > s;
     p *= 0.5f * r;
     s += p;
-    m += u1 > s;
+    m += v > s;
     p *= (1.f / 3.f) * r;
     s += p;
-    if (u1 > s) {
+    if (v > s) {
         m = 4;
         p *= 0.25f * r;
         s += p;
-        while (u1 > s && m < 16) {
+        while (v > s && m < 16) {
             ++m;
             p *= __fdividef(r, (float)m);
             s += p;
@@ -166,12 +183,21 @@ __device__ __forceinline__ float poisson_tab(const PoisTab &t, float lam, float 
     return (float)(k + m);
 }
 
-// Standard normal from two 32-bit words (Box-Muller, the cosine branch).
-__device__ __forceinline__ float bm_normal(uint32_t a, uint32_t b) {
-    const float r = sqrtf(-2.0f * __logf(sc::u01f(a)));
+// Two independent standard normals from two 32-bit words (Box-Muller: the
+// cosine and the sine branch).  The radius is x rsqrt(x) (relative error a
+// few 1e-7, far below what any test of the draws resolves).
+__device__ __forceinline__ void bm_pair(uint32_t a, uint32_t b, float &n0, float &n1) {
+    const float x = -2.0f * __logf(sc::u01f(a));
+    const float r = x * rsqrtf(x);
     float sn, cs;
     sc::sincos_2pi(sc::u01f(b), &sn, &cs);
-    return r * cs;
+    n0 = r * cs;
+    n1 = r * sn;
+}
+
+// Uniform in (0, 1) from one 32-bit word, double precision.
+__device__ __forceinline__ double u01d32(uint32_t x) {
+    return ((double)x + 0.5) * (1.0 / 4294967296.0);
 }
 
 // EMCCD output electrons with the reference's law (EMCCD.probability_
@@ -181,14 +207,14 @@ __device__ __forceinline__ float bm_normal(uint32_t a, uint32_t b) {
 // 5 sqrt(E) + 10.  Drawn as n ~ Poisson(E), S = rint(g Gamma(n)) for n > 0,
 // and drawn again when S leaves the support or rounds to 0 with n > 0 (the
 // law has no density mass below S = 1/2 beside the atom at 0).
-__device__ inline float emccd_native(const PoisTab &t, float e, float g, float u0, float u1,
-                              sc::rng_stream &rs, int32_t *status) {
+__device__ inline float emccd_native(const PoisTab &t, float e, float g, uint32_t u,
+                                     sc::rng_stream &rs, int32_t *status) {
     if (!(e > 0.f)) return 0.f;
     const float sig = sqrtf(e) * 5.f + 10.f;
     const float s_min = fmaxf(0.f, g * truncf(e - sig)), s_max = g * truncf(e + sig);
     for (int it = 0; it < 32; ++it) {
-        const float n = it == 0 ? poisson_tab(t, e, u0, u1, rs, status)
-                                : poisson_tab(t, e, rs.uniform(), rs.uniform(), rs, status);
+        const uint32_t w = it == 0 ? u : rs.next();
+        const float n = e < (float)kPoisJ ? poisson_u32(t, e, w) : poisson(rs, e, status);
         const float s = n > 0.f ? rintf(g * gamma_ge1(rs, n, status)) : 0.f;
         if (n > 0.f && s < 1.f) continue;
         if (s >= s_min && s < s_max) return s;
@@ -197,11 +223,73 @@ __device__ inline float emccd_native(const PoisTab &t, float e, float g, float u
     return rintf(g * e);
 }
 
+// Native draws.  Pixels 2q and 2q + 1 share one Philox4x32-10 block (key:
+// the seed; counter: (q, frame counter, 0)): word x is pixel 2q's Poisson
+// word and y pixel 2q + 1's; z and w give the pair's read noise, the cosine
+// branch of Box-Muller to pixel 2q and the sine branch to 2q + 1 (the CMOS
+// table's noise: word z, resp. w, as one uniform).  Pixel p's rare fallbacks
+// (PTRS above kPoisJ, the EMCCD gain and its redraws) use its own stream,
+// counter (p, frame counter, 1, 2, ...).  So a pixel's counts depend on its
+// index and the frame only, never on the launch shape.
+struct PairDraws {
+    uint32_t pois[2], word[2];
+    float normal[2];
+};
+
+template <int CAM>
+__device__ __forceinline__ PairDraws pair_draws(const CamConsts &c, int q, uint32_t c0,
+                                                uint32_t c1) {
+    const sc::u4 r = sc::philox4x32_10(sc::u4{(uint32_t)q, c0, c1, 0u}, (uint32_t)c.seed,
+                                       (uint32_t)(c.seed >> 32));
+    PairDraws d;
+    d.pois[0] = r.x;
+    d.pois[1] = r.y;
+    d.word[0] = r.z;
+    d.word[1] = r.w;
+    d.normal[0] = d.normal[1] = 0.f;
+    if (CAM != SC_CAM_CMOS_TABLE) bm_pair(r.z, r.w, d.normal[0], d.normal[1]);
+    return d;
+}
+
+// Poisson(lam) for means of kPoisJ and more (PTRS) on pixel p's fallback
+// stream.
+__device__ __forceinline__ float poisson_far(uint64_t seed, int p, uint32_t c0, uint32_t c1,
+                                          float lam, int32_t *status) {
+    sc::rng_stream rs(seed, (uint32_t)p, c0, c1);
+    rs.ctr.w = 1;
+    return poisson(rs, lam, status);
+}
+
 // The ADC count of pixel p in native mode: expectation ef, read-noise sigma
-// sg, 1/gain g and offset o; its draws come from its own Philox stream (key:
-// the seed; counter: p and the frame counter), block 0's four words for the
-// Poisson draw (two) and the read noise (two), block 1 on for the rare
-// fallbacks (PTRS above kPoisJ, the EMCCD gain and its redraws).
+// sg, 1/gain g and offset o, with the pixel's half h of its pair's draws.
+template <int CAM>
+__device__ __forceinline__ float pixel_adc(const CamConsts &c, const PoisTab &t, int p, float ef,
+                                           float sg, float g, float o, const PairDraws &d, int h,
+                                           uint32_t c0, uint32_t c1,
+                                           const double *__restrict__ table_value,
+                                           const double *__restrict__ table_cdf,
+                                           int32_t *status) {
+    float signal, noise;
+    if (CAM == SC_CAM_EMCCD) {
+        sc::rng_stream rs(c.seed, (uint32_t)p, c0, c1);
+        rs.ctr.w = 1;
+        signal = emccd_native(t, ef, c.emgain_f, d.pois[h], rs, status);
+        noise = c.readout_f > 0.f ? c.readout_f * d.normal[h] : 0.f;
+    } else {
+        signal = ef < (float)kPoisJ ? poisson_u32(t, ef, d.pois[h])
+                                    : poisson_far(c.seed, p, c0, c1, ef, status);
+        noise = CAM == SC_CAM_CMOS_TABLE
+                    ? (float)table_value[table_index(table_cdf, c.table_n, u01d32(d.word[h]))]
+                    : sg * d.normal[h];
+    }
+    float v = fminf(signal + noise, c.fullwell_f);
+    v = fmaf(v, g, o);
+    v = fminf(fmaxf(v, 0.f), c.adc_max_f);
+    if (c.rounding) v = rintf(v);
+    return v;
+}
+
+// The ADC count of one pixel p alone (its pair's block drawn for it).
 template <int CAM>
 __device__ __forceinline__ float native_adc(const CamConsts &c, const PoisTab &t, int p, float ef,
                                             float sg, float g, float o, uint64_t counter,
@@ -209,27 +297,9 @@ __device__ __forceinline__ float native_adc(const CamConsts &c, const PoisTab &t
                                             const double *__restrict__ table_cdf,
                                             int32_t *status) {
     const uint32_t c0 = (uint32_t)counter, c1 = (uint32_t)(counter >> 32);
-    const sc::u4 r = sc::philox4x32_10(sc::u4{(uint32_t)p, c0, c1, 0u}, (uint32_t)c.seed,
-                                       (uint32_t)(c.seed >> 32));
-    sc::rng_stream rs(c.seed, (uint32_t)p, c0, c1);
-    rs.ctr.w = 1;
-    const float u0 = sc::u01f(r.x), u1 = sc::u01f(r.y);
-    float signal, noise;
-    if (CAM == SC_CAM_EMCCD) {
-        signal = emccd_native(t, ef, c.emgain_f, u0, u1, rs, status);
-        noise = c.readout_f > 0.f ? c.readout_f * bm_normal(r.z, r.w) : 0.f;
-    } else if (CAM == SC_CAM_CMOS_TABLE) {
-        noise = (float)table_value[table_index(table_cdf, c.table_n, sc::u01d(r.z, r.w))];
-        signal = poisson_tab(t, ef, u0, u1, rs, status);
-    } else {
-        signal = poisson_tab(t, ef, u0, u1, rs, status);
-        noise = sg * bm_normal(r.z, r.w);
-    }
-    float v = fminf(signal + noise, c.fullwell_f);
-    v = v * g + o;
-    v = fminf(fmaxf(v, 0.f), c.adc_max_f);
-    if (c.rounding) v = rintf(v);
-    return v;
+    const PairDraws d = pair_draws<CAM>(c, p >> 1, c0, c1);
+    return pixel_adc<CAM>(c, t, p, ef, sg, g, o, d, p & 1, c0, c1, table_value, table_cdf,
+                          status);
 }
 
 // CamConsts of a parameter block (host).

@@ -714,9 +714,11 @@ def hbm_stages(dev, peak, steps=20, warmup=3, n_emit=1 << 22, edge=8192, seed=5)
     rooflines mean something (a 512^2 frame moves only a few MB per stage).
 
     Diffusion: n_emit emitters, reflecting walls, SUBSTEPS Philox sub-steps per
-    launch; per emitter it reads and writes the FP64 position (48 B) and reads
-    the class (4 B), per emitter-step it writes the formatted [depth, x, y, id,
-    state] row (40 B).  Camera: the workload's sCMOS camera on an edge^2 frame;
+    launch (FP32 moves); per emitter it reads and writes the position (48 B) and
+    reads the class (4 B), per emitter-step it writes the 16-byte FP32 row
+    [depth, x, y, 0] (layout 1, the rows device-trajectory frames read); the
+    FP64 [depth, x, y, id, state] rows (40 B, layout 0) are timed beside it.
+    Camera: the workload's sCMOS camera on an edge^2 frame;
     per pixel it reads photons, offset, 1/gain and readout sigma (16 B) and
     writes the expectation (4 B) and the FP32 ADC count (4 B)."""
     import torch
@@ -736,17 +738,29 @@ def hbm_stages(dev, peak, steps=20, warmup=3, n_emit=1 << 22, edge=8192, seed=5)
     traj.prepare_uniform(SUBSTEPS)
     frame = torch.zeros(1, dtype=torch.int64, device=dev)
     rows = torch.empty(SUBSTEPS * n_emit * 5, dtype=torch.float64, device=dev)
+    layout = [1]
 
     def diffuse():
-        traj.launch_frame(SUBSTEPS, rows, frame)
+        traj.launch_frame(SUBSTEPS, rows, frame, layout=layout[0])
         call("sc_counter_add", ptr(frame), 1, stream_ptr())
 
     ms = _event_ms(diffuse, steps, warmup)
-    alg = n_emit * (48 + 4) + n_emit * SUBSTEPS * 40
+    alg = n_emit * (48 + 4) + n_emit * SUBSTEPS * 16
+    # the budget of 16 B per record and 36 B of state per emitter
+    budget = n_emit * 36 + n_emit * SUBSTEPS * 16
     gbs = alg / (ms / 1e3) / 1e9
-    out["diffusion"] = {"kernel": "diffuse_kernel (sc_diffuse_steps)", "emitters": n_emit,
+    layout[0] = 0
+    ms0 = _event_ms(diffuse, steps, warmup)
+    alg0 = n_emit * (48 + 4) + n_emit * SUBSTEPS * 40
+    out["diffusion"] = {"kernel": "diffuse_native_kernel (sc_diffuse_steps, FP32 rows)",
+                        "emitters": n_emit,
                         "substeps": SUBSTEPS, "avg_launch_ms": ms, "algorithmic_bytes": alg,
                         "achieved": gbs, "unit": "GB/s", "frac": gbs / peak,
+                        "budget_bytes": budget,
+                        "frac_on_budget": budget / (ms / 1e3) / 1e9 / peak,
+                        "fp64_rows": {"avg_launch_ms": ms0, "algorithmic_bytes": alg0,
+                                      "achieved": alg0 / (ms0 / 1e3) / 1e9,
+                                      "frac": alg0 / (ms0 / 1e3) / 1e9 / peak},
                         "timing": "includes one 1-thread frame-counter launch per step"}
     del rows, traj
     torch.cuda.empty_cache()

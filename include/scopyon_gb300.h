@@ -82,6 +82,10 @@ typedef struct {
     int32_t with_optinfo;    /* 1: accumulate the 8-vector true_data per particle          */
     int32_t box_p;           /* px / res when it is an integer P (box tables built), else 0 */
     int32_t box_nq;          /* pixel offsets per box-table axis, (n_signal+P-1)/P + 1      */
+    int32_t row_layout;      /* sc_emitter_steps input rows: 0 [depth, x, y, m_id, p_state] */
+                             /* FP64; 1 [depth, x, y, 0] FP32 with m_id the slot and       */
+                             /* p_state 1 (sc_diffuse_steps layout 1)                       */
+    int32_t pad;
 } ScStepParams;
 
 typedef struct {
@@ -127,7 +131,9 @@ typedef struct {
     int32_t ndim;            /* 2: (x, y) inputs, depth 0; 3: (x, y, z)                    */
     int32_t boundary;        /* 0 none (reference), 1 periodic, 2 reflecting               */
     int32_t n_class;         /* diffusion classes in d_sigma                                */
-    int32_t pad;
+    int32_t layout;          /* sc_diffuse_steps rows: 0 [depth, x, y, id, 1] FP64 (40 B);  */
+                             /* 1 [depth, x, y, 0] FP32 (16 B; native draws and the        */
+                             /* identity transform only)                                   */
     int64_t step0;           /* global index of the frame's first sub-step (Philox counter) */
     uint64_t seed;           /* Philox key                                                  */
     const int64_t *d_frame;  /* optional device counter f: step0 += f * n_sub (graph replay) */
@@ -185,11 +191,13 @@ int sc_psf_quadrant_sat(const double *d_radial, int n_keys, int n_r, double res,
 /* Brownian sub-steps of one frame on the device.  d_pos (n x 3, sampling
  * frame, updated in place) holds the positions at the frame's first time
  * point; for each sub-step the formatted position [depth, x, y, id, 1] goes to
- * d_particles ([n_sub][n][5], the layout sc_emitter_steps reads) and the
- * particle then moves by sigma * N(0, 1) per axis, with d_sigma
+ * d_particles ([n_sub][n][5], the layout sc_emitter_steps reads; with
+ * p->layout 1, [n_sub][n] rows [depth, x, y, 0] of FP32; d_particles NULL: no
+ * rows) and the particle then moves by sigma * N(0, 1) per axis, with d_sigma
  * [n_sub][n_class][3] (sqrt(2 D dt) per step, class and axis) and d_class
- * (n, NULL = class 0).  Normals from Philox, or from d_normals
- * ([n_sub][n][ndim]) when given.  With p->d_trans, each particle's class
+ * (n, NULL = class 0).  Normals from d_normals ([n_sub][n][ndim]) when given,
+ * with FP64 moves (the reference's arithmetic); else from Philox, with the
+ * positions rounded to FP32 on entry and moved in FP32.  With p->d_trans, each particle's class
  * changes after every move as the transition table says and d_class (then
  * required) is updated in place.  Replaces move_points / sample_inputs
  * (src/scopyon/sampling.py:88-162) and sampling2.__move_points /
@@ -204,12 +212,21 @@ int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, int32_t *d_class,
  * phase-major order [key][m_x mod P][m_y mod P][m_x div P][m_y div P] (with m
  * shifted by +P), NQ = (2 n_r - 1 + P - 1) / P + 1.  Each (m_x mod P,
  * m_y mod P) phase block of NQ x NQ values starts SC_BOX_BLOCK_FLOATS(NQ)
- * floats after the previous one (NQ^2 rounded up to 16 bytes, padding zero),
+ * floats after the previous one (NQ^2 rounded up to SC_BOX_ALIGN_FLOATS
+ * floats, 16 bytes by default, padding zero),
  * so a key takes P * P * SC_BOX_BLOCK_FLOATS(NQ) floats.  Built from the
  * quadrant tables of sc_psf_quadrant_sat.  With it, one emitter's footprint
  * is one contiguous, 16-byte aligned block (the pixel sums of
  * overlay_signal_, src/scopyon/_epifm.py:277-282).                         */
-#define SC_BOX_BLOCK_FLOATS(nq) ((((nq) * (nq)) + 3) & ~3)
+#ifndef SC_BOX_ALIGN_FLOATS
+#define SC_BOX_ALIGN_FLOATS 4
+#endif
+#define SC_BOX_BLOCK_FLOATS(nq) \
+    ((((nq) * (nq)) + SC_BOX_ALIGN_FLOATS - 1) & ~(SC_BOX_ALIGN_FLOATS - 1))
+
+/* SC_BOX_BLOCK_FLOATS(nq) as this library was built (floats from one phase
+ * block's start to the next).                                             */
+int sc_box_block_floats(int nq);
 
 int sc_psf_box_table(const float *d_sat, int n_keys, int n_r, int sat_pitch, int box_p,
                      float *d_box, void *stream);
@@ -217,7 +234,9 @@ int sc_psf_box_table(const float *d_sat, int n_keys, int n_r, int sat_pitch, int
 /* Emitter physics for one frame: excitation, emitted photons, photon-budget
  * bleaching, normalisation, depth key and footprint origin per particle and
  * sub-step.  d_particles is [n_sub][n_particles][5] (depth, x, y, m_id,
- * p_state) as formatted by EPIFMSimulator.__format_data; d_present
+ * p_state) as formatted by EPIFMSimulator.__format_data, or with
+ * p->row_layout 1 the FP32 rows [n_sub][n_particles][4] of sc_diffuse_steps
+ * (layout 1) at the same address; d_present
  * ([n_sub][n_particles] bytes, NULL = all present) marks particle slots
  * absent at a sub-step; d_budget holds the
  * photon budget per particle slot (initialised by the caller at first sight,

@@ -30,7 +30,8 @@ class StepParams(ctypes.Structure):
                 ("x_sec", ctypes.c_double), ("qy", ctypes.c_double), ("beer", ctypes.c_double),
                 ("norm_coeff", ctypes.c_double),
                 ("bleaching", ctypes.c_int32), ("with_optinfo", ctypes.c_int32),
-                ("box_p", ctypes.c_int32), ("box_nq", ctypes.c_int32)]
+                ("box_p", ctypes.c_int32), ("box_nq", ctypes.c_int32),
+                ("row_layout", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class SplatParams(ctypes.Structure):
@@ -79,7 +80,7 @@ class BWParams(ctypes.Structure):
 class DiffuseParams(ctypes.Structure):
     _fields_ = [("n_particles", ctypes.c_int32), ("n_sub", ctypes.c_int32),
                 ("ndim", ctypes.c_int32), ("boundary", ctypes.c_int32),
-                ("n_class", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("n_class", ctypes.c_int32), ("layout", ctypes.c_int32),
                 ("step0", ctypes.c_int64), ("seed", ctypes.c_uint64), ("d_frame", ctypes.c_void_p),
                 ("lower", ctypes.c_double * 3), ("upper", ctypes.c_double * 3),
                 ("scale", ctypes.c_double), ("origin", ctypes.c_double * 3),
@@ -99,6 +100,7 @@ _I = ctypes.c_int
 _D = ctypes.c_double
 _SIG = {
     "sc_get_version": (_I, []),
+    "sc_box_block_floats": (_I, [_I]),
     "sc_struct_sizes": (_I, [_P, _I]),
     "sc_counter_add": (_I, [_P, ctypes.c_int64, _P]),
     "sc_stage_rows": (_I, [_P, ctypes.c_int64, _P, _P, _P]),

@@ -504,18 +504,23 @@ def _DeviceFrames(sim, cfg, pipe, traj, num_frames, start_time, exposure_time, b
         uts = numpy.zeros(n_sub)
         for i, ut in windows:
             uts[i - g0] = ut
-        part = pipe._buf("particles", max(n_sub, 1) * n * 5, torch.float64)
+        # native trajectories with the identity transform: 16-byte FP32 rows
+        layout = 1 if traj.compact_rows(transform) else 0
+        width = 4 if layout else 5
+        part = pipe._buf("particles32" if layout else "particles", max(n_sub, 1) * n * width,
+                         torch.float32 if layout else torch.float64)
         if n_sub:
-            traj.run(g0, n_sub, part, transform)
+            traj.run(g0, n_sub, part, transform, layout=layout)
             if len(pipe.psf.slot_of) < pipe.psf.max_key + 2:
-                pipe.psf.ensure(_device_depth_keys(cfg, part[: n_sub * n * 5].view(n_sub, n, 5)))
+                pipe.psf.ensure(_device_depth_keys(
+                    cfg, part[: n_sub * n * width].view(n_sub, n, width).double()))
         ut_dev = torch.from_numpy(uts).to(device)
         frame_draws = draws.next_frame() if draws is not None and draws.frames else None
         seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | int(rng.randint(0, 2 ** 31 - 1)) \
             if frame_draws is None else 0
         expect, adc, opt = pipe.run_frame_device(part, ut_dev, n_sub, n, with_optinfo=full_output,
                                                  draws=frame_draws, seed=seed, counter=f,
-                                                 bleaching=bleaching)
+                                                 bleaching=bleaching, row_layout=layout)
         pipe.check_status()
         adc_np = adc.cpu().numpy().reshape(nw, nh).astype(numpy.float64)
         info = {}

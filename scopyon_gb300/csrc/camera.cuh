@@ -185,9 +185,10 @@ __device__ __forceinline__ float poisson_u32(const PoisTab &t, float lam, uint32
 
 // Two independent standard normals from two 32-bit words (Box-Muller: the
 // cosine and the sine branch).  The radius is x rsqrt(x) (relative error a
-// few 1e-7, far below what any test of the draws resolves).
+// few 1e-7, far below what any test of the draws resolves), with x kept
+// above 0: u01f rounds its largest values to 1, and x rsqrt(x) of 0 is 0 * inf.
 __device__ __forceinline__ void bm_pair(uint32_t a, uint32_t b, float &n0, float &n1) {
-    const float x = -2.0f * __logf(sc::u01f(a));
+    const float x = fmaxf(-2.0f * __logf(sc::u01f(a)), 1e-30f);
     const float r = x * rsqrtf(x);
     float sn, cs;
     sc::sincos_2pi(sc::u01f(b), &sn, &cs);

@@ -16,11 +16,13 @@
 namespace {
 
 struct DiffConsts {
-    int n, n_sub, ndim, boundary, n_class, identity;
+    int n, n_sub, ndim, boundary, n_class, identity, layout;
+    int n_sig;  // FP32 sigma table entries staged in shared memory (0: none)
     int64_t step0;
     const int64_t *frame;
     uint64_t seed;
     double lower[3], upper[3];
+    float lower_f[3], upper_f[3];
     double scale, origin[3], ux[3], uy[3], uz[3];
     const double *class_box;  // [n_class][6] lower xyz, upper xyz (optional)
     const double *trans;      // [n_sub][n_class][n_class] cumulative transitions (optional)
@@ -79,6 +81,73 @@ __device__ __forceinline__ double wrap_axis(double x, double lo, double hi, int 
     return x;
 }
 
+// ------------------------------------------------ native moves in FP32
+// With Philox normals (native mode) a particle's position is an FP32 value,
+// held exactly in the FP64 state and rows: a move is x = fma(sigma, n, x) in
+// FP32, then the walls in FP32.  GB300 issues FP64 at about 1/64 of the FP32
+// rate, so the FP64 move cost as much as the rest of a sub-step; the FP32
+// position resolves 2^-24 of its value (0.004 nm at 40 um), and a trajectory
+// of 20,000 sub-steps drifts by well under a nanometre from an FP64 one.
+// Positions that enter a launch as FP64 values are rounded to FP32 first.
+// Exact mode (the caller's normals) keeps the FP64 moves above, bit for bit
+// the reference's.
+
+// Reflecting walls in FP32: mirrored in the wall crossed until inside (at
+// most 64 times), then clamped.
+__device__ __forceinline__ float reflect_walls_f(float x, float lo, float hi) {
+    if (x >= lo && x <= hi) return x;
+    for (int it = 0; it < 64 && !(x >= lo && x <= hi); ++it)
+        x = fmaf(2.f, x < lo ? lo : hi, -x);
+    return fminf(fmaxf(x, lo), hi);
+}
+
+__device__ __forceinline__ float wrap_axis_f(float x, float lo, float hi, int boundary) {
+    if (boundary == 1) {  // periodic, as wrap_axis
+        const float len = hi - lo;
+        if (!(len > 0.f)) return lo;
+        float r = fmodf(x - lo, len);
+        if (r < 0.f) r += len;
+        return r + lo;
+    }
+    if (boundary == 2) return reflect_walls_f(x, lo, hi);
+    return x;
+}
+
+// The FP32 walls of class cls on every axis.
+__device__ __forceinline__ void class_walls_f(const DiffConsts &c, int cls, float *lo, float *hi) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (c.class_box) {
+            lo[d] = __double2float_rn(c.class_box[cls * 6 + d]);
+            hi[d] = __double2float_rn(c.class_box[cls * 6 + 3 + d]);
+        } else {
+            lo[d] = c.lower_f[d];
+            hi[d] = c.upper_f[d];
+        }
+    }
+}
+
+// FP32 sigma of (sub-step s, class cls, axis d): from the block's shared copy
+// of the launch's table (kSig), else converted from the FP64 table.  The
+// choice is a template parameter: as a run-time test the compiler predicates
+// the conversion into every sub-step, and a predicated-off FP64 instruction
+// occupies GB300's FP64 pipe as long as an executed one.
+template <bool kSig>
+__device__ __forceinline__ float sigma_f(const DiffConsts &c, const float *s_sig,
+                                         const double *sigma, int s, int cls, int d) {
+    const int e = (s * c.n_class + cls) * 3 + d;
+    if (kSig) return s_sig[e];
+    return __double2float_rn(sigma[e]);
+}
+
+// Stages the launch's sigma table in shared memory as FP32 (all threads).
+__device__ __forceinline__ void stage_sigma(const DiffConsts &c, const double *sigma, float *s_sig) {
+    for (int e = threadIdx.x; e < c.n_sig; e += blockDim.x) s_sig[e] = __double2float_rn(sigma[e]);
+}
+
+// Largest sigma table (floats) staged in shared memory.
+constexpr int kSigMax = 6144;
+
 // Formatted position [depth, x, y] of a sampling-frame point (base.py:61-110).
 __device__ __forceinline__ void format_point(const DiffConsts &c, const double *p, double *q) {
     if (c.ndim == 2) {
@@ -106,7 +175,11 @@ __device__ __forceinline__ void philox_normals(const DiffConsts &c, int i, uint6
     const sc::u4 r = sc::philox4x32_10({(uint32_t)i, (uint32_t)g, (uint32_t)(g >> 32), 0x5d1ff05eu},
                                        (uint32_t)c.seed, (uint32_t)(c.seed >> 32));
     const float u1 = sc::u01f(r.x), u2 = sc::u01f(r.y), u3 = sc::u01f(r.z), u4 = sc::u01f(r.w);
-    const float ra = sqrtf(-2.f * __logf(u1)), rb = sqrtf(-2.f * __logf(u3));
+    // radii sqrt(-2 ln u) as x rsqrt(x) (relative error a few 1e-7); x is
+    // kept above 0, since u01f rounds its largest values to 1 and x rsqrt(x)
+    // of 0 is 0 * inf
+    const float xa = fmaxf(-2.f * __logf(u1), 1e-30f), xb = fmaxf(-2.f * __logf(u3), 1e-30f);
+    const float ra = xa * rsqrtf(xa), rb = xb * rsqrtf(xb);
     float sa, ca, sb, cb;
     sc::sincos_2pi(u2, &sa, &ca);
     sc::sincos_2pi(u4, &sb, &cb);
@@ -173,15 +246,15 @@ __device__ __forceinline__ void move_point(const DiffConsts &c, double *p, int c
 
 constexpr int kDiffThreads = 128;
 
-// One thread per particle, sub-steps in order.  Each warp stages its 32 rows
-// of a sub-step ([depth, x, y, id, state], 40 B each) in shared memory and
-// writes the 1280 contiguous bytes with five coalesced 8-byte stores per
-// lane: 40 full sectors per warp and sub-step, where a row per lane would
-// touch 32 sectors with each of its five stores.
-template <bool kInjected>
+// Exact mode (the caller's normals, FP64 moves): one thread per particle,
+// sub-steps in order.  Each warp stages its 32 rows of a sub-step ([depth,
+// x, y, id, state], 40 B each) in shared memory and writes the 1280
+// contiguous bytes with five coalesced 8-byte stores per lane: 40 full
+// sectors per warp and sub-step, where a row per lane would touch 32 sectors
+// with each of its five stores.  particles NULL: no rows.
 __global__ void __launch_bounds__(kDiffThreads)
-diffuse_kernel(DiffConsts c, double *pos, int32_t *klass, const double *sigma,
-               const double *normals, double *particles) {
+diffuse_exact_kernel(DiffConsts c, double *pos, int32_t *klass, const double *sigma,
+                     const double *normals, double *particles) {
     __shared__ double rows[kDiffThreads * 5];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
@@ -202,34 +275,131 @@ diffuse_kernel(DiffConsts c, double *pos, int32_t *klass, const double *sigma,
     const double id = (double)i;
     for (int s = 0; s < c.n_sub; ++s) {
         const size_t idx = (size_t)s * c.n + i;
-        double f[3];
-        format_point(c, p, f);
-        double *q = stage + lane * 5;
-        q[0] = f[0];
-        q[1] = f[1];
-        q[2] = f[2];
-        q[3] = id;
-        q[4] = 1.0;
-        __syncwarp();
-        double *dst = particles + ((size_t)s * c.n + first) * 5;
+        if (particles) {
+            double f[3];
+            format_point(c, p, f);
+            double *q = stage + lane * 5;
+            q[0] = f[0];
+            q[1] = f[1];
+            q[2] = f[2];
+            q[3] = id;
+            q[4] = 1.0;
+            __syncwarp();
+            double *dst = particles + ((size_t)s * c.n + first) * 5;
 #pragma unroll
-        for (int r = 0; r < 5; ++r) {
-            const int e = lane + 32 * r;
-            if (e < n_rows * 5) dst[e] = stage[e];
+            for (int r = 0; r < 5; ++r) {
+                const int e = lane + 32 * r;
+                if (e < n_rows * 5) dst[e] = stage[e];
+            }
+            __syncwarp();
         }
-        __syncwarp();
         if (!live) continue;
         // one Brownian step
         const double *sg = sigma + ((size_t)s * c.n_class + k) * 3;
-        float nrm[3] = {0.f, 0.f, 0.f};
-        if (!kInjected) philox_normals(c, i, (uint64_t)(step0 + s), nrm);
-        move_point<kInjected>(c, p, k, sg, kInjected ? normals + idx * c.ndim : nullptr, nrm);
+        move_point<true>(c, p, k, sg, normals + idx * c.ndim, nullptr);
         if (c.trans) k = transition(c, k, i, s, (uint64_t)(step0 + s));
     }
     if (!live) return;
     pos[3 * i] = p[0];
     pos[3 * i + 1] = p[1];
     pos[3 * i + 2] = p[2];
+    if (c.trans) klass[i] = k;
+}
+
+// The formatted row of an FP32 position (as format_point on its FP64 value):
+// with the identity transform a permutation, converted on the integer pipes.
+__device__ __forceinline__ void format_point_f(const DiffConsts &c, const float *p, double *f) {
+    if (c.identity && c.ndim == 3) {
+        f[0] = sc::f2d_exact(p[2]);
+        f[1] = sc::f2d_exact(p[0]);
+        f[2] = sc::f2d_exact(p[1]);
+    } else if (c.ndim == 2 && c.scale == 1.0) {
+        f[0] = 0.0;
+        f[1] = sc::f2d_exact(p[0]);
+        f[2] = sc::f2d_exact(p[1]);
+    } else {
+        const double q[3] = {sc::f2d_exact(p[0]), sc::f2d_exact(p[1]), sc::f2d_exact(p[2])};
+        format_point(c, q, f);
+    }
+}
+
+// Native mode (Philox normals, FP32 moves): one thread per particle,
+// sub-steps in order.  LAYOUT 0 writes the rows of diffuse_exact_kernel
+// (staged per warp, coalesced); LAYOUT 1 writes one 16-byte row (depth, x, y,
+// 0) as FP32 per particle and sub-step -- the formatted position exactly,
+// which the identity transform keeps FP32 -- a warp's 32 rows one 512-byte
+// coalesced store; LAYOUT 2 writes no rows (the positions only advance).
+template <int LAYOUT, bool kSig>
+__global__ void __launch_bounds__(kDiffThreads)
+diffuse_native_kernel(DiffConsts c, double *pos, int32_t *klass, const double *sigma,
+                      void *particles) {
+    extern __shared__ float s_sig[];  // [n_sub][n_class][3] FP32 when kSig
+    __shared__ double rows[LAYOUT == 0 ? kDiffThreads * 5 : 1];
+    if (kSig) {
+        stage_sigma(c, sigma, s_sig);
+        __syncthreads();
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int first = i - lane;
+    if (first >= c.n) return;
+    const bool live = i < c.n;
+    const int n_rows = min(32, c.n - first);
+    double *stage = rows + (LAYOUT == 0 ? (threadIdx.x - lane) * 5 : 0);
+    float p[3] = {0.f, 0.f, 0.f};
+    int k = 0;
+    if (live) {
+        p[0] = __double2float_rn(pos[3 * i]);
+        p[1] = __double2float_rn(pos[3 * i + 1]);
+        p[2] = __double2float_rn(pos[3 * i + 2]);
+        k = klass ? klass[i] : 0;
+    }
+    float lo[3], hi[3];
+    class_walls_f(c, k, lo, hi);
+    const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
+    const double id = (double)i;
+    for (int s = 0; s < c.n_sub; ++s) {
+        if (LAYOUT == 0) {
+            double f[3];
+            format_point_f(c, p, f);
+            double *q = stage + lane * 5;
+            q[0] = f[0];
+            q[1] = f[1];
+            q[2] = f[2];
+            q[3] = id;
+            q[4] = 1.0;
+            __syncwarp();
+            double *dst = static_cast<double *>(particles) + ((size_t)s * c.n + first) * 5;
+#pragma unroll
+            for (int r = 0; r < 5; ++r) {
+                const int e = lane + 32 * r;
+                if (e < n_rows * 5) dst[e] = stage[e];
+            }
+            __syncwarp();
+        } else if (LAYOUT == 1) {
+            if (live)
+                static_cast<float4 *>(particles)[(size_t)s * c.n + i] =
+                    make_float4(c.ndim == 3 ? p[2] : 0.f, p[0], p[1], 0.f);
+        }
+        if (!live) continue;
+        float nrm[3];
+        philox_normals(c, i, (uint64_t)(step0 + s), nrm);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (d >= c.ndim) break;
+            const float x = fmaf(sigma_f<kSig>(c, s_sig, sigma, s, k, d), nrm[d], p[d]);
+            p[d] = c.boundary ? wrap_axis_f(x, lo[d], hi[d], c.boundary) : x;
+        }
+        if (c.trans) {
+            const int k1 = transition(c, k, i, s, (uint64_t)(step0 + s));
+            if (k1 != k && c.class_box) class_walls_f(c, k1, lo, hi);
+            k = k1;
+        }
+    }
+    if (!live) return;
+    pos[3 * i] = sc::f2d_exact(p[0]);
+    pos[3 * i + 1] = sc::f2d_exact(p[1]);
+    pos[3 * i + 2] = sc::f2d_exact(p[2]);
     if (c.trans) klass[i] = k;
 }
 
@@ -273,7 +443,7 @@ inline size_t rec_shared_bytes(int chunk) {
 #ifndef SC_REC_MIN_BLOCKS
 #define SC_REC_MIN_BLOCKS 6
 #endif
-template <bool kInjected>
+template <bool kInjected, bool kSig>
 __global__ void __launch_bounds__(kRecWarps * 32, SC_REC_MIN_BLOCKS)
 native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                       int32_t *klass, const double *sigma, const double *normals,
@@ -286,6 +456,11 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
     double *s_norm1 = s_emit + chunk;
     float *s_nrm = reinterpret_cast<float *>(s_norm1 + chunk);
     double *s_e = s_norm1 + chunk;  // [chunk][32], over the normals after phase 2
+    float *s_sig = s_nrm + chunk * 32 * 3;  // native: the FP32 sigma table when c.n_sig
+    if (!kInjected && kSig) {
+        stage_sigma(c, sigma, s_sig);
+        __syncthreads();
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * 32 + lane;  // this lane's particle
     const bool live = i < c.n;
@@ -299,6 +474,8 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
     // chain state: axis `warp` (axis chains) or every axis and the class (warp
     // 0 otherwise); the photon budget on budget_warp
     double p[3] = {0.0, 0.0, 0.0}, b = 0.0;
+    float pf[3] = {0.f, 0.f, 0.f};  // native mode: the FP32 positions (see diffuse_native_kernel)
+    float lo[3], hi[3];
     int cls = 0;
     if (live) {
         if (axis_chains && warp < c.ndim) {
@@ -310,8 +487,14 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
             p[2] = pos[3 * i + 2];
             cls = klass[i];
         }
+        if (!kInjected) {
+            pf[0] = __double2float_rn(p[0]);
+            pf[1] = __double2float_rn(p[1]);
+            pf[2] = __double2float_rn(p[2]);
+        }
         if (warp == budget_warp && k.bleaching) b = budget[i];
     }
+    if (!kInjected) class_walls_f(c, cls, lo, hi);
     for (int s0 = 0; s0 < c.n_sub; s0 += chunk) {
         const int ns = min(chunk, c.n_sub - s0);
         // 1. normals; per-sub-step photons and normalisation when uniform
@@ -339,7 +522,36 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
         __syncthreads();
         // 2. the position chains (and the budget chains when uniform)
         if (live) {
-            if (axis_chains && warp < c.ndim) {
+            if (!kInjected && axis_chains && warp < c.ndim) {
+                const int d = warp;
+                float x = pf[0];
+                for (int j = 0; j < ns; ++j) {
+                    const int s = s0 + j;
+                    s_pos[(j * 32 + lane) * 3 + d] = sc::f2d_exact(x);
+                    x = fmaf(sigma_f<kSig>(c, s_sig, sigma, s, cls, d),
+                             s_nrm[(j * 32 + lane) * 3 + d], x);
+                    if (c.boundary) x = wrap_axis_f(x, lo[d], hi[d], c.boundary);
+                }
+                pf[0] = x;
+            } else if (!kInjected && !axis_chains && warp == 0) {
+                for (int j = 0; j < ns; ++j) {
+                    const int s = s0 + j;
+                    double *ps = s_pos + (j * 32 + lane) * 3;
+                    ps[0] = sc::f2d_exact(pf[0]);
+                    ps[1] = sc::f2d_exact(pf[1]);
+                    ps[2] = sc::f2d_exact(pf[2]);
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        if (d >= c.ndim) break;
+                        const float x = fmaf(sigma_f<kSig>(c, s_sig, sigma, s, cls, d),
+                                             s_nrm[(j * 32 + lane) * 3 + d], pf[d]);
+                        pf[d] = c.boundary ? wrap_axis_f(x, lo[d], hi[d], c.boundary) : x;
+                    }
+                    const int k1 = transition(c, cls, i, s, (uint64_t)(step0 + s));
+                    if (k1 != cls && c.class_box) class_walls_f(c, k1, lo, hi);
+                    cls = k1;
+                }
+            } else if (axis_chains && warp < c.ndim) {
                 const int d = warp;
                 double x = p[0];
                 const double *sgd = sigma + (size_t)cls * 3 + d;
@@ -450,6 +662,11 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
         __syncthreads();
     }
     if (live) {
+        if (!kInjected) {
+            p[0] = sc::f2d_exact(pf[0]);
+            p[1] = sc::f2d_exact(pf[1]);
+            p[2] = sc::f2d_exact(pf[2]);
+        }
         if (axis_chains) {
             if (warp < c.ndim) pos[3 * i + warp] = p[0];
         } else if (warp == 0) {
@@ -501,6 +718,14 @@ int diff_consts(const ScDiffuseParams *p, DiffConsts &c) {
                 p->unit_z[d] == ez[d];
     }
     c.identity = ident ? 1 : 0;
+    for (int d = 0; d < 3; ++d) {
+        c.lower_f[d] = (float)p->lower[d];
+        c.upper_f[d] = (float)p->upper[d];
+    }
+    SC_REQUIRE(p->layout >= 0 && p->layout <= 1, "sc_diffuse_steps: layout=%d", p->layout);
+    c.layout = p->layout;
+    const int64_t n_sig = (int64_t)p->n_sub * p->n_class * 3;
+    c.n_sig = n_sig <= kSigMax ? (int)n_sig : 0;
     return SC_OK;
 }
 
@@ -513,16 +738,36 @@ extern "C" int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, int32_t
     int rc = diff_consts(p, c);
     if (rc) return rc;
     if (c.n == 0 || c.n_sub == 0) return SC_OK;
-    SC_REQUIRE(d_pos && d_sigma && d_particles, "sc_diffuse_steps: NULL pointer");
+    SC_REQUIRE(d_pos && d_sigma, "sc_diffuse_steps: NULL pointer");
     SC_REQUIRE(!p->d_trans || d_class, "sc_diffuse_steps: transitions need the class array");
+    SC_REQUIRE(c.layout == 0 || (!d_normals && (c.ndim == 3 ? c.identity : c.scale == 1.0)),
+               "sc_diffuse_steps: FP32 rows (layout 1) need native draws and the identity "
+               "transform");
     const int block = kDiffThreads;
     const int grid = (c.n + block - 1) / block;
-    if (d_normals)
-        diffuse_kernel<true><<<grid, block, 0, sc::as_stream(stream)>>>(
-            c, d_pos, d_class, d_sigma, d_normals, d_particles);
-    else
-        diffuse_kernel<false><<<grid, block, 0, sc::as_stream(stream)>>>(
-            c, d_pos, d_class, d_sigma, d_normals, d_particles);
+    cudaStream_t st = sc::as_stream(stream);
+    if (d_normals) {
+        diffuse_exact_kernel<<<grid, block, 0, st>>>(c, d_pos, d_class, d_sigma, d_normals,
+                                                     d_particles);
+    } else {
+        const size_t smem = (size_t)c.n_sig * sizeof(float);
+        const int lay = !d_particles ? 2 : c.layout;
+#define SC_DIFF_LAUNCH(L)                                                                       \
+    if (c.n_sig)                                                                                \
+        diffuse_native_kernel<L, true><<<grid, block, smem, st>>>(c, d_pos, d_class, d_sigma,   \
+                                                                  d_particles);                 \
+    else                                                                                        \
+        diffuse_native_kernel<L, false><<<grid, block, 0, st>>>(c, d_pos, d_class, d_sigma,     \
+                                                                d_particles);
+        if (lay == 2) {
+            SC_DIFF_LAUNCH(2)
+        } else if (lay == 1) {
+            SC_DIFF_LAUNCH(1)
+        } else {
+            SC_DIFF_LAUNCH(0)
+        }
+#undef SC_DIFF_LAUNCH
+    }
     return sc::launch_status("sc_diffuse_steps");
 }
 
@@ -560,14 +805,17 @@ extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *s
         sc::bin_layout(g, (int)n_rec, d_bin_ws, bin_ws_bytes, bl);
     }
     const int chunk = c.n_sub < 32 ? c.n_sub : 32;
-    const size_t smem = rec_shared_bytes(chunk);
-    if (d_normals)
-        native_records_kernel<true><<<(c.n + 31) / 32, kRecWarps * 32, smem, sc::as_stream(stream)>>>(
-            c, k, chunk, d_pos, d_class, d_sigma, d_normals, d_unit_time, d_budget, d_key_slot,
-            d_recs, g, bl, d_status);
-    else
-        native_records_kernel<false><<<(c.n + 31) / 32, kRecWarps * 32, smem, sc::as_stream(stream)>>>(
-            c, k, chunk, d_pos, d_class, d_sigma, d_normals, d_unit_time, d_budget, d_key_slot,
-            d_recs, g, bl, d_status);
+    const bool sig = !d_normals && c.n_sig > 0;
+    const size_t smem = rec_shared_bytes(chunk) + (sig ? (size_t)c.n_sig * sizeof(float) : 0);
+    auto kern = d_normals ? native_records_kernel<true, false>
+                          : sig ? native_records_kernel<false, true> : native_records_kernel<false, false>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return sc::cuda_status(e, "sc_native_records: smem attribute");
+    }
+    kern<<<(c.n + 31) / 32, kRecWarps * 32, smem, sc::as_stream(stream)>>>(
+        c, k, chunk, d_pos, d_class, d_sigma, d_normals, d_unit_time, d_budget, d_key_slot, d_recs,
+        g, bl, d_status);
     return sc::launch_status("sc_native_records");
 }

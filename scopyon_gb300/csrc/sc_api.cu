@@ -27,6 +27,8 @@ int launch_status(const char *what) { return cuda_status(cudaGetLastError(), wha
 
 extern "C" int sc_get_version(void) { return 1; }
 
+extern "C" int sc_box_block_floats(int nq) { return SC_BOX_BLOCK_FLOATS(nq); }
+
 extern "C" int sc_struct_sizes(size_t *out, int n) {
     SC_REQUIRE(out != nullptr && n >= 6, "sc_struct_sizes: need room for 6 sizes");
     out[0] = sizeof(ScStepRec);

@@ -336,7 +336,8 @@ __device__ __forceinline__ bool bulk_tile_records(
     const int it0 = tile_start[tile], it1 = tile_start[tile + 1];
     // records of this warp: m_k = it0 + warp + NW k, k < K
     const int K = it1 - it0 > warp ? (it1 - it0 - warp + NW - 1) / NW : 0;
-    constexpr uint32_t bytes = NB * 4u;
+    // the block's values, rounded up to 16 bytes (the padding after them is not read)
+    constexpr uint32_t bytes = ((NQ * NQ + 3) & ~3) * 4u;
     const int col = lane & 15, rsel = lane >> 4;
 
     // lane l decodes records 32 q + l of chunks q (cur) and q + 1 (nxt); the

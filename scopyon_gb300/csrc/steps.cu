@@ -16,11 +16,26 @@
 
 namespace {
 
+// One input row: depth, x, y and p_state (FP64 rows, or the FP32 rows of
+// sc_diffuse_steps layout 1, converted exactly on the integer pipes).
+struct Row {
+    double d, x, y, state;
+};
+
+__device__ __forceinline__ Row load_row(const void *rows, int layout, size_t idx) {
+    if (layout == 1) {
+        const float4 v = static_cast<const float4 *>(rows)[idx];
+        return Row{sc::f2d_exact(v.x), sc::f2d_exact(v.y), sc::f2d_exact(v.z), 1.0};
+    }
+    const double *q = static_cast<const double *>(rows) + idx * 5;
+    return Row{q[0], q[1], q[2], q[4]};
+}
+
 // Pass 1, one thread per particle slot, sub-steps in order: excitation,
 // emitted photons, the photon-budget chain and the normalisation.  The
 // normalisation of each (sub-step, slot) is parked in its record's x0 field
 // for pass 2 (0: nothing to splat).
-__global__ void emitter_physics_kernel(sc::StepConsts c, const double *particles,
+__global__ void emitter_physics_kernel(sc::StepConsts c, const void *particles,
                                        const double *unit_time, const uint8_t *present,
                                        double *budget, double *optinfo, ScStepRec *recs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -32,14 +47,14 @@ __global__ void emitter_physics_kernel(sc::StepConsts c, const double *particles
     const bool epi = isinf(c.penetration);
     for (int s = 0; s < c.n_sub; ++s) {
         const size_t idx = (size_t)s * c.n_particles + i;
-        const double *q = particles + idx * 5;
         if (present && !present[idx]) {
             recs[idx].x0 = 0.0;  // absent at this sub-step: no record, no state change
             continue;
         }
+        const Row q = load_row(particles, c.row_layout, idx);
         const double ut = unit_time[s];
-        double p_state = q[4];
-        const double rel0 = q[0] - c.focal[0];
+        double p_state = q.state;
+        const double rel0 = q.d - c.focal[0];
         // amplitude0 * exp(-|depth| / inf) is amplitude0 exactly
         const double amp = epi ? c.amplitude0
                                : __dmul_rn(c.amplitude0, exp(-fabs(rel0) / c.penetration));
@@ -57,10 +72,10 @@ __global__ void emitter_physics_kernel(sc::StepConsts c, const double *particles
         if (c.with_optinfo) {
             acc[0] += ut;
             acc[1] += __dmul_rn(ut, p_state);
-            acc[2] += __dmul_rn(ut, q[1]);
-            acc[3] += __dmul_rn(ut, q[2]);
-            acc[4] += __dmul_rn(ut, q[1]);
-            acc[5] += __dmul_rn(ut, q[2]);
+            acc[2] += __dmul_rn(ut, q.x);
+            acc[3] += __dmul_rn(ut, q.y);
+            acc[4] += __dmul_rn(ut, q.x);
+            acc[5] += __dmul_rn(ut, q.y);
             acc[6] += __dmul_rn(ut, rel0);
             acc[7] += norm;
         }
@@ -73,21 +88,21 @@ __global__ void emitter_physics_kernel(sc::StepConsts c, const double *particles
 }
 
 // Pass 2, one thread per (sub-step, slot): depth key and footprint.
-__global__ void emitter_footprint_kernel(sc::StepConsts c, const double *particles,
+__global__ void emitter_footprint_kernel(sc::StepConsts c, const void *particles,
                                          const int32_t *key_slot, ScStepRec *recs,
                                          double *norm_out, int32_t *status) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (idx >= (int64_t)c.n_sub * c.n_particles) return;
     const double norm = recs[idx].x0;
     if (norm_out) norm_out[idx] = norm;
-    const double *q = particles + idx * 5;
+    const Row q = load_row(particles, c.row_layout, (size_t)idx);
     ScStepRec rec;
     const int i = (int)(idx % c.n_particles), s = (int)(idx / c.n_particles);
     if (c.focal_zero)
-        sc::make_record(c, q[0], q[1], q[2], norm, key_slot, status, i, s, rec,
+        sc::make_record(c, q.d, q.x, q.y, norm, key_slot, status, i, s, rec,
                         norm_out != nullptr);
     else
-        sc::make_record(c, q[0] - c.focal[0], q[1] - c.focal[1], q[2] - c.focal[2], norm,
+        sc::make_record(c, q.d - c.focal[0], q.x - c.focal[1], q.y - c.focal[2], norm,
                         key_slot, status, i, s, rec,
                         norm_out != nullptr);
     recs[idx] = rec;
@@ -147,6 +162,8 @@ int step_consts(const ScStepParams *p, StepConsts &c) {
     c.inv_res_df = split(c.inv_res);
     c.cut_f = (float)(p->depth_cutoff + p->res);
     c.focal_zero = p->focal[0] == 0.0 && p->focal[1] == 0.0 && p->focal[2] == 0.0;
+    SC_REQUIRE(p->row_layout == 0 || p->row_layout == 1, "row_layout=%d", p->row_layout);
+    c.row_layout = p->row_layout;
     return SC_OK;
 }
 

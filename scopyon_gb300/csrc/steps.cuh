@@ -18,6 +18,7 @@ struct StepConsts {
     df half_w_df, half_h_df, half_sig_df, nhalf_sig_df, inv_px_df, px_df, inv_res_df;
     float cut_f;      // fl32(depth_cutoff + res)
     int focal_zero;   // focal point at the origin: depths and offsets need no subtraction
+    int row_layout;   // sc_emitter_steps input rows (ScStepParams.row_layout)
 };
 
 int step_consts(const ScStepParams *p, StepConsts &c);

@@ -241,7 +241,8 @@ class PSFTables:
         self.box_p = cfg.box_p
         n_signal = 2 * self.n_r - 1
         self.box_nq = (n_signal + self.box_p - 1) // self.box_p + 1 if self.box_p else 0
-        self.box_block = (self.box_nq ** 2 + 3) & ~3  # phase blocks start on 16 bytes
+        # floats from one phase block's start to the next, as the library was built
+        self.box_block = _lib.load().sc_box_block_floats(self.box_nq) if self.box_p else 0
         self.box_floats = self.box_p ** 2 * self.box_block
         self.box = torch.empty(0, dtype=torch.float32, device=device) if self.box_p else None
 
@@ -720,8 +721,10 @@ class FramePipeline:
                                      bleaching, stream)
 
     def run_frame_device(self, part, ut, n_sub, n, with_optinfo=True, draws=None, seed=0,
-                         counter=0, present=None, bleaching=None, stream=None, d_frame=None):
-        """One frame from device tensors: part (n_sub*n*5 f64), ut (n_sub f64)."""
+                         counter=0, present=None, bleaching=None, stream=None, d_frame=None,
+                         row_layout=0):
+        """One frame from device tensors: part (n_sub*n*5 f64 rows, or with
+        row_layout 1 n_sub*n*4 f32 rows of sc_diffuse_steps), ut (n_sub f64)."""
         s = stream_ptr(stream)
         self.ensure_slots(n)
         n_rec = n_sub * n
@@ -734,6 +737,7 @@ class FramePipeline:
         norm = self._buf("norm64", max(n_rec, 1), torch.float64) if exact else None
         if n_rec:
             sp = self.step_params(n_sub, n, with_optinfo)
+            sp.row_layout = row_layout
             if bleaching is not None:
                 sp.bleaching = 1 if bleaching else 0
             call("sc_emitter_steps", sp, ptr(part), ptr(ut), ptr(present), ptr(self.psf.key_slot),

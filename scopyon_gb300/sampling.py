@@ -144,6 +144,8 @@ class DeviceTrajectories:
     def reset(self):
         pos = numpy.zeros((self.n_particles, 3))
         pos[:, : self.ndim] = self.points0[:, : self.ndim]
+        if self.native:  # native moves keep FP32 positions (sc_diffuse_steps)
+            pos = pos.astype(numpy.float32).astype(numpy.float64)
         if self._pos is None:
             self._pos = torch.from_numpy(pos).to(self.device)
             self._cls = torch.from_numpy(self.klass).to(self.device)
@@ -203,14 +205,33 @@ class DeviceTrajectories:
         p.d_class_box = None if self.class_box is None else self.class_box.data_ptr()
         return p
 
-    def run(self, g0, n, out, transform=None, stream=None):
+    @property
+    def native(self):
+        """Philox normals: positions are FP32 values, moved in FP32 on the device."""
+        return self.normals is None
+
+    def compact_rows(self, transform=None):
+        """Whether frames can use the 16-byte FP32 rows of sc_diffuse_steps
+        (layout 1): native draws and the identity preprocessing transform."""
+        t = transform or {}
+        if not self.native or float(t.get("scale", 1.0)) != 1.0:
+            return False
+        if self.ndim == 2:
+            return True
+        return (numpy.array_equal(numpy.asarray(t.get("origin", (0.0, 0.0, 0.0)), float), numpy.zeros(3))
+                and numpy.array_equal(numpy.asarray(t.get("unit_x", (1.0, 0.0, 0.0)), float), [1.0, 0.0, 0.0])
+                and numpy.array_equal(numpy.asarray(t.get("unit_y", (0.0, 1.0, 0.0)), float), [0.0, 1.0, 0.0]))
+
+    def run(self, g0, n, out, transform=None, stream=None, layout=0):
         """Write the formatted positions of time indices g0 .. g0+n-1 to ``out``
-        ([n][N][5] float64 on the device) and move the particles past them."""
+        ([n][N][5] float64 on the device; with layout 1, [n][N][4] float32
+        rows [depth, x, y, 0]; None: no rows) and move the particles past them."""
         if self._pos is None or self._index > g0:
             self.reset()
         if self._index < g0:
             self.advance_to(g0, transform, stream)
         p = self.params(g0, n, **(transform or {}))
+        p.layout = layout
         sig = torch.from_numpy(self._sigma(g0, n)).to(self.device)
         normals = None
         if self.normals is not None:
@@ -264,11 +285,13 @@ class DeviceTrajectories:
             p.d_trans = self._g_trans.data_ptr()
         return p
 
-    def launch_frame(self, n_sub, out, d_frame, transform=None, stream=None):
+    def launch_frame(self, n_sub, out, d_frame, transform=None, stream=None, layout=0):
         """Enqueue one frame's sub-steps, step index taken from the device counter
-        ``d_frame`` (frame f covers steps f * n_sub ... f * n_sub + n_sub - 1).
+        ``d_frame`` (frame f covers steps f * n_sub ... f * n_sub + n_sub - 1),
+        rows in ``out`` as ``run`` writes them for ``layout``.
         Fixed arguments only, so it can be captured in a CUDA graph."""
         p = self.graph_params(0, n_sub, transform)
+        p.layout = layout
         p.d_frame = d_frame.data_ptr()
         call("sc_diffuse_steps", p, ptr(self._pos), ptr(self._cls), ptr(self._g_sigma), None,
              ptr(out), stream_ptr(stream))
@@ -278,8 +301,7 @@ class DeviceTrajectories:
             self.reset()
         while self._index < k:
             n = min(k - self._index, 64)
-            scratch = torch.empty(n * self.n_particles * 5, dtype=torch.float64, device=self.device)
-            self.run(self._index, n, scratch, transform, stream)
+            self.run(self._index, n, None, transform, stream)  # positions only, no rows
 
 
 def concatenate(*trajs):

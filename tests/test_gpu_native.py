@@ -356,3 +356,116 @@ def test_host_inputs_fast_path_matches_general_path(sg, pin_limit, monkeypatch):
         outs.append(numpy.array(frames))
     numpy.testing.assert_array_equal(outs[0], outs[1])
     assert outs[0].std(axis=0).max() > 0
+
+
+@pytest.mark.parametrize("boundary,ndim", [("reflecting", 3), ("periodic", 3), ("none", 2)])
+def test_native_rows_layouts_agree(sg, boundary, ndim):
+    """Native (Philox) trajectories move in FP32: every position is an FP32
+    value.  The 16-byte FP32 rows (layout 1) hold the same values as the FP64
+    [depth, x, y, id, state] rows (layout 0), and a launch without rows
+    leaves the particles where a launch with rows does."""
+    n, n_sub = 1000, 7
+    t = numpy.arange(3 * n_sub + 1) * 1e-3
+    lo, hi = [-2e-6, -2e-6, -0.3e-6][:ndim], [2e-6, 2e-6, 0.3e-6][:ndim]
+    traj = sg.sample_inputs(t, N=n, lower=lo, upper=hi, D=0.5e-12, ndim=ndim,
+                            rng=numpy.random.RandomState(8), boundary=boundary)
+    a, b, c = traj.copy(), traj.copy(), traj.copy()
+    rows0 = torch.empty(n_sub * n * 5, dtype=torch.float64, device="cuda")
+    rows1 = torch.empty(n_sub * n * 4, dtype=torch.float32, device="cuda")
+    for g0 in (0, n_sub, 2 * n_sub):
+        a.run(g0, n_sub, rows0, layout=0)
+        b.run(g0, n_sub, rows1, layout=1)
+        c.run(g0, n_sub, None)
+        r0 = rows0.view(n_sub, n, 5).cpu().numpy()
+        r1 = rows1.view(n_sub, n, 4).cpu().numpy().astype(numpy.float64)
+        numpy.testing.assert_array_equal(r0[:, :, :3], r1[:, :, :3])
+        assert (r1[:, :, 3] == 0).all()
+        numpy.testing.assert_array_equal(r0[:, :, 3], numpy.broadcast_to(numpy.arange(n), (n_sub, n)))
+        numpy.testing.assert_array_equal(r0[:, :, 4], 1.0)
+        pa, pb, pc = (x._pos.cpu().numpy() for x in (a, b, c))
+        numpy.testing.assert_array_equal(pa, pb)
+        numpy.testing.assert_array_equal(pa, pc)
+        numpy.testing.assert_array_equal(pa, pa.astype(numpy.float32).astype(numpy.float64))
+        assert (r0[1:, :, 1] != r0[:-1, :, 1]).mean() > 0.9  # the particles move
+    if boundary == "reflecting":
+        for d in range(ndim):
+            assert (pa[:, d] >= numpy.float32(lo[d])).all() and (pa[:, d] <= numpy.float32(hi[d])).all()
+
+
+def test_device_frames_from_fp32_rows_equal_fp64_rows(sg, monkeypatch):
+    """generate_images on native device trajectories reads the 16-byte FP32
+    rows; forcing the FP64 rows gives the same frames, bit for bit."""
+    from scopyon_gb300.sampling import DeviceTrajectories
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {"magnification": 100,
+                            "detector": {"type": "EMCCD", "image_size": [48, 48],
+                                         "exposure_time": 0.004},
+                            "effects": {"photo_bleaching": {"switch": True, "half_life": 0.01}}}})
+    t = numpy.arange(5 * 4 + 1) * 1e-3
+    traj = sg.sample_inputs(t, N=300, lower=[-3e-6, -3e-6, -0.2e-6], upper=[3e-6, 3e-6, 0.2e-6],
+                            D=0.3e-12, ndim=3, rng=numpy.random.RandomState(21))
+    assert traj.compact_rows({"scale": 1.0})
+
+    def frames():
+        sim = sg.EPIFMSimulator(cfg, method="default", rng=numpy.random.RandomState(2))
+        return [(img.as_array(), info["expectation"], info["fluorescence_states"])
+                for img, info in sim.generate_images(traj.copy(), 4, full_output=True)]
+
+    fp32 = frames()
+    monkeypatch.setattr(DeviceTrajectories, "compact_rows", lambda self, transform=None: False)
+    fp64 = frames()
+    for (a1, e1, s1), (a0, e0, s0) in zip(fp32, fp64):
+        numpy.testing.assert_array_equal(e1, e0)
+        numpy.testing.assert_array_equal(a1, a0)
+        assert s1 == s0
+    assert fp32[0][1].max() > 0
+
+
+def _philox4x32_10(ctr, key):
+    """Philox4x32-10 of one counter (four uint32) and key (two uint32), as the
+    kernels draw it (Salmon et al., SC'11)."""
+    x, y, z, w = (int(v) & 0xffffffff for v in ctr)
+    k0, k1 = (int(v) & 0xffffffff for v in key)
+    for _ in range(10):
+        p0, p1 = 0xD2511F53 * x, 0xCD9E8D57 * z
+        x, y, z, w = ((p1 >> 32) ^ y ^ k0, p1 & 0xffffffff, (p0 >> 32) ^ w ^ k1,
+                      p0 & 0xffffffff)
+        k0, k1 = (k0 + 0x9E3779B9) & 0xffffffff, (k1 + 0xBB67AE85) & 0xffffffff
+    return x, y, z, w
+
+
+def test_box_muller_radius_at_the_largest_uniform(sg):
+    """A Philox word whose top 24 bits are all set gives the uniform 1.0 (the
+    24-bit uniform plus half a step rounds up), so the Box-Muller radius
+    sqrt(-2 ln u) is 0.  The seeds below were found by searching the key space
+    for such a word: the camera's read-noise word of pixel 0 (counter 1) and
+    the first radius of particle 0's normals at step 0.  The draws stay
+    finite and the normals 0."""
+    from scopyon_gb300 import _lib
+    from scopyon_gb300._lib import call, ptr, stream_ptr
+    from scopyon_gb300.sampling import DeviceTrajectories
+    cam_seed, dif_seed = 2656475, 14960767
+    assert _philox4x32_10((0, 1, 0, 0), (cam_seed, 0))[2] >> 8 == 0xFFFFFF
+    assert _philox4x32_10((0, 0, 0, 0x5d1ff05e), (dif_seed, 0))[0] >> 8 == 0xFFFFFF
+    dev = torch.device("cuda")
+    ph = torch.zeros(2, dtype=torch.float32, device=dev)
+    adc = torch.empty(2, dtype=torch.float64, device=dev)
+    status = torch.zeros(_lib.STATUS_WORDS, dtype=torch.int32, device=dev)
+    cp = _lib.CameraParams()
+    cp.nw, cp.nh, cp.camera, cp.exact, cp.rounding, cp.bit = 1, 2, _lib.CAM_CCD, 0, 0, 16
+    cp.qe, cp.background, cp.readout_noise, cp.emgain = 1.0, 0.0, 50.0, 1.0
+    cp.fullwell, cp.offset0, cp.gain0 = 60000.0, 100.0, 1.0
+    cp.seed, cp.counter = cam_seed, 1
+    cp.d_poisson_table = _lib.poisson_table(dev).data_ptr()
+    call("sc_camera", cp, ptr(ph), None, None, None, None, None, None, None, None, None, None,
+         None, ptr(adc), None, ptr(status), stream_ptr())
+    a = adc.cpu().numpy()
+    assert int(status[0]) == 0
+    assert numpy.isfinite(a).all()
+    assert abs(a[0] - 100.0) < 1e-6  # no photons, no read noise: the offset
+    pts = numpy.array([[0.0, 0.0, 0.0, 0.0, 1.0], [1e-7, 1e-7, 0.0, 1.0, 1.0]])
+    traj = DeviceTrajectories([0.0, 1e-3, 2e-3], pts, 1e-12, 3, dif_seed, device="cuda")
+    end = traj.copy().materialize(1)
+    assert numpy.isfinite(end).all()
+    assert abs(end[0, 0]) < 1e-18 and abs(end[0, 1]) < 1e-18  # radius 0: no move in x, y
+    assert end[0, 2] != 0.0 and end[1, 0] != float(numpy.float32(1e-7))  # the others move

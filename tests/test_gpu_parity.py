@@ -77,7 +77,8 @@ def test_box_table(lib, golden):
     lib.call("sc_psf_quadrant_sat", lib.ptr(_dev(radial)), 1, 1000, 1e-9, lib.ptr(sat), pitch,
              lib.stream_ptr())
     nq = (1999 + P - 1) // P + 1
-    nb = (nq * nq + 3) & ~3
+    nb = lib.load().sc_box_block_floats(nq)
+    assert nb >= nq * nq and nb % 4 == 0
     box = torch.full((P * P * nb,), -1.0, dtype=torch.float32, device="cuda")
     lib.call("sc_psf_box_table", lib.ptr(sat), 1, 1000, pitch, P, lib.ptr(box), lib.stream_ptr())
     blocks = box.cpu().numpy().reshape(P, P, nb)

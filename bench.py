@@ -314,7 +314,8 @@ def gb300_arm(args, rank, world):
         "config": workload_dict(),
         "run": {"depth_keys": len(pipe.psf.slot_of), "psf_tables_gb": round(tables_gb, 2),
                 "tile": pipe.tile, "warps_per_tile": pipe.warps, "stages": pipe.stages,
-                "tile_autotune_ms_per_frame": {"%dx%d/%dw/%ds" % (t, t, w, st): round(ms, 4)
+                "box_kernel": "registers" if pipe.stages == 0 else "bulk-copy ring",
+                "tile_autotune_ms_per_frame": {_tune_name(t, w, st): round(ms, 4)
                                                for (t, w, st), ms in tune.items()},
                 "step": "one frame: Brownian sub-steps, physics, binning, splat, camera; "
                         "%d frame(s) per CUDA graph replay%s" % (
@@ -801,10 +802,14 @@ def hbm_stages(dev, peak, steps=20, warmup=3, n_emit=1 << 22, edge=8192, seed=5)
     return out
 
 
+def _tune_name(t, w, st):
+    """Label of a tile choice: edge, warps, and copies in flight or 'reg'."""
+    return "%dx%d/%dw/%s" % (t, t, w, "reg" if st == 0 else "%ds" % st)
+
+
 def _tune_names(tune):
     """Autotuner results keyed by readable names."""
-    return {("%dx%d/%dw/%ds" % (k[0], k[0], k[1], k[2]) if len(k) == 3 else "%s=%s" % k): ms
-            for k, ms in tune.items()}
+    return {(_tune_name(*k) if len(k) == 3 else "%s=%s" % k): ms for k, ms in tune.items()}
 
 
 def batched_arm(args, dev, n_fields=256, frames=50, substeps=10, seed=123, loop=True):
@@ -1112,7 +1117,8 @@ def main():
                     help="splat tile edge (8 or 16); default: autotuned")
     ap.add_argument("--warps", type=int, default=4, help="warps per splat tile with --tile")
     ap.add_argument("--stages", type=int, default=4,
-                    help="box-table block copies in flight per splat warp with --tile")
+                    help="box-table block copies in flight per splat warp with --tile "
+                         "(0: the register box kernel)")
     ap.add_argument("--case", choices=["dgrad", "batched", "fwdbwd", "stages", "bwdiff"],
                     default=None,
                     help="profiling: run one workload alone and print its result object "

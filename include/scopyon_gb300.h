@@ -106,6 +106,9 @@ typedef struct {
                              /* wait; 0: the normal bound (4096), -1: none, so that wait    */
                              /* runs out at once (status bit 5) while the copies in flight  */
                              /* are still drained under the normal bound                   */
+    int32_t box_kernel;      /* box path: 0 block copies into a shared-memory ring per warp */
+                             /* (cp.async.bulk + mbarrier), 1 16-byte loads into registers  */
+    int32_t pad;
     double px, res;
 } ScSplatParams;
 
@@ -227,6 +230,15 @@ int sc_diffuse_steps(const ScDiffuseParams *p, double *d_pos, int32_t *d_class,
 /* SC_BOX_BLOCK_FLOATS(nq) as this library was built (floats from one phase
  * block's start to the next).                                             */
 int sc_box_block_floats(int nq);
+
+/* Sets the largest L2 fetch from DRAM (32, 64 or 128 bytes; 0 the driver's
+ * choice) as a hint for the current device's context in this process
+ * (cudaLimitMaxL2FetchGranularity): the splat's random 784-byte box-table
+ * blocks and 32-byte record heads then move about 842 bytes per record
+ * instead of about 1,010.  It applies to every kernel of the process until
+ * the process ends or the next call, and changes no setting of the GPU
+ * itself.  No counterpart in the reference (a CPU program).                */
+int sc_set_l2_fetch_granularity(int bytes);
 
 int sc_psf_box_table(const float *d_sat, int n_keys, int n_r, int sat_pitch, int box_p,
                      float *d_box, void *stream);

@@ -42,7 +42,8 @@ class SplatParams(ctypes.Structure):
                 ("n_images", ctypes.c_int32), ("rec_per_image", ctypes.c_int32),
                 ("box_p", ctypes.c_int32), ("box_nq", ctypes.c_int32),
                 ("n_slots", ctypes.c_int32), ("box_stages", ctypes.c_int32),
-                ("first_wait_polls", ctypes.c_int32),
+                ("first_wait_polls", ctypes.c_int32), ("box_kernel", ctypes.c_int32),
+                ("pad", ctypes.c_int32),
                 ("px", ctypes.c_double), ("res", ctypes.c_double)]
 
 
@@ -101,6 +102,7 @@ _D = ctypes.c_double
 _SIG = {
     "sc_get_version": (_I, []),
     "sc_box_block_floats": (_I, [_I]),
+    "sc_set_l2_fetch_granularity": (_I, [_I]),
     "sc_struct_sizes": (_I, [_P, _I]),
     "sc_counter_add": (_I, [_P, ctypes.c_int64, _P]),
     "sc_stage_rows": (_I, [_P, ctypes.c_int64, _P, _P, _P]),

@@ -230,6 +230,8 @@ class BatchedFields:
         times the launch's resident blocks per SM (fewer leave room for the
         next frame's records on the side stream).  Returns {choice: ms per
         frame}, a choice being (tile, warps, stages) or ('blocks_per_sm', n)."""
+        if self.persistent:  # its tiles always take the bulk-copy ring
+            candidates = [cand for cand in candidates if cand[2] > 0]
         times = tune_tiles(self.graph, candidates, frames)
         name = "%dx%d tiles, %d warps, %d stages"
         self.tuning = {name % (t, t, w, st): ms for (t, w, st), ms in times.items()}

@@ -463,6 +463,26 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * 32 + lane;  // this lane's particle
+    // native mode keeps the sub-steps' positions as FP32 values ([chunk][32][3]
+    // floats over the start of s_pos), exact mode as FP64
+    float *s_posf = reinterpret_cast<float *>(s_pos);
+    auto pos_d = [&](int j, double *q) {
+        if (kInjected) {
+            const double *ps = s_pos + (j * 32 + lane) * 3;
+            q[0] = ps[0];
+            q[1] = ps[1];
+            q[2] = ps[2];
+        } else {
+            const float *ps = s_posf + (j * 32 + lane) * 3;
+            q[0] = sc::f2d_exact(ps[0]);
+            q[1] = sc::f2d_exact(ps[1]);
+            q[2] = sc::f2d_exact(ps[2]);
+        }
+    };
+    // native records from the FP32 positions directly (no FP64 conversions):
+    // the formatted position is a permutation of them and the focal point 0
+    const bool f32_records =
+        !kInjected && k.focal_zero && (c.ndim == 3 ? c.identity != 0 : c.scale == 1.0);
     const bool live = i < c.n;
     const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
     // the excitation is the same for every particle: EPI, or a flat field
@@ -527,7 +547,7 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                 float x = pf[0];
                 for (int j = 0; j < ns; ++j) {
                     const int s = s0 + j;
-                    s_pos[(j * 32 + lane) * 3 + d] = sc::f2d_exact(x);
+                    s_posf[(j * 32 + lane) * 3 + d] = x;
                     x = fmaf(sigma_f<kSig>(c, s_sig, sigma, s, cls, d),
                              s_nrm[(j * 32 + lane) * 3 + d], x);
                     if (c.boundary) x = wrap_axis_f(x, lo[d], hi[d], c.boundary);
@@ -536,10 +556,10 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
             } else if (!kInjected && !axis_chains && warp == 0) {
                 for (int j = 0; j < ns; ++j) {
                     const int s = s0 + j;
-                    double *ps = s_pos + (j * 32 + lane) * 3;
-                    ps[0] = sc::f2d_exact(pf[0]);
-                    ps[1] = sc::f2d_exact(pf[1]);
-                    ps[2] = sc::f2d_exact(pf[2]);
+                    float *ps = s_posf + (j * 32 + lane) * 3;
+                    ps[0] = pf[0];
+                    ps[1] = pf[1];
+                    ps[2] = pf[2];
 #pragma unroll
                     for (int d = 0; d < 3; ++d) {
                         if (d >= c.ndim) break;
@@ -612,8 +632,8 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
         if (!uniform) {
             if (live) {
                 for (int j = warp; j < ns; j += kRecWarps) {
-                    const double *ps = s_pos + (j * 32 + lane) * 3;
-                    const double q[3] = {ps[0], ps[1], ps[2]};
+                    double q[3];
+                    pos_d(j, q);
                     double f[3];
                     format_point(c, q, f);
                     const double rel0 = f[0] - k.focal[0];
@@ -644,17 +664,26 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
         if (live) {
             for (int j = warp; j < ns; j += kRecWarps) {
                 const int s = s0 + j;
-                const double *ps = s_pos + (j * 32 + lane) * 3;
-                const double q[3] = {ps[0], ps[1], c.ndim == 3 ? ps[2] : 0.0};
-                double f[3];
-                format_point(c, q, f);
                 const double norm = s_norm[j * 32 + lane];
                 ScStepRec rec;
-                if (k.focal_zero)
-                    sc::make_record(k, f[0], f[1], f[2], norm, key_slot, status, i, s, rec);
-                else
-                    sc::make_record(k, f[0] - k.focal[0], f[1] - k.focal[1], f[2] - k.focal[2],
-                                    norm, key_slot, status, i, s, rec);
+                if (f32_records) {
+                    const float *ps = s_posf + (j * 32 + lane) * 3;
+                    sc::make_record<float>(k, c.ndim == 3 ? ps[2] : 0.f, ps[0], ps[1], norm,
+                                           key_slot, status, i, s, rec);
+                } else {
+                    double q[3];
+                    pos_d(j, q);
+                    if (c.ndim != 3) q[2] = 0.0;
+                    double f[3];
+                    format_point(c, q, f);
+                    if (k.focal_zero)
+                        sc::make_record<double>(k, f[0], f[1], f[2], norm, key_slot, status, i, s,
+                                                rec);
+                    else
+                        sc::make_record<double>(k, f[0] - k.focal[0], f[1] - k.focal[1],
+                                                f[2] - k.focal[2], norm, key_slot, status, i, s,
+                                                rec);
+                }
                 recs[(size_t)s * c.n + i] = rec;
                 if (bl.count) sc::bin_record(g, rec, s * c.n + i, bl.count, bl.rec_bin, sc::rank_array(bl));
             }

@@ -29,6 +29,13 @@ extern "C" int sc_get_version(void) { return 1; }
 
 extern "C" int sc_box_block_floats(int nq) { return SC_BOX_BLOCK_FLOATS(nq); }
 
+extern "C" int sc_set_l2_fetch_granularity(int bytes) {
+    SC_REQUIRE(bytes == 0 || bytes == 32 || bytes == 64 || bytes == 128,
+               "sc_set_l2_fetch_granularity: %d bytes (0, 32, 64 or 128)", bytes);
+    return sc::cuda_status(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t)bytes),
+                           "sc_set_l2_fetch_granularity");
+}
+
 extern "C" int sc_struct_sizes(size_t *out, int n) {
     SC_REQUIRE(out != nullptr && n >= 6, "sc_struct_sizes: need room for 6 sizes");
     out[0] = sizeof(ScStepRec);

@@ -491,6 +491,173 @@ int launch_bulk(const ScStepRec *recs, const int32_t *tile_start, const int32_t 
     return sc::launch_status("sc_splat bulk-copy box");
 }
 
+// ------------------------------------------------ register-path box splat
+// The same box-path records as splat_box_bulk_kernel, with the blocks moved
+// by ordinary 16-byte loads: lane l holds the block's floats 4l .. 4l + 3 and,
+// when there are more than 128, 128 + 4l .. 128 + 4l + 3.  Float f of the
+// block (row f / NQ, column f % NQ) is added into the warp's tile buffer at a
+// lane-constant offset from the record's corner; the buffer is row-major
+// with row stride S (chosen on the host so that a warp's 32 adds touch each
+// bank at most twice) and one margin row and column.  Each warp loads its
+// next record's block before it adds the current one, and the SM's many
+// resident warps (no staging buffers: about 3 KB of shared memory per warp)
+// keep enough blocks in flight to cover the DRAM latency of random reads.
+// Record m of the tile's box list goes to warp m mod NW, in list order, so a
+// pixel's sums are formed in the same order as in the bulk-copy kernel.
+template <int NQ>
+struct RegRec {
+    float4 a, b;  // the block's values this lane holds
+    float w;
+    int dd;       // (dr + 128) | (dc + 128) << 8
+    int flags;    // bit 0 splat it, bit 1 the unconditional path applies
+};
+
+template <int NW, int NQ>
+__global__ void __launch_bounds__(NW * 32)
+splat_box_reg_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
+                     const int32_t *__restrict__ items, SplatConsts c, int S, int rows,
+                     int64_t table_floats, float *__restrict__ ws, int32_t *status) {
+    extern __shared__ __align__(16) float smem_reg[];
+    constexpr int NF = NQ * NQ;
+    constexpr int NB = SC_BOX_BLOCK_FLOATS(NQ);
+    constexpr int N1 = (NB - 128) / 4;  // lanes that hold a second float4
+    static_assert(NB > 128 && NB <= 256 && NB % 4 == 0, "block of 129 .. 256 floats");
+    const int E = c.edge, EE = c.edge * c.edge;
+    const int BS = (rows * S + 31) & ~31;
+    float *acc = smem_reg;  // [NW][BS]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x;
+    const int t = tile % c.tiles_per_image;
+    const int x0 = (t / c.tiles_y) * c.tile, y0 = (t % c.tiles_y) * c.tile;
+    for (int i = threadIdx.x; i < NW * BS; i += blockDim.x) acc[i] = 0.f;
+    __syncthreads();
+    float *my = acc + warp * BS;
+    // offsets of this lane's floats from the record's corner; the padding
+    // floats after NF (zero in the table) land in the margin rows below
+    int off[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int f = (j < 4 ? 4 * lane + j : 128 + 4 * lane + j - 4);
+        off[j] = (f / NQ) * S + f % NQ;
+    }
+    const int it0 = tile_start[tile], it1 = tile_start[tile + 1];
+    const int K = it1 - it0 > warp ? (it1 - it0 - warp + NW - 1) / NW : 0;
+    // lane l keeps the decoded descriptor of record 32 q + l of chunk q
+    int chunk = -1;
+    int4 my_desc = make_int4(0, 0, 0, 0);
+    const float *my_src = c.box;
+    auto fetch = [&](int k, RegRec<NQ> &r) {
+        if ((k >> 5) != chunk) {
+            chunk = k >> 5;
+            const int kk = 32 * chunk + lane;
+            my_desc = decode_record<NQ>(recs, items, it0 + warp + NW * kk, kk < K, x0, y0, c,
+                                        table_floats, NB, my_src, status, tile);
+        }
+        const int src_lane = k & 31;
+        r.w = __int_as_float(__shfl_sync(0xffffffffu, my_desc.x, src_lane));
+        r.dd = __shfl_sync(0xffffffffu, my_desc.y, src_lane);
+        r.flags = __shfl_sync(0xffffffffu, my_desc.w, src_lane);
+        const uint64_t sp = __shfl_sync(0xffffffffu, (unsigned long long)(uintptr_t)my_src, src_lane);
+        const float4 *src = reinterpret_cast<const float4 *>((uintptr_t)sp);
+        r.a = make_float4(0.f, 0.f, 0.f, 0.f);
+        r.b = r.a;
+        if (r.flags & 1) {
+            r.a = __ldg(src + lane);
+            if (lane < N1) r.b = __ldg(src + 32 + lane);
+        }
+    };
+    RegRec<NQ> cur, nxt;
+    if (K > 0) fetch(0, cur);
+    for (int k = 0; k < K; ++k) {
+        if (k + 1 < K) fetch(k + 1, nxt);
+        if (cur.flags & 1) {
+            const int dr = (cur.dd & 0xff) - 128, dc = ((cur.dd >> 8) & 0xff) - 128;
+            const float v[8] = {cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, cur.b.z, cur.b.w};
+            float *D = my + (dr + 1) * S + dc + 1;
+            if (cur.flags & 2) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) D[off[j]] = fmaf(cur.w, v[j], D[off[j]]);
+                if (lane < N1) {
+#pragma unroll
+                    for (int j = 4; j < 8; ++j) D[off[j]] = fmaf(cur.w, v[j], D[off[j]]);
+                }
+            } else {
+                // clipped by the image's low edges: rows and columns from 0,
+                // rows below the tile buffer's edge
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int f = (j < 4 ? 4 * lane + j : 128 + 4 * lane + j - 4);
+                    const int r = dr + f / NQ, cc = dc + f % NQ;
+                    if ((j < 4 || lane < N1) && f < NF && r >= 0 && r < E && cc >= 0)
+                        D[off[j]] = fmaf(cur.w, v[j], D[off[j]]);
+                }
+            }
+        }
+        cur = nxt;
+    }
+    __syncthreads();
+    float *out = ws + (size_t)tile * EE;
+    for (int p = threadIdx.x; p < EE; p += blockDim.x) {
+        const int r = p / E, cc = p - (p / E) * E;
+        const int o = (r + 1) * S + cc + 1;
+        float sum = 0.f;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) sum += acc[w * BS + o];
+        out[p] = sum;
+    }
+}
+
+// Row stride of the register kernel's tile buffers: at least `min_s`, the
+// smallest with the fewest shared-memory bank conflicts over the lanes' adds.
+inline int reg_row_stride(int nq, int min_s) {
+    const int nb = SC_BOX_BLOCK_FLOATS(nq);
+    int best = min_s, best_cost = INT_MAX;
+    for (int S = min_s; S < min_s + 48; ++S) {
+        int cost = 0;
+        for (int part = 0; part < 2; ++part)
+            for (int j = 0; j < 4; ++j) {
+                int count[32] = {0};
+                int worst = 0;
+                for (int l = 0; l < 32; ++l) {
+                    const int f = part * 128 + 4 * l + j;
+                    if (f >= nb) continue;
+                    const int bank = ((f / nq) * S + f % nq) & 31;
+                    worst = worst > ++count[bank] ? worst : count[bank];
+                }
+                cost += worst;
+            }
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = S;
+        }
+    }
+    return best;
+}
+
+template <int NW, int NQ>
+int launch_reg(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
+               const SplatConsts &c, int n_tiles, int n_slots, float *ws, int32_t *status,
+               cudaStream_t s, bool &done) {
+    done = false;
+    if (n_slots <= 0 || c.box_nq != NQ) return SC_OK;
+    // buffer rows and columns -1 .. tile + NQ (the padding floats land at row NQ)
+    const int span = max(c.edge, c.tile + NQ) + 2;
+    const int S = reg_row_stride(NQ, span);
+    const int rows = span + 1;
+    const int64_t table_floats = (int64_t)n_slots * c.box_p * c.box_p * SC_BOX_BLOCK_FLOATS(NQ);
+    const size_t smem = (size_t)NW * ((rows * S + 31) & ~31) * sizeof(float);
+    if (smem > 160 * 1024) return SC_OK;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(splat_box_reg_kernel<NW, NQ>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return sc::cuda_status(e, "sc_splat: smem attribute");
+    }
+    splat_box_reg_kernel<NW, NQ><<<n_tiles, NW * 32, smem, s>>>(recs, tile_start, items, c, S, rows,
+                                                                table_floats, ws, status);
+    done = true;
+    return sc::launch_status("sc_splat register box");
+}
+
 // Summed-area path: the tile's second bin.  Adds into the tile buffer the box
 // kernel wrote (accumulate = 1) or writes it (accumulate = 0, no box tables).
 template <int NW>
@@ -633,9 +800,24 @@ __global__ void splat_merge_kernel(const float *__restrict__ ws, SplatConsts c, 
 template <int NW>
 int launch_splat(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
                  const float2 *sat, const SplatConsts &c, int n_tiles, int n_slots, int stages,
-                 bool box, float *ws, int32_t *status, cudaStream_t s) {
+                 int box_kernel, bool box, float *ws, int32_t *status, cudaStream_t s) {
     const int ee = c.edge * c.edge;
     const int bs = (ee + 31) & ~31;
+    if (box && box_kernel == 1) {
+        // register kernel for blocks of 12..16 rows
+        bool done = false;
+        int rc = SC_OK;
+        switch (c.box_nq) {
+            case 12: rc = launch_reg<NW, 12>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            case 13: rc = launch_reg<NW, 13>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            case 14: rc = launch_reg<NW, 14>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            case 15: rc = launch_reg<NW, 15>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            case 16: rc = launch_reg<NW, 16>(recs, tile_start, items, c, n_tiles, n_slots, ws, status, s, done); break;
+            default: break;
+        }
+        if (rc) return rc;
+        if (done) box = false;  // the summed-area pass below accumulates
+    }
     if (box) {
         // bulk-copy kernel for blocks of 12..16 rows (pixels of 134..181 grid rows)
         bool done = false;
@@ -1030,6 +1212,8 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
     SC_REQUIRE(d_tile_start && d_image && d_ws, "sc_splat: NULL pointer");
     SC_REQUIRE(p->box_stages >= 0 && p->box_stages <= 8, "sc_splat: box_stages=%d not in 0..8",
                p->box_stages);
+    SC_REQUIRE(p->box_kernel == 0 || p->box_kernel == 1, "sc_splat: box_kernel=%d",
+               p->box_kernel);
     SC_REQUIRE_CAP(ws_bytes >= sc_splat_workspace_bytes(p), "sc_splat: workspace %zu < %zu bytes",
                ws_bytes, sc_splat_workspace_bytes(p));
     if (d_box) {
@@ -1046,10 +1230,10 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
     float *ws = static_cast<float *>(d_ws);
     const bool box = d_box != nullptr;
     switch (g.warps) {
-        case 1: rc = launch_splat<1>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, box, ws, d_status, s); break;
-        case 2: rc = launch_splat<2>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, box, ws, d_status, s); break;
-        case 4: rc = launch_splat<4>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, box, ws, d_status, s); break;
-        default: rc = launch_splat<8>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, box, ws, d_status, s); break;
+        case 1: rc = launch_splat<1>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, p->box_kernel, box, ws, d_status, s); break;
+        case 2: rc = launch_splat<2>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, p->box_kernel, box, ws, d_status, s); break;
+        case 4: rc = launch_splat<4>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, p->box_kernel, box, ws, d_status, s); break;
+        default: rc = launch_splat<8>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, p->box_kernel, box, ws, d_status, s); break;
     }
     if (rc) return rc;
     const int64_t total = (int64_t)g.nw * g.nh * g.n_images;

@@ -95,9 +95,17 @@ __global__ void emitter_footprint_kernel(sc::StepConsts c, const void *particles
     if (idx >= (int64_t)c.n_sub * c.n_particles) return;
     const double norm = recs[idx].x0;
     if (norm_out) norm_out[idx] = norm;
-    const Row q = load_row(particles, c.row_layout, (size_t)idx);
     ScStepRec rec;
     const int i = (int)(idx % c.n_particles), s = (int)(idx / c.n_particles);
+    if (c.row_layout == 1 && c.focal_zero) {
+        // FP32 rows: the record from the FP32 values (as from their FP64 ones)
+        const float4 v = static_cast<const float4 *>(particles)[idx];
+        sc::make_record<float>(c, v.x, v.y, v.z, norm, key_slot, status, i, s, rec,
+                               norm_out != nullptr);
+        recs[idx] = rec;
+        return;
+    }
+    const Row q = load_row(particles, c.row_layout, (size_t)idx);
     if (c.focal_zero)
         sc::make_record(c, q.d, q.x, q.y, norm, key_slot, status, i, s, rec,
                         norm_out != nullptr);

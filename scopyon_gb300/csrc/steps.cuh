@@ -57,13 +57,27 @@ __device__ __forceinline__ bool df_ceil(df q, int &v) {
     return fabsf(d) > kDfMargin;
 }
 
+// A coordinate as a double-float, an FP64 value and an FP32 value: exact
+// conversions, on the FP64 pipe for an FP64 coordinate and with no FP64 work
+// for an FP32 one (the native trajectories), so that a record built from an
+// FP32 coordinate equals, bit for bit, the record built from its FP64 value.
+__device__ __forceinline__ df df_of(double x) { return df_from(x); }
+__device__ __forceinline__ df df_of(float x) { return df{x, 0.f}; }
+__device__ __forceinline__ double as_d(double x) { return x; }
+__device__ __forceinline__ double as_d(float x) { return f2d_exact(x); }
+__device__ __forceinline__ float as_f(double x) { return __double2float_rn(x); }
+__device__ __forceinline__ float as_f(float x) { return x; }
+__device__ __forceinline__ double abs_of(double x) { return fabs(x); }
+__device__ __forceinline__ float abs_of(float x) { return fabsf(x); }
+
 // Footprint of one axis: first pixel, number of bounds, and the first bound's
 // unrounded value a = (start px - origin) / res as a double-float.  Returns
 // false when the footprint misses the image.
+template <typename T>
 __device__ __forceinline__ bool axis_footprint(const StepConsts &c, double half_len, df hl,
-                                               double coord, int n_pix, int16_t &start,
+                                               T coord, int n_pix, int16_t &start,
                                                int16_t &count, float &a_hi, float &a_lo) {
-    const df x = df_from(coord);
+    const df x = df_of(coord);
     const df centre = df_add(hl, x);
     const df org = df_add(centre, c.nhalf_sig_df);
     const df top = df_add(centre, c.half_sig_df);
@@ -73,8 +87,8 @@ __device__ __forceinline__ bool axis_footprint(const StepConsts &c, double half_
     qlo.hi = fmaxf(qlo.hi, -8.f);  // only the clamped first pixel 0 matters below this
     qhi.hi = fminf(qhi.hi, (float)n_pix + 8.f);
     int lo, hi;
-    if (!df_floor(qlo, lo)) lo = (int)floor(((half_len + coord) - c.half_sig) / c.px);
-    if (!df_ceil(qhi, hi)) hi = (int)ceil(((half_len + coord) + c.half_sig) / c.px);
+    if (!df_floor(qlo, lo)) lo = (int)floor(((half_len + as_d(coord)) - c.half_sig) / c.px);
+    if (!df_ceil(qhi, hi)) hi = (int)ceil(((half_len + as_d(coord)) + c.half_sig) / c.px);
     const int i0 = max(lo, 0), i1 = min(hi, n_pix);
     if (i1 < i0) return false;
     start = (int16_t)i0;
@@ -90,9 +104,11 @@ __device__ __forceinline__ bool axis_footprint(const StepConsts &c, double half_
 // stride apart, and the weight w = norm * res^2.  rel0..2 are the emitter's
 // depth, x and y relative to the focal point.
 // origins: also give box-path records their FP64 footprint origins (x0, y0),
-// which the FP64 splat's exact bound decisions read.
-__device__ __forceinline__ void make_record(const StepConsts &c, double rel0, double rel1,
-                                            double rel2, double norm, const int32_t *key_slot,
+// which the FP64 splat's exact bound decisions read.  T: double, or float for
+// FP32 positions (the same record as for their FP64 values, with less FP64 work).
+template <typename T>
+__device__ __forceinline__ void make_record(const StepConsts &c, T rel0, T rel1, T rel2,
+                                            double norm, const int32_t *key_slot,
                                             int32_t *status, int i, int s, ScStepRec &rec,
                                             bool origins = false) {
     rec.box_off = 0;
@@ -112,15 +128,16 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
         return;
     }
     // depth key: int(|depth| / res) inside depth_cutoff + res, else -1 (_epifm.py:76-88)
-    const double depth = fabs(rel0);
-    const float df32 = __double2float_rn(depth);
+    const T depth = abs_of(rel0);
+    const float df32 = as_f(depth);
     bool inside = df32 < c.cut_f * (1.f - 1e-6f);
-    if (!(inside || df32 > c.cut_f * (1.f + 1e-6f))) inside = depth < c.depth_cutoff + c.res;
+    if (!(inside || df32 > c.cut_f * (1.f + 1e-6f))) inside = as_d(depth) < c.depth_cutoff + c.res;
     int key = -1;
     if (inside) {
         const float q = df32 * c.inv_res_f;  // three roundings: |error| < 2e-7 q
         const float r = rintf(q);
-        key = fabsf(q - r) > 5e-7f * fmaxf(1.f, q) ? (int)floorf(q) : (int)floor(depth / c.res);
+        key = fabsf(q - r) > 5e-7f * fmaxf(1.f, q) ? (int)floorf(q)
+                                                   : (int)floor(as_d(depth) / c.res);
         if (key > c.max_key) {
             flag_status(status, 0, i, s, 0);
             return;
@@ -154,12 +171,12 @@ __device__ __forceinline__ void make_record(const StepConsts &c, double rel0, do
         rec.box_off = (int64_t)slot * ((int64_t)P * P * NB) + (int64_t)phase * NB +
                       (mx / P) * NQ + my / P;
         if (origins) {
-            rec.x0 = (c.half_w + rel1) - c.half_sig;
-            rec.y0 = (c.half_h + rel2) - c.half_sig;
+            rec.x0 = (c.half_w + as_d(rel1)) - c.half_sig;
+            rec.y0 = (c.half_h + as_d(rel2)) - c.half_sig;
         }
     } else {
-        rec.x0 = (c.half_w + rel1) - c.half_sig;
-        rec.y0 = (c.half_h + rel2) - c.half_sig;
+        rec.x0 = (c.half_w + as_d(rel1)) - c.half_sig;
+        rec.y0 = (c.half_h + as_d(rel2)) - c.half_sig;
     }
     rec.ax_hi = axh;
     rec.ax_lo = axl;

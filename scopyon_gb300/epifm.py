@@ -118,6 +118,10 @@ class EngineConfig:
         self.adc_rounding = str(_gpu_opt(raw, "adc_rounding", "none")) == "round"
         self.boundary = str(_gpu_opt(raw, "boundary", "none"))
         self.tile = int(_gpu_opt(raw, "tile", 0))
+        self.l2_fetch_bytes = int(_gpu_opt(raw, "l2_fetch_bytes", 32))
+        if self.l2_fetch_bytes not in (0, 32, 64, 128):
+            raise ValueError("gpu.l2_fetch_bytes must be 0, 32, 64 or 128 (got %r)"
+                             % self.l2_fetch_bytes)
         self.use_box = bool(_gpu_opt(raw, "box_tables", True))
         self.catalog_dir = _gpu_opt(raw, "catalog_dir")
         table = _gpu_opt(raw, "cmos_table")
@@ -374,6 +378,11 @@ class FramePipeline:
         self.cfg = cfg
         self.device = torch.device(device or "cuda")
         _lib.load()
+        if cfg.l2_fetch_bytes:
+            # the splat reads random 784-byte blocks and 32-byte record heads:
+            # smaller L2 fetches read fewer bytes it does not use
+            with torch.cuda.device(self.device):
+                call("sc_set_l2_fetch_granularity", cfg.l2_fetch_bytes)
         self.psf = psf or PSFTables(cfg, self.device)
         nw, nh = cfg.image_size
         self.nw, self.nh = nw, nh
@@ -414,9 +423,10 @@ class FramePipeline:
 
     def set_tiles(self, tile, warps, stages=4):
         """Use tiles of tile x tile pixels, `warps` warps per splat CTA and
-        `stages` box-table block copies in flight per warp."""
-        if tile not in (8, 16, 32) or warps not in (1, 2, 4, 8) or not 1 <= stages <= 8:
-            raise ValueError("tile must be 8, 16 or 32, warps 1, 2, 4 or 8, stages 1..8")
+        `stages` box-table block copies in flight per warp (0: the register
+        kernel, which loads each block with 16-byte loads instead)."""
+        if tile not in (8, 16, 32) or warps not in (1, 2, 4, 8) or not 0 <= stages <= 8:
+            raise ValueError("tile must be 8, 16 or 32, warps 1, 2, 4 or 8, stages 0..8")
         nw, nh = self.nw, self.nh
         self.tile, self.warps, self.stages = int(tile), int(warps), int(stages)
         self.tiles_x = (nw + self.tile - 1) // self.tile
@@ -514,7 +524,10 @@ class FramePipeline:
         p.n_images, p.rec_per_image = n_images, rec_per_image
         p.box_p, p.box_nq = self.psf.box_p, self.psf.box_nq
         p.n_slots = self.psf.capacity
-        p.box_stages = self.stages
+        # stages 0: the register box kernel (the persistent batched frame,
+        # which has no register form, then keeps 4 copies in flight)
+        p.box_stages = self.stages if self.stages > 0 else 4
+        p.box_kernel = 1 if self.stages == 0 else 0
         p.first_wait_polls = int(self.first_wait_polls)
         p.px, p.res = self.cfg.px, PSF_RES
         return p
@@ -759,7 +772,10 @@ class FramePipeline:
         return self.expect, self.adc32, opt
 
 
-TILE_CANDIDATES = ((8, 4, 4), (8, 4, 8), (8, 2, 6), (16, 4, 4), (16, 8, 4), (16, 4, 8))
+# (tile edge, warps per splat CTA, block copies in flight per warp; 0: the
+# register kernel)
+TILE_CANDIDATES = ((8, 4, 4), (8, 4, 8), (8, 2, 6), (16, 4, 4), (16, 8, 4), (16, 4, 8),
+                   (8, 4, 0), (8, 8, 0), (16, 8, 0))
 
 
 def tune_tiles(graph, candidates=TILE_CANDIDATES, frames=3):

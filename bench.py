@@ -162,11 +162,13 @@ def splat_algorithmic_bytes(n_rec, tile, halo):
             + 4 * IMAGE * IMAGE)
 
 
-# DRAM bytes (read + write) of the three splat kernels per splatted record:
-# 387.0 MB over 383,289 box records in one frame of
-# `bench.py --small --tile 8 --warps 4` (ncu --set full,
-# dram__bytes_read.sum + dram__bytes_write.sum).
-SPLAT_TRAFFIC_PER_RECORD = 387.0e6 / 383289
+# DRAM bytes (read + write) of the three splat kernels per splatted record,
+# with the L2 fetch granularity hint at 32 bytes: 333.5 MB over 368,363
+# records in one frame of `bench.py --small --tile 8 --warps 4`
+# (dram__bytes_read.sum + dram__bytes_write.sum: 328.25 MB for
+# splat_box_bulk_kernel under ncu --set full, 5.25 MB for splat_merge_kernel
+# and 0.03 MB for splat_sat_kernel).
+SPLAT_TRAFFIC_PER_RECORD = 333.5e6 / 368363
 
 
 def load_peaks():

@@ -428,7 +428,11 @@ diffuse_native_kernel(DiffConsts c, double *pos, int32_t *klass, const double *s
 // for bit: every quantity is formed by the same FP64 expression as there.
 // FP64 work runs with full warps only (GB300's FP64 rate is ~1/64 of FP32, so
 // a warp with a few active lanes wastes it).
-constexpr int kRecWarps = 4;
+#ifndef SC_REC_WARPS
+#define SC_REC_WARPS 4
+#endif
+constexpr int kRecWarps = SC_REC_WARPS;
+static_assert(kRecWarps >= 4, "the chain phase takes warps 0-2 and the last warp");
 
 // Shared memory of one CTA for `chunk` sub-steps: positions [chunk][32][3] and
 // normalisations [chunk][32] (FP64), per-sub-step photons and normalisation

@@ -512,8 +512,11 @@ struct RegRec {
     int flags;    // bit 0 splat it, bit 1 the unconditional path applies
 };
 
+#ifndef SC_REG_WARPS_PER_SM
+#define SC_REG_WARPS_PER_SM 32
+#endif
 template <int NW, int NQ>
-__global__ void __launch_bounds__(NW * 32)
+__global__ void __launch_bounds__(NW * 32, SC_REG_WARPS_PER_SM / NW)
 splat_box_reg_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
                      const int32_t *__restrict__ items, SplatConsts c, int S, int rows,
                      int64_t table_floats, float *__restrict__ ws, int32_t *status) {

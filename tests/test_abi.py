@@ -154,3 +154,40 @@ def test_undersized_workspace_is_a_capacity_error():
         _lib.call("sc_splat", fake, fake, fake, fake, None, ctypes.byref(p), fake, 0, fake,
                   None, None)
     assert err.value.code == _lib.SC_ERR_CAPACITY
+
+
+def test_layout_and_kernel_choices_are_checked_on_the_host():
+    """Row layouts, the box-kernel choice and the L2 fetch hint are checked
+    before any CUDA call: SC_ERR_ARG with a message (pointers never read)."""
+    from scopyon_gb300 import _build, _lib
+    _build.build()
+    L = _lib.load()
+    P = ctypes.c_void_p
+    fake = P(1 << 20)
+    d = _lib.DiffuseParams(n_particles=100, n_sub=4, ndim=3, boundary=0, n_class=1, layout=7,
+                           scale=1.0)
+    d.unit_x[0] = d.unit_y[1] = d.unit_z[2] = 1.0
+    assert L.sc_diffuse_steps(ctypes.byref(d), fake, None, fake, None, fake, None) == _lib.SC_ERR_ARG
+    assert b"layout=7" in L.sc_last_error()
+    # FP32 rows need native draws: with the caller's normals they are refused
+    d.layout = 1
+    assert L.sc_diffuse_steps(ctypes.byref(d), fake, None, fake, fake, fake, None) == _lib.SC_ERR_ARG
+    assert b"layout 1" in L.sc_last_error()
+    # ... and the identity transform
+    d.scale = 2.0
+    assert L.sc_diffuse_steps(ctypes.byref(d), fake, None, fake, None, fake, None) == _lib.SC_ERR_ARG
+    s = _lib.StepParams(px=1.6e-7, res=1e-9, depth_cutoff=1e-6, nw=64, nh=64, n_signal=1999,
+                        n_sub=4, n_particles=100, max_key=1000, row_layout=3)
+    assert L.sc_emitter_steps(ctypes.byref(s), fake, fake, None, fake, None, None, fake, None,
+                              None, None) == _lib.SC_ERR_ARG
+    assert b"row_layout=3" in L.sc_last_error()
+    p = _lib.SplatParams(nw=64, nh=64, tile=8, halo=14, warps=4, tiles_x=8, tiles_y=8, n_r=1000,
+                         sat_pitch=1004, n_images=1, rec_per_image=0, box_kernel=2, px=1.6e-7,
+                         res=1e-9)
+    assert L.sc_splat(fake, fake, fake, fake, None, ctypes.byref(p), fake,
+                      L.sc_splat_workspace_bytes(ctypes.byref(p)), fake, None,
+                      None) == _lib.SC_ERR_ARG
+    assert b"box_kernel=2" in L.sc_last_error()
+    assert L.sc_set_l2_fetch_granularity(17) == _lib.SC_ERR_ARG
+    assert b"17 bytes" in L.sc_last_error()
+    assert L.sc_box_block_floats(14) == 196 and L.sc_box_block_floats(13) == 172

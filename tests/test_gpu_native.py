@@ -469,3 +469,49 @@ def test_box_muller_radius_at_the_largest_uniform(sg):
     assert numpy.isfinite(end).all()
     assert abs(end[0, 0]) < 1e-18 and abs(end[0, 1]) < 1e-18  # radius 0: no move in x, y
     assert end[0, 2] != 0.0 and end[1, 0] != float(numpy.float32(1e-7))  # the others move
+
+
+def test_register_box_kernel_equals_bulk_copy_ring(sg):
+    """The box splat's register form (16-byte loads, stages 0) adds the same
+    values in the same order as the bulk-copy ring: for the same tiles and
+    warps, equal expectations bit for bit (8x8 and 16x16 tiles), including
+    footprints clipped by the image's low edges (emitters past the field);
+    other tilings group the sums differently and agree to FP32 rounding."""
+    from scopyon_gb300.base import _psf_for
+    from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {"magnification": 100,
+                            "detector": {"type": "EMCCD", "image_size": [200, 136],
+                                         "exposure_time": 0.004},
+                            "light_source": {"angle": 0.0}}})
+    t = numpy.arange(4 * 4 + 1) * 1e-3
+    traj = sg.sample_inputs(t, N=3000, lower=[-17e-6, -12e-6, -0.3e-6],
+                            upper=[17e-6, 12e-6, 0.3e-6], D=0.4e-12, ndim=3,
+                            rng=numpy.random.RandomState(12))
+    eng = EngineConfig(cfg["default"])
+    out = {}
+    for tile, warps, stages in ((8, 4, 4), (8, 4, 0), (16, 8, 4), (16, 8, 0)):
+        pipe = FramePipeline(eng, "cuda", psf=_psf_for(eng, torch.device("cuda")))
+        pipe.psf.ensure(list(range(0, 400)))
+        pipe.set_tiles(tile, warps, stages)
+        fg = FrameGraph(pipe, traj.copy(), 4, 1e-3, seed=3, use_graph=False)
+        frames = []
+        for _ in range(4):
+            fg.step()
+            frames.append(pipe.expect.cpu().numpy().copy())
+        pipe.check_status()
+        out[(tile, warps, stages)] = numpy.array(frames)
+    ref = out[(8, 4, 4)]
+    assert ref.max() > 0
+    numpy.testing.assert_array_equal(out[(8, 4, 0)], ref)
+    numpy.testing.assert_array_equal(out[(16, 8, 0)], out[(16, 8, 4)])
+    assert numpy.abs(out[(16, 8, 0)] - ref).max() <= 1e-6 * ref.max()
+
+
+def test_l2_fetch_hint_values(sg):
+    """The L2 fetch granularity hint takes 0, 32, 64 and 128 bytes."""
+    from scopyon_gb300 import _lib
+    for b in (0, 32, 64, 128, 32):
+        _lib.call("sc_set_l2_fetch_granularity", b)
+    with pytest.raises(ValueError, match="48 bytes"):  # SC_ERR_ARG
+        _lib.call("sc_set_l2_fetch_granularity", 48)

@@ -104,3 +104,13 @@ def test_corrupt_config_is_rejected_on_the_host(section, key, value):
     cfg.update({"default": {section: {key: value}}})
     with pytest.raises(ValueError, match=key):
         EngineConfig(cfg["default"], rng=numpy.random.RandomState(0))
+
+
+@pytest.mark.parametrize("value", [17, 256, -32])
+def test_l2_fetch_hint_config_is_checked(value):
+    """gpu.l2_fetch_bytes takes 0, 32, 64 or 128 (bytes); others raise ValueError."""
+    cfg = DefaultConfiguration()
+    assert EngineConfig(cfg["default"], rng=numpy.random.RandomState(0)).l2_fetch_bytes == 32
+    cfg.update({"default": {"gpu": {"l2_fetch_bytes": value}}})
+    with pytest.raises(ValueError, match="l2_fetch_bytes"):
+        EngineConfig(cfg["default"], rng=numpy.random.RandomState(0))

@@ -223,7 +223,7 @@ __device__ void warp_flip_sort(int32_t *a, int n, int lane) {
 constexpr int kSortWarps = 8;
 
 // One warp per bin: the bin's record indices sorted ascending, in registers
-// up to 512 of them (4 or 16 per lane).  Longer lists go to `big` (a count
+// up to 512 of them (1, 2, 4, 8 or 16 per lane).  Longer lists go to `big` (a count
 // and the bin indices) for bin_sort_big_kernel, or, without that list, are
 // sorted here in global memory.
 __global__ void __launch_bounds__(kSortWarps * 32)
@@ -234,8 +234,15 @@ bin_sort_kernel(const int32_t *tile_start, int n_bins, int32_t *items, int32_t *
     const int b0 = tile_start[t], n = tile_start[t + 1] - b0;
     if (n <= 1) return;
     int32_t *list = items + b0;
-    if (n <= 128)
+    // the smallest register network that holds the list
+    if (n <= 32)
+        warp_sort_list<1>(list, n, lane);
+    else if (n <= 64)
+        warp_sort_list<2>(list, n, lane);
+    else if (n <= 128)
         warp_sort_list<4>(list, n, lane);
+    else if (n <= 256)
+        warp_sort_list<8>(list, n, lane);
     else if (n <= 512)
         warp_sort_list<16>(list, n, lane);
     else if (big) {

@@ -413,22 +413,26 @@ __device__ __forceinline__ bool bulk_tile_records(
     return true;
 }
 
+// At most 64 registers: the box records' loop needs about 54; the tile's
+// summed-area records, rare, take what spills there are.
 template <int NW, int NQ>
-__global__ void __launch_bounds__(NW * 32, 20 / NW)
+__global__ void __launch_bounds__(NW * 32, 32 / NW)
 splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restrict__ tile_start,
-                      const int32_t *__restrict__ items, SplatConsts c, int stages, int half_rows,
+                      const int32_t *__restrict__ items, const float2 *__restrict__ sat,
+                      SplatConsts c, int sat_tiles, int stages, int half_rows,
                       int64_t table_floats, float *__restrict__ ws, int32_t *status) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int BSR = kBulkBsr;
     constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;  // stage buffer floats
-    constexpr int NB = SC_BOX_BLOCK_FLOATS(NQ);
     const int E = c.edge, EE = c.edge * c.edge;
     const int HB = half_rows * BSR + 16;  // odd half starts 16 banks after the even half
     const int BS = (2 * HB + 31) & ~31;
+    const int SBS = (EE + 31) & ~31;  // summed-area buffers (E-stride), in the same space
     float *acc = reinterpret_cast<float *>(smem_raw);                   // [NW][BS]
     int4 *descs = reinterpret_cast<int4 *>(acc + NW * BS);              // [NW][2][32]
     float *stage = reinterpret_cast<float *>(descs + NW * 64);          // [NW][stages][SB]
     uint64_t *bars = reinterpret_cast<uint64_t *>(stage + NW * stages * SB);  // [NW][stages]
+    int *bnd = reinterpret_cast<int *>(bars + NW * stages);  // [NW][2][E + 2] when sat_tiles
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile = blockIdx.x;
     const int t = tile % c.tiles_per_image;
@@ -454,15 +458,43 @@ splat_box_bulk_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restr
         for (int w = 0; w < NW; ++w) sum += acc[w * BS + off];
         out[p] = sum;
     }
+    // the tile's summed-area records (bin sat_tiles + tile), added as
+    // splat_sat_kernel adds them, with no launch of their own
+    if (sat_tiles == 0) return;
+    const int s0 = tile_start[sat_tiles + tile], s1 = tile_start[sat_tiles + tile + 1];
+    if (s1 == s0) return;
+    __syncthreads();
+    for (int i = threadIdx.x; i < NW * SBS; i += blockDim.x) acc[i] = 0.f;
+    __syncthreads();
+    int *bx = bnd + warp * 2 * (E + 2);
+    int *by = bx + (E + 2);
+    for (int m = s0 + warp; m < s1; m += NW) {
+        const ScStepRec &rec = recs[__ldg(items + m)];
+        const int ni = rec.n_i - 1, nj = rec.n_j - 1;
+        const int ox = rec.i_start - x0, oy = rec.j_start - y0;
+        if (!in_buffer(ox, oy, ni, nj, E)) {
+            if (lane == 0) sc::flag_status(status, 2, rec.i_start, rec.j_start, tile);
+            continue;
+        }
+        splat_sat_record(rec, ox * E + oy, sat, c, bx, by, acc + warp * SBS, lane);
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < EE; p += blockDim.x) {
+        float sum = 0.f;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) sum += acc[w * SBS + p];
+        out[p] = out[p] + sum;
+    }
 }
 
 // Bulk-copy box launch for block size NQ; done stays false when the geometry
 // does not fit it (the direct kernel then runs).
 template <int NW, int NQ>
 int launch_bulk(const ScStepRec *recs, const int32_t *tile_start, const int32_t *items,
-                const SplatConsts &c, int n_tiles, int n_slots, int want_stages, float *ws,
-                int32_t *status, cudaStream_t s, bool &done) {
-    done = false;
+                const float2 *sat, const SplatConsts &c, int n_tiles, int n_slots,
+                int want_stages, float *ws, int32_t *status, cudaStream_t s, bool &done,
+                bool &sat_done) {
+    done = sat_done = false;
     constexpr int PAIRS = (NQ + 1) / 2, SB = (2 * PAIRS * NQ + 3) & ~3;
     constexpr int NB = SC_BOX_BLOCK_FLOATS(NQ);
     // buffer rows -1 .. tile + 2 PAIRS - 2 and columns -1 .. tile + 14 are reachable
@@ -471,8 +503,12 @@ int launch_bulk(const ScStepRec *recs, const int32_t *tile_start, const int32_t 
     const int rows = max(c.edge, c.tile + 2 * PAIRS - 1) + 1;
     const int half_rows = ((rows + 1) / 2 + 3) & ~3;  // multiple of 4: halves 16 banks apart
     const int64_t table_floats = (int64_t)n_slots * c.box_p * c.box_p * NB;
-    const size_t fixed = (size_t)NW * ((2 * (half_rows * kBulkBsr + 16) + 31) & ~31) * sizeof(float) +
-                         (size_t)NW * 64 * sizeof(int4);
+    const int bs = (2 * (half_rows * kBulkBsr + 16) + 31) & ~31;
+    // the summed-area records go in the same kernel when their E-stride
+    // buffers fit the box buffers' space
+    const bool fuse_sat = ((c.edge * c.edge + 31) & ~31) <= bs;
+    const size_t fixed = (size_t)NW * bs * sizeof(float) + (size_t)NW * 64 * sizeof(int4) +
+                         (fuse_sat ? (size_t)NW * 2 * (c.edge + 2) * sizeof(int) : 0);
     auto bulk_smem = [&](int st) {
         return fixed + (size_t)NW * st * SB * sizeof(float) + (size_t)NW * st * sizeof(uint64_t);
     };
@@ -486,8 +522,10 @@ int launch_bulk(const ScStepRec *recs, const int32_t *tile_start, const int32_t 
         if (e != cudaSuccess) return sc::cuda_status(e, "sc_splat: smem attribute");
     }
     splat_box_bulk_kernel<NW, NQ><<<n_tiles, NW * 32, smem, s>>>(
-        recs, tile_start, items, c, stages, half_rows, table_floats, ws, status);
+        recs, tile_start, items, sat, c, fuse_sat ? n_tiles : 0, stages, half_rows, table_floats,
+        ws, status);
     done = true;
+    sat_done = fuse_sat;
     return sc::launch_status("sc_splat bulk-copy box");
 }
 
@@ -823,18 +861,19 @@ int launch_splat(const ScStepRec *recs, const int32_t *tile_start, const int32_t
     }
     if (box) {
         // bulk-copy kernel for blocks of 12..16 rows (pixels of 134..181 grid rows)
-        bool done = false;
+        bool done = false, sat_done = false;
         int rc = SC_OK;
         switch (c.box_nq) {
-            case 12: rc = launch_bulk<NW, 12>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
-            case 13: rc = launch_bulk<NW, 13>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
-            case 14: rc = launch_bulk<NW, 14>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
-            case 15: rc = launch_bulk<NW, 15>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
-            case 16: rc = launch_bulk<NW, 16>(recs, tile_start, items, c, n_tiles, n_slots, stages, ws, status, s, done); break;
+            case 12: rc = launch_bulk<NW, 12>(recs, tile_start, items, sat, c, n_tiles, n_slots, stages, ws, status, s, done, sat_done); break;
+            case 13: rc = launch_bulk<NW, 13>(recs, tile_start, items, sat, c, n_tiles, n_slots, stages, ws, status, s, done, sat_done); break;
+            case 14: rc = launch_bulk<NW, 14>(recs, tile_start, items, sat, c, n_tiles, n_slots, stages, ws, status, s, done, sat_done); break;
+            case 15: rc = launch_bulk<NW, 15>(recs, tile_start, items, sat, c, n_tiles, n_slots, stages, ws, status, s, done, sat_done); break;
+            case 16: rc = launch_bulk<NW, 16>(recs, tile_start, items, sat, c, n_tiles, n_slots, stages, ws, status, s, done, sat_done); break;
             default: break;
         }
         if (rc) return rc;
-        if (done) box = false;  // the summed-area pass below accumulates
+        if (sat_done) return SC_OK;  // the kernel added the summed-area records too
+        if (done) box = false;       // the summed-area pass below accumulates
     }
     const bool staged = !box && c.box != nullptr;
     if (box) {

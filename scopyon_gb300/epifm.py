@@ -953,12 +953,18 @@ class FrameGraph:
 
     @property
     def launches_per_frame(self):
-        # native records (counting into bins), bin scan, then place + sort or,
-        # from 2^20 records on, three kernels per radix digit pass; splat
-        # box/sat/merge, camera, counter (plus one memset)
+        # native records (counting into bins), bin scan, then place + sort +
+        # long-list sort or, from 2^20 records on, three kernels per radix
+        # digit pass; splat box (the bulk-copy kernel also adds the summed-area
+        # records), summed-area pass otherwise, merge; camera, counter (plus
+        # one memset)
+        pipe = self.pipe
+        fused = (pipe.stages > 0 and pipe.psf.box_p > 0 and 12 <= pipe.psf.box_nq <= 16 and
+                 pipe.tile + 15 <= 32)
+        splat = 2 if fused else 3
         n_rec = self.n_sub * self.n
         if n_rec < (1 << 20):
-            return 9
-        n_bins = 2 * self.pipe.tiles_x * self.pipe.tiles_y
+            return 7 + splat
+        n_bins = 2 * pipe.tiles_x * pipe.tiles_y
         bits = max(1, n_bins.bit_length())  # keys 0 .. n_bins
-        return 7 + 3 * (-(-bits // 9))
+        return 4 + splat + 3 * (-(-bits // 9))

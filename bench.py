@@ -148,27 +148,26 @@ class ClockSampler:
 
 
 def splat_algorithmic_bytes(n_rec, tile, halo):
-    """Bytes one splat (halo kernel + merge) must move.
+    """Bytes one splat (the box kernel, which also adds the summed-area
+    records) must move.
 
     Per emitter-step: its item index (4 B), the 32-byte record head, and the
     footprint's box-table block: (n_px)^2 FP32 pixel sums, n_px =
     1998 nm / px + 1 pixels per axis on average.  Per tile: the FP32
-    (tile + halo)^2 buffer written and read back by the merge; per pixel one
-    FP32 image write.
+    (tile + halo)^2 buffer written (the merge that reads it back runs in the
+    camera pass, sc_merge_camera).
     """
     n_px = 1998e-9 / PX + 1
     n_tiles = (IMAGE // tile) ** 2
-    return (n_rec * (4 + 32 + 4 * n_px * n_px) + n_tiles * (tile + halo) ** 2 * 4 * 2
-            + 4 * IMAGE * IMAGE)
+    return n_rec * (4 + 32 + 4 * n_px * n_px) + n_tiles * (tile + halo) ** 2 * 4
 
 
-# DRAM bytes (read + write) of the three splat kernels per splatted record,
-# with the L2 fetch granularity hint at 32 bytes: 333.5 MB over 368,363
-# records in one frame of `bench.py --small --tile 8 --warps 4`
-# (dram__bytes_read.sum + dram__bytes_write.sum: 328.25 MB for
-# splat_box_bulk_kernel under ncu --set full, 5.25 MB for splat_merge_kernel
-# and 0.03 MB for splat_sat_kernel).
-SPLAT_TRAFFIC_PER_RECORD = 333.5e6 / 368363
+# DRAM bytes (read + write) of the splat per splatted record, with the L2
+# fetch granularity hint at 32 bytes: 328.25 MB over 368,363 records in one
+# frame of `bench.py --small --tile 8 --warps 4` (dram__bytes_read.sum +
+# dram__bytes_write.sum of splat_box_bulk_kernel under ncu --set full; the
+# summed-area records it now adds itself moved 0.03 MB in their own pass).
+SPLAT_TRAFFIC_PER_RECORD = 328.28e6 / 368363
 
 
 def load_peaks():
@@ -335,7 +334,7 @@ def gb300_arm(args, rank, world):
         "batched": batched,
         "gpu_launches": fg.launches_per_frame * args.steps,
         "clocks": clk,
-        "roofline": {"kernel": "splat_box_bulk_kernel + splat_sat_kernel + splat_merge_kernel",
+        "roofline": {"kernel": "splat_box_bulk_kernel (box and summed-area records)",
                      "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
@@ -678,17 +677,21 @@ def stage_rooflines(stage_ms, pipe, n_rec, peak):
     durations on the same eager frames.  Algorithmic bytes: the records stage
     reads and writes each emitter's FP64 position (48 B), photon budget
     (16 B) and class (4 B) and writes each record (64 B) with its bin and rank
-    (8 B); the camera reads each pixel's photons (4 B), offset and 1/gain
-    (8 B, with fixed-pattern noise) and read-noise sigma (4 B, sCMOS) and
+    (8 B); the camera pass (sc_merge_camera) reads the splat's tile buffers
+    once (tiles x (tile + halo)^2 x 4 B), each pixel's offset and 1/gain
+    (8 B, with fixed-pattern noise) and read-noise sigma (4 B, sCMOS), and
     writes the expectation (4 B) and the FP32 ADC count (4 B)."""
     n_px = pipe.nw * pipe.nh
+    tiles = pipe.tiles_x * pipe.tiles_y * (pipe.tile + pipe.halo) ** 2 * 4
     out = {}
     for name, alg, bound in (
             ("records", N_EMIT * 68 + n_rec * 72,
-             "FP64 position chains and footprint arithmetic (FP64 pipe), not HBM"),
-            ("camera", n_px * (8 + (8 if pipe.pixel_maps else 0) +
-                               (4 if pipe.sigma is not None else 0) + 4),
-             "per-pixel Poisson and normal draws (FP32 and SFU pipes), not HBM")):
+             "latency of its phases (position chains, then the records of every sub-step) "
+             "and footprint arithmetic, not HBM"),
+            ("camera", tiles + n_px * (8 + (8 if pipe.pixel_maps else 0) +
+                                       (4 if pipe.sigma is not None else 0)),
+             "the tile-buffer sums and the per-pixel Poisson and normal draws (dependent "
+             "table reads), not HBM")):
         ms = stage_ms[name]
         gbs = alg / (ms / 1e3) / 1e9
         out[name] = {"avg_launch_ms": ms, "algorithmic_bytes": alg, "achieved": gbs,

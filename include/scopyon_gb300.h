@@ -523,13 +523,28 @@ size_t sc_splat_workspace_bytes(const ScSplatParams *p);
 
 /* Splat: each CTA sums the whole footprints of the records binned to its
  * tile into a (tile + halo)^2 buffer in shared memory and stores it in the
- * workspace; a second pass adds the overlapping buffers into d_image.
- * Replaces overlay_signal_ (src/scopyon/_epifm.py:224-282) for every
- * particle and sub-step.                                                    */
+ * workspace; a second pass adds the overlapping buffers into d_image
+ * (d_image NULL: no second pass, the caller merges the workspace with
+ * sc_merge_camera).  Replaces overlay_signal_ (src/scopyon/_epifm.py:224-282)
+ * for every particle and sub-step.                                          */
 int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
              const int32_t *d_items, const float *d_sat, const float *d_box,
              const ScSplatParams *p, void *d_ws, size_t ws_bytes, float *d_image,
              int32_t *d_status, void *stream);
+
+/* The merge of sc_splat and the native camera of sc_camera in one pass, for
+ * one image: for each pixel the photons are the sum of the workspace's tile
+ * buffers that cover it (d_ws of a sc_splat call with d_image NULL, same
+ * splat params), in the order sc_splat's merge adds them; then the camera
+ * as sc_camera draws it (cp->exact 0).  d_expect (may be NULL) and d_adc32
+ * equal those of sc_splat with an image followed by sc_camera, bit for bit,
+ * without the photon image's write and read.  Replaces the same reference
+ * lines as the two (src/scopyon/_epifm.py:224-282, :1430-1484).           */
+int sc_merge_camera(const ScSplatParams *sp, const void *d_ws, size_t ws_bytes,
+                    const ScCameraParams *cp, const float *d_offset_f,
+                    const float *d_inv_gain_f, const float *d_sigma,
+                    const double *d_table_value, const double *d_table_cdf, float *d_expect,
+                    float *d_adc32, int32_t *d_status, void *stream);
 
 /* Camera model and ADC.  Replaces _EPIFMSimulator.__detector_output, the
  * EMCCD / CCD / CMOS classes and __get_analog_to_digital_converter_counts

@@ -131,6 +131,8 @@ _SIG = {
                       _P, _P]),
     "sc_camera": (_I, [ctypes.POINTER(CameraParams), _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                        _P, _P, _P, _P, _P]),
+    "sc_merge_camera": (_I, [ctypes.POINTER(SplatParams), _P, ctypes.c_size_t,
+                             ctypes.POINTER(CameraParams), _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sc_emccd_exact": (_I, [_P, _D, _D, _P, _I, _D, _P, _P, _P]),
     "sc_bw_work_bytes": (ctypes.c_size_t, [ctypes.POINTER(BWParams)]),
     "sc_bw_forward": (_I, [ctypes.POINTER(BWParams), _P, _P, _P, _P, ctypes.c_size_t, _P, _P,

@@ -944,6 +944,75 @@ __device__ __forceinline__ float merge_pixel(const float *ws, const SplatConsts 
     return sum;
 }
 
+// The merge and the native camera in one pass: a thread takes a pixel pair,
+// sums the tile buffers that cover each of its pixels in splat_merge_kernel's
+// order, and draws the pair's camera as camera_native_kernel does, so the
+// expectation and the ADC counts equal those of sc_splat (with its merge)
+// followed by sc_camera, bit for bit, without the photon image's write and
+// read and one launch.
+// merge_pixel with at most MT covering tiles per axis, all loads issued
+// together: a tile that does not cover the pixel adds +0, which leaves the
+// sum as merge_pixel forms it, bit for bit (the buffers hold sums of
+// non-negative terms, so the running sum is never -0).
+template <int MT>
+__device__ __forceinline__ float merge_pixel_mt(const float *ws, const SplatConsts &c, int i,
+                                                int j) {
+    const int E = c.edge, EE = c.edge * c.edge;
+    const int tx = i / c.tile, ty = j / c.tile;
+    const int li0 = i - tx * c.tile, lj0 = j - ty * c.tile;
+    float v[MT][MT];
+#pragma unroll
+    for (int a = 0; a < MT; ++a)
+#pragma unroll
+        for (int b = 0; b < MT; ++b) {
+            const int li = li0 + a * c.tile, lj = lj0 + b * c.tile;
+            const bool ok = a <= tx && li < E && b <= ty && lj < E;
+            v[a][b] = ok ? __ldcg(ws + (size_t)((tx - a) * c.tiles_y + (ty - b)) * EE + li * E + lj)
+                         : 0.f;
+        }
+    float sum = 0.f;
+#pragma unroll
+    for (int a = 0; a < MT; ++a)
+#pragma unroll
+        for (int b = 0; b < MT; ++b) sum += v[a][b];
+    return sum;
+}
+
+template <int CAM, int MT>
+__global__ void __launch_bounds__(256)
+merge_camera_kernel(const float *__restrict__ ws, SplatConsts c, sc::cam::CamConsts cc,
+                    const void *__restrict__ ptab, const float *__restrict__ offset_f,
+                    const float *__restrict__ inv_gain_f, const float *__restrict__ sigma,
+                    const double *__restrict__ table_value, const double *__restrict__ table_cdf,
+                    float *__restrict__ expect, float *__restrict__ adc32, int32_t *status) {
+    using namespace sc::cam;
+    const PoisTab t = pois_tab(ptab);
+    const uint64_t counter = cc.counter + (cc.frame ? (uint64_t)*cc.frame : 0);
+    const uint32_t c0 = (uint32_t)counter, c1 = (uint32_t)(counter >> 32);
+    const int n = cc.n, n_pairs = (n + 1) >> 1;
+    const bool scmos = CAM == SC_CAM_SCMOS && sigma;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n_pairs;
+         q += gridDim.x * blockDim.x) {
+        const PairDraws d = pair_draws<CAM>(cc, q, c0, c1);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int p = 2 * q + h;
+            if (p >= n) break;
+            const int i = p / c.nh, j = p - (p / c.nh) * c.nh;
+            const float ph = MT > 0 ? merge_pixel_mt<(MT > 0 ? MT : 1)>(ws, c, i, j)
+                                    : merge_pixel(ws, c, i, j);
+            const float e = cc.qe_f * (ph + cc.background_f);
+            const float sg = scmos ? __ldg(sigma + p) : cc.readout_f;
+            const float g = inv_gain_f ? __ldg(inv_gain_f + p) : cc.inv_gain0_f;
+            const float o = offset_f ? __ldg(offset_f + p) : cc.offset0_f;
+            const float v = pixel_adc<CAM>(cc, t, p, e, sg, g, o, d, h, c0, c1, table_value,
+                                           table_cdf, status);
+            if (expect) expect[p] = e;
+            adc32[p] = v;
+        }
+    }
+}
+
 // Resident blocks take work entries in plan order from b.counters[0] until
 // the list is done.  An entry is claimed only when the block is free to work
 // on it (claiming the next one ahead would let a block hold a tile that other
@@ -1251,7 +1320,7 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
     SplatConsts c;
     rc = splat_consts(p, g, c);
     if (rc) return rc;
-    SC_REQUIRE(d_tile_start && d_image && d_ws, "sc_splat: NULL pointer");
+    SC_REQUIRE(d_tile_start && d_ws, "sc_splat: NULL pointer");
     SC_REQUIRE(p->box_stages >= 0 && p->box_stages <= 8, "sc_splat: box_stages=%d not in 0..8",
                p->box_stages);
     SC_REQUIRE(p->box_kernel == 0 || p->box_kernel == 1, "sc_splat: box_kernel=%d",
@@ -1278,11 +1347,74 @@ extern "C" int sc_splat(const ScStepRec *d_recs, const int32_t *d_tile_start,
         default: rc = launch_splat<8>(d_recs, d_tile_start, d_items, sat, c, g.n_tiles, p->n_slots, p->box_stages, p->box_kernel, box, ws, d_status, s); break;
     }
     if (rc) return rc;
+    if (!d_image) return SC_OK;  // the caller merges (sc_merge_camera)
     const int64_t total = (int64_t)g.nw * g.nh * g.n_images;
     int grid = (int)((total + 255) / 256);
     if (grid > 152 * 32) grid = 152 * 32;
     splat_merge_kernel<<<grid, 256, 0, s>>>(ws, c, g.n_images, d_image);
     return sc::launch_status("sc_splat merge");
+}
+
+extern "C" int sc_merge_camera(const ScSplatParams *sp, const void *d_ws, size_t ws_bytes,
+                               const ScCameraParams *cp, const float *d_offset_f,
+                               const float *d_inv_gain_f, const float *d_sigma,
+                               const double *d_table_value, const double *d_table_cdf,
+                               float *d_expect, float *d_adc32, int32_t *d_status, void *stream) {
+    sc::TileGeom g;
+    int rc = sc::tile_geom(sp, g);
+    if (rc) return rc;
+    SplatConsts c;
+    rc = splat_consts(sp, g, c);
+    if (rc) return rc;
+    SC_REQUIRE(cp != nullptr && d_ws && d_adc32, "sc_merge_camera: NULL pointer");
+    SC_REQUIRE(g.n_images == 1, "sc_merge_camera: one image per call (got %d)", g.n_images);
+    SC_REQUIRE(!cp->exact, "sc_merge_camera: native draws only");
+    SC_REQUIRE(cp->nw == g.nw && cp->nh == g.nh, "sc_merge_camera: camera %dx%d, splat %dx%d",
+               cp->nw, cp->nh, g.nw, g.nh);
+    SC_REQUIRE(cp->camera >= SC_CAM_EMCCD && cp->camera <= SC_CAM_SCMOS,
+               "sc_merge_camera: camera %d", cp->camera);
+    SC_REQUIRE(cp->d_poisson_table != nullptr,
+               "sc_merge_camera: native draws need the Poisson tables (sc_poisson_table)");
+    if (cp->camera == SC_CAM_CMOS_TABLE)
+        SC_REQUIRE(cp->table_n > 0 && d_table_value && d_table_cdf,
+                   "sc_merge_camera: CMOS table mode needs the noise table");
+    SC_REQUIRE_CAP(ws_bytes >= sc_splat_workspace_bytes(sp),
+                   "sc_merge_camera: workspace %zu < %zu bytes", ws_bytes,
+                   sc_splat_workspace_bytes(sp));
+    sc::cam::CamConsts cc;
+    rc = sc::cam::cam_consts(cp, cc);
+    if (rc) return rc;
+    cudaStream_t s = sc::as_stream(stream);
+    const float *ws = static_cast<const float *>(d_ws);
+    const int block = 256;
+    const int64_t want = (((int64_t)cc.n + 1) / 2 + block - 1) / block;
+    // covering tiles per axis: at most ceil(edge / tile)
+    const int mt = (c.edge + c.tile - 1) / c.tile;
+    const int sel = mt == 2 ? 2 : mt == 3 ? 3 : 0;
+    switch (cc.camera * 4 + sel) {
+#define SC_MC_LAUNCH(K, M)                                                                        \
+    case K * 4 + M:                                                                               \
+        merge_camera_kernel<K, M><<<sc::resident_grid((const void *)merge_camera_kernel<K, M>,      \
+                                                      block, 0, want),                            \
+                                    block, 0, s>>>(ws, c, cc, cp->d_poisson_table, d_offset_f,    \
+                                                   d_inv_gain_f, d_sigma, d_table_value,          \
+                                                   d_table_cdf, d_expect, d_adc32, d_status);     \
+        break;
+        SC_MC_LAUNCH(SC_CAM_EMCCD, 0)
+        SC_MC_LAUNCH(SC_CAM_EMCCD, 2)
+        SC_MC_LAUNCH(SC_CAM_EMCCD, 3)
+        SC_MC_LAUNCH(SC_CAM_CCD, 0)
+        SC_MC_LAUNCH(SC_CAM_CCD, 2)
+        SC_MC_LAUNCH(SC_CAM_CCD, 3)
+        SC_MC_LAUNCH(SC_CAM_CMOS_TABLE, 0)
+        SC_MC_LAUNCH(SC_CAM_CMOS_TABLE, 2)
+        SC_MC_LAUNCH(SC_CAM_CMOS_TABLE, 3)
+        SC_MC_LAUNCH(SC_CAM_SCMOS, 0)
+        SC_MC_LAUNCH(SC_CAM_SCMOS, 2)
+        SC_MC_LAUNCH(SC_CAM_SCMOS, 3)
+#undef SC_MC_LAUNCH
+    }
+    return sc::launch_status("sc_merge_camera");
 }
 
 extern "C" int sc_batch_frame(const ScStepRec *d_recs, const int32_t *d_tile_start,

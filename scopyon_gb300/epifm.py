@@ -417,6 +417,8 @@ class FramePipeline:
         self.camera_kind = self._camera_kind()
         # name -> [(start, end) CUDA events]; set to a dict to time kernels in place
         self.kernel_events = None
+        # native frames merge the splat's tile buffers inside the camera pass
+        self.merge_camera = True
         # test hook: polls of each splat warp's first block wait (0: the normal
         # bound; -1: none, so that the wait runs out and the frame reports it)
         self.first_wait_polls = 0
@@ -567,6 +569,29 @@ class FramePipeline:
         with self.timed("splat", stream):
             call("sc_splat", ptr(recs), ptr(tile_start), ptr(items), ptr(self.psf.tables),
                  ptr(self.psf.box), sp, ptr(sws), sws_bytes, ptr(image), ptr(self.status), s)
+        return sp, sws, sws_bytes
+
+    def splat_camera(self, recs, n_rec, seed=0, counter=0, d_frame=None, stream=None, tag="",
+                     binned=False, bufs=None):
+        """A native frame's splat and camera into self.expect / self.adc32: the
+        splat without its merge, then the merge and the camera in one pass
+        (sc_merge_camera), equal bit for bit to splat_records into self.image
+        followed by camera().  With merge_camera off, those two."""
+        if not self.merge_camera:
+            self.splat_records(recs, n_rec, self.image, stream=stream, tag=tag, binned=binned,
+                               bufs=bufs)
+            self.camera(self.image, self.expect, None, self.adc32, seed=seed, counter=counter,
+                        stream=stream, d_frame=d_frame)
+            return
+        sp, sws, sws_bytes = self.splat_records(recs, n_rec, None, stream=stream, tag=tag,
+                                                binned=binned, bufs=bufs)
+        cp = self.camera_params(seed, counter, d_frame)
+        maps = self.pixel_maps
+        with self.timed("camera", stream):
+            call("sc_merge_camera", sp, ptr(sws), sws_bytes, cp,
+                 ptr(self.offset_f) if maps else None, ptr(self.inv_gain_f) if maps else None,
+                 ptr(self.sigma), ptr(self.table_value), ptr(self.table_cdf), ptr(self.expect),
+                 ptr(self.adc32), ptr(self.status), stream_ptr(stream))
 
     def finish_bins(self, n_rec, tag="", stream=None, bufs=None):
         """Scan, placement and order of records already counted into the bin
@@ -766,9 +791,8 @@ class FramePipeline:
             self.camera(None, None, self.adc, seed=seed, counter=counter, draws=draws,
                         stream=stream, d_frame=d_frame, photons64=image64, expect64=expect64)
             return expect64, self.adc, opt
-        self.splat_records(recs, n_rec, self.image, stream=stream)
-        self.camera(self.image, self.expect, None, self.adc32, seed=seed, counter=counter,
-                    draws=draws, stream=stream, d_frame=d_frame)
+        self.splat_camera(recs, n_rec, seed=seed, counter=counter, d_frame=d_frame,
+                          stream=stream)
         return self.expect, self.adc32, opt
 
 
@@ -891,10 +915,8 @@ class FrameGraph:
         """Splat and camera of one frame's binned records."""
         pipe = self.pipe
         recs, bufs = recs
-        pipe.splat_records(recs, self.n_sub * self.n, pipe.image, tag=tag, binned=True,
-                           bufs=bufs)
-        pipe.camera(pipe.image, pipe.expect, None, pipe.adc32, seed=self.seed,
-                    counter=frame_offset, d_frame=self.frame)
+        pipe.splat_camera(recs, self.n_sub * self.n, seed=self.seed, counter=frame_offset,
+                          d_frame=self.frame, tag=tag, binned=True, bufs=bufs)
 
     def _launch(self):
         s = stream_ptr()
@@ -956,12 +978,14 @@ class FrameGraph:
         # native records (counting into bins), bin scan, then place + sort +
         # long-list sort or, from 2^20 records on, three kernels per radix
         # digit pass; splat box (the bulk-copy kernel also adds the summed-area
-        # records), summed-area pass otherwise, merge; camera, counter (plus
-        # one memset)
+        # records), summed-area pass otherwise; camera (with the merge),
+        # counter (plus one memset)
         pipe = self.pipe
         fused = (pipe.stages > 0 and pipe.psf.box_p > 0 and 12 <= pipe.psf.box_nq <= 16 and
                  pipe.tile + 15 <= 32)
-        splat = 2 if fused else 3
+        # box kernel, summed-area pass unless fused, merge unless it runs in
+        # the camera pass (sc_merge_camera, counted as the camera)
+        splat = (1 if fused else 2) + (0 if pipe.merge_camera else 1)
         n_rec = self.n_sub * self.n
         if n_rec < (1 << 20):
             return 7 + splat

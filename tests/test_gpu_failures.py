@@ -141,11 +141,11 @@ def test_splat_wait_runs_out_and_is_reported(lib):
     assert "ran out" in str(err.value)
     pipe.first_wait_polls = 0
     pipe.run_frame(parts, ut, with_optinfo=False, seed=5)
-    img = pipe.image.cpu().numpy().copy()
+    img = pipe.expect.cpu().numpy().copy()
     pipe.check_status()
     fresh = FramePipeline(eng, "cuda:0", psf=pipe.psf)
     fresh.run_frame(parts, ut, with_optinfo=False, seed=5)
-    numpy.testing.assert_array_equal(fresh.image.cpu().numpy(), img)
+    numpy.testing.assert_array_equal(fresh.expect.cpu().numpy(), img)
     fresh.check_status()
     assert img.sum() > 0
 

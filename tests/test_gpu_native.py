@@ -515,3 +515,49 @@ def test_l2_fetch_hint_values(sg):
         _lib.call("sc_set_l2_fetch_granularity", b)
     with pytest.raises(ValueError, match="48 bytes"):  # SC_ERR_ARG
         _lib.call("sc_set_l2_fetch_granularity", 48)
+
+
+@pytest.mark.parametrize("det,cmos_noise", [("EMCCD", None), ("CCD", None), ("CMOS", "scmos")])
+def test_merge_camera_equals_merge_then_camera(sg, det, cmos_noise):
+    """sc_merge_camera (the splat's merge inside the camera pass) gives the
+    expectation and ADC counts of sc_splat with its merge followed by
+    sc_camera, bit for bit, over frames of a frame graph (and the trajectories
+    and budgets are untouched by the choice)."""
+    from scopyon_gb300.base import _psf_for
+    from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
+    cfg = sg.DefaultConfiguration()
+    upd = {"magnification": 100,
+           "detector": {"type": det, "image_size": [96, 72], "exposure_time": 0.004},
+           "effects": {"photo_bleaching": {"switch": True, "half_life": 0.02}}}
+    if cmos_noise:
+        upd["gpu"] = {"cmos_noise": cmos_noise}
+        upd["analog_to_digital_converter"] = {"bit": 12, "offset": 100, "type": "pixel",
+                                              "count": 5.0}
+    cfg.update({"default": upd})
+    t = numpy.arange(3 * 4 + 1) * 1e-3
+    traj = sg.sample_inputs(t, N=800, lower=[-8e-6, -6e-6, -0.2e-6], upper=[8e-6, 6e-6, 0.2e-6],
+                            D=0.4e-12, ndim=3, rng=numpy.random.RandomState(31))
+    out = []
+    for fused in (True, False):
+        eng = EngineConfig(cfg["default"], rng=numpy.random.RandomState(4))
+        pipe = FramePipeline(eng, "cuda", psf=_psf_for(eng, torch.device("cuda")))
+        if pipe.camera_kind == 3:  # sCMOS: a per-pixel sigma map
+            pipe.scmos_sigma_map(numpy.random.RandomState(5))
+        pipe.psf.ensure(list(range(0, 300)))
+        pipe.merge_camera = fused
+        pipe.ensure_slots(800)
+        pipe.budget[:800].copy_(torch.from_numpy(
+            numpy.random.RandomState(6).exponential(0.02, 800) * eng.n_emit0))
+        fg = FrameGraph(pipe, traj.copy(), 4, 1e-3, seed=9, use_graph=False)
+        frames = []
+        for _ in range(3):
+            fg.step()
+            frames.append((pipe.expect.cpu().numpy().copy(), pipe.adc32.cpu().numpy().copy()))
+        pipe.check_status()
+        out.append((frames, pipe.budget[:800].cpu().numpy().copy()))
+    (f1, b1), (f0, b0) = out
+    for (e1, a1), (e0, a0) in zip(f1, f0):
+        numpy.testing.assert_array_equal(e1, e0)
+        numpy.testing.assert_array_equal(a1, a0)
+    numpy.testing.assert_array_equal(b1, b0)
+    assert f1[0][0].max() > 0 and len(numpy.unique(f1[0][1])) > 10

@@ -128,6 +128,7 @@ def test_single_emitter_footprints(lib, golden, case, depth_idx, box):
     assert eng.px == px
     assert eng.box_p == (160 if (box and case == "c40_px160") else 0)
     pipe = FramePipeline(eng, "cuda")
+    pipe.merge_camera = False  # keep the splat's photon image (pipe.image)
     depth = float(golden["psf_depths"][depth_idx])
     n_emit = eng.qy * (eng.amplitude0 * numpy.exp(-abs(depth) / eng.penetration) * eng.x_sec
                        * 1.0) * eng.beer

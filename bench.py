@@ -294,12 +294,14 @@ def gb300_arm(args, rank, world):
     ms_per_step = elapsed_ms / args.steps
     value = world * args.steps / (elapsed_ms / 1e3)
 
-    e2e = None if args.small else e2e_arm(args, cfg, dev, rank, world)
     cfg1 = None if args.small else config1_arm(args, dev)
     fwd_bwd = None if args.small else fwd_bwd_arm(args, dev)
     batched = None if args.small else batched_arm(args, dev)
     peak, peak_kind = load_peaks()
     large_stages = None if args.small else hbm_stages(dev, peak)
+    # the host-bound leg last: right after a large process exits, the host's
+    # memory reclaim slows pinned uploads for some seconds
+    e2e = None if args.small else e2e_arm(args, cfg, dev, rank, world)
 
     splat_avg_ms = sum(splat_ms) / len(splat_ms)
     n_rec = sum(splat_recs) / len(splat_recs)

@@ -492,6 +492,31 @@ class FramePipeline:
             self._cap[name] = t
         return t[:numel].numpy().reshape(shape)
 
+    def _upload_small(self, values, ring=8):
+        """A small float64 host array to a new device tensor through a ring of
+        pinned buffers: each slot is refilled only after its previous upload
+        has completed (its event)."""
+        n = values.size
+        slots = self._cap.get("small_ring")
+        if slots is None or slots[0][0].numel() < n:
+            size = max(64, n)
+            slots = [(torch.empty(size, dtype=torch.float64, pin_memory=True), None)
+                     for _ in range(ring)]
+            self._cap["small_ring"] = slots
+            self._cap["small_next"] = 0
+        k = self._cap["small_next"]
+        self._cap["small_next"] = (k + 1) % len(slots)
+        buf, ev = slots[k]
+        if ev is not None:
+            ev.synchronize()
+        buf[:n].numpy()[:] = values
+        out = torch.empty(n, dtype=torch.float64, device=self.device)
+        out.copy_(buf[:n], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        slots[k] = (buf, ev)
+        return out
+
     def ensure_slots(self, n_slots, initial=None):
         if self.budget.numel() < n_slots:
             grown = torch.zeros(n_slots, dtype=torch.float64, device=self.device)
@@ -749,9 +774,11 @@ class FramePipeline:
             ev = torch.cuda.Event()
             ev.record()
             self._cap.setdefault("upload_events", {})[host.data_ptr()] = ev
-        # a pinned copy: a pageable upload would wait for all the work queued before it
-        ut = torch.from_numpy(numpy.ascontiguousarray(unit_times, dtype=float)).pin_memory().to(
-            dev, non_blocking=True)
+        # from a pinned buffer (a pageable upload would wait for all the work
+        # queued before it), one of a ring allocated once: pinning per frame
+        # calls the driver's host allocator whenever the cached blocks are
+        # still in flight, which is slow while the OS reclaims memory
+        ut = self._upload_small(numpy.ascontiguousarray(unit_times, dtype=float).reshape(-1))
         pres = None
         if present is not None:
             pres = torch.from_numpy(numpy.ascontiguousarray(present, dtype=numpy.uint8).reshape(-1)).to(dev)

@@ -386,6 +386,8 @@ def summary(r):
     st = r["roofline"].get("stages_beyond_l2")
     if st:
         out["diffusion_frac_beyond_l2"] = round(st["diffusion"]["frac"], 3)
+        out["diffusion_frac_on_budget"] = round(st["diffusion"]["frac_on_budget"], 3)
+        out["diffusion_fp64_rows_frac"] = round(st["diffusion"]["fp64_rows"]["frac"], 3)
         out["camera_frac_beyond_l2"] = round(st["camera"]["frac"], 3)
     return out
 

@@ -550,10 +550,14 @@ int sc_merge_camera(const ScSplatParams *sp, const void *d_ws, size_t ws_bytes,
  * EMCCD / CCD / CMOS classes and __get_analog_to_digital_converter_counts
  * (src/scopyon/_epifm.py:329-433, :1430-1484).
  * Native mode (p->exact == 0): Philox draws, FP32 arithmetic with the float
- * maps d_offset_f / d_inv_gain_f (NULL: constants offset0 / 1/gain0).  The
- * Poisson draw takes no rejection below a mean of 256 (table inversion of
- * the integer part plus sequential inversion of the fraction); the EMCCD
- * output follows the reference's truncated discrete law.
+ * maps d_offset_f / d_inv_gain_f (NULL: constants offset0 / 1/gain0).  Each
+ * pixel pair shares one Philox4x32-10 block (counter: the pair index and the
+ * frame counter): one 32-bit word per pixel for its Poisson draw, which takes
+ * no rejection below a mean of 256 (table inversion of the integer part, then
+ * sequential inversion of the fraction at the word's residual in its bin),
+ * and a Box-Muller pair for the two read-noise normals; a pixel's draws so
+ * depend on its index and the frame only.  The EMCCD output follows the
+ * reference's truncated discrete law.
  * Exact mode (p->exact == 1): draws injected by the caller — d_inj_signal
  * (electrons) and d_inj_noise (electrons) or, for the CMOS table,
  * d_inj_uniform — and the reference's FP64 ADC sequence with d_offset /
@@ -568,8 +572,8 @@ int sc_camera(const ScCameraParams *p, const float *d_photons,
               float *d_adc32, int32_t *d_status, void *stream);
 
 /* Poisson tables for the camera's native draws: for every integer mean j <
- * 256, the Poisson(j) CDF in FP32 (summed in FP64) and a guide of starting
- * points for its inversion.  Built once per device into a caller buffer of
+ * 256, the Poisson(j) CDF as 32-bit fixed point (summed in FP64) and a guide
+ * of starting points for its inversion.  Built once per device into a caller buffer of
  * sc_poisson_table_bytes() bytes (16-byte aligned), read by sc_camera
  * (ScCameraParams.d_poisson_table).  Replaces the Poisson draws of
  * CCD / CMOS get_signal and the photo-electron count inside the EMCCD law

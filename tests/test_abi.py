@@ -191,3 +191,37 @@ def test_layout_and_kernel_choices_are_checked_on_the_host():
     assert L.sc_set_l2_fetch_granularity(17) == _lib.SC_ERR_ARG
     assert b"17 bytes" in L.sc_last_error()
     assert L.sc_box_block_floats(14) == 196 and L.sc_box_block_floats(13) == 172
+
+
+def test_merge_camera_checks_on_the_host():
+    """sc_merge_camera refuses, before any CUDA call, the cases it does not
+    take: injected draws, several images per call, a camera of another size,
+    no Poisson tables, an undersized workspace."""
+    from scopyon_gb300 import _build, _lib
+    _build.build()
+    L = _lib.load()
+    P = ctypes.c_void_p
+    fake = P(1 << 20)
+    sp = _lib.SplatParams(nw=64, nh=64, tile=8, halo=14, warps=4, tiles_x=8, tiles_y=8, n_r=1000,
+                          sat_pitch=1004, n_images=1, rec_per_image=0, px=1.6e-7, res=1e-9)
+    ws = L.sc_splat_workspace_bytes(ctypes.byref(sp))
+    cp = _lib.CameraParams(nw=64, nh=64, camera=_lib.CAM_SCMOS, exact=1, bit=12, qe=0.7,
+                           fullwell=30000.0, offset0=100.0, gain0=7.5)
+    cp.d_poisson_table = 1 << 20
+
+    def call(cp_, sp_, ws_bytes):
+        return L.sc_merge_camera(ctypes.byref(sp_), fake, ctypes.c_size_t(ws_bytes),
+                                 ctypes.byref(cp_), None, None, None, None, None, None, fake,
+                                 None, None)
+
+    assert call(cp, sp, ws) == _lib.SC_ERR_ARG and b"native" in L.sc_last_error()
+    cp.exact = 0
+    cp.nh = 32
+    assert call(cp, sp, ws) == _lib.SC_ERR_ARG and b"camera 64x32" in L.sc_last_error()
+    cp.nh = 64
+    cp.d_poisson_table = None
+    assert call(cp, sp, ws) == _lib.SC_ERR_ARG and b"Poisson" in L.sc_last_error()
+    cp.d_poisson_table = 1 << 20
+    assert call(cp, sp, ws - 4) == _lib.SC_ERR_CAPACITY
+    sp.n_images = 2
+    assert call(cp, sp, 2 * ws) == _lib.SC_ERR_ARG and b"one image" in L.sc_last_error()

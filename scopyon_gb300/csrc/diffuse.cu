@@ -447,7 +447,10 @@ inline size_t rec_shared_bytes(int chunk) {
 #ifndef SC_REC_MIN_BLOCKS
 #define SC_REC_MIN_BLOCKS 6
 #endif
-template <bool kInjected, bool kSig>
+// kF32: native records from the FP32 positions (focal point at the origin,
+// identity transform); a template parameter, so that each instance holds one
+// form of the record arithmetic (a smaller kernel for the instruction cache).
+template <bool kInjected, bool kSig, bool kF32>
 __global__ void __launch_bounds__(kRecWarps * 32, SC_REC_MIN_BLOCKS)
 native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
                       int32_t *klass, const double *sigma, const double *normals,
@@ -483,10 +486,8 @@ native_records_kernel(DiffConsts c, sc::StepConsts k, int chunk, double *pos,
             q[2] = sc::f2d_exact(ps[2]);
         }
     };
-    // native records from the FP32 positions directly (no FP64 conversions):
-    // the formatted position is a permutation of them and the focal point 0
-    const bool f32_records =
-        !kInjected && k.focal_zero && (c.ndim == 3 ? c.identity != 0 : c.scale == 1.0);
+    // native records from the FP32 positions directly (no FP64 conversions)
+    constexpr bool f32_records = !kInjected && kF32;
     const bool live = i < c.n;
     const int64_t step0 = c.step0 + (c.frame ? *c.frame * c.n_sub : 0);
     // the excitation is the same for every particle: EPI, or a flat field
@@ -840,8 +841,14 @@ extern "C" int sc_native_records(const ScDiffuseParams *p, const ScStepParams *s
     const int chunk = c.n_sub < 32 ? c.n_sub : 32;
     const bool sig = !d_normals && c.n_sig > 0;
     const size_t smem = rec_shared_bytes(chunk) + (sig ? (size_t)c.n_sig * sizeof(float) : 0);
-    auto kern = d_normals ? native_records_kernel<true, false>
-                          : sig ? native_records_kernel<false, true> : native_records_kernel<false, false>;
+    // native records from FP32 positions when the formatted position is a
+    // permutation of them and the focal point is the origin
+    const bool f32 = !d_normals && k.focal_zero && (c.ndim == 3 ? c.identity != 0 : c.scale == 1.0);
+    auto kern = d_normals ? native_records_kernel<true, false, false>
+                : sig ? (f32 ? native_records_kernel<false, true, true>
+                             : native_records_kernel<false, true, false>)
+                      : (f32 ? native_records_kernel<false, false, true>
+                             : native_records_kernel<false, false, false>);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);

@@ -240,6 +240,14 @@ int sc_box_block_floats(int nq);
  * itself.  No counterpart in the reference (a CPU program).                */
 int sc_set_l2_fetch_granularity(int bytes);
 
+/* Copies `bytes` from src to dst on `stream` (one cudaMemcpyAsync; the
+ * direction follows from the addresses).  For a host without a device
+ * runtime of its own: a frame's rows to the device before sc_emitter_steps,
+ * its ADC counts and status words back after the camera.  From pinned host
+ * memory the copy is asynchronous; from pageable memory it returns once the
+ * source has been read.  No counterpart in the reference (a CPU program).  */
+int sc_copy_async(void *dst, const void *src, size_t bytes, void *stream);
+
 int sc_psf_box_table(const float *d_sat, int n_keys, int n_r, int sat_pitch, int box_p,
                      float *d_box, void *stream);
 

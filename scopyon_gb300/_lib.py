@@ -103,6 +103,7 @@ _SIG = {
     "sc_get_version": (_I, []),
     "sc_box_block_floats": (_I, [_I]),
     "sc_set_l2_fetch_granularity": (_I, [_I]),
+    "sc_copy_async": (_I, [_P, _P, ctypes.c_size_t, _P]),
     "sc_struct_sizes": (_I, [_P, _I]),
     "sc_counter_add": (_I, [_P, ctypes.c_int64, _P]),
     "sc_stage_rows": (_I, [_P, ctypes.c_int64, _P, _P, _P]),
@@ -244,6 +245,13 @@ def ptr(t):
 
 
 def stream_ptr(stream=None):
+    """The CUDA stream handle of ``stream`` (a torch stream), by default of
+    the current stream of the current device (read without building a
+    stream object where torch offers that)."""
     import torch
-    s = stream if stream is not None else torch.cuda.current_stream()
-    return ctypes.c_void_p(s.cuda_stream)
+    if stream is not None:
+        return ctypes.c_void_p(stream.cuda_stream)
+    raw = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+    if raw is not None:
+        return ctypes.c_void_p(raw(torch.cuda.current_device()))
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)

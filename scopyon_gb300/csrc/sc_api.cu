@@ -36,6 +36,14 @@ extern "C" int sc_set_l2_fetch_granularity(int bytes) {
                            "sc_set_l2_fetch_granularity");
 }
 
+extern "C" int sc_copy_async(void *dst, const void *src, size_t bytes, void *stream) {
+    if (bytes == 0) return SC_OK;
+    SC_REQUIRE(dst != nullptr && src != nullptr, "sc_copy_async: NULL pointer");
+    return sc::cuda_status(
+        cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, sc::as_stream(stream)),
+        "sc_copy_async");
+}
+
 extern "C" int sc_struct_sizes(size_t *out, int n) {
     SC_REQUIRE(out != nullptr && n >= 6, "sc_struct_sizes: need room for 6 sizes");
     out[0] = sizeof(ScStepRec);

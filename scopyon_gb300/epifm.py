@@ -8,6 +8,7 @@ Device buffers are torch CUDA tensors, reused across frames.
 """
 
 import contextlib
+import ctypes
 import math
 import warnings
 
@@ -249,6 +250,7 @@ class PSFTables:
         self.box_block = _lib.load().sc_box_block_floats(self.box_nq) if self.box_p else 0
         self.box_floats = self.box_p ** 2 * self.box_block
         self.box = torch.empty(0, dtype=torch.float32, device=device) if self.box_p else None
+        self._covered = None  # a depth range whose keys are all built
 
     def _depth_of_key(self, key):
         return self.cfg.depth_cutoff if key < 0 else key * PSF_RES
@@ -305,6 +307,9 @@ class PSFTables:
         plane) can map to.  Keys grow with |depth| up to the cutoff, so the
         keys of the two extreme |depths| bound them all: a contiguous range,
         checked against the built set without sorting the per-emitter keys."""
+        cov = self._covered
+        if cov is not None and cov[0] <= dmin and dmax <= cov[1]:
+            return  # within a range already checked (keys are never dropped)
         if not (math.isfinite(dmin) and math.isfinite(dmax)):
             raise ValueError("non-finite emitter depth")
         lo = 0.0 if dmin <= 0.0 <= dmax else min(abs(dmin), abs(dmax))
@@ -316,10 +321,10 @@ class PSFTables:
             top = self.max_key if k_hi < 0 else k_hi
             wanted = list(range(k_lo, top + 1)) + ([-1] if k_hi < 0 else [])
         have = self.key_slot_host
-        if all(have[k if k >= 0 else self.max_key + 1] >= 0 for k in (wanted[0], wanted[-1])) and \
-                (have[k_lo: (self.max_key if k_hi < 0 else k_hi) + 1] >= 0).all():
-            return
-        self.ensure(wanted, stream)
+        if not (all(have[k if k >= 0 else self.max_key + 1] >= 0 for k in (wanted[0], wanted[-1]))
+                and (have[k_lo: (self.max_key if k_hi < 0 else k_hi) + 1] >= 0).all()):
+            self.ensure(wanted, stream)
+        self._covered = (dmin, dmax)
 
     def ensure_all(self, stream=None):
         self.ensure(list(range(0, self.max_key + 1)) + [-1], stream)
@@ -495,26 +500,26 @@ class FramePipeline:
     def _upload_small(self, values, ring=8):
         """A small float64 host array to a new device tensor through a ring of
         pinned buffers: each slot is refilled only after its previous upload
-        has completed (its event)."""
+        has completed (the slot's event, recorded again at each use)."""
         n = values.size
-        slots = self._cap.get("small_ring")
-        if slots is None or slots[0][0].numel() < n:
-            size = max(64, n)
-            slots = [(torch.empty(size, dtype=torch.float64, pin_memory=True), None)
-                     for _ in range(ring)]
-            self._cap["small_ring"] = slots
-            self._cap["small_next"] = 0
-        k = self._cap["small_next"]
-        self._cap["small_next"] = (k + 1) % len(slots)
-        buf, ev = slots[k]
-        if ev is not None:
+        r = self._cap.get("small_ring")
+        if r is None or r[0].shape[1] < n:
+            host = torch.empty((ring, max(64, n)), dtype=torch.float64, pin_memory=True)
+            r = (host.numpy(), host, [None] * ring, [0])
+            self._cap["small_ring"] = r
+        views, host, events, nxt = r
+        k = nxt[0]
+        nxt[0] = (k + 1) % len(events)
+        ev = events[k]
+        if ev is None:
+            ev = events[k] = torch.cuda.Event()
+        else:
             ev.synchronize()
-        buf[:n].numpy()[:] = values
+        views[k, :n] = values
         out = torch.empty(n, dtype=torch.float64, device=self.device)
-        out.copy_(buf[:n], non_blocking=True)
-        ev = torch.cuda.Event()
+        call("sc_copy_async", ptr(out), ctypes.c_void_p(views[k].ctypes.data), n * 8,
+             stream_ptr())
         ev.record()
-        slots[k] = (buf, ev)
         return out
 
     def ensure_slots(self, n_slots, initial=None):
@@ -713,15 +718,22 @@ class FramePipeline:
         name = "frame_out%d" % slot
         h = self._cap.get(name)
         if h is None or h[0].numel() < adc.numel() or h[0].dtype != adc.dtype:
-            h = (torch.empty(adc.numel(), dtype=adc.dtype, pin_memory=True),
-                 torch.empty(self.status.numel(), dtype=torch.int32, pin_memory=True))
+            counts = torch.empty(adc.numel(), dtype=adc.dtype, pin_memory=True)
+            status = torch.empty(self.status.numel(), dtype=torch.int32, pin_memory=True)
+            # the slot's event is recorded again at each use: the caller has
+            # read the slot's previous frame before it asks for the slot again
+            h = (counts, status, counts.numpy(), status.numpy(), torch.cuda.Event())
             self._cap[name] = h
-        counts = h[0][: adc.numel()]
-        counts.copy_(adc.reshape(-1), non_blocking=True)
-        h[1].copy_(self.status, non_blocking=True)
-        ev = torch.cuda.Event()
+        counts, status, counts_np, status_np, ev = h
+        if not adc.is_contiguous():
+            adc = adc.contiguous()
+        s = stream_ptr()
+        call("sc_copy_async", ctypes.c_void_p(counts.data_ptr()), ptr(adc),
+             adc.numel() * adc.element_size(), s)
+        call("sc_copy_async", ctypes.c_void_p(status.data_ptr()), ptr(self.status),
+             status.numel() * 4, s)
         ev.record()
-        return ev, counts.numpy(), h[1].numpy()
+        return ev, counts_np[: adc.numel()], status_np
 
     def raise_for_status(self, st):
         """Raises the error the status words ``st`` (read from the device)
@@ -768,12 +780,15 @@ class FramePipeline:
         n_sub, n = particles.shape[0], particles.shape[1]
         dev = self.device
         part = self._buf("particles", n_sub * n * 5, torch.float64)[: n_sub * n * 5]
-        host = torch.from_numpy(numpy.ascontiguousarray(particles, dtype=float).reshape(-1))
-        part.copy_(host, non_blocking=host.is_pinned())
-        if host.is_pinned() and track_upload:
+        host = numpy.ascontiguousarray(particles, dtype=float)
+        # one copy on the current stream (from pageable memory it returns once
+        # the source has been read)
+        call("sc_copy_async", ptr(part), ctypes.c_void_p(host.ctypes.data), host.nbytes,
+             stream_ptr(stream))
+        if track_upload and host.size and torch.from_numpy(host.reshape(-1)).is_pinned():
             ev = torch.cuda.Event()
             ev.record()
-            self._cap.setdefault("upload_events", {})[host.data_ptr()] = ev
+            self._cap.setdefault("upload_events", {})[host.ctypes.data] = ev
         # from a pinned buffer (a pageable upload would wait for all the work
         # queued before it), one of a ring allocated once: pinning per frame
         # calls the driver's host allocator whenever the cached blocks are

@@ -24,7 +24,8 @@ import numpy
 
 from . import _lib
 from . import config as _config
-from .epifm import EngineConfig, FramePipeline, InjectedDraws, PSFTables, frame_windows
+from .epifm import (EngineConfig, FramePipeline, HostRowsGraph, InjectedDraws, PSFTables,
+                    frame_windows)
 from .image import Image
 from .sampling import DeviceTrajectories
 
@@ -324,6 +325,15 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
         for k in range(len(data)):  # the formatted arrays live on in the block only
             data[k] = (data[k][0], pinned.block[k])
     pinned_ok = None  # the slot order equals the pinned block's ids
+    host_graph = None  # native frames from the pinned block: graph replays
+    seq_seed = []
+
+    def native_seed():
+        """The camera's Philox key for the sequence's native frames (drawn
+        from rng at the first; each frame's counter is its index)."""
+        if not seq_seed:
+            seq_seed.append(int(rng.randint(0, 2 ** 31 - 1)) << 31 | int(rng.randint(0, 2 ** 31 - 1)))
+        return seq_seed[0]
     for f in range(num_frames):
         ahead = None
         if pending is not None:
@@ -343,12 +353,18 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
                     pipe.ensure_slots(len(slot_ids_f))
                     pipe.psf.ensure_depth_range(lo - focal0, hi - focal0)
                     frame_draws = draws.next_frame() if draws is not None and draws.frames else None
-                    seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | \
-                        int(rng.randint(0, 2 ** 31 - 1)) if frame_draws is None else 0
-                    _, adc, _ = pipe.run_frame(particles, uts, with_optinfo=False,
-                                               draws=frame_draws, seed=seed, counter=f,
-                                               present=None, bleaching=bleaching,
-                                               track_upload=False)
+                    if frame_draws is None:
+                        n_sub = particles.shape[0]
+                        if host_graph is None or (host_graph.n_sub, host_graph.n) != \
+                                (n_sub, particles.shape[1]):
+                            host_graph = HostRowsGraph(pipe, n_sub, particles.shape[1],
+                                                       native_seed(), bleaching)
+                        adc = host_graph.run(particles, uts, f)
+                    else:
+                        _, adc, _ = pipe.run_frame(particles, uts, with_optinfo=False,
+                                                   draws=frame_draws, seed=0, counter=f,
+                                                   present=None, bleaching=bleaching,
+                                                   track_upload=False)
                     nxt = pipe.frame_out(adc, slot=f % 2)
                 except Exception:
                     if out is not None:  # the frame before first, then the error
@@ -373,8 +389,7 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
                     pipe.ensure_slots(len(slot_ids_f))
                     pipe.psf.ensure_depth_range(rng_[0] - focal0, rng_[1] - focal0)
                     frame_draws = draws.next_frame() if draws is not None and draws.frames else None
-                    seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | \
-                        int(rng.randint(0, 2 ** 31 - 1)) if frame_draws is None else 0
+                    seed = native_seed() if frame_draws is None else 0
                     _, adc, _ = pipe.run_frame(staging, uts, with_optinfo=False,
                                                draws=frame_draws, seed=seed, counter=f,
                                                present=None, bleaching=bleaching)
@@ -445,8 +460,7 @@ def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, dr
             depth = particles[:, :, 0]
             pipe.psf.ensure_depth_range(float(depth.min()) - focal0, float(depth.max()) - focal0)
         frame_draws = draws.next_frame() if draws is not None and draws.frames else None
-        seed = int(rng.randint(0, 2 ** 31 - 1)) << 31 | int(rng.randint(0, 2 ** 31 - 1)) \
-            if frame_draws is None else 0
+        seed = native_seed() if frame_draws is None else 0
         expect, adc, opt = pipe.run_frame(particles, uts, with_optinfo=full_output,
                                           draws=frame_draws, seed=seed, counter=f,
                                           present=present, bleaching=bleaching)

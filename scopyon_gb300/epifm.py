@@ -428,6 +428,19 @@ class FramePipeline:
         # bound; -1: none, so that the wait runs out and the frame reports it)
         self.first_wait_polls = 0
 
+    def graph_signature(self):
+        """Every device address and launch shape a captured frame graph of
+        this pipeline depends on: its own buffers, the PSF tables' and the
+        tile shape.  A graph is replayed only while this is unchanged."""
+        psf = self.psf
+        ts = (self.status, self.image, self.expect, self.adc, self.adc32, self.budget,
+              self.offset_f, self.inv_gain_f, self.sigma, self.table_value, self.table_cdf,
+              psf.key_slot, psf.tables, psf.box, self.poisson)
+        return (tuple(0 if t is None else t.data_ptr() for t in ts) +
+                tuple(v.data_ptr() for v in self._cap.values() if isinstance(v, torch.Tensor)) +
+                (psf.capacity, self.tile, self.warps, self.stages, self.merge_camera,
+                 self.pixel_maps, self.first_wait_polls))
+
     def set_tiles(self, tile, warps, stages=4):
         """Use tiles of tile x tile pixels, `warps` warps per splat CTA and
         `stages` box-table block copies in flight per warp (0: the register
@@ -890,6 +903,90 @@ def tune_tiles(graph, candidates=TILE_CANDIDATES, frames=3):
         raise RuntimeError("no tile configuration ran")
     pipe.set_tiles(*min(times, key=times.get))
     return times
+
+
+class HostRowsGraph:
+    """Native frames from host rows replayed from captured CUDA graphs.
+
+    A frame's rows ((n_sub, n, 5) float64 [depth, x, y, m_id, p_state], in
+    pinned host memory that stays unchanged) and unit times go to the device
+    on a copy stream, into one of two input slots, while the frame before
+    runs on the current stream; the current stream then waits for them and
+    replays the slot's graph: the records (sc_emitter_steps), the binning,
+    the splat and the merge with the camera, into ``pipe.expect`` and
+    ``pipe.adc32``.  The camera's Philox key is ``seed`` and its counter the
+    frame index, which travels with the slot's unit times.  Before each
+    replay the pipeline's ``graph_signature`` is compared with the one the
+    graphs were captured with; a change (a PSF table that grew, a buffer
+    reallocated) runs that frame eagerly and captures the graphs again.
+    """
+
+    def __init__(self, pipe, n_sub, n, seed, bleaching):
+        dev = pipe.device
+        self.pipe, self.n_sub, self.n = pipe, int(n_sub), int(n)
+        self.seed, self.bleaching = int(seed), bleaching
+        self.part = [torch.empty(max(self.n_sub * self.n * 5, 1), dtype=torch.float64, device=dev)
+                     for _ in range(2)]
+        # per slot: the unit times (float64) then the frame index (int64)
+        self.small = [torch.empty(self.n_sub + 1, dtype=torch.int64, device=dev) for _ in range(2)]
+        self.h_small = torch.empty((2, self.n_sub + 1), dtype=torch.int64, pin_memory=True)
+        self.h_small_np = self.h_small.numpy()
+        self.copy_stream = torch.cuda.Stream(device=dev)
+        for t in self.part + self.small:
+            t.record_stream(self.copy_stream)  # freed only after the copies queued on it
+        self.copied = [torch.cuda.Event(), torch.cuda.Event()]
+        self.done = [torch.cuda.Event(), torch.cuda.Event()]
+        self.used = [False, False]
+        self.graphs = [None, None]
+        self.sig = None
+        self.k = 0
+        self.captures = 0
+
+    def _frame(self, k):
+        """The frame's kernels on the current stream, from input slot k."""
+        small = self.small[k]
+        self.pipe.run_frame_device(self.part[k], small[: self.n_sub].view(torch.float64),
+                                   self.n_sub, self.n, with_optinfo=False, seed=self.seed,
+                                   counter=0, bleaching=self.bleaching,
+                                   d_frame=small[self.n_sub:])
+
+    def run(self, rows, unit_times, frame):
+        """Frame ``frame`` from ``rows`` (pinned, C-contiguous, not changed
+        afterwards) and ``unit_times`` (n_sub); returns ``pipe.adc32``."""
+        k = self.k % 2
+        self.k += 1
+        main, cs = torch.cuda.current_stream(), self.copy_stream
+        if self.used[k]:
+            self.copied[k].synchronize()  # the slot's host values have been copied
+            cs.wait_event(self.done[k])  # the slot's last frame has read its inputs
+        else:
+            cs.wait_stream(main)
+        hs = self.h_small_np[k]
+        hs[: self.n_sub].view(numpy.float64)[:] = unit_times
+        hs[self.n_sub] = int(frame)
+        s = stream_ptr(cs)
+        call("sc_copy_async", ptr(self.part[k]), ctypes.c_void_p(rows.ctypes.data), rows.nbytes, s)
+        call("sc_copy_async", ptr(self.small[k]), ctypes.c_void_p(hs.ctypes.data), hs.nbytes, s)
+        self.copied[k].record(cs)
+        main.wait_event(self.copied[k])
+        self.used[k] = True
+        sig = self.pipe.graph_signature()
+        if self.graphs[k] is not None and sig == self.sig:
+            self.graphs[k].replay()
+        else:
+            # eagerly (which allocates what the frame needs), then capture
+            # both slots' graphs on the buffers as they now are
+            self._frame(k)
+            self.graphs = [None, None]
+            for j in range(2):
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    self._frame(j)
+                self.graphs[j] = g
+            self.sig = self.pipe.graph_signature()
+            self.captures += 1
+        self.done[k].record(main)
+        return self.pipe.adc32
 
 
 class FrameGraph:

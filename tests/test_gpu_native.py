@@ -358,6 +358,46 @@ def test_host_inputs_fast_path_matches_general_path(sg, pin_limit, monkeypatch):
     assert outs[0].std(axis=0).max() > 0
 
 
+def test_host_rows_graph_recaptures_when_the_psf_tables_grow(sg, monkeypatch):
+    """Native frames from a pinned block of host rows replay captured graphs
+    (records, binning, splat, camera), with each frame's rows uploaded on a
+    copy stream while the frame before runs.  When the depths reach new PSF
+    keys mid-sequence, the tables are reallocated and the graphs captured
+    again; every frame still equals the general path's (no graphs) bit for
+    bit."""
+    from scopyon_gb300 import base
+    monkeypatch.setattr(base, "_PSF_CACHE", {})  # tables that start empty and grow
+    made = []
+
+    class Recording(base.HostRowsGraph):
+        def __init__(self, *a, **k):
+            super().__init__(*a, **k)
+            made.append(self)
+
+    monkeypatch.setattr(base, "HostRowsGraph", Recording)
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {
+        "magnification": 100,
+        "detector": {"type": "EMCCD", "image_size": [56, 48], "exposure_time": 0.004}}})
+    rng = numpy.random.RandomState(4)
+    n, n_frames = 200, 6
+    ids = numpy.arange(n, dtype=float)
+    inputs = []
+    for k in range(n_frames * 4 + 1):
+        z_half = 0.05e-6 if k < 8 else 0.6e-6  # frames 2 on reach deeper keys
+        xyz = numpy.column_stack([rng.uniform(-3e-6, 3e-6, n), rng.uniform(-3e-6, 3e-6, n),
+                                  rng.uniform(-z_half, z_half, n)])
+        inputs.append((k * 1e-3, numpy.hstack([xyz, ids[:, None], numpy.ones((n, 1))])))
+    outs = []
+    for full in (False, True):
+        gen = sg.generate_images(inputs, n_frames, config=cfg, rng=numpy.random.RandomState(5),
+                                 full_output=full)
+        outs.append(numpy.array([(img[0] if full else img).as_array() for img in gen]))
+    assert len(made) == 1 and made[0].captures >= 2
+    numpy.testing.assert_array_equal(outs[0], outs[1])
+    assert outs[0].std(axis=0).max() > 0
+
+
 @pytest.mark.parametrize("boundary,ndim", [("reflecting", 3), ("periodic", 3), ("none", 2)])
 def test_native_rows_layouts_agree(sg, boundary, ndim):
     """Native (Philox) trajectories move in FP32: every position is an FP32

@@ -416,7 +416,8 @@ def e2e_arm(args, cfg, dev, rank, world):
     torch.cuda.synchronize()
     dt = max_over_ranks(time.perf_counter() - t0, world, dev)
     return {"value": world * steps / dt, "unit": "frames/s", "frames": steps,
-            "h2d_bytes_per_step": SUBSTEPS * N_EMIT * 5 * 8 + SUBSTEPS * 8,
+            # rows, then the unit times and the frame index
+            "h2d_bytes_per_step": SUBSTEPS * N_EMIT * 5 * 8 + (SUBSTEPS + 1) * 8,
             "d2h_bytes_per_step": IMAGE * IMAGE * 4 + 16}
 
 
@@ -671,7 +672,7 @@ def config1_arm(args, dev, n_emit=1000, substeps=10, seed=17):
                         "100 photons/emitter/ms, D = 0.1 um^2/s",
             "value": 1e3 / ms, "unit": "frames/s", "ms_per_frame": ms, "frames": steps,
             "e2e": {"value": 1.0 / e2e_s, "unit": "frames/s", "frames": e2e_frames,
-                    "h2d_bytes_per_step": substeps * n_emit * 5 * 8 + substeps * 8,
+                    "h2d_bytes_per_step": substeps * n_emit * 5 * 8 + (substeps + 1) * 8,
                     "d2h_bytes_per_step": 160 * 160 * 4 + 16}}
 
 

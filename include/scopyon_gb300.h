@@ -40,7 +40,9 @@ extern "C" {
  *     bit3 RNG loop bound hit, bit4 capacity, bit5 a bounded wait for an
  *     asynchronous copy ran out, bit6 a caller-built record with a negative
  *     first pixel, which is not binned, bit7 a non-finite emitter position or
- *     normalisation), [1..3] first offending index. */
+ *     normalisation, bit8 an index out of range in a library built with
+ *     -DSC_BOUNDS_CHECK: [1] the index, [2] its bound, [3] the check's site),
+ *     [1..3] first offending index. */
 #define SC_STATUS_WORDS 4
 
 /* One emitter during one exposure sub-step, ready to be splatted (64 bytes).

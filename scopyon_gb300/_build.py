@@ -3,6 +3,12 @@
 Each ``csrc/*.cu`` file is compiled for sm_103a in parallel into
 ``scopyon_gb300/_build/`` and the objects are linked into one shared library.
 Sources newer than their object are recompiled; nothing else is.
+
+``build_checked()`` builds the same sources with ``-DSC_BOUNDS_CHECK`` into
+``scopyon_gb300/_build/checked/libscopyon_gb300_checked.so``: kernels then
+range-check their data-dependent shared-memory, tile-buffer and bin-list
+indices, skip an access out of range and report it in the status words.
+Load it instead of the normal library with ``SCOPYON_GB300_LIB``.
 """
 
 import concurrent.futures
@@ -35,8 +41,12 @@ def _deps(src):
     return deps
 
 
-def _compile(src, extra):
-    obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+CHECKED_DIR = os.path.join(BUILD, "checked")
+CHECKED_LIB = os.path.join(CHECKED_DIR, "libscopyon_gb300_checked.so")
+
+
+def _compile(src, extra, out_dir=BUILD):
+    obj = os.path.join(out_dir, os.path.basename(src)[:-3] + ".o")
     cmd = [nvcc()] + ARCH + FLAGS + extra + ["-I", INCLUDE, "-c", src, "-o", obj]
     # the object is current when it is newer than its sources and was built
     # with the same command line (extra flags rebuild it)
@@ -54,24 +64,29 @@ def _compile(src, extra):
     return obj, None
 
 
-def build(verbose=False, extra_flags=()):
+def build(verbose=False, extra_flags=(), out_dir=BUILD, lib=LIB):
     """Compile and link the library; return its path."""
-    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(out_dir, exist_ok=True)
     sources = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
     with concurrent.futures.ThreadPoolExecutor(max_workers=min(8, len(sources))) as pool:
-        results = list(pool.map(lambda s: _compile(s, list(extra_flags)), sources))
+        results = list(pool.map(lambda s: _compile(s, list(extra_flags), out_dir), sources))
     errors = [e for _, e in results if e]
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
     objs = [o for o, _ in results]
-    if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+    if not os.path.exists(lib) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"]
         proc = subprocess.run(cmd, capture_output=True, text=True)
         if proc.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s%s" % (" ".join(cmd), proc.stdout, proc.stderr))
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
+
+
+def build_checked(verbose=False):
+    """The bounds-checked library (``-DSC_BOUNDS_CHECK``); return its path."""
+    return build(verbose, ("-DSC_BOUNDS_CHECK",), CHECKED_DIR, CHECKED_LIB)
 
 
 if __name__ == "__main__":

@@ -119,20 +119,24 @@ bin_tile_scan_kernel(const int32_t *tile_count, int n_bins, int32_t *tile_start,
 
 // Each record to its bin's offset plus its rank.
 __global__ void bin_place_kernel(const int32_t *rec_bin, const int32_t *rec_rank, int n_rec,
-                                 const int32_t *tile_start, int32_t *items) {
+                                 const int32_t *tile_start, int32_t *items, int32_t *status) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rec; r += gridDim.x * blockDim.x) {
         const int t = rec_bin[r];
-        if (t >= 0) items[__ldg(tile_start + t) + rec_rank[r]] = r;
+        if (t < 0) continue;
+        const int pos = __ldg(tile_start + t) + rec_rank[r];
+        if (sc::in_range(pos, n_rec, status, 4)) items[pos] = r;
     }
 }
 
 // Without rank storage: one atomic cursor per bin, each record's bin
 // recomputed from its head.
 __global__ void bin_scatter_kernel(const ScStepRec *recs, int n_rec, sc::TileGeom g,
-                                   int32_t *cursor, int32_t *items) {
+                                   int32_t *cursor, int32_t *items, int32_t *status) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rec; r += gridDim.x * blockDim.x) {
         const int t = sc::record_tile(recs[r], r, g);
-        if (t >= 0) items[atomicAdd(&cursor[t], 1)] = r;
+        if (t < 0 || !sc::in_range(t, 2 * g.n_tiles, status, 5)) continue;
+        const int pos = atomicAdd(&cursor[t], 1);
+        if (sc::in_range(pos, n_rec, status, 4)) items[pos] = r;
     }
 }
 
@@ -499,7 +503,8 @@ int radix_bins(int n, int n_bins, int32_t *rec_bin, int32_t *keys_tmp, int32_t *
 
 // Scan, placement and sort of counted records.
 int bin_finish(int n_rec, const sc::TileGeom &g, int32_t *tile_count, int32_t *rec_bin,
-               const sc::BinLayout &b, int32_t *tile_start, int32_t *items, cudaStream_t s) {
+               const sc::BinLayout &b, int32_t *tile_start, int32_t *items, int32_t *status,
+               cudaStream_t s) {
     const int n_bins = 2 * g.n_tiles;
     bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(tile_count, n_bins, tile_start, nullptr);
     if (b.rx_vals)
@@ -509,7 +514,7 @@ int bin_finish(int n_rec, const sc::TileGeom &g, int32_t *tile_count, int32_t *r
     int32_t *big = b.big;
     int grid = (n_rec + 255) / 256;
     if (grid > 152 * 8) grid = 152 * 8;
-    bin_place_kernel<<<grid, 256, 0, s>>>(rec_bin, rec_rank, n_rec, tile_start, items);
+    bin_place_kernel<<<grid, 256, 0, s>>>(rec_bin, rec_rank, n_rec, tile_start, items, status);
     int rc = sc::launch_status("sc_bin_finish");
     if (rc) return rc;
     return bin_sort(n_bins, tile_start, items, big, s);
@@ -618,7 +623,7 @@ extern "C" int sc_bin_finish(int n_rec, const ScSplatParams *p, void *d_ws, size
                sc_bin_workspace_bytes(n_rec, g.n_tiles));
     sc::BinLayout b;
     sc::bin_layout(g, n_rec, d_ws, ws_bytes, b);
-    return bin_finish(n_rec, g, b.count, b.rec_bin, b, d_tile_start, d_items, s);
+    return bin_finish(n_rec, g, b.count, b.rec_bin, b, d_tile_start, d_items, nullptr, s);
 }
 
 extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatParams *p,
@@ -650,9 +655,10 @@ extern "C" int sc_bin_steps(const ScStepRec *d_recs, int n_rec, const ScSplatPar
     if (grid > 152 * 8) grid = 152 * 8;
     bin_count_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.count, b.rec_bin,
                                           sc::rank_array(b), d_status);
-    if (b.rec_bin) return bin_finish(n_rec, g, b.count, b.rec_bin, b, d_tile_start, d_items, s);
+    if (b.rec_bin)
+        return bin_finish(n_rec, g, b.count, b.rec_bin, b, d_tile_start, d_items, d_status, s);
     bin_tile_scan_kernel<<<1, kScanThreads, 0, s>>>(b.count, n_bins, d_tile_start, b.cursor);
-    bin_scatter_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.cursor, d_items);
+    bin_scatter_kernel<<<grid, 256, 0, s>>>(d_recs, n_rec, g, b.cursor, d_items, d_status);
     rc = sc::launch_status("sc_bin_steps");
     if (rc) return rc;
     return bin_sort(n_bins, d_tile_start, d_items, nullptr, s);

@@ -52,6 +52,24 @@ __device__ __forceinline__ void flag_status(int32_t *status, int bit, int a, int
     }
 }
 
+// Bounds-checked build (-DSC_BOUNDS_CHECK): in_range(i, n, ...) is false for
+// an index outside [0, n) and records it (status bit 8; the index, the bound
+// and the check's site in words 1..3), and the caller then skips the access.
+// In the normal build it is the constant true and the checks compile away.
+// Sites: 1 a splat warp's tile buffer, 2 its block-copy ring, 3 the tile
+// buffers a pixel's merge reads, 4 a record's place in the bin lists, 5 its
+// bin, 6 the register splat's tile buffer.
+constexpr int kBoundsBit = 8;
+#ifdef SC_BOUNDS_CHECK
+__device__ __forceinline__ bool in_range(int64_t i, int64_t n, int32_t *status, int site) {
+    if (i >= 0 && i < n) return true;
+    flag_status(status, kBoundsBit, (int)i, (int)n, site);
+    return false;
+}
+#else
+__device__ __forceinline__ bool in_range(int64_t, int64_t, int32_t *, int) { return true; }
+#endif
+
 // ------------------------------------------------------------ double-float
 // A value v is held as hi + lo with hi = fl32(v) and lo = fl32(v - hi).
 struct df {

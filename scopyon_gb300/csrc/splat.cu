@@ -374,8 +374,13 @@ __device__ __forceinline__ bool bulk_tile_records(
             const int R = dr + 1 + rsel;
             const float *B = my_stage + s * SB + rsel * NQ + col;
             float *D = my_acc + (R & 1) * HB + (R >> 1) * BSR + dc + 1 + col;
+            // bounds-checked build: the warp's tile buffer and stage ring
+            const int d0 = (int)(D - my_acc), b0 = (int)(B - my_stage);
+            const int acc_floats = (2 * HB + 31) & ~31, stage_floats = stages * SB;
             if (d.w & 2) {
-                if (col < NQ) {
+                if (col < NQ && sc::in_range(d0, acc_floats, status, 1) &&
+                    sc::in_range(d0 + (PAIRS - 1) * BSR, acc_floats, status, 1) &&
+                    sc::in_range(b0 + 2 * (PAIRS - 1) * NQ, stage_floats, status, 2)) {
 #pragma unroll
                     for (int i = 0; i < PAIRS; ++i)
                         D[i * BSR] = fmaf(w, B[2 * i * NQ], D[i * BSR]);
@@ -386,7 +391,9 @@ __device__ __forceinline__ bool bulk_tile_records(
 #pragma unroll
                     for (int i = 0; i < PAIRS; ++i) {
                         const int q = 2 * i + rsel;
-                        if (q >= qlo && q < qhi) D[i * BSR] = fmaf(w, B[2 * i * NQ], D[i * BSR]);
+                        if (q >= qlo && q < qhi && sc::in_range(d0 + i * BSR, acc_floats, status, 1) &&
+                            sc::in_range(b0 + 2 * i * NQ, stage_floats, status, 2))
+                            D[i * BSR] = fmaf(w, B[2 * i * NQ], D[i * BSR]);
                     }
                 }
             }
@@ -615,12 +622,17 @@ splat_box_reg_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restri
             const int dr = (cur.dd & 0xff) - 128, dc = ((cur.dd >> 8) & 0xff) - 128;
             const float v[8] = {cur.a.x, cur.a.y, cur.a.z, cur.a.w, cur.b.x, cur.b.y, cur.b.z, cur.b.w};
             float *D = my + (dr + 1) * S + dc + 1;
+            const int d0 = (int)(D - my);  // bounds-checked build: the warp's buffer
             if (cur.flags & 2) {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) D[off[j]] = fmaf(cur.w, v[j], D[off[j]]);
+                for (int j = 0; j < 4; ++j)
+                    if (sc::in_range(d0 + off[j], BS, status, 6))
+                        D[off[j]] = fmaf(cur.w, v[j], D[off[j]]);
                 if (lane < N1) {
 #pragma unroll
-                    for (int j = 4; j < 8; ++j) D[off[j]] = fmaf(cur.w, v[j], D[off[j]]);
+                    for (int j = 4; j < 8; ++j)
+                        if (sc::in_range(d0 + off[j], BS, status, 6))
+                            D[off[j]] = fmaf(cur.w, v[j], D[off[j]]);
                 }
             } else {
                 // clipped by the image's low edges: rows and columns from 0,
@@ -629,7 +641,8 @@ splat_box_reg_kernel(const ScStepRec *__restrict__ recs, const int32_t *__restri
                 for (int j = 0; j < 8; ++j) {
                     const int f = (j < 4 ? 4 * lane + j : 128 + 4 * lane + j - 4);
                     const int r = dr + f / NQ, cc = dc + f % NQ;
-                    if ((j < 4 || lane < N1) && f < NF && r >= 0 && r < E && cc >= 0)
+                    if ((j < 4 || lane < N1) && f < NF && r >= 0 && r < E && cc >= 0 &&
+                        sc::in_range(d0 + off[j], BS, status, 6))
                         D[off[j]] = fmaf(cur.w, v[j], D[off[j]]);
                 }
             }
@@ -956,7 +969,7 @@ __device__ __forceinline__ float merge_pixel(const float *ws, const SplatConsts 
 // non-negative terms, so the running sum is never -0).
 template <int MT>
 __device__ __forceinline__ float merge_pixel_mt(const float *ws, const SplatConsts &c, int i,
-                                                int j) {
+                                                int j, int32_t *status) {
     const int E = c.edge, EE = c.edge * c.edge;
     const int tx = i / c.tile, ty = j / c.tile;
     const int li0 = i - tx * c.tile, lj0 = j - ty * c.tile;
@@ -967,8 +980,9 @@ __device__ __forceinline__ float merge_pixel_mt(const float *ws, const SplatCons
         for (int b = 0; b < MT; ++b) {
             const int li = li0 + a * c.tile, lj = lj0 + b * c.tile;
             const bool ok = a <= tx && li < E && b <= ty && lj < E;
-            v[a][b] = ok ? __ldcg(ws + (size_t)((tx - a) * c.tiles_y + (ty - b)) * EE + li * E + lj)
-                         : 0.f;
+            const int64_t o = (int64_t)((tx - a) * c.tiles_y + (ty - b)) * EE + li * E + lj;
+            v[a][b] = ok && sc::in_range(o, (int64_t)c.tiles_per_image * EE, status, 3)
+                          ? __ldcg(ws + o) : 0.f;
         }
     float sum = 0.f;
 #pragma unroll
@@ -999,7 +1013,7 @@ merge_camera_kernel(const float *__restrict__ ws, SplatConsts c, sc::cam::CamCon
             const int p = 2 * q + h;
             if (p >= n) break;
             const int i = p / c.nh, j = p - (p / c.nh) * c.nh;
-            const float ph = MT > 0 ? merge_pixel_mt<(MT > 0 ? MT : 1)>(ws, c, i, j)
+            const float ph = MT > 0 ? merge_pixel_mt<(MT > 0 ? MT : 1)>(ws, c, i, j, status)
                                     : merge_pixel(ws, c, i, j);
             const float e = cc.qe_f * (ph + cc.background_f);
             const float sg = scmos ? __ldg(sigma + p) : cc.readout_f;

@@ -773,6 +773,9 @@ class FramePipeline:
             if bits & 128:
                 msgs.append("non-finite emitter position or normalisation (particle %d, "
                             "sub-step %d)" % (st[1], st[2]))
+            if bits & 256:
+                msgs.append("index %d out of range %d at check site %d (bounds-checked build)"
+                            % (st[1], st[2], st[3]))
             if bits & ~(64 | 128) == 0:
                 raise _lib.ScopyonInputError(
                     _lib.SC_ERR_NAN if bits & 128 else _lib.SC_ERR_ARG, "; ".join(msgs))

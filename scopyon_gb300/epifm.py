@@ -10,6 +10,7 @@ Device buffers are torch CUDA tensors, reused across frames.
 import contextlib
 import ctypes
 import math
+import os
 import warnings
 
 import numpy
@@ -123,6 +124,9 @@ class EngineConfig:
         if self.l2_fetch_bytes not in (0, 32, 64, 128):
             raise ValueError("gpu.l2_fetch_bytes must be 0, 32, 64 or 128 (got %r)"
                              % self.l2_fetch_bytes)
+        nvtx = _gpu_opt(raw, "nvtx", False)
+        self.nvtx = (nvtx if isinstance(nvtx, bool) else str(nvtx).lower() in ("1", "true", "yes")) \
+            or os.environ.get("SCOPYON_GB300_NVTX", "") not in ("", "0")
         self.use_box = bool(_gpu_opt(raw, "box_tables", True))
         self.catalog_dir = _gpu_opt(raw, "catalog_dir")
         table = _gpu_opt(raw, "cmos_table")
@@ -602,10 +606,12 @@ class FramePipeline:
         if binned:
             pass
         elif counted:
-            call("sc_bin_finish", n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items), s)
+            with self.timed("bins", stream):
+                call("sc_bin_finish", n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items), s)
         else:
-            call("sc_bin_steps", ptr(recs), n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start),
-                 ptr(items), ptr(self.status), s)
+            with self.timed("bins", stream):
+                call("sc_bin_steps", ptr(recs), n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start),
+                     ptr(items), ptr(self.status), s)
         L = _lib.load()
         sws_bytes = L.sc_splat_workspace_bytes(sp)
         sws = self._buf("splat_ws", (sws_bytes + 3) // 4, torch.float32)
@@ -640,23 +646,33 @@ class FramePipeline:
         """Scan, placement and order of records already counted into the bin
         buffers named by ``tag`` (sc_bin_finish)."""
         sp, ws, ws_bytes, items, tile_start = bufs or self.bin_buffers(n_rec, tag=tag)
-        call("sc_bin_finish", n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items),
-             stream_ptr(stream))
+        with self.timed("bins", stream):
+            call("sc_bin_finish", n_rec, sp, ptr(ws), ws_bytes, ptr(tile_start), ptr(items),
+                 stream_ptr(stream))
 
     @contextlib.contextmanager
     def timed(self, name, stream=None):
         """CUDA events around the enclosed launches when kernel_events is a
-        dict (appended under `name`); nothing otherwise."""
-        ev = self.kernel_events
-        if ev is None:
+        dict (appended under `name`), and an NVTX range ``scopyon/<name>``
+        around them when the configuration turns NVTX ranges on (``gpu.nvtx``
+        or ``SCOPYON_GB300_NVTX=1``); nothing otherwise."""
+        nvtx = self.cfg.nvtx
+        if nvtx:
+            torch.cuda.nvtx.range_push("scopyon/" + name)
+        try:
+            ev = self.kernel_events
+            if ev is None:
+                yield
+                return
+            st = stream if stream is not None else torch.cuda.current_stream()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
             yield
-            return
-        st = stream if stream is not None else torch.cuda.current_stream()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        yield
-        e1.record(st)
-        ev.setdefault(name, []).append((e0, e1))
+            e1.record(st)
+            ev.setdefault(name, []).append((e0, e1))
+        finally:
+            if nvtx:
+                torch.cuda.nvtx.range_pop()
 
     def camera_params(self, seed=0, counter=0, d_frame=None, exact=False):
         """The camera's parameter block (loads the CMOS noise table when needed)."""
@@ -836,8 +852,10 @@ class FramePipeline:
             sp.row_layout = row_layout
             if bleaching is not None:
                 sp.bleaching = 1 if bleaching else 0
-            call("sc_emitter_steps", sp, ptr(part), ptr(ut), ptr(present), ptr(self.psf.key_slot),
-                 ptr(self.budget), ptr(optinfo), ptr(recs), ptr(norm), ptr(self.status), s)
+            with self.timed("records_from_rows", stream):
+                call("sc_emitter_steps", sp, ptr(part), ptr(ut), ptr(present),
+                     ptr(self.psf.key_slot), ptr(self.budget), ptr(optinfo), ptr(recs), ptr(norm),
+                     ptr(self.status), s)
         opt = optinfo[: n * 8].view(n, 8) if with_optinfo else None
         if exact:
             image64 = self._buf("image64", self.n_pix, torch.float64)[: self.n_pix]
@@ -1092,6 +1110,32 @@ class FrameGraph:
             if i + 2 < k:
                 records(i + 2)
         call("sc_counter_add", ptr(self.frame), k, s)
+
+    def state_dict(self):
+        """Checkpoint: the trajectories' state, the photon budgets and the
+        frame counter, as host arrays and numbers (picklable).  The frames
+        after ``load_state_dict`` of it equal those that followed it."""
+        n = self.n
+        frame = int(self.frame.item())
+        traj = self.traj.state_dict()
+        traj["index"] = frame * self.n_sub  # the graph counts frames on the device
+        return {"trajectories": traj,
+                "budget": self.pipe.budget[:n].cpu().numpy().copy(),
+                "frame": frame, "frames_done": int(self.frames_done),
+                "seed": self.seed, "n_sub": self.n_sub}
+
+    def load_state_dict(self, state):
+        """Resume from ``state_dict()`` in place: the device buffers keep their
+        addresses, so a captured graph replays from the restored state."""
+        if int(state["seed"]) != self.seed or int(state["n_sub"]) != self.n_sub:
+            raise ValueError("the state is of a frame graph with another seed or sub-step count")
+        budget = numpy.asarray(state["budget"], dtype=numpy.float64)
+        if budget.shape != (self.n,):
+            raise ValueError("the state holds %d budgets for %d particles" % (budget.size, self.n))
+        self.traj.load_state_dict(state["trajectories"])
+        self.pipe.budget[: self.n].copy_(torch.from_numpy(budget))
+        self.frame.fill_(int(state["frame"]))
+        self.frames_done = int(state["frames_done"])
 
     def capture(self):
         """Run one frame eagerly (allocates every buffer), then capture the next."""

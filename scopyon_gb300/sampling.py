@@ -296,6 +296,34 @@ class DeviceTrajectories:
         call("sc_diffuse_steps", p, ptr(self._pos), ptr(self._cls), ptr(self._g_sigma), None,
              ptr(out), stream_ptr(stream))
 
+    def state_dict(self):
+        """The trajectory's state as host arrays: the time index reached, the
+        positions and the classes there.  With the construction arguments
+        (and the seed) it is all that later positions depend on, since the
+        Philox normals and transition uniforms are keyed by (seed, particle,
+        step)."""
+        if self._pos is None:
+            self.reset()
+        return {"index": int(self._index), "pos": self._pos.cpu().numpy().copy(),
+                "cls": self._cls.cpu().numpy().copy(), "seed": self.seed}
+
+    def load_state_dict(self, state):
+        """Resume from ``state_dict()``: the positions and classes are copied
+        into the existing device buffers (a captured frame graph keeps
+        them)."""
+        if int(state["seed"]) != self.seed:
+            raise ValueError("the state is of trajectories with another seed")
+        pos = numpy.asarray(state["pos"], dtype=numpy.float64)
+        cls = numpy.asarray(state["cls"], dtype=numpy.int32)
+        if pos.shape != (self.n_particles, 3) or cls.shape != (self.n_particles,):
+            raise ValueError("the state holds %s positions for %d particles"
+                             % (pos.shape, self.n_particles))
+        if self._pos is None:
+            self.reset()
+        self._pos.copy_(torch.from_numpy(pos))
+        self._cls.copy_(torch.from_numpy(cls))
+        self._index = int(state["index"])
+
     def advance_to(self, k, transform=None, stream=None):
         if self._pos is None or self._index > k:
             self.reset()

@@ -549,6 +549,79 @@ def test_register_box_kernel_equals_bulk_copy_ring(sg):
     assert numpy.abs(out[(16, 8, 0)] - ref).max() <= 1e-6 * ref.max()
 
 
+def test_frame_graph_checkpoint_resumes_the_same_frames(sg, tmp_path):
+    """A frame graph's checkpoint (positions and classes of the trajectories,
+    photon budgets, frame counter) pickled to disk and loaded into a new
+    pipeline, or back into the same captured graph, continues with the
+    frames that followed it, bit for bit, bleaching included."""
+    import pickle
+    from scopyon_gb300.base import _psf_for
+    from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {"magnification": 100,
+                            "detector": {"type": "EMCCD", "image_size": [96, 80],
+                                         "exposure_time": 0.004},
+                            "effects": {"photo_bleaching": {"switch": True, "half_life": 0.01}}}})
+    t = numpy.arange(9 * 4 + 1) * 1e-3
+    traj = sg.sample_inputs(t, N=1500, lower=[-6e-6, -5e-6, -0.2e-6], upper=[6e-6, 5e-6, 0.2e-6],
+                            D=0.4e-12, ndim=3, rng=numpy.random.RandomState(21),
+                            boundary="reflecting")
+    eng = EngineConfig(cfg["default"])
+    budget0 = numpy.random.RandomState(22).exponential(0.01 / numpy.log(2.0), 1500) * eng.n_emit0
+
+    def make(k):
+        pipe = FramePipeline(eng, "cuda", psf=_psf_for(eng, torch.device("cuda")))
+        pipe.psf.ensure(list(range(0, 300)))
+        pipe.ensure_slots(1500)
+        pipe.budget[:1500].copy_(torch.from_numpy(budget0))
+        return FrameGraph(pipe, traj.copy(), 4, 1e-3, seed=11, frames_per_step=k)
+
+    def run(fg, n):
+        out = []
+        for _ in range(n):
+            fg.step()
+            out.append(fg.pipe.adc32.cpu().numpy().copy())
+        fg.pipe.check_status()
+        return numpy.array(out)
+
+    for k in (1, 2):
+        fg = make(k)
+        run(fg, 2)
+        path = tmp_path / ("state%d.pkl" % k)
+        path.write_bytes(pickle.dumps(fg.state_dict()))
+        after = run(fg, 3)
+        state = pickle.loads(path.read_bytes())
+        fg2 = make(k)
+        fg2.load_state_dict(state)
+        numpy.testing.assert_array_equal(run(fg2, 3), after)
+        fg.load_state_dict(state)  # back into the graph that ran on
+        numpy.testing.assert_array_equal(run(fg, 3), after)
+        assert after.std() > 0
+        b = fg.pipe.budget[:1500].cpu().numpy()
+        assert (b == 0).any() and (b > 0).any()  # some emitters bleached, not all
+    with pytest.raises(ValueError, match="another seed"):
+        FrameGraph(make(1).pipe, traj.copy(), 4, 1e-3, seed=12).load_state_dict(state)
+
+
+def test_nvtx_ranges_leave_the_frames_unchanged(sg, monkeypatch):
+    """With NVTX ranges on (scopyon/records, bins, splat, camera around the
+    launches) the frames are those with them off, bit for bit."""
+    cfg = sg.DefaultConfiguration()
+    cfg.update({"default": {"magnification": 100,
+                            "detector": {"type": "EMCCD", "image_size": [48, 40],
+                                         "exposure_time": 0.004}}})
+    t = numpy.arange(3 * 4 + 1) * 1e-3
+    inputs = [(float(a), p) for a, p in sg.sampling.sample_inputs(
+        t, N=150, lower=[-3e-6, -3e-6, -0.2e-6], upper=[3e-6, 3e-6, 0.2e-6], D=0.3e-12, ndim=3,
+        rng=numpy.random.RandomState(2), exact=True)]
+    outs = []
+    for on in ("0", "1"):
+        monkeypatch.setenv("SCOPYON_GB300_NVTX", on)
+        gen = sg.generate_images(inputs, 3, config=cfg, rng=numpy.random.RandomState(9))
+        outs.append(numpy.array([img.as_array() for img in gen]))
+    numpy.testing.assert_array_equal(outs[0], outs[1])
+
+
 def test_l2_fetch_hint_values(sg):
     """The L2 fetch granularity hint takes 0, 32, 64 and 128 bytes."""
     from scopyon_gb300 import _lib

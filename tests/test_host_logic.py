@@ -114,3 +114,16 @@ def test_l2_fetch_hint_config_is_checked(value):
     cfg.update({"default": {"gpu": {"l2_fetch_bytes": value}}})
     with pytest.raises(ValueError, match="l2_fetch_bytes"):
         EngineConfig(cfg["default"], rng=numpy.random.RandomState(0))
+
+
+def test_nvtx_ranges_config(monkeypatch):
+    """NVTX ranges around the frame's launches are off by default and turned
+    on by gpu.nvtx or by SCOPYON_GB300_NVTX=1."""
+    monkeypatch.delenv("SCOPYON_GB300_NVTX", raising=False)
+    cfg = DefaultConfiguration()
+    assert EngineConfig(cfg["default"], rng=numpy.random.RandomState(0)).nvtx is False
+    monkeypatch.setenv("SCOPYON_GB300_NVTX", "1")
+    assert EngineConfig(cfg["default"], rng=numpy.random.RandomState(0)).nvtx is True
+    monkeypatch.setenv("SCOPYON_GB300_NVTX", "0")
+    cfg.update({"default": {"gpu": {"nvtx": True}}})
+    assert EngineConfig(cfg["default"], rng=numpy.random.RandomState(0)).nvtx is True

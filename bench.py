@@ -34,7 +34,8 @@ sys.path.insert(0, ROOT)
 N_EMIT = 20000
 IMAGE = 512
 SUBSTEPS = 20
-E2E_FRAMES = 20  # frames timed through the public API with host trajectories
+E2E_FRAMES = 20  # frames timed through the public API with host trajectories, per run
+E2E_RUNS = 5  # sequences timed; the e2e value is their median
 EXPOSURE = 0.010
 PX = 16e-6 / 100
 HALF = IMAGE * PX / 2
@@ -403,19 +404,27 @@ def e2e_arm(args, cfg, dev, rank, world):
     # host inputs exactly as scopyon.sample_inputs returns them: [(t, (N, 5) [x, y, z, id, 1])]
     inputs = [(float(t), numpy.hstack([pos[k], ids[:, None], numpy.ones((N_EMIT, 1))]))
               for k, t in enumerate(times)]
-    gen = sg.generate_images(inputs, n_frames, config=cfg, rng=numpy.random.RandomState(3 + rank),
-                             device=dev)
-    for _ in range(args.warmup):
-        next(gen)
-    torch.cuda.synchronize()
-    replica_barrier(world)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        img = next(gen)
-        img.as_array()
-    torch.cuda.synchronize()
-    dt = max_over_ranks(time.perf_counter() - t0, world, dev)
-    return {"value": world * steps / dt, "unit": "frames/s", "frames": steps,
+    # the leg is host-bound (Python per frame), and a window of a few
+    # milliseconds on a shared host catches stalls: the median of E2E_RUNS
+    # sequences, each through a new generator, and all of them reported
+    runs = []
+    for run in range(E2E_RUNS):
+        gen = sg.generate_images(inputs, n_frames, config=cfg,
+                                 rng=numpy.random.RandomState(3 + rank + 1000 * run), device=dev)
+        for _ in range(args.warmup):
+            next(gen)
+        torch.cuda.synchronize()
+        replica_barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            img = next(gen)
+            img.as_array()
+        torch.cuda.synchronize()
+        dt = max_over_ranks(time.perf_counter() - t0, world, dev)
+        runs.append(world * steps / dt)
+        gen.close()
+    return {"value": float(numpy.median(runs)), "unit": "frames/s", "frames": steps,
+            "runs": [round(v, 1) for v in runs], "statistic": "median of the runs",
             # rows, then the unit times and the frame index
             "h2d_bytes_per_step": SUBSTEPS * N_EMIT * 5 * 8 + (SUBSTEPS + 1) * 8,
             "d2h_bytes_per_step": IMAGE * IMAGE * 4 + 16}
@@ -658,20 +667,24 @@ def config1_arm(args, dev, n_emit=1000, substeps=10, seed=17):
             pts = pts.copy()
             pts[:, :2] += math.sqrt(2 * 0.1e-12 * dt) * hrng.standard_normal((n_emit, 2))
         inputs.append((float(t), pts))
-    gen = sg.generate_images(inputs, args.warmup + e2e_frames, config=cfg,
-                             rng=numpy.random.RandomState(seed + 2), device=dev)
-    for _ in range(args.warmup):
-        next(gen).as_array()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_frames):
-        next(gen).as_array()
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_frames
+    runs = []  # the median of E2E_RUNS sequences, as in the main e2e leg
+    for run in range(E2E_RUNS):
+        gen = sg.generate_images(inputs, args.warmup + e2e_frames, config=cfg,
+                                 rng=numpy.random.RandomState(seed + 2 + 1000 * run), device=dev)
+        for _ in range(args.warmup):
+            next(gen).as_array()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_frames):
+            next(gen).as_array()
+        torch.cuda.synchronize()
+        runs.append(e2e_frames / (time.perf_counter() - t0))
+        gen.close()
     return {"workload": "plain TIRF: 1,000 emitters, 160^2 px EMCCD, 10 sub-steps of 3 ms, "
                         "100 photons/emitter/ms, D = 0.1 um^2/s",
             "value": 1e3 / ms, "unit": "frames/s", "ms_per_frame": ms, "frames": steps,
-            "e2e": {"value": 1.0 / e2e_s, "unit": "frames/s", "frames": e2e_frames,
+            "e2e": {"value": float(numpy.median(runs)), "unit": "frames/s", "frames": e2e_frames,
+                    "runs": [round(v, 1) for v in runs], "statistic": "median of the runs",
                     "h2d_bytes_per_step": substeps * n_emit * 5 * 8 + (substeps + 1) * 8,
                     "d2h_bytes_per_step": 160 * 160 * 4 + 16}}
 

@@ -295,7 +295,23 @@ def _finish(pipe, out, nw, nh):
 
 def _Frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, draws,
             full_output=True):
-    """Frame generator: host bookkeeping around FramePipeline.run_frame."""
+    """Frame generator: host bookkeeping around FramePipeline.run_frame.
+
+    When it ends or is closed, it waits for the device: the uploads and
+    read-backs it issued through the library (one cudaMemcpyAsync each) are
+    not known to torch's pinned-memory cache, which could otherwise hand a
+    pinned buffer they still use to a new allocation."""
+    import torch
+    try:
+        yield from _frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching,
+                           draws, full_output)
+    finally:
+        if torch.cuda.is_initialized():
+            torch.cuda.synchronize(torch.device(sim._device()))
+
+
+def _frames(sim, cfg, data, num_frames, start_time, exposure_time, bleaching, draws,
+            full_output):
     import torch
     rng = sim._rng()
     device = torch.device(sim._device())

@@ -570,11 +570,18 @@ def born_wolf_fwd_bwd_case(dev, steps, warmup, seed=15, n_emit=N_EMIT):
         loss = dm.poisson_nll(dm.born_wolf_image(emit, bg, model), counts)
         return torch.autograd.grad(loss, [emit, bg])
 
-    fwd_ms = _event_ms(forward, steps, warmup)
-    fb_ms = _event_ms(step, steps, warmup)
+    # eager launches with a host check each: the median of three timings of
+    # each, interleaved, so that a stall of the shared host skews neither
+    fwd_runs, fb_runs = [], []
+    for _ in range(3):
+        fwd_runs.append(_event_ms(forward, steps, warmup))
+        fb_runs.append(_event_ms(step, steps, warmup))
+    fwd_ms, fb_ms = float(numpy.median(fwd_runs)), float(numpy.median(fb_runs))
     return {"model": "differentiable Born-Wolf image (cells integrated over each pixel, "
                      "adjacent depth keys blended)", "emitters": n_emit,
             "image": [IMAGE, IMAGE], "forward_ms": fwd_ms, "fwd_bwd_ms": fb_ms,
+            "forward_runs_ms": [round(v, 3) for v in fwd_runs],
+            "fwd_bwd_runs_ms": [round(v, 3) for v in fb_runs],
             "fwd_bwd_over_forward": fb_ms / fwd_ms,
             "fwd_bwd_frames_per_s": 1e3 / fb_ms,
             "timing": "eager launches with CUDA events (the forward checks the depth keys "

@@ -221,10 +221,12 @@ def gb300_arm(args, rank, world):
     psf_build_s = time.time() - t0
 
     # trajectories on the device: two populations (D = 0.01 and 1 um^2/s), Philox normals
-    n_timing = 4
+    n_timing = 16  # eager single frames timed kernel by kernel
     # several frames per graph replay, the records of the next frame running
-    # beside the splat of this one: 4 when the timed frames divide by 4
-    fps = next(k for k in (4, 2, 1) if args.steps % k == 0)
+    # beside the splat of this one: the most (up to 16) that divide the timed
+    # frames.  Each replay fills and drains that pipeline once, so more
+    # frames per replay hide more of it; every frame keeps its own outputs
+    fps = max(k for k in range(1, 17) if args.steps % k == 0)
     n_frames = 4 * (args.warmup + args.steps + n_timing) + 8000 + 20 * len(TILE_CANDIDATES)
     dt = EXPOSURE / SUBSTEPS
     t = numpy.arange(n_frames * SUBSTEPS + 1) * dt
@@ -246,11 +248,19 @@ def gb300_arm(args, rank, world):
     else:
         # every choice runs the same frames; the tuner restores the state after
         tune = tune_tiles(fg, frames=3)  # 5 steps per choice
+    # the sequence's first frames are the ones timed, whatever the frames per
+    # replay: its state at frame 0 (positions, budgets, frame counter) is
+    # restored after the warm-up (emitters bleach as the sequence goes on, so
+    # later frames hold fewer live emitters and less work)
+    state0 = fg.state_dict()
     fg.capture()  # one eager step of fps frames, then the capture
-    for _ in range(-(-args.warmup // fps) - 1):  # at least W warm-up frames in all
+    # at least W warm-up frames in all, and at least one replay of the graph
+    # (its first launch uploads it)
+    for _ in range(max(1, -(-args.warmup // fps) - 1)):
         fg.step()
     torch.cuda.synchronize()
     pipe.check_status()
+    fg.load_state_dict(state0)
     replica_barrier(world)
     live0 = float((pipe.budget[:N_EMIT] > 0).float().mean())
     clocks = ClockSampler(dev.index)
@@ -266,9 +276,12 @@ def gb300_arm(args, rank, world):
     replica_barrier(world)
     live1 = float((pipe.budget[:N_EMIT] > 0).float().mean())
     elapsed_ms = start.elapsed_time(end)
-    # the splat's own duration: the frames right after the timed ones, launched
-    # eagerly with events around the splat
+    # the splat's own duration: the same first frames again, launched eagerly
+    # one at a time (no records kernel beside the splat) with events around
+    # the splat and the stages
     fg.graph, fg.use_graph = None, False
+    fg.load_state_dict(state0)
+    per_replay, fg.frames_per_step = fg.frames_per_step, 1
     pipe.kernel_events = {}
     splat_recs = []
     for _ in range(n_timing):
@@ -276,6 +289,7 @@ def gb300_arm(args, rank, world):
         # records binned this frame: the last bin offset
         splat_recs.append(int(pipe._cap["tile_start"][2 * pipe.tiles_x * pipe.tiles_y]))
     torch.cuda.synchronize()
+    fg.frames_per_step = per_replay
     splat_ms = [a.elapsed_time(b) for a, b in pipe.kernel_events["splat"]]
     stage_ms = {k: sum(a.elapsed_time(b) for a, b in pipe.kernel_events[k]) /
                 len(pipe.kernel_events[k]) for k in ("records", "camera")}
@@ -322,13 +336,16 @@ def gb300_arm(args, rank, world):
                 "tile_autotune_ms_per_frame": {_tune_name(t, w, st): round(ms, 4)
                                                for (t, w, st), ms in tune.items()},
                 "step": "one frame: Brownian sub-steps, physics, binning, splat, camera; "
-                        "%d frame(s) per CUDA graph replay%s" % (
+                        "%d frame(s) per CUDA graph replay%s, each frame's expectation and "
+                        "ADC counts in a buffer of its own" % (
                             fps, ", each frame's records kernel (side stream) overlapping "
                                  "the previous frame's binning, splat and camera"
                             if fps > 1 else ""),
+                "frames_per_graph_replay": fps,
                 "parallelism": "replicas" if world > 1 else "single",
                 "boundary": "reflecting",
-                "timed_frames": [args.warmup, args.warmup + args.steps],
+                "timed_frames": [0, args.steps],
+                "warmup_frames": "the same frames, run before and rewound to frame 0",
                 "live_emitters": [round(live0, 4), round(live1, 4)],
                 "psf_build_s": round(psf_build_s, 3)},
         "e2e": e2e,
@@ -346,7 +363,9 @@ def gb300_arm(args, rank, world):
                                        "capture of the profiling case, times records",
                      "algorithmic_bytes": alg, "records": n_rec,
                      "avg_launch_ms": splat_avg_ms,
-                     "timed_on": "%d eager frames after the timed graph replays" % n_timing,
+                     "timed_on": "%d eager single frames (the splat alone, no records kernel "
+                                 "beside it) after the timed graph replays, the sequence's "
+                                 "first frames again" % n_timing,
                      "stages": stage_rooflines(stage_ms, pipe, SUBSTEPS * N_EMIT, peak),
                      "stages_beyond_l2": large_stages},
     }
@@ -643,23 +662,24 @@ def config1_arm(args, dev, n_emit=1000, substeps=10, seed=17):
     pipe.psf.ensure([0])
     dt = eng.exposure_time / substeps
     steps = max(40, 4 * args.steps)
-    n_frames = 4 * (args.warmup + steps) + 16
+    n_frames = 4 * (args.warmup + steps) + 64
     half = 80 * PX
     traj = sg.sample_inputs(numpy.arange(n_frames * substeps + 1) * dt, N=n_emit, D=0.1e-12,
                             rng=rng, lower=-half, upper=half, ndim=2, device=dev)
-    fg = FrameGraph(pipe, traj, substeps, dt, seed=seed, frames_per_step=4)
+    per = max(k for k in range(1, 17) if steps % k == 0)  # frames per replay, as above
+    fg = FrameGraph(pipe, traj, substeps, dt, seed=seed, frames_per_step=per)
     fg.capture()
-    for _ in range(-(-args.warmup // 4)):
+    for _ in range(-(-args.warmup // per)):
         fg.step()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     a.record()
-    for _ in range(steps // 4):
+    for _ in range(steps // per):
         fg.step()
     b.record()
     torch.cuda.synchronize()
     pipe.check_status()
-    ms = a.elapsed_time(b) / (4 * (steps // 4))
+    ms = a.elapsed_time(b) / steps
     # e2e: the public API on host trajectories (the reference's sample_inputs layout)
     e2e_frames = 20
     t_host = numpy.arange((args.warmup + e2e_frames) * substeps + 1) * dt
@@ -1139,7 +1159,7 @@ def reference_arm(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=32)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")

@@ -91,13 +91,14 @@ class _PersistentFrames(FrameGraph):
         sws = pipe._buf("splat_ws", (sws_bytes + 3) // 4, torch.float32)
         cp = pipe.camera_params(self.seed, frame_offset, self.frame)
         maps = pipe.pixel_maps
+        expect, adc32 = self.outputs[frame_offset]
         with pipe.timed("batch_frame"):
             _lib.call("sc_batch_frame", _lib.ptr(recs), _lib.ptr(bufs[4]), _lib.ptr(bufs[3]),
                       _lib.ptr(pipe.psf.tables), _lib.ptr(pipe.psf.box), sp, plan, cp,
                       _lib.ptr(pipe.offset_f) if maps else None,
                       _lib.ptr(pipe.inv_gain_f) if maps else None, _lib.ptr(pipe.sigma),
                       _lib.ptr(pipe.table_value), _lib.ptr(pipe.table_cdf), _lib.ptr(sws),
-                      sws_bytes, _lib.ptr(pipe.expect), _lib.ptr(pipe.adc32),
+                      sws_bytes, _lib.ptr(expect), _lib.ptr(adc32),
                       _lib.ptr(pipe.status), _lib.stream_ptr())
 
 

@@ -621,15 +621,17 @@ class FramePipeline:
         return sp, sws, sws_bytes
 
     def splat_camera(self, recs, n_rec, seed=0, counter=0, d_frame=None, stream=None, tag="",
-                     binned=False, bufs=None):
-        """A native frame's splat and camera into self.expect / self.adc32: the
-        splat without its merge, then the merge and the camera in one pass
-        (sc_merge_camera), equal bit for bit to splat_records into self.image
-        followed by camera().  With merge_camera off, those two."""
+                     binned=False, bufs=None, out=None):
+        """A native frame's splat and camera into self.expect / self.adc32 (or
+        the (expect, adc32) pair ``out``): the splat without its merge, then
+        the merge and the camera in one pass (sc_merge_camera), equal bit for
+        bit to splat_records into self.image followed by camera().  With
+        merge_camera off, those two."""
+        expect, adc32 = out if out is not None else (self.expect, self.adc32)
         if not self.merge_camera:
             self.splat_records(recs, n_rec, self.image, stream=stream, tag=tag, binned=binned,
                                bufs=bufs)
-            self.camera(self.image, self.expect, None, self.adc32, seed=seed, counter=counter,
+            self.camera(self.image, expect, None, adc32, seed=seed, counter=counter,
                         stream=stream, d_frame=d_frame)
             return
         sp, sws, sws_bytes = self.splat_records(recs, n_rec, None, stream=stream, tag=tag,
@@ -639,8 +641,8 @@ class FramePipeline:
         with self.timed("camera", stream):
             call("sc_merge_camera", sp, ptr(sws), sws_bytes, cp,
                  ptr(self.offset_f) if maps else None, ptr(self.inv_gain_f) if maps else None,
-                 ptr(self.sigma), ptr(self.table_value), ptr(self.table_cdf), ptr(self.expect),
-                 ptr(self.adc32), ptr(self.status), stream_ptr(stream))
+                 ptr(self.sigma), ptr(self.table_value), ptr(self.table_cdf), ptr(expect),
+                 ptr(adc32), ptr(self.status), stream_ptr(stream))
 
     def finish_bins(self, n_rec, tag="", stream=None, bufs=None):
         """Scan, placement and order of records already counted into the bin
@@ -1026,8 +1028,10 @@ class FrameGraph:
     a high-priority side stream, each into one of two record and bin buffer
     sets, while the main stream splats and images the frame before.  Frame i + 2's
     records wait for frame i's image to free its buffer set.  The frames and
-    their results are those of k single steps; only the last frame's outputs
-    remain after the step.
+    their results are those of k single steps.  Frame i of a step writes its
+    expectation and ADC counts into ``outputs[i]``; the last frame's pair is
+    ``pipe.expect`` / ``pipe.adc32``, so all k frames' images remain after
+    the step.
     """
 
     def __init__(self, pipe, traj, n_sub, unit_time, first_frame=0, transform=None, seed=0,
@@ -1051,6 +1055,9 @@ class FrameGraph:
         self.frames_done = 0
         # the second frame's records: a side stream that the scheduler serves first
         self._side = torch.cuda.Stream(device=dev, priority=-1) if frames_per_step > 1 else None
+        # (expect, adc32) of each frame of a step, the last one the pipeline's
+        self.outputs = [(torch.empty_like(pipe.expect), torch.empty_like(pipe.adc32))
+                        for _ in range(self.frames_per_step - 1)] + [(pipe.expect, pipe.adc32)]
 
     def _records(self, tag, first_step):
         """Records of one frame (sub-steps first_step .. + n_sub of the frame
@@ -1076,7 +1083,8 @@ class FrameGraph:
         pipe = self.pipe
         recs, bufs = recs
         pipe.splat_camera(recs, self.n_sub * self.n, seed=self.seed, counter=frame_offset,
-                          d_frame=self.frame, tag=tag, binned=True, bufs=bufs)
+                          d_frame=self.frame, tag=tag, binned=True, bufs=bufs,
+                          out=self.outputs[frame_offset])
 
     def _launch(self):
         s = stream_ptr()

@@ -238,7 +238,9 @@ def test_poisson_sampler_distribution(sg):
 
 
 def test_frame_graph_replay_matches_eager(sg):
-    """Frames replayed from one captured CUDA graph equal eagerly launched frames."""
+    """Frames replayed from one captured CUDA graph equal eagerly launched
+    frames, also with 2, 3, 8 and 16 frames per replay, every frame's
+    outputs kept."""
     from scopyon_gb300.base import _psf_for
     from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
     cfg = sg.DefaultConfiguration()
@@ -248,24 +250,27 @@ def test_frame_graph_replay_matches_eager(sg):
         "effects": {"photo_bleaching": {"switch": True, "half_life": 0.01}},
         "gpu": {"cmos_noise": "scmos"}}})
     outs = []
-    for use_graph, per_step in ((False, 1), (True, 1), (False, 2), (True, 2), (True, 3)):
+    cases = ((False, 1), (True, 1), (False, 2), (True, 2), (True, 3), (True, 8), (True, 16))
+    n_frames = 48
+    for use_graph, per_step in cases:
         rng = numpy.random.RandomState(6)
         eng = EngineConfig(cfg["default"], rng=rng)
         pipe = FramePipeline(eng, "cuda", psf=_psf_for(eng, torch.device("cuda")))
         pipe.scmos_sigma_map(rng)
-        t = numpy.arange(6 * 4 + 1) * 1e-3
+        t = numpy.arange(n_frames * 4 + 1) * 1e-3
         traj = sg.sample_inputs(t, N=300, lower=[-3e-6, -3e-6, -0.3e-6], upper=[3e-6, 3e-6, 0.3e-6],
-                                D=0.5e-12, ndim=3, rng=rng)
+                                D=0.5e-12, ndim=3, rng=rng, boundary="reflecting")
         pipe.psf.ensure(list(range(0, 700)))
         pipe.ensure_slots(300)
         pipe.budget[:300].copy_(torch.from_numpy(rng.exponential(0.02, 300) * eng.n_emit0))
         fg = FrameGraph(pipe, traj, 4, 1e-3, seed=77, use_graph=use_graph,
                         frames_per_step=per_step)
         frames = []
-        for _ in range(6 // per_step):
+        for _ in range(n_frames // per_step):
             fg.step()
-            # a two-frame step leaves the second frame's outputs
-            frames.append(pipe.adc32.cpu().numpy().copy())
+            # every frame of a step keeps its own outputs, the last in pipe.adc32
+            assert fg.outputs[-1][1] is pipe.adc32
+            frames.extend(adc.cpu().numpy().copy() for _, adc in fg.outputs)
         pipe.check_status()
         pos = traj._pos.cpu().numpy().copy()
         outs.append((numpy.array(frames), pos))
@@ -273,8 +278,8 @@ def test_frame_graph_replay_matches_eager(sg):
     assert outs[0][0].std(axis=0).max() > 0  # frames differ from one another
     # several frames per step (each frame's records overlapping the previous
     # frame's splat) give the same frames and trajectories
-    for k, per_step in ((2, 2), (3, 2), (4, 3)):
-        numpy.testing.assert_array_equal(outs[k][0], outs[0][0][per_step - 1::per_step])
+    for k in range(2, len(cases)):
+        numpy.testing.assert_array_equal(outs[k][0], outs[0][0], err_msg=str(cases[k]))
         numpy.testing.assert_array_equal(outs[k][1], outs[0][1])
 
 

@@ -1055,6 +1055,9 @@ class FrameGraph:
         self.frames_done = 0
         # the second frame's records: a side stream that the scheduler serves first
         self._side = torch.cuda.Stream(device=dev, priority=-1) if frames_per_step > 1 else None
+        # record and bin buffer sets: the records run up to this many frames
+        # ahead of the image
+        self.record_sets = 2
         # (expect, adc32) of each frame of a step, the last one the pipeline's
         self.outputs = [(torch.empty_like(pipe.expect), torch.empty_like(pipe.adc32))
                         for _ in range(self.frames_per_step - 1)] + [(pipe.expect, pipe.adc32)]
@@ -1093,30 +1096,30 @@ class FrameGraph:
             call("sc_counter_add", ptr(self.frame), 1, s)
             return
         main, side, k = torch.cuda.current_stream(), self._side, self.frames_per_step
-        tags = ("", "_b")
+        n_sets = self.record_sets
+        tags = ("",) + tuple("_%d" % j for j in range(1, n_sets))
         recs, ready, imaged = [None] * k, [None] * k, [None] * k
 
         def records(i):
-            if i >= 2:
-                side.wait_event(imaged[i - 2])  # frame i - 2 is done with this buffer set
+            if i >= n_sets:  # frame i - n_sets is done with this buffer set
+                side.wait_event(imaged[i - n_sets])
             with torch.cuda.stream(side):
-                recs[i] = self._records(tags[i % 2], i * self.n_sub)
+                recs[i] = self._records(tags[i % n_sets], i * self.n_sub)
             ready[i] = torch.cuda.Event()
             ready[i].record(side)
 
         fork = torch.cuda.Event()
         fork.record(main)
         side.wait_event(fork)
-        records(0)
-        if k > 1:
-            records(1)
+        for i in range(min(n_sets, k)):
+            records(i)
         for i in range(k):
             main.wait_event(ready[i])
-            self._image(recs[i], tags[i % 2], i)
+            self._image(recs[i], tags[i % n_sets], i)
             imaged[i] = torch.cuda.Event()
             imaged[i].record(main)
-            if i + 2 < k:
-                records(i + 2)
+            if i + n_sets < k:
+                records(i + n_sets)
         call("sc_counter_add", ptr(self.frame), k, s)
 
     def state_dict(self):

@@ -239,8 +239,8 @@ def test_poisson_sampler_distribution(sg):
 
 def test_frame_graph_replay_matches_eager(sg):
     """Frames replayed from one captured CUDA graph equal eagerly launched
-    frames, also with 2, 3, 8 and 16 frames per replay, every frame's
-    outputs kept."""
+    frames, also with 2, 3, 8 and 16 frames per replay and with the records
+    running up to 2 or 3 frames ahead, every frame's outputs kept."""
     from scopyon_gb300.base import _psf_for
     from scopyon_gb300.epifm import EngineConfig, FrameGraph, FramePipeline
     cfg = sg.DefaultConfiguration()
@@ -250,9 +250,11 @@ def test_frame_graph_replay_matches_eager(sg):
         "effects": {"photo_bleaching": {"switch": True, "half_life": 0.01}},
         "gpu": {"cmos_noise": "scmos"}}})
     outs = []
-    cases = ((False, 1), (True, 1), (False, 2), (True, 2), (True, 3), (True, 8), (True, 16))
+    # (graph, frames per replay, record and bin buffer sets)
+    cases = ((False, 1, 2), (True, 1, 2), (False, 2, 2), (True, 2, 2), (True, 3, 2),
+             (True, 8, 2), (True, 16, 2), (True, 3, 3), (True, 16, 3))
     n_frames = 48
-    for use_graph, per_step in cases:
+    for use_graph, per_step, sets in cases:
         rng = numpy.random.RandomState(6)
         eng = EngineConfig(cfg["default"], rng=rng)
         pipe = FramePipeline(eng, "cuda", psf=_psf_for(eng, torch.device("cuda")))
@@ -265,6 +267,7 @@ def test_frame_graph_replay_matches_eager(sg):
         pipe.budget[:300].copy_(torch.from_numpy(rng.exponential(0.02, 300) * eng.n_emit0))
         fg = FrameGraph(pipe, traj, 4, 1e-3, seed=77, use_graph=use_graph,
                         frames_per_step=per_step)
+        fg.record_sets = sets
         frames = []
         for _ in range(n_frames // per_step):
             fg.step()
